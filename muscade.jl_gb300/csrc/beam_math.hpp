@@ -1,0 +1,587 @@
+// EulerBeam3D residual and exact Newton tangent, closed form over the
+// corotational kinematics, for the GB300 element kernels (host-compilable too).
+//
+// Reference behaviour (toolbox/BeamElement.jl):
+//   residual   :151-174    R = Σ_gp (fᵢ ε∂X₀ + mᵢ·κ∂X₀ + fₑ·x∂X₀ + mₑ·vₛₘ∂X₀) dL
+//   kinematics :177-189,  corotated :193-208,  resultants :28-64
+//   rotations  toolbox/Rotations.jl:13-182 (sinc1 branches, scac Taylor
+//              branch, norm3 zeroing below 1e-14 -- all mirrored here)
+//
+// Formulation used here (mathematically identical to the reference):
+//  * The rotation core (r₁, r₂, Δv = ½Rod⁻¹(r₂r₁ᵀ), rₛₘ = Rod(Δv) r₁ rₘ, vₛₘ)
+//    depends only on the six rotation dofs; it is evaluated in truncated
+//    Taylor arithmetic (tj.hpp) which yields values, gradients, Hessians and
+//    the time jets needed by inertia and drag.
+//  * With t,n,b the columns of rₛₘ and d = ½(u₂-u₁)+½tgₘ, the local quantities
+//    are uₗ₂ = rₛₘᵀd − ½L e₁ and vₗ₂ = rₛₘᵀΔv, hence ε = 2|d|/L − 1,
+//    κ = (κₐ t·Δv, κᵤ n·d + κᵥ b·Δv, κᵤ b·d − κᵥ n·Δv) and the Gauss point
+//    position x = yᵤ d + (yₐ−yᵤ)(t·d) t + yᵥ Δv×t + ½(u₁+u₂) + cₘ.
+//  * Σ_gp(fᵢ ε∂X₀ + mᵢ·κ∂X₀)dL is the gradient of the quadratic strain energy
+//    Π; the external terms are the gradient of ψ = Σ_gp dL f_gp·x_gp +
+//    Σ_gp dL mₑ·vₛₘ with the loads held fixed.  R = ∇(Π+ψ) and the tangent is
+//    ∇²(Π+ψ) plus Σ_gp dL x∂X₀ᵀ δf_gp + vₛₘ∂X₀ᵀ δmₑ (load variation).
+// Output layout: R[12], K[i + 12 j] = ∂R_i/∂X_j (column-major, like asm[2]).
+#pragma once
+#include "tj.hpp"
+
+namespace mgpu {
+
+// ---- special functions (toolbox/Rotations.jl) -------------------------------
+// sinc1(x)=sin(x)/x and its derivatives with the reference's branch points.
+MG_HD double sinc1_0(double x) {
+  const double y = x * 0.31830988618379067154;  // x/π (Base.sinc of x/π)
+  if (fabs(y) < 1e-3) {
+    const double p2 = 9.8696044010893586188;  // π²
+    const double y2 = y * y;
+    return 1.0 + y2 * (-p2 / 6.0 + y2 * (p2 * p2 / 120.0));
+  }
+  return sin(x) / x;
+}
+MG_HD double sinc1_1(double x) {
+  if (fabs(x) > 1e-3) {
+    double s, c;
+    sincos(x, &s, &c);
+    return c / x - s / (x * x);
+  }
+  const double x2 = x * x;
+  return x * (-1.0 / 3.0 + x2 / 30.0);
+}
+MG_HD double sinc1_2(double x) {
+  if (fabs(x) > 1e-1) {
+    double s, c;
+    sincos(x, &s, &c);
+    return -s / x - 2.0 * c / (x * x) + 2.0 * s / (x * x * x);
+  }
+  const double x2 = x * x;
+  return -1.0 / 3.0 + x2 * (1.0 / 10.0 + x2 * (-1.0 / 168.0 + x2 * (1.0 / 6480.0)));
+}
+MG_HD double sinc1_3(double x) {
+  if (fabs(x) > 0.4) {
+    double s, c;
+    sincos(x, &s, &c);
+    const double x2 = x * x;
+    return -c / x + 3.0 * s / x2 + 6.0 * c / (x2 * x) - 6.0 * s / (x2 * x2);
+  }
+  const double x2 = x * x;
+  return x * (1.0 / 5.0 + x2 * (-1.0 / 42.0 + x2 * (1.0 / 1080.0 + x2 * (-1.0 / 55440.0 + x2 * (1.0 / 4717440.0)))));
+}
+
+// scac(x) = sinc1(acos x) with the reference's degree-5 Taylor branch near 1;
+// f[0..3] = value and first three derivatives.
+MG_HD void scac_derivs(double x, double f[4]) {
+  const double dx = x - 1.0;
+  if (fabs(dx) > 1e-3) {
+    const double th = acos(x);
+    const double q = 1.0 - x * x;
+    const double sq = sqrt(q);
+    const double t1 = -1.0 / sq;
+    const double t2 = -x / (q * sq);
+    const double t3 = -(1.0 + 2.0 * x * x) / (q * q * sq);
+    const double s0 = sinc1_0(th), s1 = sinc1_1(th), s2 = sinc1_2(th), s3 = sinc1_3(th);
+    f[0] = s0;
+    f[1] = s1 * t1;
+    f[2] = s2 * t1 * t1 + s1 * t2;
+    f[3] = s3 * t1 * t1 * t1 + 3.0 * s2 * t1 * t2 + s1 * t3;
+    return;
+  }
+  const double c1 = 1.0 / 3.0, c2 = -2.0 / 90.0, c3 = 0.0052911879917544626, c4 = -0.0016229317117234072, c5 = 0.0005625;
+  f[0] = 1.0 + dx * (c1 + dx * (c2 + dx * (c3 + dx * (c4 + dx * c5))));
+  f[1] = c1 + dx * (2.0 * c2 + dx * (3.0 * c3 + dx * (4.0 * c4 + dx * (5.0 * c5))));
+  f[2] = 2.0 * c2 + dx * (6.0 * c3 + dx * (12.0 * c4 + dx * (20.0 * c5)));
+  f[3] = 6.0 * c3 + dx * (24.0 * c4 + dx * (60.0 * c5));
+}
+
+// ---- rotations in Taylor arithmetic ----------------------------------------
+// Rodrigues(v) = I + sinc1(θ) S + ½ sinc1(θ/2)² S²,  θ = norm3(v)   (Rotations.jl:131-135)
+template <bool D>
+MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
+  const TJ<D> s2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  TJ<D> A, B;
+  const double th = sqrt(s2.v);
+  if (th < 1e-14) {  // norm3 returns an exact zero: sinc1 terms become constants
+    A = tj_const<D>(1.0);
+    B = tj_const<D>(0.5);
+  } else {
+    const double r = 1.0 / th;
+    // θ = √s2
+    const TJ<D> t = tj_apply(s2, th, 0.5 * r, -0.25 * r * r * r, 0.375 * r * r * r * r * r);
+    A = tj_apply(t, sinc1_0(th), sinc1_1(th), sinc1_2(th), sinc1_3(th));
+    const double h = 0.5 * th;
+    const TJ<D> sh = tj_apply(t, sinc1_0(h), 0.5 * sinc1_1(h), 0.25 * sinc1_2(h), 0.125 * sinc1_3(h));
+    B = (sh * sh) * 0.5;
+  }
+  // S = spin(v): S[2,1]=v3, S[3,1]=-v2, S[1,2]=-v3, S[3,2]=v1, S[1,3]=v2, S[2,3]=-v1
+  // S² = v vᵀ - |v|² I  (spin², Rotations.jl:114-122)
+  const TJ<D> ab = v[0] * v[1], ca = v[2] * v[0], bc = v[1] * v[2];
+  const TJ<D> aa = v[0] * v[0], bb = v[1] * v[1], cc = v[2] * v[2];
+  R[0] = B * (-(bb + cc)) + 1.0;
+  R[4] = B * (-(aa + cc)) + 1.0;
+  R[8] = B * (-(aa + bb)) + 1.0;
+  const TJ<D> Bab = B * ab, Bca = B * ca, Bbc = B * bc;
+  const TJ<D> Av0 = A * v[0], Av1 = A * v[1], Av2 = A * v[2];
+  R[1] = Av2 + Bab;   // [2,1]
+  R[3] = Bab - Av2;   // [1,2]
+  R[2] = Bca - Av1;   // [3,1]
+  R[6] = Av1 + Bca;   // [1,3]
+  R[5] = Av0 + Bbc;   // [3,2]
+  R[7] = Bbc - Av0;   // [2,3]
+}
+
+// Rodrigues⁻¹(m) = spin⁻¹(m) / scac((tr m − 1)/2)   (Rotations.jl:105)
+template <bool D>
+MG_HD void rodrigues_inv(const TJ<D> m[9], TJ<D> w[3]) {
+  const TJ<D> c = (m[0] + m[4] + m[8] + (-1.0)) * 0.5;
+  double f[4];
+  scac_derivs(c.v, f);
+  const TJ<D> s = tj_apply(c, f[0], f[1], f[2], f[3]);
+  const double iv = 1.0 / s.v;
+  const TJ<D> is = tj_apply(s, iv, -iv * iv, 2.0 * iv * iv * iv, -6.0 * iv * iv * iv * iv);
+  w[0] = ((m[5] - m[7]) * 0.5) * is;  // (m32 - m23)/2
+  w[1] = ((m[6] - m[2]) * 0.5) * is;  // (m13 - m31)/2
+  w[2] = ((m[1] - m[3]) * 0.5) * is;  // (m21 - m12)/2
+}
+
+// C = A Bᵀ  (both Taylor)
+template <bool D>
+MG_HD void mul_abt(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[i + 3 * j] = A[i] * B[j] + A[i + 3] * B[j + 3] + A[i + 6] * B[j + 6];
+}
+// C = A B
+template <bool D>
+MG_HD void mul_ab(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[1 + 3 * j] + A[i + 6] * B[2 + 3 * j];
+}
+// C = A M with M a constant matrix
+template <bool D>
+MG_HD void mul_ac(const TJ<D> A[9], const double M[9], TJ<D> C[9]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[i + 3 * j] = A[i] * M[3 * j] + A[i + 3] * M[1 + 3 * j] + A[i + 6] * M[2 + 3 * j];
+}
+
+// ---- per-element constants, precomputed at create time ----------------------
+struct BeamConst {
+  double rm[9];   // as-meshed frame (column-major)
+  double tgm[3];  // c₂ − c₁
+  double L;
+  // strain energy Π = ½kε ε² + ½kt θt² + ½k3v θb² + k3uv wn θb + ½k3u wn²
+  //                 + ½k2v θn² − k2uv wb θn + ½k2u wb²
+  double ke, kt, k3u, k3uv, k3v, k2u, k2uv, k2v;
+  double S0;                                    // Σ dL
+  double dL[4], ya[4], yu[4], yv[4];            // Gauss data
+  double mu, iota1, w, Ca[3], Cl[3], Cq[3];     // cross section (dynamic part)
+};
+
+// Newton variation of the state: X₀ += p0 δ, X₁ += p1 δ, X₂ += p2 δ
+// (SweepX{0}: 1,0,0;  Newmark: 1,a₁,b₁;  diffed K/C/M: unit vectors).
+struct Perturb {
+  double p0, p1, p2;
+};
+
+template <class T>
+MG_HD T dot3(const T a[3], const T b[3]) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// rotation-dof index (0..5) of element dof j, or -1 for translations
+MG_HD int rot_index(int j) { return (j >= 3 && j < 6) ? j - 3 : (j >= 9 ? j - 6 : -1); }
+
+// Full element evaluation.
+//   X0,X1,X2: element dofs and their first/second time derivatives (X1,X2 ignored if !D)
+//   U: U-dof loads per unit length (nullptr if none)
+//   out R[12], K[144];  rdir[12] (optional): derivative along X₁ += a δr, X₂ += b δr
+//   H[36] (optional): ∂R/∂U, column-major 12x3
+template <bool D>
+MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, const double* X2, const double* U,
+                        Perturb pt, const double* av, const double* bv, double* R, double* K, double* rdir,
+                        double* H) {
+  // ---- rotation core
+  TJ<D> v1[3], v2[3];
+  for (int i = 0; i < 3; ++i) {
+    if constexpr (D) {
+      v1[i] = tj_var<D>(X0[3 + i], i, X1[3 + i], X2[3 + i]);
+      v2[i] = tj_var<D>(X0[9 + i], 3 + i, X1[9 + i], X2[9 + i]);
+    } else {
+      v1[i] = tj_var<D>(X0[3 + i], i);
+      v2[i] = tj_var<D>(X0[9 + i], 3 + i);
+    }
+  }
+  TJ<D> r1[9], rsm[9], dv[3];
+  {
+    TJ<D> r2[9], Q[9];
+    rodrigues(v1, r1);
+    rodrigues(v2, r2);
+    mul_abt(r2, r1, Q);
+    TJ<D> wv[3];
+    rodrigues_inv(Q, wv);
+    for (int i = 0; i < 3; ++i) dv[i] = wv[i] * 0.5;
+  }
+  {
+    TJ<D> rD[9], rs[9];
+    rodrigues(dv, rD);
+    mul_ab(rD, r1, rs);
+    mul_ac(rs, c.rm, rsm);
+  }
+  const TJ<D>* t = rsm;      // first column
+  const TJ<D>* n = rsm + 3;  // second column
+  const TJ<D>* b = rsm + 6;  // third column
+
+  // ---- translations (d = ½(u₂−u₁)+½tgₘ enters linearly)
+  double d[3], dd1[3], dd2[3];
+  for (int i = 0; i < 3; ++i) {
+    d[i] = 0.5 * (X0[6 + i] - X0[i]) + 0.5 * c.tgm[i];
+    dd1[i] = D ? 0.5 * (X1[6 + i] - X1[i]) : 0.0;
+    dd2[i] = D ? 0.5 * (X2[6 + i] - X2[i]) : 0.0;
+  }
+  const double dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const double dh[3] = {d[0] / dn, d[1] / dn, d[2] / dn};
+  const double eps = dn * 2.0 / c.L - 1.0;
+
+  // ---- strain measures
+  const TJ<D> th_t = dot3(t, dv), th_n = dot3(n, dv), th_b = dot3(b, dv);
+  const TJ<D> w_n = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
+  const TJ<D> w_b = b[0] * d[0] + b[1] * d[1] + b[2] * d[2];
+  // frozen stresses σ = ∂Π/∂q
+  const double s_e = c.ke * eps;
+  const double s_t = c.kt * th_t.v;
+  const double s_wn = c.k3u * w_n.v + c.k3uv * th_b.v;
+  const double s_b = c.k3uv * w_n.v + c.k3v * th_b.v;
+  const double s_wb = c.k2u * w_b.v - c.k2uv * th_n.v;
+  const double s_n = -c.k2uv * w_b.v + c.k2v * th_n.v;
+
+  // ---- Gauss point positions: x = yᵤ d + (yₐ−yᵤ) m + yᵥ w + ½(u₁+u₂) + cₘ
+  TJ<D> dT[3];
+  for (int i = 0; i < 3; ++i) {
+    dT[i] = tj_const<D>(d[i]);
+    if constexpr (D) {
+      dT[i].vt = dd1[i];
+      dT[i].vtt = 0.5 * dd2[i];
+    }
+  }
+  const TJ<D> td = dot3(t, dT);
+  TJ<D> mv[3], wv[3];  // m = (t·d) t,  w = Δv × t
+  for (int i = 0; i < 3; ++i) mv[i] = td * t[i];
+  wv[0] = dv[1] * t[2] - dv[2] * t[1];
+  wv[1] = dv[2] * t[0] - dv[0] * t[2];
+  wv[2] = dv[0] * t[1] - dv[1] * t[0];
+
+  // ---- loads per Gauss point (frozen) and their sums
+  double fg[4][3];
+  double r0[9];
+  for (int k = 0; k < 9; ++k) r0[k] = rsm[k].v;
+  double xd[4][3], xdd[4][3];  // Gauss point velocity / acceleration
+  double vi21 = 0.0;
+  TJ<D> vsm[3];
+  const bool rotinertia = D && (c.iota1 != 0.0);
+  for (int g = 0; g < 4; ++g) {
+    for (int i = 0; i < 3; ++i) {
+      fg[g][i] = 0.0;
+      xd[g][i] = 0.0;
+      xdd[g][i] = 0.0;
+    }
+    fg[g][2] = c.w;
+    if (U)
+      for (int i = 0; i < 3; ++i) fg[g][i] -= U[i];
+  }
+  if constexpr (D) {
+    for (int g = 0; g < 4; ++g) {
+      const double ya = c.ya[g], yu = c.yu[g], yv = c.yv[g];
+      for (int i = 0; i < 3; ++i) {
+        // x = yu d + (ya-yu) m + yv w + c: time coefficients
+        const double c1 = 0.5 * (X1[i] + X1[6 + i]);
+        const double c2 = 0.5 * (X2[i] + X2[6 + i]);
+        xd[g][i] = yu * dd1[i] + (ya - yu) * mv[i].vt + yv * wv[i].vt + c1;
+        xdd[g][i] = yu * dd2[i] + 2.0 * ((ya - yu) * mv[i].vtt + yv * wv[i].vtt) + c2;
+      }
+      double xl1[3], xl2[3];
+      for (int k = 0; k < 3; ++k) {
+        xl1[k] = r0[3 * k] * xd[g][0] + r0[3 * k + 1] * xd[g][1] + r0[3 * k + 2] * xd[g][2];
+        xl2[k] = r0[3 * k] * xdd[g][0] + r0[3 * k + 1] * xdd[g][1] + r0[3 * k + 2] * xdd[g][2];
+      }
+      double fl[3];
+      for (int k = 0; k < 3; ++k) {
+        double fq = c.Cq[k] * xl1[k] * xl1[k];
+        if (xl1[k] < 0.0) fq = -fq;
+        fl[k] = c.Ca[k] * xl2[k] + c.Cl[k] * xl1[k] + fq;
+      }
+      for (int i = 0; i < 3; ++i)
+        fg[g][i] += c.mu * xdd[g][i] + r0[i] * fl[0] + r0[i + 3] * fl[1] + r0[i + 6] * fl[2];
+    }
+    if (rotinertia) {
+      // vᵢ₂ = spin⁻¹(ṙᵀṙ + rᵀr̈);  the ṙᵀṙ part is symmetric and drops out
+      double ndd[3], bdd[3];
+      for (int i = 0; i < 3; ++i) {
+        ndd[i] = 2.0 * n[i].vtt;
+        bdd[i] = 2.0 * b[i].vtt;
+      }
+      vi21 = 0.5 * (r0[6] * ndd[0] + r0[7] * ndd[1] + r0[8] * ndd[2] - (r0[3] * bdd[0] + r0[4] * bdd[1] + r0[5] * bdd[2]));
+      // vₛₘ = Rodrigues⁻¹(rₛₘ) (static part only is used)
+      rodrigues_inv(rsm, vsm);
+    }
+  }
+  // sums over Gauss points (frozen loads)
+  double Au[3] = {0, 0, 0}, Aa[3] = {0, 0, 0}, Av[3] = {0, 0, 0}, A0[3] = {0, 0, 0};
+  for (int g = 0; g < 4; ++g)
+    for (int i = 0; i < 3; ++i) {
+      const double f = c.dL[g] * fg[g][i];
+      Au[i] += c.yu[g] * f;
+      Aa[i] += (c.ya[g] - c.yu[g]) * f;
+      Av[i] += c.yv[g] * f;
+      A0[i] += f;
+    }
+  double me[3] = {0, 0, 0};
+  if (rotinertia)
+    for (int i = 0; i < 3; ++i) me[i] = c.S0 * c.iota1 * vi21 * r0[i];
+
+  // ---- Φ_v: scalar with frozen multipliers, Taylor in the rotation dofs
+  TJ<D> Phi = th_t * s_t + th_n * s_n + th_b * s_b + w_n * s_wn + w_b * s_wb;
+  {
+    const TJ<D> tAa = t[0] * Aa[0] + t[1] * Aa[1] + t[2] * Aa[2];
+    const TJ<D> tdv = t[0] * d[0] + t[1] * d[1] + t[2] * d[2];
+    Phi = Phi + tdv * tAa + (wv[0] * Av[0] + wv[1] * Av[1] + wv[2] * Av[2]);
+    if (rotinertia) Phi = Phi + (vsm[0] * me[0] + vsm[1] * me[1] + vsm[2] * me[2]);
+    // P = ∂Φ/∂d (value and rotation gradient)
+    TJ<D> P[3];
+    for (int i = 0; i < 3; ++i)
+      P[i] = n[i] * s_wn + b[i] * s_wb + tAa * t[i] + (s_e * 2.0 / c.L * dh[i] + Au[i]);
+    // residual
+    for (int i = 0; i < 3; ++i) {
+      R[i] = -0.5 * P[i].v + 0.5 * A0[i];
+      R[6 + i] = 0.5 * P[i].v + 0.5 * A0[i];
+      R[3 + i] = Phi.g[i];
+      R[9 + i] = Phi.g[3 + i];
+    }
+    // ---- tangent: geometric part ∇²Φ (frozen loads), scaled by p0
+    const double p0 = pt.p0;
+    for (int k = 0; k < 144; ++k) K[k] = 0.0;
+    // rot-rot
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) {
+        const int a = i < 3 ? 3 + i : 6 + i, bb = j < 3 ? 3 + j : 6 + j;
+        K[a + 12 * bb] = p0 * Phi.h[i <= j ? hidx(i, j) : hidx(j, i)];
+      }
+    // rot-trans:  ∂²/∂v_j∂u₁ = −½ ∂P/∂v_j,  ∂²/∂v_j∂u₂ = +½ ∂P/∂v_j
+    for (int j = 0; j < 6; ++j) {
+      const int a = j < 3 ? 3 + j : 6 + j;
+      for (int k = 0; k < 3; ++k) {
+        const double q = 0.5 * p0 * P[k].g[j];
+        K[a + 12 * k] -= q;
+        K[k + 12 * a] -= q;
+        K[a + 12 * (6 + k)] += q;
+        K[(6 + k) + 12 * a] += q;
+      }
+    }
+  }
+  // trans-trans: σε ∂²ε/∂d² with ∂d/∂u₁ = −½, ∂d/∂u₂ = ½
+  {
+    const double f = pt.p0 * s_e * (2.0 / c.L) / dn;
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) {
+        const double h = f * ((k == l ? 1.0 : 0.0) - dh[k] * dh[l]) * 0.25;
+        K[k + 12 * l] += h;
+        K[(6 + k) + 12 * (6 + l)] += h;
+        K[k + 12 * (6 + l)] -= h;
+        K[(6 + k) + 12 * l] -= h;
+      }
+  }
+  // ---- material part Gᵀ D G over q = (ε, θt, θn, θb, wn, wb)
+  {
+    double G[6][12];
+    for (int q = 0; q < 6; ++q)
+      for (int j = 0; j < 12; ++j) G[q][j] = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      G[0][k] = -dh[k] / c.L;
+      G[0][6 + k] = dh[k] / c.L;
+      G[4][k] = -0.5 * n[k].v;
+      G[4][6 + k] = 0.5 * n[k].v;
+      G[5][k] = -0.5 * b[k].v;
+      G[5][6 + k] = 0.5 * b[k].v;
+    }
+    for (int j = 0; j < 6; ++j) {
+      const int a = j < 3 ? 3 + j : 6 + j;
+      G[1][a] = th_t.g[j];
+      G[2][a] = th_n.g[j];
+      G[3][a] = th_b.g[j];
+      G[4][a] = w_n.g[j];
+      G[5][a] = w_b.g[j];
+    }
+    // DG rows
+    const double p0 = pt.p0;
+    for (int j = 0; j < 12; ++j) {
+      const double DG0 = c.ke * G[0][j];
+      const double DG1 = c.kt * G[1][j];
+      const double DG2 = c.k2v * G[2][j] - c.k2uv * G[5][j];
+      const double DG3 = c.k3v * G[3][j] + c.k3uv * G[4][j];
+      const double DG4 = c.k3uv * G[3][j] + c.k3u * G[4][j];
+      const double DG5 = -c.k2uv * G[2][j] + c.k2u * G[5][j];
+      for (int i = 0; i < 12; ++i)
+        K[i + 12 * j] += p0 * (G[0][i] * DG0 + G[1][i] * DG1 + G[2][i] * DG2 + G[3][i] * DG3 + G[4][i] * DG4 +
+                               G[5][i] * DG5);
+    }
+  }
+
+  // ---- load variation (dynamic loads) and U-derivative
+  const bool need_jx = D || (H != nullptr);
+  if (!need_jx) return;
+  // Jx_g: ∂x_g/∂X₀ (3x12):  rot: yu*0 + (ya-yu) m.g + yv w.g ; trans: s M_g + ½ I
+  // M_g = yu I + (ya-yu) t tᵀ
+  const double tv[3] = {t[0].v, t[1].v, t[2].v};
+  if (H) {
+    for (int k = 0; k < 36; ++k) H[k] = 0.0;
+  }
+  // accumulate per Gauss point
+  for (int g = 0; g < 4; ++g) {
+    const double ya = c.ya[g], yu = c.yu[g], yv = c.yv[g], yd = ya - yu, wq = c.dL[g];
+    double Jx[3][12];
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 6; ++j) {
+        const int a = j < 3 ? 3 + j : 6 + j;
+        Jx[i][a] = yd * mv[i].g[j] + yv * wv[i].g[j];
+      }
+      for (int k = 0; k < 3; ++k) {
+        const double M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
+        Jx[i][k] = -0.5 * M + (i == k ? 0.5 : 0.0);
+        Jx[i][6 + k] = 0.5 * M + (i == k ? 0.5 : 0.0);
+      }
+    }
+    if (H) {
+      for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 12; ++a) H[a + 12 * k] -= wq * Jx[k][a];
+    }
+    if constexpr (D) {
+      // derivatives of load with respect to x-dot, x-ddot and r₀ (local frame)
+      double xl1[3];
+      for (int k = 0; k < 3; ++k) xl1[k] = r0[3 * k] * xd[g][0] + r0[3 * k + 1] * xd[g][1] + r0[3 * k + 2] * xd[g][2];
+      double xl2[3];
+      for (int k = 0; k < 3; ++k)
+        xl2[k] = r0[3 * k] * xdd[g][0] + r0[3 * k + 1] * xdd[g][1] + r0[3 * k + 2] * xdd[g][2];
+      double fl[3], dfl1[3];
+      for (int k = 0; k < 3; ++k) {
+        double fq = c.Cq[k] * xl1[k] * xl1[k];
+        if (xl1[k] < 0.0) fq = -fq;
+        fl[k] = c.Ca[k] * xl2[k] + c.Cl[k] * xl1[k] + fq;
+        dfl1[k] = c.Cl[k] + 2.0 * c.Cq[k] * fabs(xl1[k]);
+      }
+      // Ṁ, M̈ for translation columns
+      double td1[3], td2[3];
+      for (int i = 0; i < 3; ++i) {
+        td1[i] = t[i].vt;
+        td2[i] = 2.0 * t[i].vtt;
+      }
+      // direction loop (12 Newton directions, plus δr)
+      const int ndir = rdir ? 13 : 12;
+      for (int j = 0; j < ndir; ++j) {
+        double dx1[3], dx2[3], dr0[9];
+        for (int k = 0; k < 9; ++k) dr0[k] = 0.0;
+        if (j < 12) {
+          const int e = rot_index(j);
+          if (e >= 0) {
+            for (int i = 0; i < 3; ++i) {
+              const double gx = yd * mv[i].g[e] + yv * wv[i].g[e];
+              const double gtx = yd * mv[i].gt[e] + yv * wv[i].gt[e];
+              const double gttx = yd * mv[i].gtt[e] + yv * wv[i].gtt[e];
+              dx1[i] = gtx * pt.p0 + gx * pt.p1;
+              dx2[i] = 2.0 * gttx * pt.p0 + 2.0 * gtx * pt.p1 + gx * pt.p2;
+            }
+            for (int k = 0; k < 9; ++k) dr0[k] = rsm[k].g[e] * pt.p0;
+          } else {
+            const int k = j < 3 ? j : j - 6;
+            const double s = j < 3 ? -0.5 : 0.5;
+            for (int i = 0; i < 3; ++i) {
+              const double M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
+              const double M1 = yd * (td1[i] * tv[k] + tv[i] * td1[k]);
+              const double M2 = yd * (td2[i] * tv[k] + 2.0 * td1[i] * td1[k] + tv[i] * td2[k]);
+              const double I = (i == k ? 0.5 : 0.0);
+              dx1[i] = s * (M1 * pt.p0 + M * pt.p1) + I * pt.p1;
+              dx2[i] = s * (M2 * pt.p0 + 2.0 * M1 * pt.p1 + M * pt.p2) + I * pt.p2;
+            }
+          }
+        } else {
+          // δr: X₁ += a δr, X₂ += b δr
+          for (int i = 0; i < 3; ++i) {
+            dx1[i] = 0.0;
+            dx2[i] = 0.0;
+          }
+          for (int jj = 0; jj < 12; ++jj) {
+            const int e = rot_index(jj);
+            for (int i = 0; i < 3; ++i) {
+              double gx, gtx;
+              if (e >= 0) {
+                gx = yd * mv[i].g[e] + yv * wv[i].g[e];
+                gtx = yd * mv[i].gt[e] + yv * wv[i].gt[e];
+              } else {
+                const int k = jj < 3 ? jj : jj - 6;
+                const double s = jj < 3 ? -0.5 : 0.5;
+                const double M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
+                const double M1 = yd * (td1[i] * tv[k] + tv[i] * td1[k]);
+                gx = s * M + (i == k ? 0.5 : 0.0);
+                gtx = s * M1;
+              }
+              dx1[i] += gx * av[jj];
+              dx2[i] += 2.0 * gtx * av[jj] + gx * bv[jj];
+            }
+          }
+        }
+        // δ(local components):  δ(r₀ᵀy) = δr₀ᵀ y + r₀ᵀ δy
+        double dl1[3], dl2[3];
+        for (int k = 0; k < 3; ++k) {
+          dl1[k] = dr0[3 * k] * xd[g][0] + dr0[3 * k + 1] * xd[g][1] + dr0[3 * k + 2] * xd[g][2] +
+                   r0[3 * k] * dx1[0] + r0[3 * k + 1] * dx1[1] + r0[3 * k + 2] * dx1[2];
+          dl2[k] = dr0[3 * k] * xdd[g][0] + dr0[3 * k + 1] * xdd[g][1] + dr0[3 * k + 2] * xdd[g][2] +
+                   r0[3 * k] * dx2[0] + r0[3 * k + 1] * dx2[1] + r0[3 * k + 2] * dx2[2];
+        }
+        double dfl[3];
+        for (int k = 0; k < 3; ++k) dfl[k] = c.Ca[k] * dl2[k] + dfl1[k] * dl1[k];
+        double df[3];
+        for (int i = 0; i < 3; ++i)
+          df[i] = c.mu * dx2[i] + dr0[i] * fl[0] + dr0[i + 3] * fl[1] + dr0[i + 6] * fl[2] + r0[i] * dfl[0] +
+                  r0[i + 3] * dfl[1] + r0[i + 6] * dfl[2];
+        double* col = (j < 12) ? (K + 12 * j) : rdir;
+        if (j == 12 && g == 0)
+          for (int a = 0; a < 12; ++a) rdir[a] = 0.0;
+        for (int a = 0; a < 12; ++a) col[a] += wq * (Jx[0][a] * df[0] + Jx[1][a] * df[1] + Jx[2][a] * df[2]);
+      }
+    }
+  }
+  if constexpr (D) {
+    if (rdir == nullptr && false) return;
+    if (rotinertia) {
+      // rotational inertia: S0 vₛₘ∂X₀ᵀ δmₑ,  mₑ = ι₁ vᵢ₂[1] t
+      const int ndir = rdir ? 13 : 12;
+      for (int j = 0; j < ndir; ++j) {
+        double dvi = 0.0, dt[3] = {0, 0, 0};
+        if (j < 12) {
+          const int e = rot_index(j);
+          if (e < 0) continue;
+          for (int i = 0; i < 3; ++i) {
+            const double dn_ = n[i].g[e] * pt.p0, db_ = b[i].g[e] * pt.p0;
+            const double dndd = 2.0 * n[i].gtt[e] * pt.p0 + 2.0 * n[i].gt[e] * pt.p1 + n[i].g[e] * pt.p2;
+            const double dbdd = 2.0 * b[i].gtt[e] * pt.p0 + 2.0 * b[i].gt[e] * pt.p1 + b[i].g[e] * pt.p2;
+            dvi += 0.5 * (db_ * 2.0 * n[i].vtt + r0[6 + i] * dndd - dn_ * 2.0 * b[i].vtt - r0[3 + i] * dbdd);
+            dt[i] = t[i].g[e] * pt.p0;
+          }
+        } else {
+          for (int jj = 0; jj < 12; ++jj) {
+            const int e = rot_index(jj);
+            if (e < 0) continue;
+            for (int i = 0; i < 3; ++i) {
+              const double dndd = 2.0 * n[i].gt[e] * av[jj] + n[i].g[e] * bv[jj];
+              const double dbdd = 2.0 * b[i].gt[e] * av[jj] + b[i].g[e] * bv[jj];
+              dvi += 0.5 * (r0[6 + i] * dndd - r0[3 + i] * dbdd);
+            }
+          }
+        }
+        double dme[3];
+        for (int i = 0; i < 3; ++i) dme[i] = c.S0 * c.iota1 * (dvi * r0[i] + vi21 * dt[i]);
+        double* col = (j < 12) ? (K + 12 * j) : rdir;
+        for (int a2 = 0; a2 < 6; ++a2) {
+          const int a = a2 < 3 ? 3 + a2 : 6 + a2;
+          col[a] += vsm[0].g[a2] * dme[0] + vsm[1].g[a2] * dme[1] + vsm[2].g[a2] * dme[2];
+        }
+      }
+    }
+  }
+}
+
+}  // namespace mgpu

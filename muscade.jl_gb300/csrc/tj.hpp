@@ -1,0 +1,219 @@
+// Truncated multivariate Taylor arithmetic over the 6 nodal rotation dofs of a
+// beam element, with an optional second-order time jet.
+//
+// A value y carries the coefficients of the monomials
+//     1, ε_j, ε_i ε_j                       (static part, "T2": 1+6+21)
+//     τ, τ², τ ε_j, τ² ε_j                  (time jet, only when DYN)
+// where ε are perturbations of the rotation dofs X₀[3:5], X₀[9:11] and τ is
+// time:  y(τ, ε) = v + g·ε + ½ εᵀHε + vt τ + vtt τ² + (gt·ε) τ + (gtt·ε) τ²
+// truncated to that monomial set.  The set is closed under products (its
+// complement is a monomial ideal), so products and compositions computed here
+// are exact for every retained coefficient.  `h` stores the Hessian H packed
+// (i ≤ j), so that the coefficient of ε_iε_j (i<j) is h_ij and of ε_i² is ½h_ii.
+//
+// This carries exactly the derivative information the reference's nested
+// duals carry on this path (Newton variation × time derivatives × the
+// revariated Jacobian, src/Taylor.jl and src/Adiff.jl), restricted to the six
+// variables the rotation maps depend on.
+#pragma once
+#include <math.h>
+#include <type_traits>
+
+#ifdef __CUDACC__
+#define MG_HD __host__ __device__ __forceinline__
+#else
+#define MG_HD inline
+#endif
+
+namespace mgpu {
+
+constexpr int NV = 6;
+constexpr int NH = 21;
+
+// packed index of (i,j), i<=j
+MG_HD constexpr int hidx(int i, int j) { return i * NV - (i * (i - 1)) / 2 + (j - i); }
+
+struct NoJet {};
+struct TimeJet {
+  double vt, vtt;
+  double gt[NV], gtt[NV];
+};
+
+template <bool DYN>
+struct TJ : public std::conditional<DYN, TimeJet, NoJet>::type {
+  double v;
+  double g[NV];
+  double h[NH];
+};
+
+template <bool DYN>
+MG_HD TJ<DYN> tj_const(double c) {
+  TJ<DYN> r;
+  r.v = c;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) r.g[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < NH; ++i) r.h[i] = 0.0;
+  if constexpr (DYN) {
+    r.vt = 0.0;
+    r.vtt = 0.0;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      r.gt[i] = 0.0;
+      r.gtt[i] = 0.0;
+    }
+  }
+  return r;
+}
+
+// independent variable ε_j with value x₀, rate x₁ and acceleration x₂
+template <bool DYN>
+MG_HD TJ<DYN> tj_var(double x0, int j, double x1 = 0.0, double x2 = 0.0) {
+  TJ<DYN> r = tj_const<DYN>(x0);
+  r.g[j] = 1.0;
+  if constexpr (DYN) {
+    r.vt = x1;
+    r.vtt = 0.5 * x2;
+  }
+  return r;
+}
+
+template <bool DYN>
+MG_HD TJ<DYN> operator+(const TJ<DYN>& a, const TJ<DYN>& b) {
+  TJ<DYN> r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) r.g[i] = a.g[i] + b.g[i];
+#pragma unroll
+  for (int i = 0; i < NH; ++i) r.h[i] = a.h[i] + b.h[i];
+  if constexpr (DYN) {
+    r.vt = a.vt + b.vt;
+    r.vtt = a.vtt + b.vtt;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      r.gt[i] = a.gt[i] + b.gt[i];
+      r.gtt[i] = a.gtt[i] + b.gtt[i];
+    }
+  }
+  return r;
+}
+template <bool DYN>
+MG_HD TJ<DYN> operator-(const TJ<DYN>& a, const TJ<DYN>& b) {
+  TJ<DYN> r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) r.g[i] = a.g[i] - b.g[i];
+#pragma unroll
+  for (int i = 0; i < NH; ++i) r.h[i] = a.h[i] - b.h[i];
+  if constexpr (DYN) {
+    r.vt = a.vt - b.vt;
+    r.vtt = a.vtt - b.vtt;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      r.gt[i] = a.gt[i] - b.gt[i];
+      r.gtt[i] = a.gtt[i] - b.gtt[i];
+    }
+  }
+  return r;
+}
+template <bool DYN>
+MG_HD TJ<DYN> tj_scale(const TJ<DYN>& a, double s) {
+  TJ<DYN> r;
+  r.v = a.v * s;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) r.g[i] = a.g[i] * s;
+#pragma unroll
+  for (int i = 0; i < NH; ++i) r.h[i] = a.h[i] * s;
+  if constexpr (DYN) {
+    r.vt = a.vt * s;
+    r.vtt = a.vtt * s;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      r.gt[i] = a.gt[i] * s;
+      r.gtt[i] = a.gtt[i] * s;
+    }
+  }
+  return r;
+}
+template <bool DYN>
+MG_HD TJ<DYN> operator-(const TJ<DYN>& a) {
+  return tj_scale(a, -1.0);
+}
+template <bool DYN>
+MG_HD TJ<DYN> operator*(const TJ<DYN>& a, double s) { return tj_scale(a, s); }
+template <bool DYN>
+MG_HD TJ<DYN> operator*(double s, const TJ<DYN>& a) { return tj_scale(a, s); }
+template <bool DYN>
+MG_HD TJ<DYN> operator+(const TJ<DYN>& a, double s) {
+  TJ<DYN> r = a;
+  r.v += s;
+  return r;
+}
+
+// product, truncated to the retained monomials
+template <bool DYN>
+MG_HD TJ<DYN> operator*(const TJ<DYN>& a, const TJ<DYN>& b) {
+  TJ<DYN> r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) r.g[i] = fma(a.g[i], b.v, a.v * b.g[i]);
+#pragma unroll
+  for (int i = 0; i < NV; ++i)
+#pragma unroll
+    for (int j = i; j < NV; ++j) {
+      const int k = hidx(i, j);
+      double s = fma(a.h[k], b.v, a.v * b.h[k]);
+      s = fma(a.g[i], b.g[j], s);
+      r.h[k] = fma(a.g[j], b.g[i], s);
+    }
+  if constexpr (DYN) {
+    r.vt = fma(a.vt, b.v, a.v * b.vt);
+    r.vtt = fma(a.vtt, b.v, fma(a.vt, b.vt, a.v * b.vtt));
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      r.gt[i] = fma(a.gt[i], b.v, fma(a.vt, b.g[i], fma(a.g[i], b.vt, a.v * b.gt[i])));
+      double s = fma(a.gtt[i], b.v, a.vtt * b.g[i]);
+      s = fma(a.gt[i], b.vt, s);
+      s = fma(a.vt, b.gt[i], s);
+      s = fma(a.g[i], b.vtt, s);
+      r.gtt[i] = fma(a.v, b.gtt[i], s);
+    }
+  }
+  return r;
+}
+
+// composition f(a) from f and its first three derivatives at a.v
+template <bool DYN>
+MG_HD TJ<DYN> tj_apply(const TJ<DYN>& a, double f0, double f1, double f2, double f3) {
+  TJ<DYN> r;
+  r.v = f0;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) r.g[i] = f1 * a.g[i];
+#pragma unroll
+  for (int i = 0; i < NV; ++i)
+#pragma unroll
+    for (int j = i; j < NV; ++j) {
+      const int k = hidx(i, j);
+      r.h[k] = fma(f1, a.h[k], f2 * a.g[i] * a.g[j]);
+    }
+  if constexpr (DYN) {
+    r.vt = f1 * a.vt;
+    r.vtt = fma(f1, a.vtt, 0.5 * f2 * a.vt * a.vt);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      r.gt[i] = fma(f1, a.gt[i], f2 * a.g[i] * a.vt);
+      double s = f2 * a.g[i] * a.vtt;
+      s = fma(f1, a.gtt[i], s);
+      s = fma(0.5 * f3 * a.g[i], a.vt * a.vt, s);
+      r.gtt[i] = fma(f2 * a.vt, a.gt[i], s);
+    }
+  }
+  return r;
+}
+
+template <bool DYN>
+MG_HD bool tj_is_zero_value(const TJ<DYN>& a) {
+  return a.v == 0.0;
+}
+
+}  // namespace mgpu
