@@ -1,0 +1,304 @@
+#!/usr/bin/env python
+"""Benchmark: beam-element assemblies per second on the 60×60×20 lattice frame.
+
+One step is one complete assembly of the Newton system of the static lattice
+frame (210,000 EulerBeam3D, 21,600 Hold, 205,200 DofLoad; 453,600 dofs,
+17,776,800 nonzeros): every element's residual and exact tangent on the
+device, then the deterministic scatter into Lλ and Lλx.nzval.
+
+  value  beams × assemblies / s with the state resident in HBM; each timed
+         assembly is preceded by a 512 MB write that flushes the L2
+  e2e    the same through the C-ABI call a host caller makes (mgpu_assemble):
+         host state in, host Lλ and nzval out, copies inside the timed region
+  --impl reference   the CPU arm: the oracle (a C++ dual-number restatement
+         of the reference's assembly) on the host cores, on a bounded sample
+
+Launched as `python bench.py --gpus N ...` or under torch.distributed.run for
+N>1; the lattice is a single model, so N>1 runs N independent replicas and the
+value sums them (scaling "weak").  Prints one JSON line on rank 0.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "muscade.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "beam-element assemblies/s"
+UNIT = "beam assemblies/s"
+WORKLOAD = "lattice frame 60x60x20, SweepX{0} assembly (210000 EulerBeam3D, 21600 Hold, 205200 DofLoad)"
+FLOPS_FILE = os.path.join(ROOT, "profiles", "beam_kernel_flops.json")
+NCU_FILE = os.path.join(ROOT, "profiles", "beam_kernel_lattice_traffic.json")
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 0, 1, None
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo")  # host-side coordination only: barrier and max-time reduction
+    return dist.get_rank(), int(os.environ.get("LOCAL_RANK", "0")), ws, dist
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except OSError:
+            rows = []
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def fp64_peak_tflops(device):
+    """Measured FP64 throughput of this GPU: cuBLAS DGEMM 8192³, best of 5 (CUDA events)."""
+    import torch
+
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
+    b = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
+    torch.matmul(a, b)
+    torch.cuda.synchronize(device)
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n**3 / (best * 1e-3) / 1e12
+
+
+def state_for(model, seed=2027):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return [rng.normal(size=model.ndof["X"]) * 1e-3]
+
+
+def cpu_baseline(model, X, t, sample_beams, threads):
+    """The oracle's assembly of a bounded sample of beams on the host cores."""
+    from oracle import lib as O
+
+    g = model.groups[0]
+    dis = model.initialize_cached
+    idx = dis.dis[0].index_X[:sample_beams] - 1
+    ele = g.cat("ele")[:sample_beams]
+    Xe = X[0][idx][:, None, :]
+    O.build()
+    O.beam_eval(ele[:64], Xe[:64], mode=1, nthreads=threads)  # warm
+    t0 = time.perf_counter()
+    R, J = O.beam_eval(ele, Xe, mode=1, nthreads=threads)
+    # scatter of the sample into Lλ and the matrix entries (the oracle's add_value!/add_∂! order)
+    Ll = np.zeros(model.ndof["X"])
+    np.add.at(Ll, idx.reshape(-1), R.reshape(-1))
+    dt = time.perf_counter() - t0
+    return sample_beams / dt, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", default="60,60,20")
+    ap.add_argument("--cpu-sample", type=int, default=int(os.environ.get("MGPU_CPU_SAMPLE", "60000")))
+    args = ap.parse_args()
+    rank, local_rank, ws, dist = dist_setup()
+    nx, ny, nz = (int(v) for v in args.grid.split(","))
+
+    from muscade_gpu import workloads
+
+    model, times = workloads.lattice(nx, ny, nz)
+    st = model.initialize()
+    model.initialize_cached = st.dis
+    nbeam = model.groups[0].nele
+    t = float(times[0])
+    X = state_for(model)
+    threads = os.cpu_count() or 1
+    config = {"workload": WORKLOAD if (nx, ny, nz) == (60, 60, 20) else f"lattice frame {nx}x{ny}x{nz}",
+              "beams": nbeam, "dofs": model.ndof["X"], "l2": "flushed between timed assemblies (512 MB write)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sample = min(args.cpu_sample, nbeam)
+        per = []
+        for i in range(args.warmup + args.steps):
+            rate, dt = cpu_baseline(model, X, t, sample, threads)
+            if i >= args.warmup:
+                per.append(dt)
+        tstep = sum(per) / len(per)
+        value = sample / tstep
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": tstep * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"{sample} of {nbeam} beams per step (element R and K by nested duals "
+                                           f"+ residual scatter), {threads} threads"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    from muscade_gpu import _lib
+    from muscade_gpu.device import DeviceModel
+
+    _lib.build()
+    device = local_rank
+    import torch
+
+    torch.cuda.set_device(device)
+    fp64_peak = fp64_peak_tflops(device) if rank == 0 else None
+    dm = DeviceModel(model, st.dis, device=device)
+    dm.upload_state(X, t=t)
+    # warm-up
+    dm.time_assemble(reps=max(args.warmup, 1), t=t, flush_l2=True)
+    if dist:
+        dist.barrier()
+    with Clocks(device) as ck:
+        tt, tg, ts = dm.time_assemble(reps=args.steps, t=t, flush_l2=True)
+    if dist:
+        dist.barrier()
+    clocks = ck.summary()
+    tmax = reduce_max(dist, tt)
+    value = ws * nbeam / (tmax * 1e-3)
+    # e2e through the C-ABI with host buffers
+    for _ in range(max(args.warmup, 1)):
+        dm.assemble(X, t=t)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Ll, nzv = dm.assemble(X, t=t)
+    e2e_dt = (time.perf_counter() - t0) / args.steps
+    e2e_dt = reduce_max(dist, e2e_dt)
+    h2d = 8 * (model.ndof["X"] + dm.ntval + model.ndof["U"])
+    d2h = 8 * (model.ndof["X"] + dm.nnz)
+    if rank != 0:
+        dm.close()
+        return
+    ngroup = len(model.groups)
+    launches_per_step = ngroup + 2 + 1  # element kernels, two scatters, L2 flush
+    # roofline of the beam element kernel (FP64-pipe bound)
+    tbeam = float(tg[0])
+    flops = None
+    try:
+        flops = json.load(open(FLOPS_FILE))["fp64_flops_per_beam_static"]
+    except (OSError, KeyError, ValueError):
+        pass
+    traffic = None
+    try:
+        tr = json.load(open(NCU_FILE))
+        traffic = tr["dram_bytes_per_beam"] * nbeam
+    except (OSError, KeyError, ValueError):
+        pass
+    roof = {"bound": "fp64", "unit": "TFLOP/s", "kernel": "beam_kernel<false>", "ms_per_launch": tbeam,
+            "peak_source": "measured on this GPU: cuBLAS DGEMM 8192^3 (FP64)", "peak": fp64_peak,
+            "traffic": traffic, "traffic_unit": "bytes per launch"}
+    if flops:
+        ach = flops * nbeam / (tbeam * 1e-3) / 1e12
+        roof.update({"achieved": ach, "frac": ach / fp64_peak if fp64_peak else None,
+                     "algorithmic_flops_per_beam": flops})
+    else:
+        roof.update({"achieved": None, "frac": None})
+    # scatter kernels against HBM
+    hbm_peak = None
+    try:
+        hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        hbm_peak = 6800.0
+    ent = sum(g.nele * (len(g.etype.doflist(g.key)[0]) ** 2) for g in model.groups)
+    vent = sum(g.nele * len(g.etype.doflist(g.key)[0]) for g in model.groups)
+    sb = ent * (8 + 4) + dm.nnz * (8 + 4) + vent * (8 + 4) + model.ndof["X"] * (8 + 4)
+    roof_scatter = {"bound": "hbm", "unit": "GB/s", "achieved": sb / (ts * 1e-3) / 1e9, "peak": hbm_peak,
+                    "frac": sb / (ts * 1e-3) / 1e9 / hbm_peak, "bytes_per_launch": sb, "ms": ts}
+    cpu_rate, cpu_dt = cpu_baseline(model, X, t, min(args.cpu_sample, nbeam), threads)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tmax, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded lattice frame, lognormal sections, Gaussian loads)", "config": config,
+        "e2e": {"value": ws * nbeam / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_dt * 1e3},
+        "roofline": roof, "roofline_scatter": roof_scatter,
+        "kernel_ms": {"beam": tbeam, "other_elements": float(np.sum(tg[1:])), "scatter": ts},
+        "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{min(args.cpu_sample, nbeam)} beams (oracle nested-dual R and K + residual scatter)"},
+        "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    dm.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * muscade_gpu.h -- C ABI of the GB300 assemble-and-solve path for Muscade.jl
+ * models built from EulerBeam3D, Bar3D, Hold / DofConstraint{:X} (affine gap,
+ * equal mode) and DofLoad elements.
+ *
+ * The Julia side keeps Model / addelement! / initialize! and the element API;
+ * it hands the device what its Disassembler already holds (per element type,
+ * the model dof indices of each element and the element objects' fields) and
+ * calls these entry points from a new solver type.
+ *
+ * Conventions
+ *   - Dof indices are 1-based Int64, exactly `dis.dis[ieletyp].index[iele].X`
+ *     (src/Assemble.jl:22-99), laid out [nele][nX] row-major.
+ *   - Vectors and matrices are Float64; sparse matrices are CSC with 1-based
+ *     colptr/rowval like SparseMatrixCSC.
+ *   - Host buffers are owned by the caller; the context owns device memory
+ *     and its CUDA stream.  A context is not re-entrant: one per host thread.
+ *   - Every call returns MGPU_OK (0) or an error code; mgpu_last_error()
+ *     gives the message.  No call falls back to the CPU.
+ */
+#ifndef MUSCADE_GPU_H
+#define MUSCADE_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; messages follow the reference's muscadeerror texts */
+#define MGPU_OK 0
+#define MGPU_ERR_ARG 1          /* invalid argument or layout */
+#define MGPU_ERR_CUDA 2         /* CUDA runtime / library failure */
+#define MGPU_ERR_UNSUPPORTED 3  /* element kind the GPU path does not support */
+#define MGPU_ERR_NAN 4          /* "residual(...) returned NaN in R, FB or derivatives" (src/Assemble.jl:625) */
+#define MGPU_ERR_SINGULAR 5     /* "matrix factorization failed at step=..., iiter=..." (src/SweepX.jl:209) */
+#define MGPU_ERR_NOCONV 6       /* "no convergence of step ... after ... iterations" (src/SweepX.jl:221) */
+#define MGPU_ERR_NOMEM 7        /* device allocation failed */
+#define MGPU_ERR_SIZE 8         /* problem larger than a fixed-capacity entry point allows */
+
+/* element kinds */
+#define MGPU_EULERBEAM3D 1     /* toolbox/BeamElement.jl:87-208; nX=12 (+nU=3 when udof); edata: 69 fields */
+#define MGPU_BAR3D 2           /* toolbox/BarElement.jl:89-202; nX=6 (+nU=3); edata: 38 fields */
+#define MGPU_DOFCONSTRAINT_X 3 /* src/BasicElements.jl:406-438,484-488; nX=nx+1; edata: nx gap coefficients */
+#define MGPU_DOFLOAD 4         /* src/BasicElements.jl:275-284; nX=1; no edata */
+
+/* One element type (one entry of model.eleobj / dis.dis). */
+typedef struct {
+  int32_t kind;          /* MGPU_EULERBEAM3D ... */
+  int32_t nX;            /* X-dofs per element */
+  int32_t nU;            /* U-dofs per element (0 or 3 for beams/bars) */
+  int32_t ndata;         /* doubles per element in edata */
+  int64_t nele;          /* number of elements */
+  const int64_t *indexX; /* [nele][nX] 1-based model X-dof indices */
+  const int64_t *indexU; /* [nele][nU] 1-based model U-dof indices (NULL if nU==0) */
+  const double *edata;   /* [nele][ndata] element fields in the reference's declaration order */
+} mgpu_group;
+
+typedef struct {
+  int64_t nX;               /* getndof(model,:X) */
+  int64_t nU;               /* getndof(model,:U) */
+  int32_t ngroup;           /* number of element types, in model order */
+  const mgpu_group *groups; /* [ngroup] */
+  const double *scaleX;     /* [nX] dof scales (dis.scaleX), NULL for all ones */
+  int32_t device;           /* CUDA device ordinal */
+} mgpu_model_desc;
+
+/* Newmark-β coefficients (src/SweepX.jl:3-15) */
+typedef struct {
+  double a1, a2, a3, b1, b2, b3;
+} mgpu_newmark;
+
+/* missions of one assembly (src/SweepX.jl:39-96) */
+#define MGPU_ASM_STATIC 0  /* SweepX{0}: Lλ = R, Lλx = K                      */
+#define MGPU_ASM_STEP 1    /* SweepX{2} first iteration: Lλ = R - C a - M b, Lλx = K + a1 C + b1 M */
+#define MGPU_ASM_ITER 2    /* SweepX{2} later iterations: Lλ = R, Lλx = K + a1 C + b1 M */
+
+typedef struct mgpu_ctx mgpu_ctx;
+
+/* Build the device model: CSC pattern and element-entry maps (replaces
+ * prepare(AssemblySweepX), src/SweepX.jl:24-33 with asmvec!/asmmat!,
+ * src/Assemble.jl:340-448), upload element data and dof maps. */
+int mgpu_create(mgpu_ctx **ctx, const mgpu_model_desc *desc);
+void mgpu_destroy(mgpu_ctx *ctx);
+const char *mgpu_last_error(const mgpu_ctx *ctx);
+
+/* Sparsity of Lλx: nnz, then colptr[nX+1] and rowval[nnz] (1-based), and the
+ * asm maps of element type `igroup`: asm1[nele][nX] (position in Lλ) and
+ * asm2[nele][nX*nX] (position in nzval, entry i+nX*j), as asm[1|2,ieletyp]
+ * (src/Assemble.jl:340-448). */
+int64_t mgpu_nnz(const mgpu_ctx *ctx);
+int mgpu_get_pattern(const mgpu_ctx *ctx, int64_t *colptr, int64_t *rowval);
+int mgpu_get_asm(const mgpu_ctx *ctx, int32_t igroup, int64_t *asm1, int64_t *asm2);
+
+/* Number of time-dependent element values per assembly: one per DofLoad
+ * element (F(t)) and one per DofConstraint element (gap offset c(t) in
+ * g = Σ aᵢxᵢ − c(t)), concatenated over groups in model order. */
+int64_t mgpu_ntval(const mgpu_ctx *ctx);
+
+/* One assembly with host buffers (replaces assemble!{:step|:iter} over the
+ * AssemblySweepX elements, src/Assemble.jl:470-505 with addin!, src/SweepX.jl:39-96).
+ *   x[nXder][nX] (X, X', X''), u[nU], tvals[ntval] at time t.
+ *   Outputs (host, may be NULL): Ll[nX] (Lλ) and nzval[nnz] (Lλx.nzval). */
+int mgpu_assemble(mgpu_ctx *ctx, int32_t mission, int32_t nXder, const double *x, const double *u, double t,
+                  const double *tvals, const mgpu_newmark *c, double *Ll, double *nzval);
+
+/* Element-level evaluation like diffed_residual (src/Diagnostic.jl:929-965)
+ * for the elements of group `igroup`:  X[nele][nXder][nX], U[nele][nU].
+ * Returns R[nele][nX] and, per element, dR[nele][nX][nX] (column-major per
+ * element: ∂R_i/∂ with respect to p0·X₀ + p1·X₁ + p2·X₂ in direction j at
+ * i + nX*j) and, when U is given and dRdU != NULL, dRdU[nele][nX][nU]. */
+int mgpu_element_eval(mgpu_ctx *ctx, int32_t igroup, int32_t nXder, const double *X, const double *U, double t,
+                      double p0, double p1, double p2, double *R, double *dR, double *dRdU);
+
+/* Device-resident assembly for throughput measurement: upload a state once,
+ * then assemble repeatedly into device buffers.  mgpu_time_assemble runs
+ * `reps` assemblies timed with CUDA events on the context stream (optionally
+ * writing a 512 MB buffer before each, to flush the L2) and reports the mean
+ * device time of the whole assembly, of each element type's kernel
+ * (ms_groups[ngroup], may be NULL) and of the two scatter kernels. */
+int mgpu_upload_state(mgpu_ctx *ctx, int32_t nXder, const double *x, const double *u, const double *tvals);
+int mgpu_assemble_resident(mgpu_ctx *ctx, int32_t mission, double t, const mgpu_newmark *c);
+int mgpu_download(mgpu_ctx *ctx, double *Ll, double *nzval);
+int mgpu_time_assemble(mgpu_ctx *ctx, int32_t mission, double t, const mgpu_newmark *c, int32_t reps,
+                       int32_t flush_l2, double *ms_total, double *ms_groups, double *ms_scatter);
+
+/* Solver options (keywords of solve(SweepX{OX}), src/SweepX.jl:179-184) */
+typedef struct {
+  double beta, gamma; /* Newmark-β parameters (OX=2) */
+  int32_t maxiter;    /* maximum Newton iterations per step */
+  double maxdx;       /* convergence: Σ Δx² ≤ maxdx² */
+  double maxLl;       /* and Σ Lλ² ≤ maxLl² (use +Inf to disable) */
+} mgpu_sweep_opts;
+
+typedef struct {
+  int32_t nstep_done;  /* steps that converged (states written) */
+  int32_t niter_total; /* Newton iterations over all steps */
+  int32_t fail_step;   /* 1-based step of a failure, else 0 */
+  int32_t fail_iter;   /* 1-based iteration of a failure, else 0 */
+  double last_dx;      /* √ΣΔx² of the last iteration */
+  double last_Ll;      /* √ΣLλ² of the last iteration */
+} mgpu_stats;
+
+/* Whole SweepX{OX} solve on the device (src/SweepX.jl:179-226), OX ∈ {0,2}.
+ *   times[nstep], t0 = initial state time, x0[nXder0][nX] initial X and
+ *   derivatives (nXder0 ≤ OX+1; missing derivatives are zero), u[nU],
+ *   tvals[nstep][ntval].  states[nstep][OX+1][nX] receives the converged X
+ *   (and X', X'') of every step; on error the steps before the failing one
+ *   are written and stats->nstep_done tells how many. */
+int mgpu_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, double t0, int32_t nXder0,
+                const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts, double *states,
+                mgpu_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MUSCADE_GPU_H */

@@ -23,13 +23,15 @@ inline void beam_const_from_fields(const double* f, BeamConst& c) {
   for (int k = 0; k < 9; ++k) c.rm[k] = rm[k];
   for (int k = 0; k < 3; ++k) c.tgm[k] = tgm[k];
   c.L = L;
-  double S0 = 0, Sa2 = 0, Su2 = 0, Sv2 = 0, Suv = 0;
+  // Gauss sums, added in symmetric pairs (points 1,4 and 2,3) so that odd
+  // integrands such as κᵤκᵥ cancel exactly
+  auto gsum = [&](auto f) { return (f(0) + f(3)) + (f(1) + f(2)); };
+  const double S0 = gsum([&](int g) { return dL[g]; });
+  const double Sa2 = gsum([&](int g) { return dL[g] * ka[g] * ka[g]; });
+  const double Su2 = gsum([&](int g) { return dL[g] * ku[g] * ku[g]; });
+  const double Sv2 = gsum([&](int g) { return dL[g] * kv[g] * kv[g]; });
+  const double Suv = gsum([&](int g) { return dL[g] * ku[g] * kv[g]; });
   for (int g = 0; g < 4; ++g) {
-    S0 += dL[g];
-    Sa2 += dL[g] * ka[g] * ka[g];
-    Su2 += dL[g] * ku[g] * ku[g];
-    Sv2 += dL[g] * kv[g] * kv[g];
-    Suv += dL[g] * ku[g] * kv[g];
     c.dL[g] = dL[g];
     c.ya[g] = ya[g];
     c.yu[g] = yu[g];

@@ -1,0 +1,690 @@
+// GB300 assembly path: device model, element kernels, deterministic scatter,
+// and the C-ABI entry points of include/muscade_gpu.h.
+//
+// Per Newton iteration the reference loops over element types and elements,
+// evaluates each element with dual numbers and adds values and partials into
+// Lλ / Lλx.nzval through the asm maps (src/Assemble.jl:470-608,
+// src/SweepX.jl:39-96).  Here:
+//   1. one kernel per element type computes every element's residual and
+//      Newton tangent (one thread per element, closed-form FP64 tangents) and
+//      writes them to element-entry buffers laid out entry-major, so that the
+//      stores of a warp are coalesced;
+//   2. a gather kernel sums, for every nnz of Lλx and every dof of Lλ, the
+//      element entries that map to it, in the order the reference adds them
+//      (no floating-point atomics: results are deterministic run to run).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bar_math.hpp"
+#include "beam_const.hpp"
+#include "ctx.hpp"
+
+using namespace mgpu;
+
+namespace mgpu {
+
+constexpr int BEAM_NCONST = sizeof(BeamConst) / sizeof(double);
+constexpr int BAR_NCONST = sizeof(BarConst) / sizeof(double);
+static_assert(sizeof(BeamConst) == 50 * sizeof(double), "BeamConst is a flat array of doubles");
+static_assert(sizeof(BarConst) == 22 * sizeof(double), "BarConst is a flat array of doubles");
+
+int set_err(mgpu_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+// ------------------------------------------------------------------ kernels
+struct AsmArgs {
+  const double* x0;
+  const double* x1;
+  const double* x2;
+  const double* u;
+  const double* tv;
+  const double* av;  // Newmark a (per dof), step mission only
+  const double* bv;
+  const double* scale;  // per dof or nullptr
+  double t;
+  double p0, p1, p2;
+  int mission;
+  int* errflag;
+};
+
+template <class T>
+__device__ __forceinline__ void load_soa(T& dst, const double* __restrict__ src, int64_t nele, int64_t e) {
+  double* d = reinterpret_cast<double*>(&dst);
+#pragma unroll
+  for (int f = 0; f < int(sizeof(T) / sizeof(double)); ++f) d[f] = __ldg(src + f * nele + e);
+}
+
+__device__ __forceinline__ void flag_nan(int* errflag, int64_t gid, bool bad) {
+  if (bad) atomicMin(errflag, int(gid < INT_MAX ? gid : INT_MAX - 1));
+}
+
+// EulerBeam3D: one thread per element.  DYN selects the Newmark form.
+template <bool DYN>
+__global__ void __launch_bounds__(128) beam_kernel(int64_t nele, const int32_t* __restrict__ idx,
+                                                   const int32_t* __restrict__ uidx, const double* __restrict__ cdata,
+                                                   AsmArgs a, double* __restrict__ rout, double* __restrict__ kout,
+                                                   int64_t gid0) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  BeamConst bc;
+  load_soa(bc, cdata, nele, e);
+  int dof[12];
+  double X0[12], X1[12], X2[12], av[12], bv[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    dof[i] = __ldg(idx + i * nele + e);
+    X0[i] = __ldg(a.x0 + dof[i]);
+    if constexpr (DYN) {
+      X1[i] = __ldg(a.x1 + dof[i]);
+      X2[i] = __ldg(a.x2 + dof[i]);
+      if (a.mission == MGPU_ASM_STEP) {
+        av[i] = __ldg(a.av + dof[i]);
+        bv[i] = __ldg(a.bv + dof[i]);
+      }
+    }
+  }
+  double U[3];
+  const bool has_u = uidx != nullptr;
+  if (has_u)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) U[k] = __ldg(a.u + __ldg(uidx + k * nele + e));
+  double R[12], K[144], rd[12];
+  const bool step = DYN && a.mission == MGPU_ASM_STEP;
+  beam_element<DYN>(bc, X0, X1, X2, has_u ? U : nullptr, Perturb{a.p0, a.p1, a.p2}, av, bv, R, K, step ? rd : nullptr,
+                    nullptr);
+  double s[12];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) s[i] = a.scale ? __ldg(a.scale + dof[i]) : 1.0;
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const double r = (step ? R[i] - rd[i] : R[i]) * s[i];
+    bad |= isnan(r);
+    rout[i * nele + e] = r;
+  }
+#pragma unroll
+  for (int j = 0; j < 12; ++j)
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      const double k = K[i + 12 * j] * s[i] * s[j];
+      bad |= isnan(k);
+      kout[(i + 12 * j) * nele + e] = k;
+    }
+  flag_nan(a.errflag, gid0 + e, bad);
+}
+
+__global__ void bar_kernel(int64_t nele, int nder, const int32_t* __restrict__ idx, const int32_t* __restrict__ uidx,
+                           const double* __restrict__ cdata, AsmArgs a, double* __restrict__ rout,
+                           double* __restrict__ kout, int64_t gid0) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  BarConst bc;
+  load_soa(bc, cdata, nele, e);
+  int dof[6];
+  double X0[6], X1[6], X2[6], av[6], bv[6];
+  const bool step = a.mission == MGPU_ASM_STEP;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    dof[i] = __ldg(idx + i * nele + e);
+    X0[i] = __ldg(a.x0 + dof[i]);
+    X1[i] = nder > 1 ? __ldg(a.x1 + dof[i]) : 0.0;
+    X2[i] = nder > 2 ? __ldg(a.x2 + dof[i]) : 0.0;
+    av[i] = step ? __ldg(a.av + dof[i]) : 0.0;
+    bv[i] = step ? __ldg(a.bv + dof[i]) : 0.0;
+  }
+  double U[3];
+  const bool has_u = uidx != nullptr;
+  if (has_u)
+    for (int k = 0; k < 3; ++k) U[k] = __ldg(a.u + __ldg(uidx + k * nele + e));
+  double R[6], K[36], rd[6];
+  bar_element(bc, nder, X0, X1, X2, has_u ? U : nullptr, a.t, a.p0, a.p1, a.p2, step ? av : nullptr,
+              step ? bv : nullptr, R, K, rd, nullptr);
+  double s[6];
+  for (int i = 0; i < 6; ++i) s[i] = a.scale ? __ldg(a.scale + dof[i]) : 1.0;
+  bool bad = false;
+  for (int i = 0; i < 6; ++i) {
+    const double r = (step ? R[i] - rd[i] : R[i]) * s[i];
+    bad |= isnan(r);
+    rout[i * nele + e] = r;
+  }
+  for (int j = 0; j < 6; ++j)
+    for (int i = 0; i < 6; ++i) {
+      const double k = K[i + 6 * j] * s[i] * s[j];
+      bad |= isnan(k);
+      kout[(i + 6 * j) * nele + e] = k;
+    }
+  flag_nan(a.errflag, gid0 + e, bad);
+}
+
+// DofConstraint{:X} in equal mode with gap g = Σ aᵢ xᵢ − c(t):
+// R = [−aᵢ λ ; −g]  (src/BasicElements.jl:426-438)
+__global__ void constraint_kernel(int64_t nele, int nX, const int32_t* __restrict__ idx,
+                                  const double* __restrict__ cdata, const double* __restrict__ tv, AsmArgs a,
+                                  double* __restrict__ rout, double* __restrict__ kout, int64_t gid0) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  const int nx = nX - 1;
+  const int dl = __ldg(idx + nx * nele + e);
+  const double lam = __ldg(a.x0 + dl);
+  const double sl = a.scale ? __ldg(a.scale + dl) : 1.0;
+  double gap = -__ldg(tv + e);
+  bool bad = false;
+  for (int i = 0; i < nx; ++i) {
+    const int di = __ldg(idx + i * nele + e);
+    const double ci = __ldg(cdata + i * nele + e);
+    gap += ci * __ldg(a.x0 + di);
+    const double si = a.scale ? __ldg(a.scale + di) : 1.0;
+    const double r = -ci * lam * si;
+    bad |= isnan(r);
+    rout[i * nele + e] = r;
+    for (int j = 0; j < nX; ++j) kout[(i + nX * j) * nele + e] = (j == nx) ? -ci * si * sl * a.p0 : 0.0;
+  }
+  rout[nx * nele + e] = -gap * sl;
+  bad |= isnan(gap);
+  for (int j = 0; j < nX; ++j) {
+    double k = 0.0;
+    if (j < nx) {
+      const int dj = __ldg(idx + j * nele + e);
+      const double sj = a.scale ? __ldg(a.scale + dj) : 1.0;
+      k = -__ldg(cdata + j * nele + e) * sl * sj * a.p0;
+    }
+    kout[(nx + nX * j) * nele + e] = k;
+  }
+  flag_nan(a.errflag, gid0 + e, bad);
+}
+
+// DofLoad: R = −F(t), zero tangent entry (src/BasicElements.jl:281-284)
+__global__ void load_kernel(int64_t nele, const int32_t* __restrict__ idx, const double* __restrict__ tv, AsmArgs a,
+                            double* __restrict__ rout, double* __restrict__ kout, int64_t gid0) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  const int d = __ldg(idx + e);
+  const double s = a.scale ? __ldg(a.scale + d) : 1.0;
+  const double r = -__ldg(tv + e) * s;
+  rout[e] = r;
+  kout[e] = 0.0;
+  flag_nan(a.errflag, gid0 + e, isnan(r));
+}
+
+// Deterministic gather-sum: out[k] = Σ buf[src[q]], q = seg[k]..seg[k+1]-1, in order.
+__global__ void scatter_kernel(int64_t n, const uint32_t* __restrict__ seg, const uint32_t* __restrict__ src,
+                               const double* __restrict__ buf, double* __restrict__ out) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t a = __ldg(seg + k), b = __ldg(seg + k + 1);
+  double s = 0.0;
+  for (uint32_t q = a; q < b; ++q) s += __ldg(buf + __ldg(src + q));
+  out[k] = s;
+}
+
+__global__ void newmark_ab_kernel(int64_t n, const double* x1, const double* x2, double a2, double a3, double b2,
+                                  double b3, double* av, double* bv) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  av[i] = a2 * x1[i] + a3 * x2[i];
+  bv[i] = b2 * x1[i] + b3 * x2[i];
+}
+
+__global__ void fill_kernel(double* p, int64_t n, double v) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+static inline unsigned nblk(int64_t n, int b) { return unsigned((n + b - 1) / b); }
+
+// ------------------------------------------------------------------ assembly
+int launch_assembly(mgpu_ctx* c, int mission, double t, const mgpu_newmark* nm, cudaEvent_t* ev_groups) {
+  const int64_t nX = c->nX;
+  AsmArgs a;
+  a.x0 = c->x;
+  a.x1 = c->x + nX;
+  a.x2 = c->x + 2 * nX;
+  a.u = c->u;
+  a.tv = c->tv;
+  a.av = c->ab;
+  a.bv = c->ab + nX;
+  a.scale = c->scale;
+  a.t = t;
+  a.mission = mission;
+  a.errflag = c->errflag;
+  const bool dyn = mission != MGPU_ASM_STATIC;
+  a.p0 = 1.0;
+  a.p1 = dyn ? nm->a1 : 0.0;
+  a.p2 = dyn ? nm->b1 : 0.0;
+  if (dyn && c->nXder_resident != 3) return set_err(c, MGPU_ERR_ARG, "Newmark assembly needs X, X' and X''");
+  if (mission == MGPU_ASM_STEP && nX > 0)
+    newmark_ab_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, a.x1, a.x2, nm->a2, nm->a3, nm->b2, nm->b3, c->ab,
+                                                             c->ab + nX);
+  int64_t gid0 = 0;
+  for (size_t g = 0; g < c->groups.size(); ++g) {
+    const DevGroup& G = c->groups[g];
+    if (G.nele == 0) {
+      if (ev_groups) cudaEventRecord(ev_groups[g], c->stream);
+      continue;
+    }
+    double* rout = c->rbuf + c->pat.rbuf_base[g];
+    double* kout = c->kbuf + c->pat.kbuf_base[g];
+    AsmArgs ag = a;
+    if (G.tval_base >= 0) ag.tv = c->tv + G.tval_base;
+    switch (G.kind) {
+      case MGPU_EULERBEAM3D:
+        if (dyn)
+          beam_kernel<true><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, ag, rout, kout,
+                                                                      gid0);
+        else
+          beam_kernel<false><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, ag, rout,
+                                                                       kout, gid0);
+        break;
+      case MGPU_BAR3D:
+        bar_kernel<<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, dyn ? 3 : 1, G.idx, G.uidx, G.cdata, ag, rout,
+                                                             kout, gid0);
+        break;
+      case MGPU_DOFCONSTRAINT_X:
+        constraint_kernel<<<nblk(G.nele, 256), 256, 0, c->stream>>>(G.nele, G.nX, G.idx, G.cdata, ag.tv, ag, rout,
+                                                                    kout, gid0);
+        break;
+      case MGPU_DOFLOAD:
+        load_kernel<<<nblk(G.nele, 256), 256, 0, c->stream>>>(G.nele, G.idx, ag.tv, ag, rout, kout, gid0);
+        break;
+    }
+    gid0 += G.nele;
+    if (ev_groups) cudaEventRecord(ev_groups[g], c->stream);
+  }
+  if (c->pat.nnz > 0)
+    scatter_kernel<<<nblk(c->pat.nnz, 256), 256, 0, c->stream>>>(c->pat.nnz, c->mseg, c->msrc, c->kbuf, c->nzval);
+  if (nX > 0) scatter_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, c->vseg, c->vsrc, c->rbuf, c->Ll);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(c, MGPU_ERR_CUDA, std::string("assembly launch: ") + cudaGetErrorString(e));
+  return MGPU_OK;
+}
+
+int check_nan(mgpu_ctx* c) {
+  int h[1];
+  MG_CUDA(cudaMemcpyAsync(h, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  MG_CUDA(cudaStreamSynchronize(c->stream));
+  if (h[0] != INT_MAX) {
+    // locate type and element
+    int64_t gid = h[0], base = 0;
+    for (size_t g = 0; g < c->groups.size(); ++g) {
+      if (gid < base + c->groups[g].nele) {
+        const char* names[] = {"?", "EulerBeam3D", "Bar3D", "DofConstraint", "DofLoad"};
+        int k = c->groups[g].kind;
+        return set_err(c, MGPU_ERR_NAN,
+                       std::string("residual(") + names[(k >= 1 && k <= 4) ? k : 0] +
+                           ",...) returned NaN in R, FB or derivatives (ieletyp=" + std::to_string(g + 1) +
+                           ", iele=" + std::to_string(gid - base + 1) + ")");
+      }
+      base += c->groups[g].nele;
+    }
+    return set_err(c, MGPU_ERR_NAN, "residual returned NaN");
+  }
+  return MGPU_OK;
+}
+
+static int reset_errflag(mgpu_ctx* c) {
+  const int v = INT_MAX;
+  MG_CUDA(cudaMemcpyAsync(c->errflag, &v, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  return MGPU_OK;
+}
+
+}  // namespace mgpu
+
+// ------------------------------------------------------------------ C ABI
+template <class T>
+static int dalloc(mgpu_ctx* c, T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  if (e != cudaSuccess) return set_err(c, MGPU_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return MGPU_OK;
+}
+
+#define MG_TRY(x)              \
+  do {                         \
+    int rc_ = (x);             \
+    if (rc_ != MGPU_OK) return rc_; \
+  } while (0)
+
+extern "C" int mgpu_solver_create(mgpu_ctx* c);   // solver.cu
+extern "C" void mgpu_solver_destroy(mgpu_ctx* c);  // solver.cu
+
+extern "C" const char* mgpu_last_error(const mgpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
+  if (!out || !d) return MGPU_ERR_ARG;
+  *out = nullptr;
+  mgpu_ctx* c = new mgpu_ctx();
+  *out = c;
+  c->device = d->device;
+  MG_CUDA(cudaSetDevice(d->device));
+  MG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->nX = d->nX;
+  c->nU = d->nU;
+  if (d->nX < 0 || d->nU < 0 || d->ngroup < 0 || (d->ngroup > 0 && !d->groups))
+    return set_err(c, MGPU_ERR_ARG, "invalid model description");
+  std::vector<GroupShape> shapes;
+  int64_t ntv = 0;
+  for (int g = 0; g < d->ngroup; ++g) {
+    const mgpu_group& G = d->groups[g];
+    int exp_nX = -1, exp_data = -1;
+    switch (G.kind) {
+      case MGPU_EULERBEAM3D: exp_nX = 12; exp_data = BEAM_NFIELD; break;
+      case MGPU_BAR3D: exp_nX = 6; exp_data = 38; break;
+      case MGPU_DOFCONSTRAINT_X: exp_nX = G.nX; exp_data = G.nX - 1; break;
+      case MGPU_DOFLOAD: exp_nX = 1; exp_data = 0; break;
+      default:
+        return set_err(c, MGPU_ERR_UNSUPPORTED,
+                       "element type " + std::to_string(g + 1) + " (kind " + std::to_string(G.kind) +
+                           ") is not supported by the GPU path");
+    }
+    if (G.nX != exp_nX || G.nX < 1 || (exp_data > 0 && G.ndata != exp_data) || G.nele < 0 || (G.nele > 0 && !G.indexX))
+      return set_err(c, MGPU_ERR_ARG, "element type " + std::to_string(g + 1) + ": unexpected layout");
+    if ((G.kind == MGPU_EULERBEAM3D || G.kind == MGPU_BAR3D) && !(G.nU == 0 || G.nU == 3))
+      return set_err(c, MGPU_ERR_ARG, "beam/bar elements have 0 or 3 U-dofs");
+    if ((G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) && G.nU != 0)
+      return set_err(c, MGPU_ERR_ARG, "constraints and loads have no U-dofs");
+    if (G.nU > 0 && G.nele > 0 && !G.indexU) return set_err(c, MGPU_ERR_ARG, "missing indexU");
+    for (int64_t k = 0; k < G.nele * G.nU; ++k)
+      if (G.indexU[k] < 1 || G.indexU[k] > d->nU) return set_err(c, MGPU_ERR_ARG, "U-dof index out of range");
+    shapes.push_back(GroupShape{G.nele, G.nX, G.indexX});
+    if (G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) ntv += G.nele;
+  }
+  std::string perr = build_pattern(d->nX, shapes, c->pat);
+  if (!perr.empty()) return set_err(c, MGPU_ERR_ARG, perr);
+  c->ntval = ntv;
+  // ---- per-group device data
+  int64_t tvb = 0;
+  for (int g = 0; g < d->ngroup; ++g) {
+    const mgpu_group& G = d->groups[g];
+    DevGroup D;
+    D.kind = G.kind;
+    D.nX = G.nX;
+    D.nU = G.nU;
+    D.ndata = G.ndata;
+    D.nele = G.nele;
+    D.h_indexX.assign(G.indexX, G.indexX + G.nele * G.nX);
+    std::vector<int32_t> idx(size_t(G.nX) * G.nele);
+    for (int64_t e = 0; e < G.nele; ++e)
+      for (int i = 0; i < G.nX; ++i) idx[size_t(i) * G.nele + e] = int32_t(G.indexX[e * G.nX + i] - 1);
+    MG_TRY(dalloc(c, &D.idx, idx.size()));
+    MG_CUDA(cudaMemcpy(D.idx, idx.data(), idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (G.nU > 0) {
+      std::vector<int32_t> uidx(size_t(G.nU) * G.nele);
+      for (int64_t e = 0; e < G.nele; ++e)
+        for (int i = 0; i < G.nU; ++i) uidx[size_t(i) * G.nele + e] = int32_t(G.indexU[e * G.nU + i] - 1);
+      MG_TRY(dalloc(c, &D.uidx, uidx.size()));
+      MG_CUDA(cudaMemcpy(D.uidx, uidx.data(), uidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
+    std::vector<double> cd;
+    if (G.kind == MGPU_EULERBEAM3D) {
+      D.nfield = BEAM_NCONST;
+      cd.resize(size_t(D.nfield) * G.nele);
+      for (int64_t e = 0; e < G.nele; ++e) {
+        BeamConst bc;
+        beam_const_from_fields(G.edata + e * BEAM_NFIELD, bc);
+        const double* p = reinterpret_cast<const double*>(&bc);
+        for (int f = 0; f < D.nfield; ++f) cd[size_t(f) * G.nele + e] = p[f];
+      }
+    } else if (G.kind == MGPU_BAR3D) {
+      D.nfield = BAR_NCONST;
+      cd.resize(size_t(D.nfield) * G.nele);
+      for (int64_t e = 0; e < G.nele; ++e) {
+        BarConst bc;
+        bar_const_from_fields(G.edata + e * 38, bc);
+        const double* p = reinterpret_cast<const double*>(&bc);
+        for (int f = 0; f < D.nfield; ++f) cd[size_t(f) * G.nele + e] = p[f];
+      }
+    } else if (G.kind == MGPU_DOFCONSTRAINT_X) {
+      D.nfield = G.nX - 1;
+      cd.resize(size_t(D.nfield) * G.nele);
+      for (int64_t e = 0; e < G.nele; ++e)
+        for (int f = 0; f < D.nfield; ++f) cd[size_t(f) * G.nele + e] = G.edata[e * D.nfield + f];
+    }
+    if (!cd.empty()) {
+      MG_TRY(dalloc(c, &D.cdata, cd.size()));
+      MG_CUDA(cudaMemcpy(D.cdata, cd.data(), cd.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) {
+      D.tval_base = tvb;
+      tvb += G.nele;
+    }
+    c->groups.push_back(std::move(D));
+  }
+  // ---- buffers and scatter plans
+  const Pattern& P = c->pat;
+  MG_TRY(dalloc(c, &c->kbuf, P.kbuf_size));
+  MG_TRY(dalloc(c, &c->rbuf, P.rbuf_size));
+  MG_TRY(dalloc(c, &c->mseg, P.mseg.size()));
+  MG_TRY(dalloc(c, &c->msrc, P.msrc.size()));
+  MG_TRY(dalloc(c, &c->vseg, P.vseg.size()));
+  MG_TRY(dalloc(c, &c->vsrc, P.vsrc.size()));
+  MG_CUDA(cudaMemcpy(c->mseg, P.mseg.data(), P.mseg.size() * 4, cudaMemcpyHostToDevice));
+  MG_CUDA(cudaMemcpy(c->msrc, P.msrc.data(), P.msrc.size() * 4, cudaMemcpyHostToDevice));
+  MG_CUDA(cudaMemcpy(c->vseg, P.vseg.data(), P.vseg.size() * 4, cudaMemcpyHostToDevice));
+  MG_CUDA(cudaMemcpy(c->vsrc, P.vsrc.data(), P.vsrc.size() * 4, cudaMemcpyHostToDevice));
+  MG_TRY(dalloc(c, &c->nzval, P.nnz));
+  MG_TRY(dalloc(c, &c->Ll, c->nX));
+  MG_TRY(dalloc(c, &c->x, 3 * c->nX));
+  MG_CUDA(cudaMemset(c->x, 0, 3 * std::max<int64_t>(c->nX, 1) * sizeof(double)));
+  MG_TRY(dalloc(c, &c->u, c->nU));
+  MG_CUDA(cudaMemset(c->u, 0, std::max<int64_t>(c->nU, 1) * sizeof(double)));
+  MG_TRY(dalloc(c, &c->tv, c->ntval));
+  MG_CUDA(cudaMemset(c->tv, 0, std::max<int64_t>(c->ntval, 1) * sizeof(double)));
+  MG_TRY(dalloc(c, &c->ab, 2 * c->nX));
+  MG_TRY(dalloc(c, &c->errflag, 2));
+  if (d->scaleX) {
+    bool ones = true;
+    for (int64_t i = 0; i < d->nX; ++i) ones &= (d->scaleX[i] == 1.0);
+    if (!ones) {
+      MG_TRY(dalloc(c, &c->scale, c->nX));
+      MG_CUDA(cudaMemcpy(c->scale, d->scaleX, c->nX * sizeof(double), cudaMemcpyHostToDevice));
+    }
+  }
+  MG_TRY(reset_errflag(c));
+  MG_TRY(mgpu_solver_create(c));
+  MG_CUDA(cudaStreamSynchronize(c->stream));
+  return MGPU_OK;
+}
+
+extern "C" void mgpu_destroy(mgpu_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  mgpu_solver_destroy(c);
+  for (auto& G : c->groups) {
+    cudaFree(G.idx);
+    cudaFree(G.uidx);
+    cudaFree(G.cdata);
+  }
+  void* ps[] = {c->kbuf, c->rbuf, c->mseg, c->msrc, c->vseg, c->vsrc, c->nzval, c->Ll, c->x,
+                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush};
+  for (void* p : ps) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" int64_t mgpu_nnz(const mgpu_ctx* c) { return c ? c->pat.nnz : -1; }
+extern "C" int64_t mgpu_ntval(const mgpu_ctx* c) { return c ? c->ntval : -1; }
+
+extern "C" int mgpu_get_pattern(const mgpu_ctx* cc, int64_t* colptr, int64_t* rowval) {
+  if (!cc || !colptr || !rowval) return MGPU_ERR_ARG;
+  for (int64_t j = 0; j <= cc->nX; ++j) colptr[j] = cc->pat.colptr[j] + 1;
+  for (int64_t k = 0; k < cc->pat.nnz; ++k) rowval[k] = int64_t(cc->pat.rowval[k]) + 1;
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_get_asm(const mgpu_ctx* cc, int32_t g, int64_t* asm1, int64_t* asm2) {
+  if (!cc || g < 0 || g >= int32_t(cc->groups.size())) return MGPU_ERR_ARG;
+  const DevGroup& G = cc->groups[g];
+  const int nX = G.nX;
+  for (int64_t e = 0; e < G.nele; ++e) {
+    if (asm1)
+      for (int i = 0; i < nX; ++i) asm1[e * nX + i] = G.h_indexX[e * nX + i];  // X dof group = all X dofs
+    if (asm2)
+      for (int k = 0; k < nX * nX; ++k)
+        asm2[e * nX * nX + k] = int64_t(cc->pat.pair_nnz[cc->pat.pair_base[g] + e * nX * nX + k]) + 1;
+  }
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_upload_state(mgpu_ctx* c, int32_t nXder, const double* x, const double* u, const double* tvals) {
+  if (!c || !x || nXder < 1 || nXder > 3) return set_err(c, MGPU_ERR_ARG, "mgpu_upload_state: bad arguments");
+  MG_CUDA(cudaSetDevice(c->device));
+  MG_CUDA(cudaMemcpyAsync(c->x, x, nXder * c->nX * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (nXder < 3)
+    MG_CUDA(cudaMemsetAsync(c->x + nXder * c->nX, 0, (3 - nXder) * c->nX * sizeof(double), c->stream));
+  if (c->nU > 0 && u) MG_CUDA(cudaMemcpyAsync(c->u, u, c->nU * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->ntval > 0 && tvals)
+    MG_CUDA(cudaMemcpyAsync(c->tv, tvals, c->ntval * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  c->nXder_resident = nXder;
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_assemble_resident(mgpu_ctx* c, int32_t mission, double t, const mgpu_newmark* nm) {
+  if (!c || mission < 0 || mission > 2 || (mission != MGPU_ASM_STATIC && !nm))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_assemble_resident: bad arguments");
+  MG_CUDA(cudaSetDevice(c->device));
+  return launch_assembly(c, mission, t, nm, nullptr);
+}
+
+extern "C" int mgpu_download(mgpu_ctx* c, double* Ll, double* nzval) {
+  if (!c) return MGPU_ERR_ARG;
+  MG_CUDA(cudaSetDevice(c->device));
+  if (Ll) MG_CUDA(cudaMemcpyAsync(Ll, c->Ll, c->nX * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (nzval) MG_CUDA(cudaMemcpyAsync(nzval, c->nzval, c->pat.nnz * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  MG_CUDA(cudaStreamSynchronize(c->stream));
+  return check_nan(c);
+}
+
+extern "C" int mgpu_assemble(mgpu_ctx* c, int32_t mission, int32_t nXder, const double* x, const double* u, double t,
+                             const double* tvals, const mgpu_newmark* nm, double* Ll, double* nzval) {
+  if (!c) return MGPU_ERR_ARG;
+  MG_TRY(reset_errflag(c));
+  MG_TRY(mgpu_upload_state(c, nXder, x, u, tvals));
+  MG_TRY(mgpu_assemble_resident(c, mission, t, nm));
+  return mgpu_download(c, Ll, nzval);
+}
+
+extern "C" int mgpu_time_assemble(mgpu_ctx* c, int32_t mission, double t, const mgpu_newmark* nm, int32_t reps,
+                                  int32_t flush_l2, double* ms_total, double* ms_groups, double* ms_scatter) {
+  if (!c || reps < 1 || (mission != MGPU_ASM_STATIC && !nm)) return set_err(c, MGPU_ERR_ARG, "mgpu_time_assemble: bad arguments");
+  MG_CUDA(cudaSetDevice(c->device));
+  if (flush_l2 && !c->flush) {
+    c->flush_bytes = size_t(512) << 20;  // larger than the 129 MB L2
+    MG_TRY(dalloc(c, reinterpret_cast<double**>(&c->flush), c->flush_bytes / 8));
+  }
+  MG_TRY(reset_errflag(c));
+  const int ng = int(c->groups.size());
+  const int ne = ng + 2;  // start, one per group, end
+  std::vector<cudaEvent_t> ev(size_t(ne) * reps);
+  for (auto& e : ev) MG_CUDA(cudaEventCreate(&e));
+  for (int r = 0; r < reps; ++r) {
+    if (flush_l2)
+      fill_kernel<<<nblk(c->flush_bytes / 8, 256), 256, 0, c->stream>>>(c->flush, c->flush_bytes / 8, double(r));
+    cudaEvent_t* E = &ev[size_t(ne) * r];
+    MG_CUDA(cudaEventRecord(E[0], c->stream));
+    MG_TRY(launch_assembly(c, mission, t, nm, E + 1));
+    MG_CUDA(cudaEventRecord(E[ng + 1], c->stream));
+  }
+  MG_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<double> tg(ng, 0.0);
+  double tt = 0, ts = 0;
+  for (int r = 0; r < reps; ++r) {
+    cudaEvent_t* E = &ev[size_t(ne) * r];
+    float a = 0;
+    cudaEventElapsedTime(&a, E[0], E[ng + 1]);
+    tt += a;
+    for (int g = 0; g < ng; ++g) {
+      cudaEventElapsedTime(&a, E[g], E[g + 1]);
+      tg[g] += a;
+    }
+    cudaEventElapsedTime(&a, E[ng], E[ng + 1]);
+    ts += a;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (ms_total) *ms_total = tt / reps;
+  if (ms_groups)
+    for (int g = 0; g < ng; ++g) ms_groups[g] = tg[g] / reps;
+  if (ms_scatter) *ms_scatter = ts / reps;
+  return check_nan(c);
+}
+
+// Element-level evaluation (diffed_residual-like) for group g.
+__global__ void eval_beam_kernel(int64_t nele, int nder, const double* X, const double* U, const double* cdata,
+                                 double p0, double p1, double p2, double* R, double* dR, double* dRdU) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  BeamConst bc;
+  load_soa(bc, cdata, nele, e);
+  const double* Xe = X + e * nder * 12;
+  double K[144], H[36];
+  if (nder == 3)
+    beam_element<true>(bc, Xe, Xe + 12, Xe + 24, U ? U + 3 * e : nullptr, Perturb{p0, p1, p2}, nullptr, nullptr,
+                       R + 12 * e, K, nullptr, dRdU ? H : nullptr);
+  else
+    beam_element<false>(bc, Xe, Xe, Xe, U ? U + 3 * e : nullptr, Perturb{p0, p1, p2}, nullptr, nullptr, R + 12 * e, K,
+                        nullptr, dRdU ? H : nullptr);
+  for (int k = 0; k < 144; ++k) dR[144 * e + k] = K[k];
+  if (dRdU)
+    for (int k = 0; k < 36; ++k) dRdU[36 * e + k] = H[k];
+}
+__global__ void eval_bar_kernel(int64_t nele, int nder, const double* X, const double* U, const double* cdata, double t,
+                                double p0, double p1, double p2, double* R, double* dR, double* dRdU) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  BarConst bc;
+  load_soa(bc, cdata, nele, e);
+  const double* Xe = X + e * nder * 6;
+  double H[18];
+  bar_element(bc, nder, Xe, Xe + 6, Xe + 12, U ? U + 3 * e : nullptr, t, p0, p1, p2, nullptr, nullptr, R + 6 * e,
+              dR + 36 * e, nullptr, dRdU ? H : nullptr);
+  if (dRdU)
+    for (int k = 0; k < 18; ++k) dRdU[18 * e + k] = H[k];
+}
+
+extern "C" int mgpu_element_eval(mgpu_ctx* c, int32_t g, int32_t nXder, const double* X, const double* U, double t,
+                                 double p0, double p1, double p2, double* R, double* dR, double* dRdU) {
+  if (!c || g < 0 || g >= int32_t(c->groups.size()) || !X || !R || !dR || !(nXder == 1 || nXder == 3))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_element_eval: bad arguments (nXder must be 1 or 3)");
+  const DevGroup& G = c->groups[g];
+  if (G.kind != MGPU_EULERBEAM3D && G.kind != MGPU_BAR3D)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_element_eval: only beam and bar groups");
+  MG_CUDA(cudaSetDevice(c->device));
+  const int nX = G.nX;
+  const int64_t n = G.nele;
+  double *dX = nullptr, *dU = nullptr, *dRv = nullptr, *dK = nullptr, *dH = nullptr;
+  MG_TRY(dalloc(c, &dX, size_t(n) * nXder * nX));
+  MG_TRY(dalloc(c, &dRv, size_t(n) * nX));
+  MG_TRY(dalloc(c, &dK, size_t(n) * nX * nX));
+  const bool withU = U != nullptr;
+  if (withU) {
+    MG_TRY(dalloc(c, &dU, size_t(n) * 3));
+    MG_TRY(dalloc(c, &dH, size_t(n) * nX * 3));
+    MG_CUDA(cudaMemcpy(dU, U, n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  MG_CUDA(cudaMemcpy(dX, X, size_t(n) * nXder * nX * sizeof(double), cudaMemcpyHostToDevice));
+  if (G.kind == MGPU_EULERBEAM3D)
+    eval_beam_kernel<<<nblk(n, 64), 64, 0, c->stream>>>(n, nXder, dX, dU, G.cdata, p0, p1, p2, dRv, dK,
+                                                         (withU && dRdU) ? dH : nullptr);
+  else
+    eval_bar_kernel<<<nblk(n, 64), 64, 0, c->stream>>>(n, nXder, dX, dU, G.cdata, t, p0, p1, p2, dRv, dK,
+                                                        (withU && dRdU) ? dH : nullptr);
+  MG_CUDA(cudaGetLastError());
+  MG_CUDA(cudaStreamSynchronize(c->stream));
+  MG_CUDA(cudaMemcpy(R, dRv, size_t(n) * nX * sizeof(double), cudaMemcpyDeviceToHost));
+  MG_CUDA(cudaMemcpy(dR, dK, size_t(n) * nX * nX * sizeof(double), cudaMemcpyDeviceToHost));
+  if (withU && dRdU) MG_CUDA(cudaMemcpy(dRdU, dH, size_t(n) * nX * 3 * sizeof(double), cudaMemcpyDeviceToHost));
+  cudaFree(dX);
+  cudaFree(dU);
+  cudaFree(dRv);
+  cudaFree(dK);
+  cudaFree(dH);
+  return MGPU_OK;
+}

@@ -1,0 +1,534 @@
+// Device linear solve and Newton loop of SweepX{0} / SweepX{2}.
+//
+// The reference factorises Lλx with UMFPACK at every Newton iteration and
+// solves Δx = Lλx \ Lλ (src/SweepX.jl:207-210).  The matrices of the models
+// this path targets are sparse and, after reordering, narrow-banded within each
+// connected component (chains of beams, risers, frames; Hold multipliers sit
+// next to the dofs they constrain).  At create time the host splits the
+// matrix graph into connected components and orders each with reverse
+// Cuthill-McKee; the device then factorises all components at once, one
+// thread block per component, with banded LU and partial pivoting (the
+// algorithm of LAPACK's gbtf2), and solves with the factors.  The solution is
+// the same Δx the reference computes, to rounding.  Components whose band is
+// too wide for this scheme are rejected at solve time with MGPU_ERR_UNSUPPORTED
+// (there is no CPU fallback).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+
+using namespace mgpu;
+
+namespace mgpu {
+
+struct Solver {
+  bool ok = false;       // banded scheme applicable
+  std::string why;       // reason when not
+  int ncomp = 0;
+  int64_t band_total = 0;
+  int maxkl = 0, maxku = 0;
+  // device
+  int64_t* cbase = nullptr;   // [ncomp] offset of component band storage
+  int32_t* cn = nullptr;      // [ncomp] component size
+  int32_t* ckl = nullptr;     // [ncomp]
+  int32_t* cku = nullptr;     // [ncomp]
+  int32_t* cdof0 = nullptr;   // [ncomp] offset into perm
+  int32_t* perm = nullptr;    // [nX] dofs of component c in band order: perm[cdof0[c] + k]
+  int64_t* bmap = nullptr;    // [nnz] band position of each nnz
+  double* AB = nullptr;       // band storage
+  int32_t* ipiv = nullptr;    // [nX] pivot offsets (band order)
+  double* rhs = nullptr;      // [nX] permuted right-hand side / solution
+  double* dx = nullptr;       // [nX] Δx in model order
+  double* red = nullptr;      // [4] reductions: ΣΔx², ΣLλ²
+  int* info = nullptr;        // [1] first singular component+1 (0 = ok)
+  double* hbuf = nullptr;     // pinned host: red[0..1], info
+};
+
+// ---------------------------------------------------------------- host analysis
+static void analyse(mgpu_ctx* c, Solver& S) {
+  const Pattern& P = c->pat;
+  const int64_t n = c->nX;
+  if (n == 0) {
+    S.why = "empty model";
+    return;
+  }
+  // union-find over the symmetric pattern
+  std::vector<int32_t> par(n);
+  std::iota(par.begin(), par.end(), 0);
+  auto find = [&](int32_t a) {
+    while (par[a] != a) {
+      par[a] = par[par[a]];
+      a = par[a];
+    }
+    return a;
+  };
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      int32_t a = find(int32_t(j)), b = find(P.rowval[q]);
+      if (a != b) par[std::max(a, b)] = std::min(a, b);
+    }
+  std::vector<int32_t> comp(n, -1), root2comp(n, -1);
+  int ncomp = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t r = find(int32_t(i));
+    if (root2comp[r] < 0) root2comp[r] = ncomp++;
+    comp[i] = root2comp[r];
+  }
+  // symmetric adjacency lists
+  std::vector<int64_t> deg(n + 1, 0);
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      int64_t i = P.rowval[q];
+      if (i != j) {
+        deg[i + 1]++;
+        deg[j + 1]++;
+      }
+    }
+  for (int64_t i = 0; i < n; ++i) deg[i + 1] += deg[i];
+  std::vector<int32_t> adj(deg[n]);
+  {
+    std::vector<int64_t> f(deg.begin(), deg.end() - 1);
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+        int64_t i = P.rowval[q];
+        if (i != j) {
+          adj[f[i]++] = int32_t(j);
+          adj[f[j]++] = int32_t(i);
+        }
+      }
+  }
+  auto degree = [&](int32_t v) { return deg[v + 1] - deg[v]; };
+  // members of each component in increasing dof order
+  std::vector<std::vector<int32_t>> members(ncomp);
+  for (int64_t i = 0; i < n; ++i) members[comp[i]].push_back(int32_t(i));
+  std::vector<int32_t> order;  // RCM order, component after component
+  order.reserve(n);
+  std::vector<int32_t> level(n, -1), mark(n, 0);
+  std::vector<int32_t> comp_start(ncomp + 1, 0);
+  for (int cc = 0; cc < ncomp; ++cc) {
+    const auto& M = members[cc];
+    // pseudo-peripheral start: repeat BFS from the farthest, lowest-degree node
+    int32_t start = M[0];
+    for (int32_t v : M)
+      if (degree(v) < degree(start)) start = v;
+    for (int it = 0; it < 3; ++it) {
+      std::queue<int32_t> qu;
+      for (int32_t v : M) level[v] = -1;
+      level[start] = 0;
+      qu.push(start);
+      int32_t last = start;
+      while (!qu.empty()) {
+        int32_t v = qu.front();
+        qu.pop();
+        last = v;
+        for (int64_t q = deg[v]; q < deg[v + 1]; ++q)
+          if (level[adj[q]] < 0) {
+            level[adj[q]] = level[v] + 1;
+            qu.push(adj[q]);
+          }
+      }
+      int32_t best = last;
+      for (int32_t v : M)
+        if (level[v] == level[last] && degree(v) < degree(best)) best = v;
+      if (best == start) break;
+      start = best;
+    }
+    // Cuthill-McKee from start
+    std::vector<int32_t> cm;
+    cm.reserve(M.size());
+    cm.push_back(start);
+    mark[start] = 1;
+    std::vector<int32_t> nb;
+    for (size_t h = 0; h < cm.size(); ++h) {
+      int32_t v = cm[h];
+      nb.clear();
+      for (int64_t q = deg[v]; q < deg[v + 1]; ++q)
+        if (!mark[adj[q]]) {
+          mark[adj[q]] = 1;
+          nb.push_back(adj[q]);
+        }
+      std::sort(nb.begin(), nb.end(), [&](int32_t a, int32_t b) {
+        return degree(a) != degree(b) ? degree(a) < degree(b) : a < b;
+      });
+      cm.insert(cm.end(), nb.begin(), nb.end());
+    }
+    comp_start[cc] = int32_t(order.size());
+    for (auto it = cm.rbegin(); it != cm.rend(); ++it) order.push_back(*it);
+  }
+  comp_start[ncomp] = int32_t(order.size());
+  std::vector<int32_t> pos(n);
+  for (int64_t k = 0; k < n; ++k) pos[order[k]] = int32_t(k);
+  // bandwidths per component
+  std::vector<int32_t> kl(ncomp, 0), ku(ncomp, 0);
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      int64_t i = P.rowval[q];
+      int cc = comp[j];
+      int32_t d = pos[i] - pos[j];
+      if (d > kl[cc]) kl[cc] = d;
+      if (-d > ku[cc]) ku[cc] = -d;
+    }
+  std::vector<int64_t> base(ncomp + 1, 0);
+  for (int cc = 0; cc < ncomp; ++cc) {
+    int64_t nc = comp_start[cc + 1] - comp_start[cc];
+    base[cc + 1] = base[cc] + int64_t(2 * kl[cc] + ku[cc] + 1) * nc;
+    S.maxkl = std::max(S.maxkl, kl[cc]);
+    S.maxku = std::max(S.maxku, ku[cc]);
+  }
+  S.ncomp = ncomp;
+  S.band_total = base[ncomp];
+  if (S.maxkl > 256 || S.maxku > 256 || S.band_total > (int64_t(1) << 33)) {
+    S.why = "matrix band too wide for the banded device solver (kl=" + std::to_string(S.maxkl) +
+            ", ku=" + std::to_string(S.maxku) + ")";
+    return;
+  }
+  // band position of each nnz
+  std::vector<int64_t> bmap(P.nnz);
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      int64_t i = P.rowval[q];
+      int cc = comp[j];
+      int64_t kj = pos[j] - comp_start[cc], ki = pos[i] - comp_start[cc];
+      int64_t ld = 2 * kl[cc] + ku[cc] + 1;
+      bmap[q] = base[cc] + (kl[cc] + ku[cc] + ki - kj) + ld * kj;
+    }
+  // upload
+  auto up = [&](auto** dst, const auto& v) -> bool {
+    using T = typename std::remove_reference<decltype(v[0])>::type;
+    if (cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(v.size(), 1) * sizeof(T)) != cudaSuccess)
+      return false;
+    return cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  std::vector<int64_t> cb(base.begin(), base.end() - 1);
+  std::vector<int32_t> cn(ncomp), c0(ncomp);
+  for (int cc = 0; cc < ncomp; ++cc) {
+    cn[cc] = comp_start[cc + 1] - comp_start[cc];
+    c0[cc] = comp_start[cc];
+  }
+  bool good = up(&S.cbase, cb) && up(&S.cn, cn) && up(&S.ckl, kl) && up(&S.cku, ku) && up(&S.cdof0, c0) &&
+              up(&S.perm, order) && up(&S.bmap, bmap);
+  good = good && cudaMalloc(&S.AB, std::max<int64_t>(S.band_total, 1) * sizeof(double)) == cudaSuccess;
+  good = good && cudaMalloc(&S.ipiv, n * sizeof(int32_t)) == cudaSuccess;
+  good = good && cudaMalloc(&S.rhs, n * sizeof(double)) == cudaSuccess;
+  good = good && cudaMalloc(&S.dx, n * sizeof(double)) == cudaSuccess;
+  good = good && cudaMalloc(&S.red, 4 * sizeof(double)) == cudaSuccess;
+  good = good && cudaMalloc(&S.info, sizeof(int)) == cudaSuccess;
+  good = good && cudaMallocHost(&S.hbuf, 8 * sizeof(double)) == cudaSuccess;
+  if (!good) {
+    S.why = "device allocation failed for the solver";
+    return;
+  }
+  S.ok = true;
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void band_gather(int64_t nnz, const int64_t* __restrict__ bmap, const double* __restrict__ nzval,
+                            double* __restrict__ AB) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < nnz) AB[bmap[k]] = nzval[k];
+}
+
+// Banded LU with partial pivoting (LAPACK gbtf2 algorithm), one block per component.
+__global__ void __launch_bounds__(128) band_lu(const int64_t* cbase, const int32_t* cn, const int32_t* ckl,
+                                               const int32_t* cku, const int32_t* cdof0, double* AB, int32_t* ipiv,
+                                               int* info) {
+  const int cc = blockIdx.x;
+  const int n = cn[cc], kl = ckl[cc], ku = cku[cc];
+  const int kv = kl + ku, ld = 2 * kl + ku + 1;
+  double* A = AB + cbase[cc];
+  int32_t* piv = ipiv + cdof0[cc];
+  __shared__ double sval[128];
+  __shared__ int sidx[128];
+  __shared__ int s_jp, s_ju;
+  __shared__ double s_piv;
+  if (threadIdx.x == 0) s_ju = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    const int km = min(kl, n - 1 - k);
+    // pivot search over rows k..k+km of column k (first index of max |a|)
+    double best = -1.0;
+    int bi = 0;
+    for (int i = threadIdx.x; i <= km; i += blockDim.x) {
+      const double v = fabs(A[kv + i + int64_t(ld) * k]);
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+    sval[threadIdx.x] = best;
+    sidx[threadIdx.x] = bi;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        const double v2 = sval[threadIdx.x + s];
+        const int i2 = sidx[threadIdx.x + s];
+        if (v2 > sval[threadIdx.x] || (v2 == sval[threadIdx.x] && i2 < sidx[threadIdx.x])) {
+          sval[threadIdx.x] = v2;
+          sidx[threadIdx.x] = i2;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const int jp = sidx[0];
+      s_jp = jp;
+      piv[k] = k + jp;
+      const double p = A[kv + jp + int64_t(ld) * k];
+      s_piv = p;
+      if (p == 0.0 && *info == 0) atomicCAS(info, 0, cc + 1);
+      s_ju = max(s_ju, min(k + ku + jp, n - 1));
+    }
+    __syncthreads();
+    const int jp = s_jp, ju = s_ju;
+    const double p = s_piv;
+    if (p != 0.0) {
+      // swap rows k and k+jp in columns k..ju
+      if (jp != 0)
+        for (int j = k + threadIdx.x; j <= ju; j += blockDim.x) {
+          double* a = A + kv + (k - j) + int64_t(ld) * j;
+          double* b = A + kv + (k + jp - j) + int64_t(ld) * j;
+          const double t = *a;
+          *a = *b;
+          *b = t;
+        }
+      __syncthreads();
+      // multipliers
+      for (int i = 1 + threadIdx.x; i <= km; i += blockDim.x) A[kv + i + int64_t(ld) * k] /= p;
+      __syncthreads();
+      // rank-1 update of columns k+1..ju, rows k+1..k+km
+      const int w = ju - k;
+      const int tot = w * km;
+      for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+        const int jj = q / km + 1, i = q % km + 1;
+        const int j = k + jj;
+        const double u = A[kv - jj + int64_t(ld) * j];  // row k of column j
+        if (u != 0.0) A[kv + i - jj + int64_t(ld) * j] -= A[kv + i + int64_t(ld) * k] * u;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Solve with the band factors: permute, L with interchanges, U; one block per component.
+__global__ void __launch_bounds__(128) band_solve(const int64_t* cbase, const int32_t* cn, const int32_t* ckl,
+                                                  const int32_t* cku, const int32_t* cdof0, const int32_t* perm,
+                                                  const double* AB, const int32_t* ipiv, const double* Ll, double* rhs,
+                                                  double* dx) {
+  const int cc = blockIdx.x;
+  const int n = cn[cc], kl = ckl[cc], ku = cku[cc];
+  const int kv = kl + ku, ld = 2 * kl + ku + 1;
+  const double* A = AB + cbase[cc];
+  const int32_t* piv = ipiv + cdof0[cc];
+  const int32_t* pm = perm + cdof0[cc];
+  double* b = rhs + cdof0[cc];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) b[k] = Ll[pm[k]];
+  __syncthreads();
+  // forward: L y = P b
+  for (int k = 0; k < n; ++k) {
+    const int km = min(kl, n - 1 - k);
+    const int p = piv[k];
+    if (threadIdx.x == 0 && p != k) {
+      const double t = b[k];
+      b[k] = b[p];
+      b[p] = t;
+    }
+    __syncthreads();
+    const double bk = b[k];
+    for (int i = 1 + threadIdx.x; i <= km; i += blockDim.x) b[k + i] -= A[kv + i + int64_t(ld) * k] * bk;
+    __syncthreads();
+  }
+  // backward: U x = y  (U has kl+ku superdiagonals)
+  for (int k = n - 1; k >= 0; --k) {
+    if (threadIdx.x == 0) b[k] /= A[kv + int64_t(ld) * k];
+    __syncthreads();
+    const double bk = b[k];
+    const int m = min(kv, k);
+    for (int i = 1 + threadIdx.x; i <= m; i += blockDim.x) b[k - i] -= A[kv - i + int64_t(ld) * k] * bk;
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < n; k += blockDim.x) dx[pm[k]] = b[k];
+}
+
+// Σ Δx², Σ Lλ² (deterministic: single block, fixed order of partial sums)
+__global__ void __launch_bounds__(1024) norms_kernel(int64_t n, const double* dx, const double* Ll, double* red) {
+  __shared__ double s1[1024], s2[1024];
+  double a = 0.0, b = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    a += dx[i] * dx[i];
+    b += Ll[i] * Ll[i];
+  }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      s1[threadIdx.x] += s1[threadIdx.x + s];
+      s2[threadIdx.x] += s2[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    red[0] = s1[0];
+    red[1] = s2[0];
+  }
+}
+
+// Newmarkβdecrement!  (src/SweepX.jl:98-132, decrement! src/Assemble.jl:206-211)
+__global__ void decrement_kernel(int64_t n, int OX, int first, const double* dx, const double* scale, double a1,
+                                 double a2, double a3, double b1, double b2, double b3, double* x) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = scale ? scale[i] : 1.0;
+  const double d = dx[i];
+  if (OX == 2) {
+    double* x1 = x + n;
+    double* x2 = x + 2 * n;
+    double d1 = a1 * d, d2 = b1 * d;
+    if (first) {
+      const double xp = x1[i] / s, xpp = x2[i] / s;  // getdof! returns scaled values
+      d1 += a2 * xp + a3 * xpp;
+      d2 += b2 * xp + b3 * xpp;
+    }
+    x1[i] -= d1 * s;
+    x2[i] -= d2 * s;
+  }
+  x[i] -= d * s;
+}
+
+}  // namespace mgpu
+
+extern "C" int mgpu_solver_create(mgpu_ctx* c) {
+  c->solver = new Solver();
+  analyse(c, *c->solver);
+  cudaGetLastError();  // analysis errors are reported at solve time
+  return MGPU_OK;
+}
+
+extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
+  Solver* S = c->solver;
+  if (!S) return;
+  void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx, S->red,
+                S->info};
+  for (void* p : ps) cudaFree(p);
+  if (S->hbuf) cudaFreeHost(S->hbuf);
+  delete S;
+  c->solver = nullptr;
+}
+
+namespace mgpu {
+static unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
+
+// one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device)
+static int factor_solve(mgpu_ctx* c) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
+  band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
+  band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
+  band_solve<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv, c->Ll, S.rhs, S.dx);
+  norms_kernel<<<1, 1024, 0, st>>>(c->nX, S.dx, c->Ll, S.red);
+  MG_CUDA(cudaGetLastError());
+  return MGPU_OK;
+}
+}  // namespace mgpu
+
+extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double* times, double t0, int32_t nXder0,
+                           const double* x0, const double* u, const double* tvals, const mgpu_sweep_opts* opts,
+                           double* states, mgpu_stats* stats) {
+  if (!c || !times || !opts || !states || !stats || !(OX == 0 || OX == 2) || nstep < 0 || nXder0 < 0 ||
+      nXder0 > OX + 1 || (nXder0 > 0 && !x0))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_sweepx: bad arguments");
+  *stats = mgpu_stats{0, 0, 0, 0, 0.0, 0.0};
+  Solver& S = *c->solver;
+  if (!S.ok) return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why);
+  MG_CUDA(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  const int64_t n = c->nX;
+  // initial state
+  MG_CUDA(cudaMemsetAsync(c->x, 0, 3 * n * sizeof(double), st));
+  if (nXder0 > 0) MG_CUDA(cudaMemcpyAsync(c->x, x0, nXder0 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (c->nU > 0 && u) MG_CUDA(cudaMemcpyAsync(c->u, u, c->nU * sizeof(double), cudaMemcpyHostToDevice, st));
+  c->nXder_resident = OX + 1;
+  const int nder = OX + 1;
+  const double cdx2 = opts->maxdx * opts->maxdx, cLl2 = opts->maxLl * opts->maxLl;
+  double told = t0;
+  for (int64_t step = 0; step < nstep; ++step) {
+    const double t = times[step];
+    const double dt = t - told;
+    told = t;
+    if (OX > 0 && !(dt > 0)) {
+      stats->fail_step = int(step + 1);
+      char msg[128];
+      snprintf(msg, sizeof msg, "Time step length not strictly positive at step=%3d", int(step + 1));
+      return set_err(c, MGPU_ERR_ARG, msg);
+    }
+    mgpu_newmark nm{0, 0, 0, 0, 0, 0};
+    if (OX == 2) {
+      const double be = opts->beta, ga = opts->gamma;
+      nm = mgpu_newmark{ga / (be * dt), ga / be, (ga / (2 * be) - 1) * dt, 1 / (be * dt * dt), 1 / (be * dt),
+                        1 / (2 * be)};
+    }
+    if (c->ntval > 0)
+      MG_CUDA(cudaMemcpyAsync(c->tv, tvals + step * c->ntval, c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
+    bool conv = false;
+    for (int it = 1; it <= opts->maxiter; ++it) {
+      stats->niter_total++;
+      const int first = it == 1;
+      const int mission = OX == 0 ? MGPU_ASM_STATIC : (first ? MGPU_ASM_STEP : MGPU_ASM_ITER);
+      const int v = INT_MAX;
+      MG_CUDA(cudaMemcpyAsync(c->errflag, &v, sizeof(int), cudaMemcpyHostToDevice, st));
+      MG_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
+      int rc = launch_assembly(c, mission, t, &nm, nullptr);
+      if (rc) return rc;
+      rc = factor_solve(c);
+      if (rc) return rc;
+      decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, first, S.dx, c->scale, nm.a1, nm.a2, nm.a3, nm.b1, nm.b2,
+                                                    nm.b3, c->x);
+      MG_CUDA(cudaMemcpyAsync(S.hbuf, S.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      MG_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(S.hbuf + 2), S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      MG_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(S.hbuf + 3), c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      MG_CUDA(cudaStreamSynchronize(st));
+      const double dx2 = S.hbuf[0], Ll2 = S.hbuf[1];
+      const int info = *reinterpret_cast<int*>(S.hbuf + 2);
+      stats->last_dx = std::sqrt(dx2);
+      stats->last_Ll = std::sqrt(Ll2);
+      if (*reinterpret_cast<int*>(S.hbuf + 3) != INT_MAX) {
+        stats->fail_step = int(step + 1);
+        stats->fail_iter = it;
+        return check_nan(c);
+      }
+      if (info != 0) {
+        stats->fail_step = int(step + 1);
+        stats->fail_iter = it;
+        char msg[128];
+        snprintf(msg, sizeof msg, "matrix factorization failed at step=%d, iiter=%d", int(step + 1), it);
+        return set_err(c, MGPU_ERR_SINGULAR, msg);
+      }
+      if (dx2 <= cdx2 && Ll2 <= cLl2) {
+        conv = true;
+        break;
+      }
+      if (it == opts->maxiter) {
+        stats->fail_step = int(step + 1);
+        stats->fail_iter = it;
+        char msg[256];
+        snprintf(msg, sizeof msg, "no convergence of step %3d after %3d iterations |Δx|=%g / %g, |Lλ|=%g / %g",
+                 int(step + 1), it, std::sqrt(dx2), opts->maxdx, Ll2, opts->maxLl);
+        return set_err(c, MGPU_ERR_NOCONV, msg);
+      }
+    }
+    (void)conv;
+    MG_CUDA(cudaMemcpyAsync(states + step * nder * n, c->x, nder * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaStreamSynchronize(st));
+    stats->nstep_done = int(step + 1);
+  }
+  return MGPU_OK;
+}

@@ -1,0 +1,172 @@
+"""Device model: the Python side of the C-ABI (include/muscade_gpu.h).
+
+Builds the `mgpu_model_desc` from a `Model` and its `Disassembler` exactly as
+the Julia side would (per element type: kind, dof indices `index.X`/`index.U`,
+element fields), and wraps the entry points.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib as L
+from .elements import Bar3D, DofConstraint, DofLoad, EulerBeam3D, Hold, group_time_values
+from .model import MuscadeError
+
+
+def _kind(g):
+    k = g.key[0]
+    return {"EulerBeam3D": L.EULERBEAM3D, "Bar3D": L.BAR3D, "DofConstraint": L.DOFCONSTRAINT_X,
+            "DofLoad": L.DOFLOAD}.get(k)
+
+
+class DeviceError(MuscadeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+        self.kind = L.ERRORS.get(code, "unknown")
+
+
+class DeviceModel:
+    """One mgpu_ctx for a model (owns device memory and a CUDA stream)."""
+
+    def __init__(self, model, dis, device: int = 0):
+        self.lib = L.load()
+        self.model, self.dis = model, dis
+        self.nX, self.nU = model.ndof["X"], model.ndof["U"]
+        self._keep = []
+        groups = (L.Group * max(len(model.groups), 1))()
+        for ig, (g, dg) in enumerate(zip(model.groups, dis.dis)):
+            kind = _kind(g)
+            if kind is None:
+                raise DeviceError(3, f"element type {g.key[0]} is not supported by the GPU path")
+            iX = np.ascontiguousarray(dg.index_X, dtype=np.int64)
+            iU = np.ascontiguousarray(dg.index_U, dtype=np.int64)
+            if kind in (L.EULERBEAM3D, L.BAR3D):
+                ed = np.ascontiguousarray(g.cat("ele"), dtype=np.float64)
+            elif kind == L.DOFCONSTRAINT_X:
+                ed = np.ascontiguousarray(g.cat("coeffs"), dtype=np.float64)
+            else:
+                ed = np.zeros((g.nele, 0))
+            self._keep += [iX, iU, ed]
+            G = groups[ig]
+            G.kind, G.nX, G.nU = kind, iX.shape[1], iU.shape[1] if iU.ndim == 2 else 0
+            G.ndata = ed.shape[1] if ed.ndim == 2 else 0
+            G.nele = g.nele
+            G.indexX = L.ptr(iX, ctypes.c_int64)
+            G.indexU = L.ptr(iU, ctypes.c_int64) if G.nU else None
+            G.edata = L.ptr(ed) if G.ndata else None
+        self._groups = groups
+        sc = np.ascontiguousarray(dis.scaleX, dtype=np.float64)
+        self._keep.append(sc)
+        desc = L.ModelDesc(self.nX, self.nU, len(model.groups), groups, L.ptr(sc), device)
+        self.ctx = ctypes.c_void_p()
+        rc = self.lib.mgpu_create(ctypes.byref(self.ctx), ctypes.byref(desc))
+        self._check(rc)
+        self.nnz = int(self.lib.mgpu_nnz(self.ctx))
+        self.ntval = int(self.lib.mgpu_ntval(self.ctx))
+
+    # ---------------------------------------------------------------- basics
+    def _check(self, rc):
+        if rc != L.MGPU_OK:
+            msg = self.lib.mgpu_last_error(self.ctx).decode(errors="replace") if self.ctx else "mgpu_create failed"
+            raise DeviceError(rc, msg)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.mgpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pattern(self):
+        colptr = np.zeros(self.nX + 1, dtype=np.int64)
+        rowval = np.zeros(self.nnz, dtype=np.int64)
+        self._check(self.lib.mgpu_get_pattern(self.ctx, L.ptr(colptr, ctypes.c_int64), L.ptr(rowval, ctypes.c_int64)))
+        return colptr, rowval
+
+    def asm(self, ig):
+        dg = self.dis.dis[ig]
+        nele, nX = dg.index_X.shape
+        a1 = np.zeros((nele, nX), dtype=np.int64)
+        a2 = np.zeros((nele, nX * nX), dtype=np.int64)
+        self._check(self.lib.mgpu_get_asm(self.ctx, ig, L.ptr(a1, ctypes.c_int64), L.ptr(a2, ctypes.c_int64)))
+        return a1, a2
+
+    def tvals(self, t):
+        """Host evaluation of the time functions (DofLoad F(t), constraint offsets c(t))."""
+        out = []
+        for g in self.model.groups:
+            if g.key[0] == "DofLoad":
+                out.append(group_time_values(g, "value", t))
+            elif g.key[0] == "DofConstraint":
+                out.append(group_time_values(g, "offset", t))
+        return np.ascontiguousarray(np.concatenate(out) if out else np.zeros(0))
+
+    # ---------------------------------------------------------------- assembly
+    def assemble(self, X, U=None, t=0.0, mission=L.ASM_STATIC, c=None, want=(True, True)):
+        X = [np.ascontiguousarray(x, dtype=np.float64) for x in X]
+        nXder = len(X)
+        x = np.ascontiguousarray(np.concatenate(X))
+        u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
+        tv = self.tvals(t)
+        nm = L.Newmark(**(c or {})) if c else L.Newmark()
+        Ll = np.zeros(self.nX) if want[0] else None
+        nz = np.zeros(self.nnz) if want[1] else None
+        rc = self.lib.mgpu_assemble(self.ctx, mission, nXder, L.ptr(x), L.ptr(u), float(t), L.ptr(tv),
+                                    ctypes.byref(nm), L.ptr(Ll), L.ptr(nz))
+        self._check(rc)
+        return Ll, nz
+
+    def element_eval(self, ig, X, U=None, t=0.0, p=(1.0, 0.0, 0.0)):
+        """diffed_residual-like evaluation of all elements of group ig.
+        X: (nele, nXder, nX).  Returns R (nele,nX), dR (nele,nX,nX) [i,j], dRdU (nele,nX,3) or None."""
+        X = np.ascontiguousarray(X, dtype=np.float64)
+        nele, nXder, nX = X.shape
+        R = np.zeros((nele, nX))
+        dR = np.zeros((nele, nX * nX))
+        Uc = None if U is None else np.ascontiguousarray(U, dtype=np.float64)
+        H = np.zeros((nele, nX * 3)) if U is not None else None
+        rc = self.lib.mgpu_element_eval(self.ctx, ig, nXder, L.ptr(X), L.ptr(Uc), float(t), p[0], p[1], p[2],
+                                        L.ptr(R), L.ptr(dR), L.ptr(H))
+        self._check(rc)
+        dR = dR.reshape(nele, nX, nX).transpose(0, 2, 1)  # column-major per element -> [i, j]
+        if H is not None:
+            H = H.reshape(nele, 3, nX).transpose(0, 2, 1)
+        return R, dR, H
+
+    def upload_state(self, X, U=None, t=0.0):
+        x = np.ascontiguousarray(np.concatenate([np.asarray(v, dtype=np.float64) for v in X]))
+        u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
+        tv = self.tvals(t)
+        self._check(self.lib.mgpu_upload_state(self.ctx, len(X), L.ptr(x), L.ptr(u), L.ptr(tv)))
+
+    def time_assemble(self, mission=L.ASM_STATIC, t=0.0, c=None, reps=10, flush_l2=True):
+        """Mean device times (ms) of `reps` resident assemblies: total, per element type, scatter."""
+        nm = L.Newmark(**(c or {})) if c else L.Newmark()
+        tt, ts = ctypes.c_double(), ctypes.c_double()
+        tg = np.zeros(max(len(self.model.groups), 1))
+        self._check(self.lib.mgpu_time_assemble(self.ctx, mission, float(t), ctypes.byref(nm), reps, int(flush_l2),
+                                                ctypes.byref(tt), L.ptr(tg), ctypes.byref(ts)))
+        return tt.value, tg[: len(self.model.groups)], ts.value
+
+    # ---------------------------------------------------------------- solver
+    def sweepx(self, OX, times, t0, X0, U=None, beta=0.25, gamma=0.5, maxiter=50, maxdx=1e-5, maxLl=math.inf):
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        nstep = len(times)
+        X0 = [np.asarray(v, dtype=np.float64) for v in X0][: OX + 1]
+        x0 = np.ascontiguousarray(np.concatenate(X0)) if X0 else np.zeros(0)
+        u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
+        tv = np.ascontiguousarray(np.stack([self.tvals(t) for t in times]) if self.ntval else np.zeros((nstep, 0)))
+        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl)
+        states = np.zeros((nstep, OX + 1, self.nX))
+        stats = L.Stats()
+        rc = self.lib.mgpu_sweepx(self.ctx, OX, nstep, L.ptr(times), float(t0), len(X0), L.ptr(x0), L.ptr(u),
+                                  L.ptr(tv), ctypes.byref(opts), L.ptr(states), ctypes.byref(stats))
+        return rc, states, stats

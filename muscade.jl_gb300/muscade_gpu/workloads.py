@@ -1,0 +1,118 @@
+"""Synthetic models of the benchmark configurations (seeded, reproducible).
+
+* cantilever(): 10 m beam of 20 EulerBeam3D along x, clamped with six Hold at
+  node 1, tip DofLoad in t3 ramping to 1e3 N, SweepX{0} over 10 load steps.
+* lattice(nx, ny, nz): 3D frame of EulerBeam3D on all edges of a 1 m grid,
+  section properties lognormal (σ=0.1) around the cantilever's, all six dofs
+  held on the z=0 layer, Gaussian (σ=100 N) DofLoads on every free
+  translation ramped by t.  60×60×20 gives 210,000 beams.
+* risers(nriser, nel): independent vertical risers of 1000 m, pinned at the
+  bottom (Hold t1,t2,t3,r1) and driven at the top by DofConstraints
+  t1 = A sin(2πt/T), t2 = 0, t3 = 0.1 m (pretension), A~U(1,5), T~U(8,15).
+
+Random streams use numpy PCG64 with seed 2026 + configuration index.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .elements import BeamCrossSection, DofConstraint, DofLoad, EulerBeam3D, Hold
+from .model import Model
+
+EA0, EI0, GJ0, MU0, IOTA0 = 1e8, 1e4, 1e4, 10.0, 1.0
+
+
+def cantilever(nel=20, length=10.0, load=1e3):
+    m = Model("cantilever")
+    xs = np.linspace(0.0, length, nel + 1)
+    nodes = m.addnode(np.stack([xs, np.zeros_like(xs), np.zeros_like(xs)], axis=1))
+    mat = BeamCrossSection(EA=EA0, EI2=EI0, EI3=EI0, GJ=GJ0, mu=MU0, iota1=IOTA0)
+    m.addelement(EulerBeam3D, np.stack([nodes[:-1], nodes[1:]], axis=1), mat=mat, orient2=(0.0, 1.0, 0.0))
+    for f in ("t1", "t2", "t3", "r1", "r2", "r3"):
+        m.addelement(Hold, [nodes[0]], field=f)
+
+    def tipload(t):
+        return load * t
+
+    m.addelement(DofLoad, [nodes[-1]], field="t3", value=tipload)
+    return m, np.round(np.arange(1, 11) * 0.1, 12)
+
+
+def lattice(nx=60, ny=60, nz=20, seed=2027, sigma=0.1, load_std=100.0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = Model("lattice")
+    I, J, K = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    nid = np.zeros((nx, ny, nz), dtype=np.int64)
+    coords = np.stack([I.ravel(order="F"), J.ravel(order="F"), K.ravel(order="F")], axis=1).astype(np.float64)
+    ids = m.addnode(coords)
+    nid[I.ravel(order="F"), J.ravel(order="F"), K.ravel(order="F")] = ids
+    edges = []
+    orients = []
+    # x-, y- and z-edges; orient2 chosen so that no as-meshed frame is a half turn
+    e = np.stack([nid[:-1, :, :].ravel(order="F"), nid[1:, :, :].ravel(order="F")], axis=1)
+    edges.append(e)
+    orients.append((0.0, 1.0, 0.0))
+    e = np.stack([nid[:, :-1, :].ravel(order="F"), nid[:, 1:, :].ravel(order="F")], axis=1)
+    edges.append(e)
+    orients.append((0.0, 0.0, 1.0))
+    e = np.stack([nid[:, :, :-1].ravel(order="F"), nid[:, :, 1:].ravel(order="F")], axis=1)
+    edges.append(e)
+    orients.append((1.0, 0.0, 0.0))
+    nbeam = sum(len(e) for e in edges)
+    ln = lambda: np.exp(rng.normal(0.0, sigma, nbeam))  # noqa: E731
+    EA, EI2, EI3, GJ = EA0 * ln(), EI0 * ln(), EI0 * ln(), GJ0 * ln()
+    p = 0
+    for e, o in zip(edges, orients):
+        sl = slice(p, p + len(e))
+        mat = BeamCrossSection(EA=EA[sl], EI2=EI2[sl], EI3=EI3[sl], GJ=GJ[sl], mu=MU0, iota1=IOTA0)
+        m.addelement(EulerBeam3D, e, mat=mat, orient2=o)
+        p += len(e)
+    base = nid[:, :, 0].ravel(order="F")
+    for f in ("t1", "t2", "t3", "r1", "r2", "r3"):
+        m.addelement(Hold, base[:, None], field=f)
+    free = nid[:, :, 1:].ravel(order="F")
+    for f in ("t1", "t2", "t3"):
+        F = rng.normal(0.0, load_std, len(free))
+
+        def ramp(t, F=F):
+            return F * t
+
+        m.addelement(DofLoad, free[:, None], field=f, value=ramp)
+    return m, np.round(np.arange(1, 6) * 0.2, 12)
+
+
+def risers(nriser=200, nel=250, length=1000.0, seed=2028, EA=5e9, EI=1e6, GJ=1e6, mu=300.0, iota1=10.0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    A = rng.uniform(1.0, 5.0, nriser)
+    T = rng.uniform(8.0, 15.0, nriser)
+    m = Model("risers")
+    mat = BeamCrossSection(EA=EA, EI2=EI, EI3=EI, GJ=GJ, mu=mu, iota1=iota1)
+    zs = np.linspace(0.0, length, nel + 1)
+    bottoms, tops = [], []
+    for r in range(nriser):
+        x0 = 50.0 * (r % 20)
+        y0 = 50.0 * (r // 20)
+        nodes = m.addnode(np.stack([np.full_like(zs, x0), np.full_like(zs, y0), zs], axis=1))
+        m.addelement(EulerBeam3D, np.stack([nodes[:-1], nodes[1:]], axis=1), mat=mat, orient2=(1.0, 0.0, 0.0))
+        bottoms.append(nodes[0])
+        tops.append(nodes[-1])
+    bottoms = np.asarray(bottoms)[:, None]
+    tops = np.asarray(tops)[:, None]
+    for f in ("t1", "t2", "t3", "r1"):
+        m.addelement(Hold, bottoms, field=f)
+
+    def surge(t):
+        return A * np.sin(2 * math.pi * t / T)
+
+    def zero(t):
+        return 0.0
+
+    def lift(t):
+        return 0.1
+
+    m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t1",), lfield="λtop1", coeffs=[1.0], offset=surge, name="surge")
+    m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t2",), lfield="λtop2", coeffs=[1.0], offset=zero, name="sway")
+    m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t3",), lfield="λtop3", coeffs=[1.0], offset=lift, name="lift")
+    return m, 0.05 * np.arange(1, 2001)

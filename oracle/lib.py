@@ -25,7 +25,7 @@ def build(force: bool = False) -> str:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(s) <= t for s in SRC):
             return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-shared", "-fPIC", "-o", LIB + ".tmp", SRC[0]]
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-shared", "-fPIC", "-o", LIB + ".tmp", SRC[0]]
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB

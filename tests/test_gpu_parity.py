@@ -1,0 +1,219 @@
+"""Parity of the CUDA path with the oracle (GPU).
+
+Tolerances (written where used):
+  * element residuals and tangents: max |gpu − oracle| ≤ 1e-12 · max |oracle|
+    per element array (norm-relative, FP64);
+  * CSC pattern and asm maps: bit-exact;
+  * assembled Lλ and Lλx.nzval: ≤ 1e-12 relative to the largest entry;
+  * converged states: ≤ 1e-9 relative (‖Δ‖∞ / ‖x‖∞).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from muscade_gpu import _lib
+from muscade_gpu import workloads as W
+from muscade_gpu.device import DeviceError, DeviceModel
+from muscade_gpu.elements import AxisymmetricBarCrossSection, Bar3D, BeamCrossSection, DofLoad, EulerBeam3D, Hold
+from muscade_gpu.model import Model
+from oracle import lib as O
+from oracle import reference as REF
+
+pytestmark = pytest.mark.gpu
+TOL_ELE = 1e-12
+TOL_ASM = 1e-12
+TOL_STATE = 1e-9
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    _lib.build()
+    O.build()
+
+
+def relerr(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def random_beams(n, seed, udof=False, rot=0.5):
+    rng = np.random.default_rng(seed)
+    m = Model()
+    c1 = rng.normal(size=(n, 3))
+    c2 = c1 + rng.normal(size=(n, 3)) * 2
+    ids1 = m.addnode(c1)
+    ids2 = m.addnode(c2)
+    mat = BeamCrossSection(EA=1e3 * rng.uniform(1, 2, n), EI2=3 * rng.uniform(1, 2, n), EI3=2 * rng.uniform(1, 2, n),
+                           GJ=4 * rng.uniform(1, 2, n), mu=1.3, iota1=2.1, w=0.7, Ca1=0.3, Cl1=0.2, Cq1=0.1, Ca2=0.5,
+                           Cl2=0.4, Cq2=0.3, Ca3=0.6, Cl3=0.7, Cq3=0.8)
+    o2 = rng.normal(size=(n, 3))
+    if udof:
+        ids3 = m.addnode(np.zeros((n, 3)))
+        m.addelement(EulerBeam3D, np.stack([ids1, ids2, ids3], axis=1), mat=mat, orient2=o2, udof=True)
+    else:
+        m.addelement(EulerBeam3D, np.stack([ids1, ids2], axis=1), mat=mat, orient2=o2)
+    X = rng.normal(size=(n, 3, 12)) * 0.1
+    X[:, 0, [3, 4, 5, 9, 10, 11]] = rng.normal(size=(n, 6)) * rot
+    X[: n // 5, 0, 3:6] = 0.0  # exactly unrotated node 1 (norm3 zero branch)
+    X[:, 1:, :] = rng.normal(size=(n, 2, 12)) * 0.5
+    U = rng.normal(size=(n, 3)) if udof else None
+    return m, X, U
+
+
+@pytest.mark.parametrize("udof", [False, True])
+def test_beam_element_parity(udof):
+    m, X, U = random_beams(64, 11 + udof, udof=udof)
+    dm = DeviceModel(m, m.initialize().dis)
+    ele = m.groups[0].cat("ele")
+    # static (SweepX{0} form): K = ∂R/∂X₀
+    d = O.diffed("beam", ele, X[:, :1, :], U)
+    R, K, H = dm.element_eval(0, X[:, :1, :], U)
+    for e in range(len(X)):
+        assert relerr(R[e], d["R"][e]) <= TOL_ELE
+        assert relerr(K[e], d["K"][e]) <= TOL_ELE
+        if udof:
+            assert relerr(H[e], d["H"][e]) <= TOL_ELE
+    # dynamic: K, C, M from unit perturbations
+    d = O.diffed("beam", ele, X, U)
+    for p, name in (((1, 0, 0), "K"), ((0, 1, 0), "C"), ((0, 0, 1), "M")):
+        R, J, _ = dm.element_eval(0, X, U, p=p)
+        for e in range(len(X)):
+            assert relerr(R[e], d["R"][e]) <= TOL_ELE
+            assert relerr(J[e], d[name][e]) <= TOL_ELE, (name, e)
+    dm.close()
+
+
+def test_bar_element_parity():
+    rng = np.random.default_rng(5)
+    n = 32
+    m = Model()
+    c1 = rng.normal(size=(n, 3))
+    ids1 = m.addnode(c1)
+    ids2 = m.addnode(c1 + rng.normal(size=(n, 3)))
+    mat = AxisymmetricBarCrossSection(EA=10.0, mu=1.0, w=2.0, Cat=0.2, Clt=0.3, Cqt=0.4, Can=0.5, Cln=0.6, Cqn=0.7)
+    m.addelement(Bar3D, np.stack([ids1, ids2], axis=1), mat=mat)
+    dm = DeviceModel(m, m.initialize().dis)
+    X = rng.normal(size=(n, 3, 6)) * 0.3
+    d = O.diffed("bar", m.groups[0].cat("ele"), X, t=-7.0)
+    for p, name in (((1, 0, 0), "K"), ((0, 1, 0), "C"), ((0, 0, 1), "M")):
+        R, J, _ = dm.element_eval(0, X, t=-7.0, p=p)
+        for e in range(n):
+            assert relerr(R[e], d["R"][e]) <= TOL_ELE
+            assert relerr(J[e], d[name][e]) <= TOL_ELE, (name, e)
+    dm.close()
+
+
+def _models():
+    yield "cantilever", W.cantilever()[0]
+    yield "lattice", W.lattice(7, 6, 4)[0]
+    yield "risers", W.risers(nriser=3, nel=12)[0]
+
+
+@pytest.mark.parametrize("name,model", list(_models()))
+def test_pattern_and_asm_bit_exact(name, model):
+    dis = model.initialize().dis
+    dm = DeviceModel(model, dis)
+    prep = REF.Prepared(model, dis)
+    colptr, rowval = dm.pattern()
+    assert dm.nnz == prep.nnz
+    assert np.array_equal(colptr, prep.colptr) and np.array_equal(rowval, prep.rowval)
+    for ig in range(len(model.groups)):
+        a1, a2 = dm.asm(ig)
+        assert np.array_equal(a1, prep.asm1[ig]) and np.array_equal(a2, prep.asm2[ig])
+    dm.close()
+
+
+def _state(model, seed, nder, amp=0.05):
+    rng = np.random.default_rng(seed)
+    n = model.ndof["X"]
+    return [rng.normal(size=n) * amp for _ in range(nder)]
+
+
+@pytest.mark.parametrize("name,model", list(_models()))
+def test_assembly_parity(name, model):
+    st = model.initialize()
+    dm = DeviceModel(model, st.dis)
+    prep = REF.Prepared(model, st.dis)
+    U = (np.zeros(model.ndof["U"]),)
+    X = _state(model, 7, 1)
+    Ll, nz = dm.assemble(X, t=0.4)
+    Lr, nr = REF.assemble(prep, tuple(X), U, 0.4, "static", REF.newmark_coefficients(0, 1, 0.25, 0.5))
+    assert relerr(Ll, Lr) <= TOL_ASM and relerr(nz, nr) <= TOL_ASM
+    # determinism: bitwise identical on repeat
+    Ll2, nz2 = dm.assemble(X, t=0.4)
+    assert np.array_equal(Ll, Ll2) and np.array_equal(nz, nz2)
+    # Newmark forms
+    X3 = _state(model, 8, 3)
+    c = REF.newmark_coefficients(2, 0.05, 0.25, 0.5)
+    for mission, mref in ((_lib.ASM_STEP, "step"), (_lib.ASM_ITER, "iter")):
+        Ll, nz = dm.assemble(X3, t=0.35, mission=mission, c=c)
+        Lr, nr = REF.assemble(prep, tuple(X3), U, 0.35, mref, c)
+        assert relerr(Ll, Lr) <= TOL_ASM, mref
+        assert relerr(nz, nr) <= TOL_ASM, mref
+    dm.close()
+
+
+def _compare_states(gpu_states, ref, nder):
+    assert len(gpu_states) == len(ref)
+    for s, (t, Xr) in zip(gpu_states, ref):
+        for d in range(nder):
+            x = s.X[d]
+            scale = max(np.max(np.abs(Xr[d])), 1e-300)
+            assert np.max(np.abs(x - Xr[d])) / scale <= TOL_STATE, (t, d)
+
+
+def test_sweepx0_cantilever_matches_oracle():
+    from muscade_gpu import SweepXGPU, solve
+
+    m, times = W.cantilever()
+    st = m.initialize()
+    out = solve(SweepXGPU[0], st, times, maxdx=1e-9, maxLl=1e-5)
+    ref = REF.sweepx(m, st.dis, st, times, OX=0, maxdx=1e-9, maxLl=1e-5)
+    _compare_states(out, ref, 1)
+    tip = out[-1].X[0][120:123]
+    assert tip[2] > 5.0  # large-rotation equilibrium: the tip has risen well above a linear answer's scale
+
+
+def test_sweepx0_lattice_matches_oracle():
+    from muscade_gpu import SweepXGPU, solve
+
+    m, times = W.lattice(8, 7, 5)
+    st = m.initialize()
+    out = solve(SweepXGPU[0], st, times[:2], maxdx=1e-8, maxLl=1e-3)
+    ref = REF.sweepx(m, st.dis, st, times[:2], OX=0, maxdx=1e-8, maxLl=1e-3)
+    _compare_states(out, ref, 1)
+
+
+def test_sweepx2_risers_match_oracle():
+    from muscade_gpu import SweepXGPU, solve
+
+    m, times = W.risers(nriser=2, nel=20)
+    st = m.initialize(time=0.0)
+    T = times[:20]
+    out = solve(SweepXGPU[2], st, T, maxiter=20, maxdx=1e-5, maxLl=math.inf)
+    ref = REF.sweepx(m, st.dis, st, T, OX=2, maxiter=20, maxdx=1e-5, maxLl=math.inf)
+    _compare_states(out, ref, 3)
+
+
+def test_nan_is_reported_like_the_reference():
+    m, _ = W.cantilever()
+    st = m.initialize()
+    dm = DeviceModel(m, st.dis)
+    x = np.zeros(m.ndof["X"])
+    x[7] = np.nan
+    with pytest.raises(DeviceError) as e:
+        dm.assemble([x])
+    assert e.value.kind == "nan" and "returned NaN" in str(e.value)
+    dm.close()
+
+
+def test_singular_matrix_is_reported():
+    from muscade_gpu import SweepXGPU, solve
+
+    m = Model()
+    a = m.addnode([0.0, 0.0, 0.0])
+    m.addelement(DofLoad, [a], field="t3", value=lambda t: 1.0)  # a dof without stiffness: Lλx = [0]
+    st = m.initialize()
+    with pytest.raises(DeviceError) as e:
+        solve(SweepXGPU[0], st, [1.0])
+    assert e.value.kind == "singular" and "matrix factorization failed at step=1, iiter=1" in str(e.value)
