@@ -28,63 +28,63 @@ namespace mgpu {
 
 // ---- special functions (toolbox/Rotations.jl) -------------------------------
 // sinc1(x)=sin(x)/x and its derivatives with the reference's branch points.
-MG_HD double sinc1_0(double x) {
-  const double y = x * 0.31830988618379067154;  // x/π (Base.sinc of x/π)
+MG_HD real sinc1_0(real x) {
+  const real y = x * 0.31830988618379067154;  // x/π (Base.sinc of x/π)
   if (fabs(y) < 1e-3) {
-    const double p2 = 9.8696044010893586188;  // π²
-    const double y2 = y * y;
+    const real p2 = 9.8696044010893586188;  // π²
+    const real y2 = y * y;
     return 1.0 + y2 * (-p2 / 6.0 + y2 * (p2 * p2 / 120.0));
   }
   return sin(x) / x;
 }
-MG_HD double sinc1_1(double x) {
+MG_HD real sinc1_1(real x) {
   if (fabs(x) > 1e-3) {
-    double s, c;
+    real s, c;
     sincos(x, &s, &c);
     return c / x - s / (x * x);
   }
-  const double x2 = x * x;
+  const real x2 = x * x;
   return x * (-1.0 / 3.0 + x2 / 30.0);
 }
-MG_HD double sinc1_2(double x) {
+MG_HD real sinc1_2(real x) {
   if (fabs(x) > 1e-1) {
-    double s, c;
+    real s, c;
     sincos(x, &s, &c);
     return -s / x - 2.0 * c / (x * x) + 2.0 * s / (x * x * x);
   }
-  const double x2 = x * x;
+  const real x2 = x * x;
   return -1.0 / 3.0 + x2 * (1.0 / 10.0 + x2 * (-1.0 / 168.0 + x2 * (1.0 / 6480.0)));
 }
-MG_HD double sinc1_3(double x) {
+MG_HD real sinc1_3(real x) {
   if (fabs(x) > 0.4) {
-    double s, c;
+    real s, c;
     sincos(x, &s, &c);
-    const double x2 = x * x;
+    const real x2 = x * x;
     return -c / x + 3.0 * s / x2 + 6.0 * c / (x2 * x) - 6.0 * s / (x2 * x2);
   }
-  const double x2 = x * x;
+  const real x2 = x * x;
   return x * (1.0 / 5.0 + x2 * (-1.0 / 42.0 + x2 * (1.0 / 1080.0 + x2 * (-1.0 / 55440.0 + x2 * (1.0 / 4717440.0)))));
 }
 
 // scac(x) = sinc1(acos x) with the reference's degree-5 Taylor branch near 1;
 // f[0..3] = value and first three derivatives.
-MG_HD void scac_derivs(double x, double f[4]) {
-  const double dx = x - 1.0;
+MG_HD void scac_derivs(real x, real f[4]) {
+  const real dx = x - 1.0;
   if (fabs(dx) > 1e-3) {
-    const double th = acos(x);
-    const double q = 1.0 - x * x;
-    const double sq = sqrt(q);
-    const double t1 = -1.0 / sq;
-    const double t2 = -x / (q * sq);
-    const double t3 = -(1.0 + 2.0 * x * x) / (q * q * sq);
-    const double s0 = sinc1_0(th), s1 = sinc1_1(th), s2 = sinc1_2(th), s3 = sinc1_3(th);
+    const real th = acos(x);
+    const real q = 1.0 - x * x;
+    const real sq = sqrt(q);
+    const real t1 = -1.0 / sq;
+    const real t2 = -x / (q * sq);
+    const real t3 = -(1.0 + 2.0 * x * x) / (q * q * sq);
+    const real s0 = sinc1_0(th), s1 = sinc1_1(th), s2 = sinc1_2(th), s3 = sinc1_3(th);
     f[0] = s0;
     f[1] = s1 * t1;
     f[2] = s2 * t1 * t1 + s1 * t2;
     f[3] = s3 * t1 * t1 * t1 + 3.0 * s2 * t1 * t2 + s1 * t3;
     return;
   }
-  const double c1 = 1.0 / 3.0, c2 = -2.0 / 90.0, c3 = 0.0052911879917544626, c4 = -0.0016229317117234072, c5 = 0.0005625;
+  const real c1 = 1.0 / 3.0, c2 = -2.0 / 90.0, c3 = 0.0052911879917544626, c4 = -0.0016229317117234072, c5 = 0.0005625;
   f[0] = 1.0 + dx * (c1 + dx * (c2 + dx * (c3 + dx * (c4 + dx * c5))));
   f[1] = c1 + dx * (2.0 * c2 + dx * (3.0 * c3 + dx * (4.0 * c4 + dx * (5.0 * c5))));
   f[2] = 2.0 * c2 + dx * (6.0 * c3 + dx * (12.0 * c4 + dx * (20.0 * c5)));
@@ -97,16 +97,16 @@ template <bool D>
 MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
   const TJ<D> s2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
   TJ<D> A, B;
-  const double th = sqrt(s2.v);
+  const real th = sqrt(s2.v);
   if (th < 1e-14) {  // norm3 returns an exact zero: sinc1 terms become constants
     A = tj_const<D>(1.0);
     B = tj_const<D>(0.5);
   } else {
-    const double r = 1.0 / th;
+    const real r = 1.0 / th;
     // θ = √s2
     const TJ<D> t = tj_apply(s2, th, 0.5 * r, -0.25 * r * r * r, 0.375 * r * r * r * r * r);
     A = tj_apply(t, sinc1_0(th), sinc1_1(th), sinc1_2(th), sinc1_3(th));
-    const double h = 0.5 * th;
+    const real h = 0.5 * th;
     const TJ<D> sh = tj_apply(t, sinc1_0(h), 0.5 * sinc1_1(h), 0.25 * sinc1_2(h), 0.125 * sinc1_3(h));
     B = (sh * sh) * 0.5;
   }
@@ -131,10 +131,10 @@ MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
 template <bool D>
 MG_HD void rodrigues_inv(const TJ<D> m[9], TJ<D> w[3]) {
   const TJ<D> c = (m[0] + m[4] + m[8] + (-1.0)) * 0.5;
-  double f[4];
+  real f[4];
   scac_derivs(c.v, f);
   const TJ<D> s = tj_apply(c, f[0], f[1], f[2], f[3]);
-  const double iv = 1.0 / s.v;
+  const real iv = 1.0 / s.v;
   const TJ<D> is = tj_apply(s, iv, -iv * iv, 2.0 * iv * iv * iv, -6.0 * iv * iv * iv * iv);
   w[0] = ((m[5] - m[7]) * 0.5) * is;  // (m32 - m23)/2
   w[1] = ((m[6] - m[2]) * 0.5) * is;  // (m13 - m31)/2
@@ -228,27 +228,27 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   const TJ<D>* b = rsm + 6;  // third column
 
   // ---- translations (d = ½(u₂−u₁)+½tgₘ enters linearly)
-  double d[3], dd1[3], dd2[3];
+  real d[3], dd1[3], dd2[3];
   for (int i = 0; i < 3; ++i) {
     d[i] = 0.5 * (X0[6 + i] - X0[i]) + 0.5 * c.tgm[i];
     dd1[i] = D ? 0.5 * (X1[6 + i] - X1[i]) : 0.0;
     dd2[i] = D ? 0.5 * (X2[6 + i] - X2[i]) : 0.0;
   }
-  const double dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-  const double dh[3] = {d[0] / dn, d[1] / dn, d[2] / dn};
-  const double eps = dn * 2.0 / c.L - 1.0;
+  const real dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const real dh[3] = {d[0] / dn, d[1] / dn, d[2] / dn};
+  const real eps = dn * 2.0 / c.L - 1.0;
 
   // ---- strain measures
   const TJ<D> th_t = dot3(t, dv), th_n = dot3(n, dv), th_b = dot3(b, dv);
   const TJ<D> w_n = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
   const TJ<D> w_b = b[0] * d[0] + b[1] * d[1] + b[2] * d[2];
   // frozen stresses σ = ∂Π/∂q
-  const double s_e = c.ke * eps;
-  const double s_t = c.kt * th_t.v;
-  const double s_wn = c.k3u * w_n.v + c.k3uv * th_b.v;
-  const double s_b = c.k3uv * w_n.v + c.k3v * th_b.v;
-  const double s_wb = c.k2u * w_b.v - c.k2uv * th_n.v;
-  const double s_n = -c.k2uv * w_b.v + c.k2v * th_n.v;
+  const real s_e = c.ke * eps;
+  const real s_t = c.kt * th_t.v;
+  const real s_wn = c.k3u * w_n.v + c.k3uv * th_b.v;
+  const real s_b = c.k3uv * w_n.v + c.k3v * th_b.v;
+  const real s_wb = c.k2u * w_b.v - c.k2uv * th_n.v;
+  const real s_n = -c.k2uv * w_b.v + c.k2v * th_n.v;
 
   // ---- Gauss point positions: x = yᵤ d + (yₐ−yᵤ) m + yᵥ w + ½(u₁+u₂) + cₘ
   TJ<D> dT[3];
@@ -267,11 +267,11 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   wv[2] = dv[0] * t[1] - dv[1] * t[0];
 
   // ---- loads per Gauss point (frozen) and their sums
-  double fg[4][3];
-  double r0[9];
+  real fg[4][3];
+  real r0[9];
   for (int k = 0; k < 9; ++k) r0[k] = rsm[k].v;
-  double xd[4][3], xdd[4][3];  // Gauss point velocity / acceleration
-  double vi21 = 0.0;
+  real xd[4][3], xdd[4][3];  // Gauss point velocity / acceleration
+  real vi21 = 0.0;
   TJ<D> vsm[3];
   const bool rotinertia = D && (c.iota1 != 0.0);
   for (int g = 0; g < 4; ++g) {
@@ -286,22 +286,22 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   }
   if constexpr (D) {
     for (int g = 0; g < 4; ++g) {
-      const double ya = c.ya[g], yu = c.yu[g], yv = c.yv[g];
+      const real ya = c.ya[g], yu = c.yu[g], yv = c.yv[g];
       for (int i = 0; i < 3; ++i) {
         // x = yu d + (ya-yu) m + yv w + c: time coefficients
-        const double c1 = 0.5 * (X1[i] + X1[6 + i]);
-        const double c2 = 0.5 * (X2[i] + X2[6 + i]);
+        const real c1 = 0.5 * (X1[i] + X1[6 + i]);
+        const real c2 = 0.5 * (X2[i] + X2[6 + i]);
         xd[g][i] = yu * dd1[i] + (ya - yu) * mv[i].vt + yv * wv[i].vt + c1;
         xdd[g][i] = yu * dd2[i] + 2.0 * ((ya - yu) * mv[i].vtt + yv * wv[i].vtt) + c2;
       }
-      double xl1[3], xl2[3];
+      real xl1[3], xl2[3];
       for (int k = 0; k < 3; ++k) {
         xl1[k] = r0[3 * k] * xd[g][0] + r0[3 * k + 1] * xd[g][1] + r0[3 * k + 2] * xd[g][2];
         xl2[k] = r0[3 * k] * xdd[g][0] + r0[3 * k + 1] * xdd[g][1] + r0[3 * k + 2] * xdd[g][2];
       }
-      double fl[3];
+      real fl[3];
       for (int k = 0; k < 3; ++k) {
-        double fq = c.Cq[k] * xl1[k] * xl1[k];
+        real fq = c.Cq[k] * xl1[k] * xl1[k];
         if (xl1[k] < 0.0) fq = -fq;
         fl[k] = c.Ca[k] * xl2[k] + c.Cl[k] * xl1[k] + fq;
       }
@@ -310,7 +310,7 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
     }
     if (rotinertia) {
       // vᵢ₂ = spin⁻¹(ṙᵀṙ + rᵀr̈);  the ṙᵀṙ part is symmetric and drops out
-      double ndd[3], bdd[3];
+      real ndd[3], bdd[3];
       for (int i = 0; i < 3; ++i) {
         ndd[i] = 2.0 * n[i].vtt;
         bdd[i] = 2.0 * b[i].vtt;
@@ -321,16 +321,16 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
     }
   }
   // sums over Gauss points (frozen loads)
-  double Au[3] = {0, 0, 0}, Aa[3] = {0, 0, 0}, Av[3] = {0, 0, 0}, A0[3] = {0, 0, 0};
+  real Au[3] = {0, 0, 0}, Aa[3] = {0, 0, 0}, Av[3] = {0, 0, 0}, A0[3] = {0, 0, 0};
   for (int g = 0; g < 4; ++g)
     for (int i = 0; i < 3; ++i) {
-      const double f = c.dL[g] * fg[g][i];
+      const real f = c.dL[g] * fg[g][i];
       Au[i] += c.yu[g] * f;
       Aa[i] += (c.ya[g] - c.yu[g]) * f;
       Av[i] += c.yv[g] * f;
       A0[i] += f;
     }
-  double me[3] = {0, 0, 0};
+  real me[3] = {0, 0, 0};
   if (rotinertia)
     for (int i = 0; i < 3; ++i) me[i] = c.S0 * c.iota1 * vi21 * r0[i];
 
@@ -347,47 +347,47 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
       P[i] = n[i] * s_wn + b[i] * s_wb + tAa * t[i] + (s_e * 2.0 / c.L * dh[i] + Au[i]);
     // residual
     for (int i = 0; i < 3; ++i) {
-      R[i] = -0.5 * P[i].v + 0.5 * A0[i];
-      R[6 + i] = 0.5 * P[i].v + 0.5 * A0[i];
-      R[3 + i] = Phi.g[i];
-      R[9 + i] = Phi.g[3 + i];
+      R[i] = to_d(-0.5 * P[i].v + 0.5 * A0[i]);
+      R[6 + i] = to_d(0.5 * P[i].v + 0.5 * A0[i]);
+      R[3 + i] = to_d(Phi.g[i]);
+      R[9 + i] = to_d(Phi.g[3 + i]);
     }
     // ---- tangent: geometric part ∇²Φ (frozen loads), scaled by p0
-    const double p0 = pt.p0;
+    const real p0 = pt.p0;
     for (int k = 0; k < 144; ++k) K[k] = 0.0;
     // rot-rot
     for (int i = 0; i < 6; ++i)
       for (int j = 0; j < 6; ++j) {
         const int a = i < 3 ? 3 + i : 6 + i, bb = j < 3 ? 3 + j : 6 + j;
-        K[a + 12 * bb] = p0 * Phi.h[i <= j ? hidx(i, j) : hidx(j, i)];
+        K[a + 12 * bb] = to_d(p0 * Phi.h[i <= j ? hidx(i, j) : hidx(j, i)]);
       }
     // rot-trans:  ∂²/∂v_j∂u₁ = −½ ∂P/∂v_j,  ∂²/∂v_j∂u₂ = +½ ∂P/∂v_j
     for (int j = 0; j < 6; ++j) {
       const int a = j < 3 ? 3 + j : 6 + j;
       for (int k = 0; k < 3; ++k) {
-        const double q = 0.5 * p0 * P[k].g[j];
-        K[a + 12 * k] -= q;
-        K[k + 12 * a] -= q;
-        K[a + 12 * (6 + k)] += q;
-        K[(6 + k) + 12 * a] += q;
+        const real q = 0.5 * p0 * P[k].g[j];
+        K[a + 12 * k] -= to_d(q);
+        K[k + 12 * a] -= to_d(q);
+        K[a + 12 * (6 + k)] += to_d(q);
+        K[(6 + k) + 12 * a] += to_d(q);
       }
     }
   }
   // trans-trans: σε ∂²ε/∂d² with ∂d/∂u₁ = −½, ∂d/∂u₂ = ½
   {
-    const double f = pt.p0 * s_e * (2.0 / c.L) / dn;
+    const real f = pt.p0 * s_e * (2.0 / c.L) / dn;
     for (int k = 0; k < 3; ++k)
       for (int l = 0; l < 3; ++l) {
-        const double h = f * ((k == l ? 1.0 : 0.0) - dh[k] * dh[l]) * 0.25;
-        K[k + 12 * l] += h;
-        K[(6 + k) + 12 * (6 + l)] += h;
-        K[k + 12 * (6 + l)] -= h;
-        K[(6 + k) + 12 * l] -= h;
+        const real h = f * ((k == l ? 1.0 : 0.0) - dh[k] * dh[l]) * 0.25;
+        K[k + 12 * l] += to_d(h);
+        K[(6 + k) + 12 * (6 + l)] += to_d(h);
+        K[k + 12 * (6 + l)] -= to_d(h);
+        K[(6 + k) + 12 * l] -= to_d(h);
       }
   }
   // ---- material part Gᵀ D G over q = (ε, θt, θn, θb, wn, wb)
   {
-    double G[6][12];
+    real G[6][12];
     for (int q = 0; q < 6; ++q)
       for (int j = 0; j < 12; ++j) G[q][j] = 0.0;
     for (int k = 0; k < 3; ++k) {
@@ -407,17 +407,17 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
       G[5][a] = w_b.g[j];
     }
     // DG rows
-    const double p0 = pt.p0;
+    const real p0 = pt.p0;
     for (int j = 0; j < 12; ++j) {
-      const double DG0 = c.ke * G[0][j];
-      const double DG1 = c.kt * G[1][j];
-      const double DG2 = c.k2v * G[2][j] - c.k2uv * G[5][j];
-      const double DG3 = c.k3v * G[3][j] + c.k3uv * G[4][j];
-      const double DG4 = c.k3uv * G[3][j] + c.k3u * G[4][j];
-      const double DG5 = -c.k2uv * G[2][j] + c.k2u * G[5][j];
+      const real DG0 = c.ke * G[0][j];
+      const real DG1 = c.kt * G[1][j];
+      const real DG2 = c.k2v * G[2][j] - c.k2uv * G[5][j];
+      const real DG3 = c.k3v * G[3][j] + c.k3uv * G[4][j];
+      const real DG4 = c.k3uv * G[3][j] + c.k3u * G[4][j];
+      const real DG5 = -c.k2uv * G[2][j] + c.k2u * G[5][j];
       for (int i = 0; i < 12; ++i)
-        K[i + 12 * j] += p0 * (G[0][i] * DG0 + G[1][i] * DG1 + G[2][i] * DG2 + G[3][i] * DG3 + G[4][i] * DG4 +
-                               G[5][i] * DG5);
+        K[i + 12 * j] += to_d(p0 * (G[0][i] * DG0 + G[1][i] * DG1 + G[2][i] * DG2 + G[3][i] * DG3 +
+                                    G[4][i] * DG4 + G[5][i] * DG5));
     }
   }
 
@@ -426,45 +426,45 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   if (!need_jx) return;
   // Jx_g: ∂x_g/∂X₀ (3x12):  rot: yu*0 + (ya-yu) m.g + yv w.g ; trans: s M_g + ½ I
   // M_g = yu I + (ya-yu) t tᵀ
-  const double tv[3] = {t[0].v, t[1].v, t[2].v};
+  const real tv[3] = {t[0].v, t[1].v, t[2].v};
   if (H) {
     for (int k = 0; k < 36; ++k) H[k] = 0.0;
   }
   // accumulate per Gauss point
   for (int g = 0; g < 4; ++g) {
-    const double ya = c.ya[g], yu = c.yu[g], yv = c.yv[g], yd = ya - yu, wq = c.dL[g];
-    double Jx[3][12];
+    const real ya = c.ya[g], yu = c.yu[g], yv = c.yv[g], yd = ya - yu, wq = c.dL[g];
+    real Jx[3][12];
     for (int i = 0; i < 3; ++i) {
       for (int j = 0; j < 6; ++j) {
         const int a = j < 3 ? 3 + j : 6 + j;
         Jx[i][a] = yd * mv[i].g[j] + yv * wv[i].g[j];
       }
       for (int k = 0; k < 3; ++k) {
-        const double M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
+        const real M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
         Jx[i][k] = -0.5 * M + (i == k ? 0.5 : 0.0);
         Jx[i][6 + k] = 0.5 * M + (i == k ? 0.5 : 0.0);
       }
     }
     if (H) {
       for (int k = 0; k < 3; ++k)
-        for (int a = 0; a < 12; ++a) H[a + 12 * k] -= wq * Jx[k][a];
+        for (int a = 0; a < 12; ++a) H[a + 12 * k] -= to_d(wq * Jx[k][a]);
     }
     if constexpr (D) {
       // derivatives of load with respect to x-dot, x-ddot and r₀ (local frame)
-      double xl1[3];
+      real xl1[3];
       for (int k = 0; k < 3; ++k) xl1[k] = r0[3 * k] * xd[g][0] + r0[3 * k + 1] * xd[g][1] + r0[3 * k + 2] * xd[g][2];
-      double xl2[3];
+      real xl2[3];
       for (int k = 0; k < 3; ++k)
         xl2[k] = r0[3 * k] * xdd[g][0] + r0[3 * k + 1] * xdd[g][1] + r0[3 * k + 2] * xdd[g][2];
-      double fl[3], dfl1[3];
+      real fl[3], dfl1[3];
       for (int k = 0; k < 3; ++k) {
-        double fq = c.Cq[k] * xl1[k] * xl1[k];
+        real fq = c.Cq[k] * xl1[k] * xl1[k];
         if (xl1[k] < 0.0) fq = -fq;
         fl[k] = c.Ca[k] * xl2[k] + c.Cl[k] * xl1[k] + fq;
         dfl1[k] = c.Cl[k] + 2.0 * c.Cq[k] * fabs(xl1[k]);
       }
       // Ṁ, M̈ for translation columns
-      double td1[3], td2[3];
+      real td1[3], td2[3];
       for (int i = 0; i < 3; ++i) {
         td1[i] = t[i].vt;
         td2[i] = 2.0 * t[i].vtt;
@@ -472,27 +472,27 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
       // direction loop (12 Newton directions, plus δr)
       const int ndir = rdir ? 13 : 12;
       for (int j = 0; j < ndir; ++j) {
-        double dx1[3], dx2[3], dr0[9];
+        real dx1[3], dx2[3], dr0[9];
         for (int k = 0; k < 9; ++k) dr0[k] = 0.0;
         if (j < 12) {
           const int e = rot_index(j);
           if (e >= 0) {
             for (int i = 0; i < 3; ++i) {
-              const double gx = yd * mv[i].g[e] + yv * wv[i].g[e];
-              const double gtx = yd * mv[i].gt[e] + yv * wv[i].gt[e];
-              const double gttx = yd * mv[i].gtt[e] + yv * wv[i].gtt[e];
+              const real gx = yd * mv[i].g[e] + yv * wv[i].g[e];
+              const real gtx = yd * mv[i].gt[e] + yv * wv[i].gt[e];
+              const real gttx = yd * mv[i].gtt[e] + yv * wv[i].gtt[e];
               dx1[i] = gtx * pt.p0 + gx * pt.p1;
               dx2[i] = 2.0 * gttx * pt.p0 + 2.0 * gtx * pt.p1 + gx * pt.p2;
             }
             for (int k = 0; k < 9; ++k) dr0[k] = rsm[k].g[e] * pt.p0;
           } else {
             const int k = j < 3 ? j : j - 6;
-            const double s = j < 3 ? -0.5 : 0.5;
+            const real s = j < 3 ? -0.5 : 0.5;
             for (int i = 0; i < 3; ++i) {
-              const double M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
-              const double M1 = yd * (td1[i] * tv[k] + tv[i] * td1[k]);
-              const double M2 = yd * (td2[i] * tv[k] + 2.0 * td1[i] * td1[k] + tv[i] * td2[k]);
-              const double I = (i == k ? 0.5 : 0.0);
+              const real M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
+              const real M1 = yd * (td1[i] * tv[k] + tv[i] * td1[k]);
+              const real M2 = yd * (td2[i] * tv[k] + 2.0 * td1[i] * td1[k] + tv[i] * td2[k]);
+              const real I = (i == k ? 0.5 : 0.0);
               dx1[i] = s * (M1 * pt.p0 + M * pt.p1) + I * pt.p1;
               dx2[i] = s * (M2 * pt.p0 + 2.0 * M1 * pt.p1 + M * pt.p2) + I * pt.p2;
             }
@@ -506,15 +506,15 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
           for (int jj = 0; jj < 12; ++jj) {
             const int e = rot_index(jj);
             for (int i = 0; i < 3; ++i) {
-              double gx, gtx;
+              real gx, gtx;
               if (e >= 0) {
                 gx = yd * mv[i].g[e] + yv * wv[i].g[e];
                 gtx = yd * mv[i].gt[e] + yv * wv[i].gt[e];
               } else {
                 const int k = jj < 3 ? jj : jj - 6;
-                const double s = jj < 3 ? -0.5 : 0.5;
-                const double M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
-                const double M1 = yd * (td1[i] * tv[k] + tv[i] * td1[k]);
+                const real s = jj < 3 ? -0.5 : 0.5;
+                const real M = (i == k ? yu : 0.0) + yd * tv[i] * tv[k];
+                const real M1 = yd * (td1[i] * tv[k] + tv[i] * td1[k]);
                 gx = s * M + (i == k ? 0.5 : 0.0);
                 gtx = s * M1;
               }
@@ -524,23 +524,23 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
           }
         }
         // δ(local components):  δ(r₀ᵀy) = δr₀ᵀ y + r₀ᵀ δy
-        double dl1[3], dl2[3];
+        real dl1[3], dl2[3];
         for (int k = 0; k < 3; ++k) {
           dl1[k] = dr0[3 * k] * xd[g][0] + dr0[3 * k + 1] * xd[g][1] + dr0[3 * k + 2] * xd[g][2] +
                    r0[3 * k] * dx1[0] + r0[3 * k + 1] * dx1[1] + r0[3 * k + 2] * dx1[2];
           dl2[k] = dr0[3 * k] * xdd[g][0] + dr0[3 * k + 1] * xdd[g][1] + dr0[3 * k + 2] * xdd[g][2] +
                    r0[3 * k] * dx2[0] + r0[3 * k + 1] * dx2[1] + r0[3 * k + 2] * dx2[2];
         }
-        double dfl[3];
+        real dfl[3];
         for (int k = 0; k < 3; ++k) dfl[k] = c.Ca[k] * dl2[k] + dfl1[k] * dl1[k];
-        double df[3];
+        real df[3];
         for (int i = 0; i < 3; ++i)
           df[i] = c.mu * dx2[i] + dr0[i] * fl[0] + dr0[i + 3] * fl[1] + dr0[i + 6] * fl[2] + r0[i] * dfl[0] +
                   r0[i + 3] * dfl[1] + r0[i + 6] * dfl[2];
         double* col = (j < 12) ? (K + 12 * j) : rdir;
         if (j == 12 && g == 0)
           for (int a = 0; a < 12; ++a) rdir[a] = 0.0;
-        for (int a = 0; a < 12; ++a) col[a] += wq * (Jx[0][a] * df[0] + Jx[1][a] * df[1] + Jx[2][a] * df[2]);
+        for (int a = 0; a < 12; ++a) col[a] += to_d(wq * (Jx[0][a] * df[0] + Jx[1][a] * df[1] + Jx[2][a] * df[2]));
       }
     }
   }
@@ -550,14 +550,14 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
       // rotational inertia: S0 vₛₘ∂X₀ᵀ δmₑ,  mₑ = ι₁ vᵢ₂[1] t
       const int ndir = rdir ? 13 : 12;
       for (int j = 0; j < ndir; ++j) {
-        double dvi = 0.0, dt[3] = {0, 0, 0};
+        real dvi = 0.0, dt[3] = {0, 0, 0};
         if (j < 12) {
           const int e = rot_index(j);
           if (e < 0) continue;
           for (int i = 0; i < 3; ++i) {
-            const double dn_ = n[i].g[e] * pt.p0, db_ = b[i].g[e] * pt.p0;
-            const double dndd = 2.0 * n[i].gtt[e] * pt.p0 + 2.0 * n[i].gt[e] * pt.p1 + n[i].g[e] * pt.p2;
-            const double dbdd = 2.0 * b[i].gtt[e] * pt.p0 + 2.0 * b[i].gt[e] * pt.p1 + b[i].g[e] * pt.p2;
+            const real dn_ = n[i].g[e] * pt.p0, db_ = b[i].g[e] * pt.p0;
+            const real dndd = 2.0 * n[i].gtt[e] * pt.p0 + 2.0 * n[i].gt[e] * pt.p1 + n[i].g[e] * pt.p2;
+            const real dbdd = 2.0 * b[i].gtt[e] * pt.p0 + 2.0 * b[i].gt[e] * pt.p1 + b[i].g[e] * pt.p2;
             dvi += 0.5 * (db_ * 2.0 * n[i].vtt + r0[6 + i] * dndd - dn_ * 2.0 * b[i].vtt - r0[3 + i] * dbdd);
             dt[i] = t[i].g[e] * pt.p0;
           }
@@ -566,18 +566,18 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
             const int e = rot_index(jj);
             if (e < 0) continue;
             for (int i = 0; i < 3; ++i) {
-              const double dndd = 2.0 * n[i].gt[e] * av[jj] + n[i].g[e] * bv[jj];
-              const double dbdd = 2.0 * b[i].gt[e] * av[jj] + b[i].g[e] * bv[jj];
+              const real dndd = 2.0 * n[i].gt[e] * av[jj] + n[i].g[e] * bv[jj];
+              const real dbdd = 2.0 * b[i].gt[e] * av[jj] + b[i].g[e] * bv[jj];
               dvi += 0.5 * (r0[6 + i] * dndd - r0[3 + i] * dbdd);
             }
           }
         }
-        double dme[3];
+        real dme[3];
         for (int i = 0; i < 3; ++i) dme[i] = c.S0 * c.iota1 * (dvi * r0[i] + vi21 * dt[i]);
         double* col = (j < 12) ? (K + 12 * j) : rdir;
         for (int a2 = 0; a2 < 6; ++a2) {
           const int a = a2 < 3 ? 3 + a2 : 6 + a2;
-          col[a] += vsm[0].g[a2] * dme[0] + vsm[1].g[a2] * dme[1] + vsm[2].g[a2] * dme[2];
+          col[a] += to_d(vsm[0].g[a2] * dme[0] + vsm[1].g[a2] * dme[1] + vsm[2].g[a2] * dme[2]);
         }
       }
     }

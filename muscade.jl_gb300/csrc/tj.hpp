@@ -19,6 +19,12 @@
 #include <math.h>
 #include <type_traits>
 
+// Arithmetic type of the element math: real on the device; a counting type
+// when the host flop-count tool instantiates the same code.
+#ifndef MGPU_REAL
+#define MGPU_REAL double
+#endif
+
 #ifdef __CUDACC__
 #define MG_HD __host__ __device__ __forceinline__
 #else
@@ -26,6 +32,11 @@
 #endif
 
 namespace mgpu {
+
+using real = MGPU_REAL;
+#ifndef MGPU_HAVE_TO_D
+MG_HD double to_d(double x) { return x; }
+#endif
 
 constexpr int NV = 6;
 constexpr int NH = 21;
@@ -35,19 +46,19 @@ MG_HD constexpr int hidx(int i, int j) { return i * NV - (i * (i - 1)) / 2 + (j 
 
 struct NoJet {};
 struct TimeJet {
-  double vt, vtt;
-  double gt[NV], gtt[NV];
+  real vt, vtt;
+  real gt[NV], gtt[NV];
 };
 
 template <bool DYN>
 struct TJ : public std::conditional<DYN, TimeJet, NoJet>::type {
-  double v;
-  double g[NV];
-  double h[NH];
+  real v;
+  real g[NV];
+  real h[NH];
 };
 
 template <bool DYN>
-MG_HD TJ<DYN> tj_const(double c) {
+MG_HD TJ<DYN> tj_const(real c) {
   TJ<DYN> r;
   r.v = c;
 #pragma unroll
@@ -68,7 +79,7 @@ MG_HD TJ<DYN> tj_const(double c) {
 
 // independent variable ε_j with value x₀, rate x₁ and acceleration x₂
 template <bool DYN>
-MG_HD TJ<DYN> tj_var(double x0, int j, double x1 = 0.0, double x2 = 0.0) {
+MG_HD TJ<DYN> tj_var(real x0, int j, real x1 = 0.0, real x2 = 0.0) {
   TJ<DYN> r = tj_const<DYN>(x0);
   r.g[j] = 1.0;
   if constexpr (DYN) {
@@ -117,7 +128,7 @@ MG_HD TJ<DYN> operator-(const TJ<DYN>& a, const TJ<DYN>& b) {
   return r;
 }
 template <bool DYN>
-MG_HD TJ<DYN> tj_scale(const TJ<DYN>& a, double s) {
+MG_HD TJ<DYN> tj_scale(const TJ<DYN>& a, real s) {
   TJ<DYN> r;
   r.v = a.v * s;
 #pragma unroll
@@ -140,11 +151,11 @@ MG_HD TJ<DYN> operator-(const TJ<DYN>& a) {
   return tj_scale(a, -1.0);
 }
 template <bool DYN>
-MG_HD TJ<DYN> operator*(const TJ<DYN>& a, double s) { return tj_scale(a, s); }
+MG_HD TJ<DYN> operator*(const TJ<DYN>& a, real s) { return tj_scale(a, s); }
 template <bool DYN>
-MG_HD TJ<DYN> operator*(double s, const TJ<DYN>& a) { return tj_scale(a, s); }
+MG_HD TJ<DYN> operator*(real s, const TJ<DYN>& a) { return tj_scale(a, s); }
 template <bool DYN>
-MG_HD TJ<DYN> operator+(const TJ<DYN>& a, double s) {
+MG_HD TJ<DYN> operator+(const TJ<DYN>& a, real s) {
   TJ<DYN> r = a;
   r.v += s;
   return r;
@@ -162,7 +173,7 @@ MG_HD TJ<DYN> operator*(const TJ<DYN>& a, const TJ<DYN>& b) {
 #pragma unroll
     for (int j = i; j < NV; ++j) {
       const int k = hidx(i, j);
-      double s = fma(a.h[k], b.v, a.v * b.h[k]);
+      real s = fma(a.h[k], b.v, a.v * b.h[k]);
       s = fma(a.g[i], b.g[j], s);
       r.h[k] = fma(a.g[j], b.g[i], s);
     }
@@ -172,7 +183,7 @@ MG_HD TJ<DYN> operator*(const TJ<DYN>& a, const TJ<DYN>& b) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
       r.gt[i] = fma(a.gt[i], b.v, fma(a.vt, b.g[i], fma(a.g[i], b.vt, a.v * b.gt[i])));
-      double s = fma(a.gtt[i], b.v, a.vtt * b.g[i]);
+      real s = fma(a.gtt[i], b.v, a.vtt * b.g[i]);
       s = fma(a.gt[i], b.vt, s);
       s = fma(a.vt, b.gt[i], s);
       s = fma(a.g[i], b.vtt, s);
@@ -184,7 +195,7 @@ MG_HD TJ<DYN> operator*(const TJ<DYN>& a, const TJ<DYN>& b) {
 
 // composition f(a) from f and its first three derivatives at a.v
 template <bool DYN>
-MG_HD TJ<DYN> tj_apply(const TJ<DYN>& a, double f0, double f1, double f2, double f3) {
+MG_HD TJ<DYN> tj_apply(const TJ<DYN>& a, real f0, real f1, real f2, real f3) {
   TJ<DYN> r;
   r.v = f0;
 #pragma unroll
@@ -202,7 +213,7 @@ MG_HD TJ<DYN> tj_apply(const TJ<DYN>& a, double f0, double f1, double f2, double
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
       r.gt[i] = fma(f1, a.gt[i], f2 * a.g[i] * a.vt);
-      double s = f2 * a.g[i] * a.vtt;
+      real s = f2 * a.g[i] * a.vtt;
       s = fma(f1, a.gtt[i], s);
       s = fma(0.5 * f3 * a.g[i], a.vt * a.vt, s);
       r.gtt[i] = fma(f2 * a.vt, a.gt[i], s);

@@ -52,8 +52,11 @@ def random_beams(n, seed, udof=False, rot=0.5):
         m.addelement(EulerBeam3D, np.stack([ids1, ids2, ids3], axis=1), mat=mat, orient2=o2, udof=True)
     else:
         m.addelement(EulerBeam3D, np.stack([ids1, ids2], axis=1), mat=mat, orient2=o2)
+    # nodal rotations up to ~1.5 rad, relative rotation across an element ≲ 0.3 rad
+    # (away from the half-turn where Rodrigues⁻¹ is singular in the reference too)
     X = rng.normal(size=(n, 3, 12)) * 0.1
-    X[:, 0, [3, 4, 5, 9, 10, 11]] = rng.normal(size=(n, 6)) * rot
+    X[:, 0, 3:6] = rng.normal(size=(n, 3)) * rot
+    X[:, 0, 9:12] = X[:, 0, 3:6] + rng.normal(size=(n, 3)) * 0.1
     X[: n // 5, 0, 3:6] = 0.0  # exactly unrotated node 1 (norm3 zero branch)
     X[:, 1:, :] = rng.normal(size=(n, 2, 12)) * 0.5
     U = rng.normal(size=(n, 3)) if udof else None
