@@ -118,25 +118,14 @@ class Clocks:
 
 
 def fp64_peak_tflops(device):
-    """Measured FP64 throughput of this GPU: cuBLAS DGEMM 8192³, best of 5 (CUDA events)."""
-    import torch
+    """FP64 FMA throughput of this GPU, measured by the library (independent DFMA chains)."""
+    import ctypes
 
-    n = 8192
-    a = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
-    b = torch.randn(n, n, dtype=torch.float64, device=f"cuda:{device}")
-    torch.matmul(a, b)
-    torch.cuda.synchronize(device)
-    best = 1e30
-    for _ in range(5):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        torch.matmul(a, b)
-        e.record()
-        e.synchronize()
-        best = min(best, s.elapsed_time(e))
-    del a, b
-    torch.cuda.empty_cache()
-    return 2.0 * n**3 / (best * 1e-3) / 1e12
+    from muscade_gpu import _lib
+
+    v = ctypes.c_double()
+    rc = _lib.load().mgpu_measure_fp64_peak(device, ctypes.byref(v))
+    return v.value if rc == 0 else None
 
 
 def state_for(model, seed=2027):
@@ -214,9 +203,6 @@ def main():
 
     _lib.build()
     device = local_rank
-    import torch
-
-    torch.cuda.set_device(device)
     fp64_peak = fp64_peak_tflops(device) if rank == 0 else None
     dm = DeviceModel(model, st.dis, device=device)
     dm.upload_state(X, t=t)
@@ -262,7 +248,7 @@ def main():
     except (OSError, KeyError, ValueError):
         pass
     roof = {"bound": "fp64", "unit": "TFLOP/s", "kernel": "beam_kernel<false>", "ms_per_launch": tbeam,
-            "peak_source": "measured on this GPU: cuBLAS DGEMM 8192^3 (FP64)", "peak": fp64_peak,
+            "peak_source": "measured on this GPU: DFMA throughput of independent FMA chains (mgpu_measure_fp64_peak)", "peak": fp64_peak,
             "traffic": traffic, "traffic_unit": "bytes per launch"}
     if flops:
         ach = flops * nbeam / (tbeam * 1e-3) / 1e12

@@ -150,6 +150,11 @@ int mgpu_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, d
                 const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts, double *states,
                 mgpu_stats *stats);
 
+/* Measurement utility (no counterpart in the reference): FP64 FMA throughput
+ * of `device` in TFLOP/s, from independent DFMA chains timed with CUDA events;
+ * the roofline denominator of the FP64-bound element kernels. */
+int mgpu_measure_fp64_peak(int32_t device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif
