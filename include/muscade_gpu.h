@@ -150,6 +150,32 @@ int mgpu_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, d
                 const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts, double *states,
                 mgpu_stats *stats);
 
+/* Beam assembly that allocates nothing (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc where they assemble -- inside a
+ * captured CUDA graph, in a loop whose device memory was fixed beforehand, or
+ * when device memory belongs to another runtime's pool.  Every argument is
+ * device memory the caller owns:
+ *   fields[nele][69]   EulerBeam3D fields (as mgpu_group.edata)
+ *   indexX[nele][12]   1-based model X-dofs of each beam
+ *   asm1[nele][12]     1-based positions in Lλ      (asm[1,ieletyp], 0 = skip)
+ *   asm2[nele][144]    1-based positions in nzval   (asm[2,ieletyp], 0 = skip)
+ *   x[nX]              state X
+ *   Ll[nX], nzval[nnz] outputs, overwritten (zeroed, then summed)
+ * It computes the SweepX{0} residual and tangent of the beams (as
+ * mgpu_assemble with MGPU_ASM_STATIC on a model of these beams) and enqueues
+ * the work on `stream` (a cudaStream_t, NULL for the legacy stream) without
+ * synchronising.  Its scratch is one fixed device array that every GPU loading
+ * the library holds until exit, so nele is limited to MGPU_NOALLOC_MAX_BEAMS
+ * (returns MGPU_ERR_SIZE above it).  All calls on a device share that array:
+ * calls that overlap on the GPU (different streams, or host threads without
+ * ordering) race and must be serialised by the caller.  The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture. */
+#define MGPU_NOALLOC_MAX_BEAMS 4096
+int mgpu_assemble_beams_noalloc(int64_t nele, int64_t nX, int64_t nnz, const double *fields, const int64_t *indexX,
+                                const int64_t *asm1, const int64_t *asm2, const double *x, double *Ll,
+                                double *nzval, void *stream);
+
 /* Measurement utility (no counterpart in the reference): FP64 FMA throughput
  * of `device` in TFLOP/s, from independent DFMA chains timed with CUDA events;
  * the roofline denominator of the FP64-bound element kernels. */

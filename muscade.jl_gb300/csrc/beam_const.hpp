@@ -8,7 +8,7 @@ namespace mgpu {
 
 constexpr int BEAM_NFIELD = 69;
 
-inline void beam_const_from_fields(const double* f, BeamConst& c) {
+MG_HD void beam_const_from_fields(const double* f, BeamConst& c) {
   const double* rm = f + 3;
   const double* tgm = f + 18;
   const double* ya = f + 24;

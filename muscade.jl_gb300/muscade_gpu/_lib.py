@@ -15,7 +15,7 @@ PKG = os.path.dirname(HERE)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
-SOURCES = ["mgpu.cu", "solver.cu", "peak.cu", "pattern.cpp"]
+SOURCES = ["mgpu.cu", "solver.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
 HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -86,7 +86,8 @@ class Stats(ctypes.Structure):
 # every symbol the header declares (checked by the CPU test suite)
 SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_get_pattern", "mgpu_get_asm",
            "mgpu_ntval", "mgpu_assemble", "mgpu_element_eval", "mgpu_upload_state", "mgpu_assemble_resident",
-           "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak"]
+           "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
+           "mgpu_assemble_beams_noalloc"]
 
 _lib = None
 
@@ -122,6 +123,7 @@ def load():
     L.mgpu_time_assemble.argtypes = [vp, i32, d, P(Newmark), i32, i32, pd, pd, pd]
     L.mgpu_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), pd, P(Stats)]
     L.mgpu_measure_fp64_peak.argtypes = [i32, pd]
+    L.mgpu_assemble_beams_noalloc.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp]
     for name in SYMBOLS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int and name not in ("mgpu_destroy",):
