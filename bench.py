@@ -161,8 +161,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="60,60,20")
     ap.add_argument("--cpu-sample", type=int, default=int(os.environ.get("MGPU_CPU_SAMPLE", "60000")))
+    ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever"],
+                    help="lattice: the headline assembly metric; risers/cantilever: whole SweepX solves")
+    ap.add_argument("--risers", type=int, default=200)
     args = ap.parse_args()
     rank, local_rank, ws, dist = dist_setup()
+    if args.config != "lattice":
+        return bench_solve(args, rank, local_rank, ws, dist)
     nx, ny, nz = (int(v) for v in args.grid.split(","))
 
     from muscade_gpu import workloads
@@ -284,6 +289,73 @@ def main():
     dm.close()
     if dist:
         dist.destroy_process_group()
+
+
+def bench_solve(args, rank, local_rank, ws, dist):
+    """Whole device SweepX runs: Newmark risers (3 Newton iterations per step) or the static cantilever."""
+    from muscade_gpu import _lib, workloads
+    from muscade_gpu.device import DeviceModel
+    from oracle import reference as REF
+
+    _lib.build()
+    if args.config == "risers":
+        model, times = workloads.risers(nriser=args.risers)
+        st = model.initialize(time=0.0)
+        OX, kw = 2, dict(fixed_iter=3)
+        nstep_w, nstep = args.warmup, args.steps
+        nbeam = model.groups[0].nele
+    else:
+        model, times = workloads.cantilever()
+        st = model.initialize()
+        OX, kw = 0, dict(maxdx=1e-9, maxLl=1e-5)
+        nstep_w, nstep = 0, len(times)
+        nbeam = model.groups[0].nele
+    dm = DeviceModel(model, st.dis, device=local_rank)
+    X0 = list(st.X)[: OX + 1]
+    T = np.asarray(times[: nstep_w + nstep], dtype=np.float64)
+    if args.config == "risers" and nstep_w:
+        dm.sweepx(OX, T[:nstep_w], st.time, X0, **kw)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    rc, states, stats = dm.sweepx(OX, T if args.config == "cantilever" else T[:nstep], st.time, X0, **kw)
+    dt = time.perf_counter() - t0
+    if rc != 0:
+        raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
+    dt = reduce_max(dist, dt)
+    if rank != 0:
+        return
+    steps_run = stats.nstep_done
+    ms_step = dt / steps_run * 1e3
+    iters = stats.niter_total
+    value = ws * nbeam * iters / dt
+    # CPU arm on a bounded sample: the oracle's SweepX on a reduced model of the same kind
+    if args.config == "risers":
+        sm, stimes = workloads.risers(nriser=2)
+        sst = sm.initialize(time=0.0)
+        c0 = time.perf_counter()
+        try:
+            REF.sweepx(sm, sst.dis, sst, stimes[:3], OX=2, maxiter=60, maxdx=1e-5)
+        except Exception:
+            pass
+        cdt = time.perf_counter() - c0
+        cpu_rate = sm.groups[0].nele * 3 * 3 / cdt
+        sample = "2 risers x 3 Newmark steps (oracle assembly + SuperLU)"
+    else:
+        c0 = time.perf_counter()
+        ref = REF.sweepx(model, st.dis, st, times, OX=0, maxdx=1e-9, maxLl=1e-5)
+        cdt = time.perf_counter() - c0
+        cpu_rate = None
+        sample = f"whole cantilever solve: {cdt * 1e3:.1f} ms"
+    line = {"metric": "ms per " + ("Newmark step (3 Newton iterations)" if args.config == "risers" else "load step"),
+            "value": ms_step, "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": steps_run,
+            "warmup": nstep_w, "ms_per_step": ms_step, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.config, "beams": nbeam, "dofs": model.ndof["X"], "newton_iterations": iters},
+            "beam_assemblies_per_s": value, "e2e": {"value": ms_step, "unit": "ms", "note": "whole solve incl. copies"},
+            "cpu_baseline": {"value": cpu_rate, "unit": "beam assemblies/s", "kind": "port", "sample": sample,
+                             "cores": os.cpu_count()}}
+    print(json.dumps(line), flush=True)
+    dm.close()
 
 
 if __name__ == "__main__":

@@ -129,6 +129,8 @@ typedef struct {
   int32_t maxiter;    /* maximum Newton iterations per step */
   double maxdx;       /* convergence: Σ Δx² ≤ maxdx² */
   double maxLl;       /* and Σ Lλ² ≤ maxLl² (use +Inf to disable) */
+  int32_t fixed_iter; /* > 0: exactly this many iterations per step, no convergence test
+                         (the reference has no such option; used for fixed-cost time stepping) */
 } mgpu_sweep_opts;
 
 typedef struct {

@@ -478,8 +478,8 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
     }
     if (c->ntval > 0)
       MG_CUDA(cudaMemcpyAsync(c->tv, tvals + step * c->ntval, c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
-    bool conv = false;
-    for (int it = 1; it <= opts->maxiter; ++it) {
+    const int itmax = opts->fixed_iter > 0 ? opts->fixed_iter : opts->maxiter;
+    for (int it = 1; it <= itmax; ++it) {
       stats->niter_total++;
       const int first = it == 1;
       const int mission = OX == 0 ? MGPU_ASM_STATIC : (first ? MGPU_ASM_STEP : MGPU_ASM_ITER);
@@ -512,10 +512,11 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
         snprintf(msg, sizeof msg, "matrix factorization failed at step=%d, iiter=%d", int(step + 1), it);
         return set_err(c, MGPU_ERR_SINGULAR, msg);
       }
-      if (dx2 <= cdx2 && Ll2 <= cLl2) {
-        conv = true;
-        break;
+      if (opts->fixed_iter > 0) {
+        if (it == opts->fixed_iter) break;
+        continue;
       }
+      if (dx2 <= cdx2 && Ll2 <= cLl2) break;
       if (it == opts->maxiter) {
         stats->fail_step = int(step + 1);
         stats->fail_iter = it;
@@ -525,7 +526,6 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
         return set_err(c, MGPU_ERR_NOCONV, msg);
       }
     }
-    (void)conv;
     MG_CUDA(cudaMemcpyAsync(states + step * nder * n, c->x, nder * n * sizeof(double), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaStreamSynchronize(st));
     stats->nstep_done = int(step + 1);
