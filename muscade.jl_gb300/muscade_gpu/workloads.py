@@ -8,7 +8,8 @@
   translation ramped by t.  60×60×20 gives 210,000 beams.
 * risers(nriser, nel): independent vertical risers of 1000 m, pinned at the
   bottom (Hold t1,t2,t3,r1) and driven at the top by DofConstraints
-  t1 = A sin(2πt/T), t2 = 0, t3 = 0.1 m (pretension), A~U(1,5), T~U(8,15).
+  t1 = A sin(2πt/T)·ρ(t), t2 = 0, t3 = 0.1 m·ρ(t) (pretension), A~U(1,5),
+  T~U(8,15), with ρ a cosine ramp from 0 to 1 over the first 5 s.
 
 Random streams use numpy PCG64 with seed 2026 + configuration index.
 """
@@ -103,14 +104,17 @@ def risers(nriser=200, nel=250, length=1000.0, seed=2028, EA=5e9, EI=1e6, GJ=1e6
     for f in ("t1", "t2", "t3", "r1"):
         m.addelement(Hold, bottoms, field=f)
 
+    def ramp(t):  # smooth start of the prescribed top motion over the first 5 s
+        return 0.5 * (1.0 - math.cos(math.pi * min(t, 5.0) / 5.0))
+
     def surge(t):
-        return A * np.sin(2 * math.pi * t / T)
+        return A * np.sin(2 * math.pi * t / T) * ramp(t)
 
     def zero(t):
         return 0.0
 
     def lift(t):
-        return 0.1
+        return 0.1 * ramp(t)
 
     m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t1",), lfield="λtop1", coeffs=[1.0], offset=surge, name="surge")
     m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t2",), lfield="λtop2", coeffs=[1.0], offset=zero, name="sway")
