@@ -23,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include "band_warp.cuh"
 #include "ctx.hpp"
 
 using namespace mgpu;
@@ -300,8 +301,9 @@ __global__ void __launch_bounds__(128) band_lu(const int64_t* cbase, const int32
           *b = t;
         }
       __syncthreads();
-      // multipliers
-      for (int i = 1 + threadIdx.x; i <= km; i += blockDim.x) A[kv + i + int64_t(ld) * k] /= p;
+      // multipliers (scaled by the reciprocal pivot, like gbtf2)
+      const double rp = 1.0 / p;
+      for (int i = 1 + threadIdx.x; i <= km; i += blockDim.x) A[kv + i + int64_t(ld) * k] *= rp;
       __syncthreads();
       // rank-1 update of columns k+1..ju, rows k+1..k+km
       const int w = ju - k;
@@ -432,8 +434,17 @@ static int factor_solve(mgpu_ctx* c) {
   cudaStream_t st = c->stream;
   MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
   band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
-  band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
-  band_solve<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv, c->Ll, S.rhs, S.dx);
+  if (S.maxkl < BW_ROWS && S.maxkl + S.maxku + 1 <= 32 * BW_SLOTS) {
+    // narrow bands: one warp per component, active window in registers
+    const unsigned blocks = unsigned((S.ncomp + 3) / 4);
+    band_lu_warp<<<blocks, 128, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
+    band_solve_warp<<<blocks, 128, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv,
+                                            c->Ll, S.rhs, S.dx);
+  } else {
+    band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
+    band_solve<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv, c->Ll, S.rhs,
+                                        S.dx);
+  }
   norms_kernel<<<1, 1024, 0, st>>>(c->nX, S.dx, c->Ll, S.red);
   MG_CUDA(cudaGetLastError());
   return MGPU_OK;

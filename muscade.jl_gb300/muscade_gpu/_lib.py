@@ -16,7 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
 SOURCES = ["mgpu.cu", "solver.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
-HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp"]
+HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_warp.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes
