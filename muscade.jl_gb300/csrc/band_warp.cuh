@@ -61,6 +61,19 @@ __global__ void __launch_bounds__(128) band_lu_warp(int ncomp, const int64_t* __
   for (int k = 0; k < n; ++k) {
     const int km = min(kl, n - 1 - k);
     const int olane = q0 & 31, oslot = q0 >> 5;
+    // prefetch what enters the window after this step (untouched until then):
+    // row k+1+kl of the other window columns, and column k+W for the owner of column k
+    const int rn = k + 1 + kl, jn = k + W;
+    double nrow[BW_SLOTS], ncol[BW_ROWS];
+#pragma unroll
+    for (int s = 0; s < BW_SLOTS; ++s) {
+      const int j = col[s];
+      nrow[s] = (j > k && rn < n) ? A[kv + rn - j + int64_t(ld) * j] : 0.0;
+    }
+    const bool owner = (lane == olane);
+#pragma unroll
+    for (int r = 0; r < BW_ROWS; ++r)
+      ncol[r] = (owner && jn < n && r <= kl && k + 1 + r < n) ? A[kv + (k + 1 + r) - jn + int64_t(ld) * jn] : 0.0;
     // pivot search by the owner of column k
     int jp = 0;
     if (lane == olane) {
@@ -133,18 +146,15 @@ __global__ void __launch_bounds__(128) band_lu_warp(int ncomp, const int64_t* __
     for (int s = 0; s < BW_SLOTS; ++s) {
       const int j = col[s];
       if (j == k) {
-        const int jn = k + W;
         if (jn < n) {
           col[s] = jn;
 #pragma unroll
-          for (int r = 0; r < BW_ROWS; ++r)
-            act[s][r] = (r <= kl && k + 1 + r < n) ? A[kv + (k + 1 + r) - jn + int64_t(ld) * jn] : 0.0;
+          for (int r = 0; r < BW_ROWS; ++r) act[s][r] = ncol[r];
         } else {
           col[s] = -1;
         }
       } else if (j > k) {
-        const int rn = k + 1 + kl;  // row entering the active set
-        const double nv = (rn < n) ? A[kv + rn - j + int64_t(ld) * j] : 0.0;
+        const double nv = nrow[s];  // row k+1+kl entering the active set
 #pragma unroll
         for (int r = 0; r < BW_ROWS - 1; ++r) act[s][r] = (r == kl) ? nv : act[s][r + 1];
         act[s][BW_ROWS - 1] = (BW_ROWS - 1 == kl) ? nv : 0.0;
@@ -180,6 +190,9 @@ __global__ void __launch_bounds__(128) band_solve_warp(int ncomp, const int64_t*
   double y = (lane <= kl && lane < n) ? b[lane] : 0.0;
   for (int k = 0; k < n; ++k) {
     const int km = min(kl, n - 1 - k);
+    const int rn = k + 1 + kl;
+    const double bnew = (lane == kl && rn < n) ? b[rn] : 0.0;  // prefetch the entering entry
+    const double lk = (lane >= 1 && lane <= km) ? A[kv + lane + int64_t(ld) * k] : 0.0;
     const int jp = piv[k] - k;
     if (jp != 0) {
       const double y0 = __shfl_sync(FULL, y, 0);
@@ -188,11 +201,10 @@ __global__ void __launch_bounds__(128) band_solve_warp(int ncomp, const int64_t*
       if (lane == jp) y = y0;
     }
     const double bk = __shfl_sync(FULL, y, 0);
-    if (lane >= 1 && lane <= km) y -= A[kv + lane + int64_t(ld) * k] * bk;
+    if (lane >= 1 && lane <= km) y -= lk * bk;
     if (lane == 0) b[k] = y;  // final forward value
     const double nxt = __shfl_down_sync(FULL, y, 1);
-    const int rn = k + 1 + kl;
-    y = (lane == kl) ? ((rn < n) ? b[rn] : 0.0) : ((lane < kl) ? nxt : 0.0);
+    y = (lane == kl) ? bnew : ((lane < kl) ? nxt : 0.0);
   }
   __syncwarp();
   // backward: position p = lane + 32 s holds y[k-p], p ≤ kv
@@ -204,20 +216,27 @@ __global__ void __launch_bounds__(128) band_solve_warp(int ncomp, const int64_t*
     z[s] = (p <= kv && i >= 0) ? b[i] : 0.0;
   }
   for (int k = n - 1; k >= 0; --k) {
+    // loads of this step issued before the dependent arithmetic
+    const int inew = k - 1 - kv;
+    const double vnew = (inew >= 0 && lane == (kv & 31)) ? b[inew] : 0.0;
     const double d = A[kv + int64_t(ld) * k];
+    double uk[BW_SLOTS];
+#pragma unroll
+    for (int s = 0; s < BW_SLOTS; ++s) {
+      const int p = lane + 32 * s;
+      uk[s] = (p >= 1 && p <= kv && p <= k) ? A[kv - p + int64_t(ld) * k] : 0.0;
+    }
     const double xk = __shfl_sync(FULL, z[0], 0) / d;
     if (lane == 0) b[k] = xk;
 #pragma unroll
     for (int s = 0; s < BW_SLOTS; ++s) {
       const int p = lane + 32 * s;
-      if (p >= 1 && p <= kv && p <= k) z[s] -= A[kv - p + int64_t(ld) * k] * xk;
+      if (p >= 1 && p <= kv && p <= k) z[s] -= uk[s] * xk;
     }
     // shift the window by one position: p <- p+1, new entry y[k-1-kv] at p = kv
     const double carry = __shfl_sync(FULL, z[1], 0);
     const double d0 = __shfl_down_sync(FULL, z[0], 1);
     const double d1 = __shfl_down_sync(FULL, z[1], 1);
-    const int inew = k - 1 - kv;
-    const double vnew = (inew >= 0) ? b[inew] : 0.0;
 #pragma unroll
     for (int s = 0; s < BW_SLOTS; ++s) {
       const int p = lane + 32 * s;

@@ -435,10 +435,10 @@ static int factor_solve(mgpu_ctx* c) {
   MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
   band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
   if (S.maxkl < BW_ROWS && S.maxkl + S.maxku + 1 <= 32 * BW_SLOTS) {
-    // narrow bands: one warp per component, active window in registers
-    const unsigned blocks = unsigned((S.ncomp + 3) / 4);
-    band_lu_warp<<<blocks, 128, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
-    band_solve_warp<<<blocks, 128, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv,
+    // narrow bands: one warp per component (one per block, so that the
+    // components spread over all SMs and their FP64 pipes), window in registers
+    band_lu_warp<<<S.ncomp, 32, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
+    band_solve_warp<<<S.ncomp, 32, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv,
                                             c->Ll, S.rhs, S.dx);
   } else {
     band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
