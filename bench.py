@@ -164,6 +164,8 @@ def main():
     ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever"],
                     help="lattice: the headline assembly metric; risers/cantilever: whole SweepX solves")
     ap.add_argument("--risers", type=int, default=200)
+    ap.add_argument("--linsolve", default="auto", choices=["auto", "f32ir", "f64", "block"],
+                    help="device linear solver of the whole-solve modes")
     args = ap.parse_args()
     rank, local_rank, ws, dist = dist_setup()
     if args.config != "lattice":
@@ -310,7 +312,7 @@ def bench_solve(args, rank, local_rank, ws, dist):
         OX, kw = 0, dict(maxdx=1e-9, maxLl=1e-5)
         nstep_w, nstep = 0, len(times)
         nbeam = model.groups[0].nele
-    dm = DeviceModel(model, st.dis, device=local_rank)
+    dm = DeviceModel(model, st.dis, device=local_rank, linsolve=args.linsolve)
     X0 = list(st.X)[: OX + 1]
     T = np.asarray(times[: nstep_w + nstep], dtype=np.float64)
     if args.config == "risers" and nstep_w:
@@ -350,7 +352,8 @@ def bench_solve(args, rank, local_rank, ws, dist):
     line = {"metric": "ms per " + ("Newmark step (3 Newton iterations)" if args.config == "risers" else "load step"),
             "value": ms_step, "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": steps_run,
             "warmup": nstep_w, "ms_per_step": ms_step, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.config, "beams": nbeam, "dofs": model.ndof["X"], "newton_iterations": iters},
+            "config": {"workload": args.config, "beams": nbeam, "dofs": model.ndof["X"], "newton_iterations": iters,
+                       "linear_solver": dm.linear_solver_info()},
             "beam_assemblies_per_s": value, "e2e": {"value": ms_step, "unit": "ms", "note": "whole solve incl. copies"},
             "cpu_baseline": {"value": cpu_rate, "unit": "beam assemblies/s", "kind": "port", "sample": sample,
                              "cores": os.cpu_count()}}

@@ -152,6 +152,35 @@ int mgpu_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, d
                 const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts, double *states,
                 mgpu_stats *stats);
 
+/* Linear solver of the Newton loops (no counterpart in the reference, which
+ * calls UMFPACK through lu/lu!/\ at src/SweepX.jl:207-210).  Every connected
+ * component of Lλx is reordered (reverse Cuthill-McKee) and factorised as a
+ * band with partial pivoting:
+ *   MGPU_LINSOLVE_AUTO   F64 where every component has kl <= 31 and
+ *                        kl+ku+1 <= 64, else BLOCK (the default)
+ *   MGPU_LINSOLVE_F32IR  FP32 factors, FP64 residuals and iterative refinement
+ *                        to working precision; a component whose refinement
+ *                        does not reach 1e-10 relative is refactorised in FP64
+ *   MGPU_LINSOLVE_F64    FP64 factors, one warp per component
+ *   MGPU_LINSOLVE_BLOCK  FP64 factors, one thread block per component, bands up to 256
+ * F64 and BLOCK give bitwise the same Δx.  Returns MGPU_ERR_UNSUPPORTED when
+ * the bands are too wide for the requested kind. */
+#define MGPU_LINSOLVE_AUTO 0
+#define MGPU_LINSOLVE_F32IR 1
+#define MGPU_LINSOLVE_F64 2
+#define MGPU_LINSOLVE_BLOCK 3
+int mgpu_set_linear_solver(mgpu_ctx *ctx, int32_t kind);
+
+typedef struct {
+  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64 or _BLOCK in use */
+  int32_t ncomp;         /* connected components of Lλx */
+  int32_t max_kl;        /* widest lower / upper band after reordering */
+  int32_t max_ku;
+  int32_t last_fallback; /* F32IR: components refactorised in FP64 in the last solve */
+  int32_t last_sweeps;   /* F32IR: most refinement sweeps any component needed in the last solve */
+} mgpu_linsolve_info;
+int mgpu_linear_solver_info(mgpu_ctx *ctx, mgpu_linsolve_info *info);
+
 /* Beam assembly that allocates nothing (no counterpart in the reference).
  * For callers that cannot call cudaMalloc where they assemble -- inside a
  * captured CUDA graph, in a loop whose device memory was fixed beforehand, or

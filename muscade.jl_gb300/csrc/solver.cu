@@ -18,20 +18,48 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <numeric>
 #include <queue>
 #include <string>
 #include <vector>
 
-#include "band_warp.cuh"
+#include "band_rows.cuh"
 #include "ctx.hpp"
 
 using namespace mgpu;
 
 namespace mgpu {
 
+enum SolverPath : int {
+  PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
+  PATH_F64ROWS = 1,  // row-band warp kernels in FP64
+  PATH_BLOCK = 2   // gbtf2-layout block kernels in FP64 (any band width up to 256)
+};
+
 struct Solver {
   bool ok = false;       // banded scheme applicable
+  int path = PATH_BLOCK;
+  int wm = 0;            // row-band register window (32 or 64), 0 if the row-band kernels do not apply
+  int nref = 8;          // refinement sweeps allowed on the FP32 path
+  // row-band layout
+  int64_t* rbase = nullptr;   // [ncomp] offset in RB / UC*
+  int64_t* lbase = nullptr;   // [ncomp] offset in LM*
+  int64_t* rbmap = nullptr;   // [nnz] position of each nnz in RB
+  int64_t rb_total = 0, lb_total = 0;
+  double* RB = nullptr;       // unfactorised rows (FP64)
+  float* RB32 = nullptr;      // the same in FP32
+  float* UC32 = nullptr;
+  float* LM32 = nullptr;
+  double* UC64 = nullptr;
+  double* LM64 = nullptr;
+  double* bw = nullptr;       // [nX] permuted right-hand side
+  double* xw = nullptr;       // [nX] solution (band order)
+  double* rw = nullptr;       // [nX] residual
+  float* tw32 = nullptr;      // [nX] substitution work
+  double* tw64 = nullptr;
+  int* flag = nullptr;        // [ncomp] FP64 fallback requested
+  int* nsweep = nullptr;      // [ncomp] refinement sweeps used
   std::string why;       // reason when not
   int ncomp = 0;
   int64_t band_total = 0;
@@ -47,6 +75,7 @@ struct Solver {
   double* AB = nullptr;       // band storage
   int32_t* ipiv = nullptr;    // [nX] pivot offsets (band order)
   double* rhs = nullptr;      // [nX] permuted right-hand side / solution
+  double* rdiag = nullptr;    // [nX] reciprocal pivots (block kernels)
   double* dx = nullptr;       // [nX] Δx in model order
   double* red = nullptr;      // [4] reductions: ΣΔx², ΣLλ²
   int* info = nullptr;        // [1] first singular component+1 (0 = ok)
@@ -216,9 +245,52 @@ static void analyse(mgpu_ctx* c, Solver& S) {
   }
   bool good = up(&S.cbase, cb) && up(&S.cn, cn) && up(&S.ckl, kl) && up(&S.cku, ku) && up(&S.cdof0, c0) &&
               up(&S.perm, order) && up(&S.bmap, bmap);
+  // row-band layout: applies when every component has kl <= 31 and kl+ku+1 <= 64
+  int maxw = 0;
+  for (int cc = 0; cc < ncomp; ++cc) maxw = std::max(maxw, kl[cc] + ku[cc] + 1);
+  if (S.maxkl <= 31 && maxw <= 64) {
+    S.wm = maxw <= 32 ? 32 : 64;
+    std::vector<int64_t> rb(ncomp + 1, 0), lb(ncomp + 1, 0);
+    for (int cc = 0; cc < ncomp; ++cc) {
+      const int64_t nc = comp_start[cc + 1] - comp_start[cc];
+      rb[cc + 1] = rb[cc] + nc * (kl[cc] + ku[cc] + 1);
+      lb[cc + 1] = lb[cc] + nc * kl[cc];
+    }
+    S.rb_total = rb[ncomp];
+    S.lb_total = lb[ncomp];
+    std::vector<int64_t> rbmap(P.nnz);
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+        const int64_t i = P.rowval[q];
+        const int cc = comp[j];
+        const int64_t kj = pos[j] - comp_start[cc], ki = pos[i] - comp_start[cc];
+        rbmap[q] = rb[cc] + ki * (kl[cc] + ku[cc] + 1) + (kj - ki + kl[cc]);
+      }
+    std::vector<int64_t> rbv(rb.begin(), rb.end() - 1), lbv(lb.begin(), lb.end() - 1);
+    const size_t nr = std::max<int64_t>(S.rb_total, 1), nl = std::max<int64_t>(S.lb_total, 1);
+    good = good && up(&S.rbase, rbv) && up(&S.lbase, lbv) && up(&S.rbmap, rbmap);
+    good = good && cudaMalloc(&S.RB, nr * sizeof(double)) == cudaSuccess &&
+           cudaMemset(S.RB, 0, nr * sizeof(double)) == cudaSuccess;
+    good = good && cudaMalloc(&S.RB32, nr * sizeof(float)) == cudaSuccess &&
+           cudaMemset(S.RB32, 0, nr * sizeof(float)) == cudaSuccess;
+    good = good && cudaMalloc(&S.UC32, nr * sizeof(float)) == cudaSuccess &&
+           cudaMalloc(&S.LM32, nl * sizeof(float)) == cudaSuccess &&
+           cudaMalloc(&S.UC64, nr * sizeof(double)) == cudaSuccess &&
+           cudaMalloc(&S.LM64, nl * sizeof(double)) == cudaSuccess;
+    good = good && cudaMalloc(&S.bw, n * sizeof(double)) == cudaSuccess &&
+           cudaMalloc(&S.xw, n * sizeof(double)) == cudaSuccess &&
+           cudaMalloc(&S.rw, n * sizeof(double)) == cudaSuccess &&
+           cudaMalloc(&S.tw32, n * sizeof(float)) == cudaSuccess &&
+           cudaMalloc(&S.tw64, n * sizeof(double)) == cudaSuccess;
+    good = good && cudaMalloc(&S.flag, ncomp * sizeof(int)) == cudaSuccess &&
+           cudaMemset(S.flag, 0, ncomp * sizeof(int)) == cudaSuccess &&
+           cudaMalloc(&S.nsweep, ncomp * sizeof(int)) == cudaSuccess &&
+           cudaMemset(S.nsweep, 0, ncomp * sizeof(int)) == cudaSuccess;
+  }
   good = good && cudaMalloc(&S.AB, std::max<int64_t>(S.band_total, 1) * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.ipiv, n * sizeof(int32_t)) == cudaSuccess;
   good = good && cudaMalloc(&S.rhs, n * sizeof(double)) == cudaSuccess;
+  good = good && cudaMalloc(&S.rdiag, n * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.dx, n * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.red, 4 * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.info, sizeof(int)) == cudaSuccess;
@@ -237,15 +309,18 @@ __global__ void band_gather(int64_t nnz, const int64_t* __restrict__ bmap, const
   if (k < nnz) AB[bmap[k]] = nzval[k];
 }
 
-// Banded LU with partial pivoting (LAPACK gbtf2 algorithm), one block per component.
+// Banded LU with partial pivoting (LAPACK gbtf2 algorithm), one block per
+// component.  Also writes the reciprocal pivots, which the backward
+// substitution multiplies by (gbtrs divides; the results differ by rounding).
 __global__ void __launch_bounds__(128) band_lu(const int64_t* cbase, const int32_t* cn, const int32_t* ckl,
                                                const int32_t* cku, const int32_t* cdof0, double* AB, int32_t* ipiv,
-                                               int* info) {
+                                               double* rdg, int* info) {
   const int cc = blockIdx.x;
   const int n = cn[cc], kl = ckl[cc], ku = cku[cc];
   const int kv = kl + ku, ld = 2 * kl + ku + 1;
   double* A = AB + cbase[cc];
   int32_t* piv = ipiv + cdof0[cc];
+  double* rdiag = rdg + cdof0[cc];  // reciprocal pivots for the backward substitution
   __shared__ double sval[128];
   __shared__ int sidx[128];
   __shared__ int s_jp, s_ju;
@@ -285,6 +360,7 @@ __global__ void __launch_bounds__(128) band_lu(const int64_t* cbase, const int32
       const double p = A[kv + jp + int64_t(ld) * k];
       s_piv = p;
       if (p == 0.0 && *info == 0) atomicCAS(info, 0, cc + 1);
+      rdiag[k] = 1.0 / p;
       s_ju = max(s_ju, min(k + ku + jp, n - 1));
     }
     __syncthreads();
@@ -322,8 +398,8 @@ __global__ void __launch_bounds__(128) band_lu(const int64_t* cbase, const int32
 // Solve with the band factors: permute, L with interchanges, U; one block per component.
 __global__ void __launch_bounds__(128) band_solve(const int64_t* cbase, const int32_t* cn, const int32_t* ckl,
                                                   const int32_t* cku, const int32_t* cdof0, const int32_t* perm,
-                                                  const double* AB, const int32_t* ipiv, const double* Ll, double* rhs,
-                                                  double* dx) {
+                                                  const double* AB, const int32_t* ipiv, const double* rdg,
+                                                  const double* Ll, double* rhs, double* dx) {
   const int cc = blockIdx.x;
   const int n = cn[cc], kl = ckl[cc], ku = cku[cc];
   const int kv = kl + ku, ld = 2 * kl + ku + 1;
@@ -349,7 +425,7 @@ __global__ void __launch_bounds__(128) band_solve(const int64_t* cbase, const in
   }
   // backward: U x = y  (U has kl+ku superdiagonals)
   for (int k = n - 1; k >= 0; --k) {
-    if (threadIdx.x == 0) b[k] /= A[kv + int64_t(ld) * k];
+    if (threadIdx.x == 0) b[k] *= rdg[cdof0[cc] + k];  // reciprocal pivot from band_lu
     __syncthreads();
     const double bk = b[k];
     const int m = min(kv, k);
@@ -409,16 +485,63 @@ __global__ void decrement_kernel(int64_t n, int OX, int first, const double* dx,
 
 extern "C" int mgpu_solver_create(mgpu_ctx* c) {
   c->solver = new Solver();
-  analyse(c, *c->solver);
+  Solver& S = *c->solver;
+  analyse(c, S);
   cudaGetLastError();  // analysis errors are reported at solve time
+  // default: the FP64 row-band kernels where they apply, else the FP64 block
+  // kernels (mgpu_set_linear_solver changes it)
+  S.path = S.wm ? PATH_F64ROWS : PATH_BLOCK;
+  if (getenv("MGPU_VERBOSE")) {
+    static const char* names[] = {"row-band FP32 + FP64 refinement", "row-band FP64", "block FP64"};
+    fprintf(stderr, "[muscade_gpu] solver: %s, %d components, max kl %d, max ku %d, %s\n",
+            S.ok ? "banded" : S.why.c_str(), S.ncomp, S.maxkl, S.maxku, names[S.path]);
+  }
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
+  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_BLOCK)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_set_linear_solver: bad arguments");
+  Solver& S = *c->solver;
+  if ((kind == MGPU_LINSOLVE_F32IR || kind == MGPU_LINSOLVE_F64) && !S.wm)
+    return set_err(c, MGPU_ERR_UNSUPPORTED,
+                   "linear solver kind needs kl <= 31 and kl+ku+1 <= 64 in every component (kl=" +
+                       std::to_string(S.maxkl) + ", ku=" + std::to_string(S.maxku) + ")");
+  S.path = kind == MGPU_LINSOLVE_AUTO ? (S.wm ? PATH_F64ROWS : PATH_BLOCK)
+           : kind == MGPU_LINSOLVE_F32IR ? PATH_F32IR
+           : kind == MGPU_LINSOLVE_F64   ? PATH_F64ROWS
+                                         : PATH_BLOCK;
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
+  if (!c || !c->solver || !info) return set_err(c, MGPU_ERR_ARG, "mgpu_linear_solver_info: bad arguments");
+  Solver& S = *c->solver;
+  info->kind = S.path == PATH_F32IR ? MGPU_LINSOLVE_F32IR : S.path == PATH_F64ROWS ? MGPU_LINSOLVE_F64 : MGPU_LINSOLVE_BLOCK;
+  info->ncomp = S.ncomp;
+  info->max_kl = S.maxkl;
+  info->max_ku = S.maxku;
+  info->last_fallback = 0;
+  info->last_sweeps = 0;
+  if (S.path == PATH_F32IR && S.ncomp > 0 && S.flag) {
+    std::vector<int> f(S.ncomp), w(S.ncomp);
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    MG_CUDA(cudaMemcpy(f.data(), S.flag, S.ncomp * sizeof(int), cudaMemcpyDeviceToHost));
+    MG_CUDA(cudaMemcpy(w.data(), S.nsweep, S.ncomp * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < S.ncomp; ++i) {
+      info->last_fallback += f[i] != 0;
+      info->last_sweeps = std::max(info->last_sweeps, w[i]);
+    }
+  }
   return MGPU_OK;
 }
 
 extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
   Solver* S = c->solver;
   if (!S) return;
-  void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx, S->red,
-                S->info};
+  void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx,
+                S->red, S->info, S->rbase, S->lbase, S->rbmap, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
+                S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -432,18 +555,40 @@ static unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 static int factor_solve(mgpu_ctx* c) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
-  MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
-  band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
-  if (S.maxkl < BW_ROWS && S.maxkl + S.maxku + 1 <= 32 * BW_SLOTS) {
-    // narrow bands: one warp per component (one per block, so that the
-    // components spread over all SMs and their FP64 pipes), window in registers
-    band_lu_warp<<<S.ncomp, 32, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
-    band_solve_warp<<<S.ncomp, 32, 0, st>>>(S.ncomp, S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv,
-                                            c->Ll, S.rhs, S.dx);
+  if (S.path == PATH_BLOCK) {
+    MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
+    band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
+    band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.rdiag, S.info);
+    band_solve<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv, S.rdiag, c->Ll,
+                                        S.rhs, S.dx);
   } else {
-    band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.info);
-    band_solve<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv, c->Ll, S.rhs,
-                                        S.dx);
+    // one warp per component, one per block, so that the components spread over all SMs
+    const RbComp cp{S.rbase, S.lbase, S.cn, S.ckl, S.cku, S.cdof0};
+    rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.rbmap, c->nzval, S.RB,
+                                                   S.path == PATH_F32IR ? S.RB32 : nullptr);
+    const int mode64 = S.path == PATH_F32IR ? RB_FALLBACK : RB_PLAIN;
+    if (S.path == PATH_F32IR) {
+      MG_CUDA(cudaMemsetAsync(S.flag, 0, S.ncomp * sizeof(int), st));
+      if (S.wm == 32) {
+        rb_lu<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, S.info);
+        rb_solve<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC32, S.LM32, S.ipiv, c->Ll, S.bw, S.xw,
+                                                    S.rw, S.tw32, S.dx, S.nref, RB_PRIMARY, S.flag, S.nsweep);
+      } else {
+        rb_lu<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, S.info);
+        rb_solve<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC32, S.LM32, S.ipiv, c->Ll, S.bw, S.xw,
+                                                    S.rw, S.tw32, S.dx, S.nref, RB_PRIMARY, S.flag, S.nsweep);
+      }
+    }
+    // FP64: the whole solve (PATH_F64ROWS) or the components flagged above
+    if (S.wm == 32) {
+      rb_lu<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, S.info);
+      rb_solve<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, c->Ll, S.bw, S.xw,
+                                                   S.rw, S.tw64, S.dx, 0, mode64, S.flag, nullptr);
+    } else {
+      rb_lu<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, S.info);
+      rb_solve<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, c->Ll, S.bw, S.xw,
+                                                   S.rw, S.tw64, S.dx, 0, mode64, S.flag, nullptr);
+    }
   }
   norms_kernel<<<1, 1024, 0, st>>>(c->nX, S.dx, c->Ll, S.red);
   MG_CUDA(cudaGetLastError());

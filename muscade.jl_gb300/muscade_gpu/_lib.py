@@ -16,7 +16,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
 SOURCES = ["mgpu.cu", "solver.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
-HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_warp.cuh"]
+HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes
@@ -83,11 +83,19 @@ class Stats(ctypes.Structure):
                 ("fail_iter", ctypes.c_int32), ("last_dx", ctypes.c_double), ("last_Ll", ctypes.c_double)]
 
 
+class LinsolveInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("ncomp", ctypes.c_int32), ("max_kl", ctypes.c_int32),
+                ("max_ku", ctypes.c_int32), ("last_fallback", ctypes.c_int32), ("last_sweeps", ctypes.c_int32)]
+
+
+LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3}
+LINSOLVE_NAME = {v: k for k, v in LINSOLVE.items()}
+
 # every symbol the header declares (checked by the CPU test suite)
 SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_get_pattern", "mgpu_get_asm",
            "mgpu_ntval", "mgpu_assemble", "mgpu_element_eval", "mgpu_upload_state", "mgpu_assemble_resident",
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
-           "mgpu_assemble_beams_noalloc"]
+           "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info"]
 
 _lib = None
 
@@ -124,6 +132,8 @@ def load():
     L.mgpu_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), pd, P(Stats)]
     L.mgpu_measure_fp64_peak.argtypes = [i32, pd]
     L.mgpu_assemble_beams_noalloc.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.mgpu_set_linear_solver.argtypes = [vp, i32]
+    L.mgpu_linear_solver_info.argtypes = [vp, P(LinsolveInfo)]
     for name in SYMBOLS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int and name not in ("mgpu_destroy",):

@@ -32,7 +32,7 @@ class DeviceError(MuscadeError):
 class DeviceModel:
     """One mgpu_ctx for a model (owns device memory and a CUDA stream)."""
 
-    def __init__(self, model, dis, device: int = 0):
+    def __init__(self, model, dis, device: int = 0, linsolve: str = "auto"):
         self.lib = L.load()
         self.model, self.dis = model, dis
         self.nX, self.nU = model.ndof["X"], model.ndof["U"]
@@ -67,6 +67,18 @@ class DeviceModel:
         self._check(rc)
         self.nnz = int(self.lib.mgpu_nnz(self.ctx))
         self.ntval = int(self.lib.mgpu_ntval(self.ctx))
+        if linsolve != "auto":
+            self.set_linear_solver(linsolve)
+
+    def set_linear_solver(self, kind: str):
+        """'auto' | 'f32ir' (FP32 factors + FP64 refinement) | 'f64' | 'block'."""
+        self._check(self.lib.mgpu_set_linear_solver(self.ctx, L.LINSOLVE[kind]))
+
+    def linear_solver_info(self):
+        info = L.LinsolveInfo()
+        self._check(self.lib.mgpu_linear_solver_info(self.ctx, ctypes.byref(info)))
+        return {"kind": L.LINSOLVE_NAME[info.kind], "ncomp": info.ncomp, "max_kl": info.max_kl,
+                "max_ku": info.max_ku, "last_fallback": info.last_fallback, "last_sweeps": info.last_sweeps}
 
     # ---------------------------------------------------------------- basics
     def _check(self, rc):

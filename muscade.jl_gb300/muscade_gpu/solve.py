@@ -26,10 +26,12 @@ class SweepXGPU:
 
 
 def solve(solver, initialstate: State, time, beta=0.25, gamma=0.5, maxiter=50, maxdx=1e-5, maxLl=math.inf,
-          pstate=None, device: int = 0, devmodel: DeviceModel | None = None, verbose=False):
+          pstate=None, device: int = 0, devmodel: DeviceModel | None = None, verbose=False, linsolve="auto"):
+    """`linsolve` picks the device linear solver: 'auto', 'f32ir', 'f64' or 'block'
+    (see DeviceModel.set_linear_solver); it is ignored when `devmodel` is given."""
     OX = solver.OX
     model, dis = initialstate.model, initialstate.dis
-    dm = devmodel or DeviceModel(model, dis, device=device)
+    dm = devmodel or DeviceModel(model, dis, device=device, linsolve=linsolve)
     try:
         X0 = list(initialstate.X)[: OX + 1]
         rc, states, stats = dm.sweepx(OX, np.asarray(time, dtype=np.float64), initialstate.time, X0,

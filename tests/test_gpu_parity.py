@@ -162,32 +162,43 @@ def test_assembly_parity(name, model):
     dm.close()
 
 
-def _compare_states(gpu_states, ref, nder, fieldX):
-    """States within TOL_STATE of the oracle, each dof class against its own scale.
+def _state_errors(gpu_states, ref, nder, fieldX):
+    """Largest deviation from the oracle over the trajectory, per dof class and
+    derivative order, relative to that class's largest value over the trajectory.
 
-    The time derivatives of the Lagrange multipliers are left out: the Newmark
-    decrement updates them like any X-dof (src/SweepX.jl:98-116) but no element
-    reads them, so they only carry the multipliers' rounding noise amplified by
-    γ/(βΔt) and 1/(βΔt²).
+    A per-step scale would be meaningless at the start of a ramped motion: the
+    displacements are then ~1e-5 m on node coordinates of ~1e3 m, so both codes
+    only resolve them to ~1e-13 m, and the Newmark update multiplies that
+    rounding by 1/(βΔt²) in the accelerations.  The time derivatives of the
+    Lagrange multipliers are left out: the Newmark decrement updates them like
+    any X-dof (src/SweepX.jl:98-116) but no element reads them, so they only
+    carry the multipliers' rounding amplified by γ/(βΔt) and 1/(βΔt²).
     """
     lam = np.array([str(f).startswith("λ") for f in fieldX])
     assert len(gpu_states) == len(ref)
-    for s, (t, Xr) in zip(gpu_states, ref):
-        for d in range(nder):
-            for sel in (~lam, lam):
-                if not sel.any() or (d > 0 and sel is lam):
-                    continue
-                x, xr = s.X[d][sel], Xr[d][sel]
-                scale = max(np.max(np.abs(xr)), 1e-300)
-                assert np.max(np.abs(x - xr)) / scale <= TOL_STATE, (t, d, "multipliers" if sel is lam else "dofs")
+    out = {}
+    for d in range(nder):
+        for name, sel in (("dofs", ~lam), ("multipliers", lam)):
+            if not sel.any() or (d > 0 and name == "multipliers"):
+                continue
+            dev = max(np.max(np.abs(s.X[d][sel] - Xr[d][sel])) for s, (t, Xr) in zip(gpu_states, ref))
+            scale = max(max(np.max(np.abs(Xr[d][sel])) for t, Xr in ref), 1e-300)
+            out[(name, d)] = dev / scale
+    return out
 
 
-def test_sweepx0_cantilever_matches_oracle():
+def _compare_states(gpu_states, ref, nder, fieldX):
+    errs = _state_errors(gpu_states, ref, nder, fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+@pytest.mark.parametrize("linsolve", ["f32ir", "f64", "block"])
+def test_sweepx0_cantilever_matches_oracle(linsolve):
     from muscade_gpu import SweepXGPU, solve
 
     m, times = W.cantilever()
     st = m.initialize()
-    out = solve(SweepXGPU[0], st, times, maxdx=1e-9, maxLl=1e-5)
+    out = solve(SweepXGPU[0], st, times, maxdx=1e-9, maxLl=1e-5, linsolve=linsolve)
     ref = REF.sweepx(m, st.dis, st, times, OX=0, maxdx=1e-9, maxLl=1e-5)
     _compare_states(out, ref, 1, st.dis.fieldX)
     tip = out[-1].X[0][120:123]
@@ -204,15 +215,62 @@ def test_sweepx0_lattice_matches_oracle():
     _compare_states(out, ref, 1, st.dis.fieldX)
 
 
-def test_sweepx2_risers_match_oracle():
+@pytest.mark.parametrize("linsolve", ["f32ir", "f64", "block"])
+def test_sweepx2_risers_match_oracle(linsolve):
     from muscade_gpu import SweepXGPU, solve
 
     m, times = W.risers(nriser=2, nel=20)
     st = m.initialize(time=0.0)
     T = times[:20]
-    out = solve(SweepXGPU[2], st, T, maxiter=20, maxdx=1e-5, maxLl=math.inf)
+    out = solve(SweepXGPU[2], st, T, maxiter=20, maxdx=1e-5, maxLl=math.inf, linsolve=linsolve)
     ref = REF.sweepx(m, st.dis, st, T, OX=2, maxiter=20, maxdx=1e-5, maxLl=math.inf)
     _compare_states(out, ref, 3, st.dis.fieldX)
+
+
+def _sweep(model, st, OX, times, linsolve, **kw):
+    dm = DeviceModel(model, st.dis, linsolve=linsolve)
+    rc, states, stats = dm.sweepx(OX, times, st.time, list(st.X), **kw)
+    info = dm.linear_solver_info()
+    dm.close()
+    assert rc == 0
+    return states, info
+
+
+def test_row_band_fp64_is_bitwise_the_block_solver():
+    """Same gbtf2/gbtrs arithmetic in two layouts: identical Newton trajectories."""
+    m, times = W.risers(nriser=3, nel=16)
+    st = m.initialize(time=0.0)
+    a, ia = _sweep(m, st, 2, times[:8], "f64", maxiter=20, maxdx=1e-5)
+    b, ib = _sweep(m, st, 2, times[:8], "block", maxiter=20, maxdx=1e-5)
+    assert ia["kind"] == "f64" and ib["kind"] == "block" and ia["ncomp"] == 3
+    assert np.array_equal(a, b)
+
+
+def test_fp32_refinement_reaches_fp64_accuracy():
+    """Risers: FP32 factors refined in FP64 give the FP64 trajectory to rounding, no fallback."""
+    m, times = W.risers(nriser=3, nel=16)
+    st = m.initialize(time=0.0)
+    a, ia = _sweep(m, st, 2, times[:8], "f32ir", maxiter=20, maxdx=1e-5)
+    b, _ = _sweep(m, st, 2, times[:8], "f64", maxiter=20, maxdx=1e-5)
+    assert ia["kind"] == "f32ir" and ia["last_fallback"] == 0 and 1 <= ia["last_sweeps"] <= 8
+    as_states = [[None, (a[k, 0], a[k, 1], a[k, 2])] for k in range(len(a))]
+    gpu = [type("S", (), {"X": X})() for _, X in as_states]
+    ref = [(0.0, (b[k, 0], b[k, 1], b[k, 2])) for k in range(len(b))]
+    errs = _state_errors(gpu, ref, 3, st.dis.fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+def test_fp32_refinement_falls_back_to_fp64_when_ill_conditioned():
+    """A 400-element cantilever (condition number ~1e12) defeats FP32 refinement:
+    the component is refactorised in FP64 and the result is the FP64 one
+    (three Newton iterations per step on both paths, small load)."""
+    m, _ = W.cantilever(nel=400, length=200.0, load=1e-3)
+    st = m.initialize()
+    times = np.array([0.1, 0.2])
+    a, ia = _sweep(m, st, 0, times, "f32ir", fixed_iter=3)
+    b, _ = _sweep(m, st, 0, times, "f64", fixed_iter=3)
+    assert ia["last_fallback"] == 1
+    assert np.array_equal(a, b)
 
 
 def test_nan_is_reported_like_the_reference():
