@@ -161,13 +161,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="60,60,20")
     ap.add_argument("--cpu-sample", type=int, default=int(os.environ.get("MGPU_CPU_SAMPLE", "60000")))
-    ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever"],
-                    help="lattice: the headline assembly metric; risers/cantilever: whole SweepX solves")
+    ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever", "batched"],
+                    help="lattice: the headline assembly metric; risers/cantilever: whole SweepX solves; "
+                         "batched: independent cantilevers and portal frames solved together")
+    ap.add_argument("--models", type=int, default=4096, help="batched: number of models")
+    ap.add_argument("--individual", type=int, default=16, help="batched: models also solved one by one")
+    ap.add_argument("--no-graph", action="store_true", help="risers: launch kernel by kernel instead of replaying "
+                                                              "a captured CUDA graph per step")
     ap.add_argument("--risers", type=int, default=200)
     ap.add_argument("--linsolve", default="auto", choices=["auto", "f32ir", "f64", "block"],
                     help="device linear solver of the whole-solve modes")
     args = ap.parse_args()
     rank, local_rank, ws, dist = dist_setup()
+    if args.config == "batched":
+        return bench_batched(args, rank, local_rank, ws, dist)
     if args.config != "lattice":
         return bench_solve(args, rank, local_rank, ws, dist)
     nx, ny, nz = (int(v) for v in args.grid.split(","))
@@ -303,7 +310,7 @@ def bench_solve(args, rank, local_rank, ws, dist):
     if args.config == "risers":
         model, times = workloads.risers(nriser=args.risers)
         st = model.initialize(time=0.0)
-        OX, kw = 2, dict(fixed_iter=3)
+        OX, kw = 2, dict(fixed_iter=3, graph=not args.no_graph)
         nstep_w, nstep = args.warmup, args.steps
         nbeam = model.groups[0].nele
     else:
@@ -353,12 +360,105 @@ def bench_solve(args, rank, local_rank, ws, dist):
             "value": ms_step, "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": steps_run,
             "warmup": nstep_w, "ms_per_step": ms_step, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.config, "beams": nbeam, "dofs": model.ndof["X"], "newton_iterations": iters,
+                       "cuda_graph": bool(kw.get("graph", False)),
                        "linear_solver": dm.linear_solver_info()},
             "beam_assemblies_per_s": value, "e2e": {"value": ms_step, "unit": "ms", "note": "whole solve incl. copies"},
             "cpu_baseline": {"value": cpu_rate, "unit": "beam assemblies/s", "kind": "port", "sample": sample,
                              "cores": os.cpu_count()}}
     print(json.dumps(line), flush=True)
     dm.close()
+
+
+
+def bench_batched(args, rank, local_rank, ws, dist):
+    """Independent models (half cantilevers, half portal frames, 10-400 beams,
+    8 load steps of SweepX{0}) solved together with per-model convergence.
+    One bench step is one whole batched solve.  Ranks solve disjoint sets of
+    models (seed per rank) with no collective: weak scaling by models."""
+    from muscade_gpu import _lib, workloads
+    from muscade_gpu.device import DeviceModel
+
+    _lib.build()
+    params = workloads.batched_params(args.models, seed=2030 + rank)
+    model, offs, times = workloads.build_batched(params)
+    st = model.initialize()
+    nbeam = model.groups[0].nele
+    kw = dict(maxdx=1e-9, maxLl=1e-5, per_component=True)
+    dm = DeviceModel(model, st.dis, device=local_rank)
+    X0 = list(st.X)
+    for _ in range(args.warmup):
+        dm.sweepx(0, times, st.time, X0, **kw)
+    if dist:
+        dist.barrier()
+    with Clocks(local_rank) as ck:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rc, xb, stats = dm.sweepx(0, times, st.time, X0, **kw)
+            if rc != 0:
+                raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
+        dt = (time.perf_counter() - t0) / args.steps
+    clocks = ck.summary()
+    dt = reduce_max(dist, dt)
+    iters = stats.niter_total
+    info64 = dm.linear_solver_info()
+    # the same batch with FP32 factors and FP64 refinement
+    dm.set_linear_solver("f32ir")
+    dm.sweepx(0, times, st.time, X0, **kw)
+    t0 = time.perf_counter()
+    rc32, x32, stats32 = dm.sweepx(0, times, st.time, X0, **kw)
+    dt32 = time.perf_counter() - t0
+    info32 = dm.linear_solver_info()
+    dm.close()
+    if rank != 0:
+        return
+    # per-model deviation of the FP32-refined states from the FP64 ones
+    bounds = list(offs) + [model.nnod]
+    worst = 0.0
+    if rc32 == 0:
+        for i in range(len(params)):
+            d = workloads.node_dofs(model, np.arange(bounds[i] + 1, bounds[i + 1] + 1))
+            d = d[d >= 0]
+            ref = xb[:, 0, d]
+            worst = max(worst, float(np.max(np.abs(x32[:, 0, d] - ref)) / max(np.max(np.abs(ref)), 1e-300)))
+    # the plain per-model path: models solved one by one (FP64), same seeded sample
+    pick = np.random.Generator(np.random.PCG64(7)).permutation(len(params))[: args.individual]
+    tind, same = [], True
+    for i in pick:
+        mi, _, _ = workloads.build_batched([params[i]])
+        si = mi.initialize()
+        di = DeviceModel(mi, si.dis, device=local_rank)
+        di.sweepx(0, times, si.time, list(si.X), maxdx=1e-9, maxLl=1e-5)  # warm
+        t0 = time.perf_counter()
+        rci, xi, _ = di.sweepx(0, times, si.time, list(si.X), maxdx=1e-9, maxLl=1e-5)
+        tind.append(time.perf_counter() - t0)
+        di.close()
+        nodes = np.arange(1, mi.nnod + 1)
+        a, b = workloads.node_dofs(mi, nodes), workloads.node_dofs(model, nodes + offs[i])
+        sel = a >= 0
+        same &= rci == 0 and bool(np.array_equal(xi[:, 0, a[sel]], xb[:, 0, b[sel]]))
+    per_model = 1.0 / float(np.mean(tind))
+    value = ws * len(params) / dt
+    h2d = 8 * (model.ndof["X"] + len(times) * dm.ntval + len(times))
+    d2h = 8 * model.ndof["X"] * len(times)
+    launches_per_iter = len(model.groups) + 2 + 9  # element kernels, scatters, solver, decrement, convergence
+    line = {"metric": "models/s (SweepX{0}, 8 load steps per model, per-model convergence)", "value": value,
+            "unit": "models/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded cantilevers and portal frames, lognormal sections, Gumbel loads)",
+            "config": {"workload": f"batched uneven models: {len(params)} models, {nbeam} beams, "
+                                   f"{model.ndof['X']} dofs", "models": len(params), "beams": nbeam,
+                       "dofs": model.ndof["X"], "newton_iterations": iters, "linear_solver": info64,
+                       "l2": "inputs larger than L2 (nzval alone is several hundred MB)"},
+            "beam_assemblies_per_s": ws * nbeam * iters / dt,
+            "e2e": {"value": value, "unit": "models/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "the whole mgpu_sweepx call with host initial state, load values and states"},
+            "per_model_path": {"models_per_s": per_model, "sample": int(len(pick)), "speedup_of_batch": value / per_model,
+                               "states_bitwise_equal_to_batch": same},
+            "fp32_refined": {"models_per_s": len(params) / dt32 if rc32 == 0 else None, "rc": rc32,
+                             "max_rel_state_dev_vs_fp64": worst, "linear_solver": info32,
+                             "newton_iterations": stats32.niter_total},
+            "gpu_launches": args.steps * iters * launches_per_iter, "clocks": clocks}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

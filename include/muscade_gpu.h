@@ -130,7 +130,14 @@ typedef struct {
   double maxdx;       /* convergence: Σ Δx² ≤ maxdx² */
   double maxLl;       /* and Σ Lλ² ≤ maxLl² (use +Inf to disable) */
   int32_t fixed_iter; /* > 0: exactly this many iterations per step, no convergence test
-                         (the reference has no such option; used for fixed-cost time stepping) */
+                         (the reference has no such option; used for fixed-cost time stepping).
+                         The steps then replay one captured CUDA graph (up to 63 iterations) and
+                         the host waits for the device only at the end of the sweep. */
+  int32_t per_component; /* != 0: the convergence test is applied to each connected component
+                            of Lλx on its own (independent models solved together); a component
+                            that passes stops iterating while the others go on, so each follows
+                            the iterations it would take alone.  Needs fixed_iter = 0. */
+  int32_t no_graph;      /* != 0: fixed-iteration steps are launched kernel by kernel */
 } mgpu_sweep_opts;
 
 typedef struct {
@@ -159,8 +166,9 @@ int mgpu_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, d
  *   MGPU_LINSOLVE_AUTO   F64 where every component has kl <= 31 and
  *                        kl+ku+1 <= 64, else BLOCK (the default)
  *   MGPU_LINSOLVE_F32IR  FP32 factors, FP64 residuals and iterative refinement
- *                        to working precision; a component whose refinement
- *                        does not reach 1e-10 relative is refactorised in FP64
+ *                        until the correction is below 1e-12 of the solution;
+ *                        a component that does not contract, or would need
+ *                        more than 8 sweeps, is refactorised in FP64
  *   MGPU_LINSOLVE_F64    FP64 factors, one warp per component
  *   MGPU_LINSOLVE_BLOCK  FP64 factors, one thread block per component, bands up to 256
  * F64 and BLOCK give bitwise the same Δx.  Returns MGPU_ERR_UNSUPPORTED when

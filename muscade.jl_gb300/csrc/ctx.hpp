@@ -57,14 +57,29 @@ struct mgpu_ctx {
   size_t flush_bytes = 0;
   int nXder_resident = 1;
   mgpu::Solver* solver = nullptr;
+  // constants of the current step, read by the kernels from device memory so
+  // that a captured step replays with new values: t, a1, a2, a3, b1, b2, b3
+  double* stepc = nullptr;   // [8] device
+  double* hstepc = nullptr;  // pinned upload ring [kStepcSlots][8]
+  cudaEvent_t stepc_ev[8] = {};
+  int stepc_slot = 0;
 };
 
 namespace mgpu {
-// launches one complete assembly on ctx->stream from the resident state;
-// ev_groups (optional) receives an event after each element type's kernel
-int launch_assembly(mgpu_ctx* c, int mission, double t, const mgpu_newmark* nm, cudaEvent_t* ev_groups);
+constexpr int kStepcSlots = 8;
+// enqueue the upload of the step constants (t and the Newmark coefficients,
+// zero when nm is NULL) to ctx->stepc
+int upload_stepc(mgpu_ctx* c, double t, const mgpu_newmark* nm);
+// launches one complete assembly on ctx->stream from the resident state and
+// step constants; ev_groups (optional) receives an event after each element
+// type's kernel.  Enqueues no copy and no synchronisation (capturable).
+int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups);
+// errflag <- INT_MAX on ctx->stream (capturable)
+void launch_reset_errflag(mgpu_ctx* c);
 int set_err(mgpu_ctx* c, int code, const std::string& msg);
 int check_nan(mgpu_ctx* c);
+// MGPU_ERR_NAN with the reference's message for an errflag value (MGPU_OK for INT_MAX)
+int nan_error(mgpu_ctx* c, int flag);
 }  // namespace mgpu
 
 #define MG_CUDA(call)                                                                    \

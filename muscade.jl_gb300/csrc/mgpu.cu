@@ -49,8 +49,8 @@ struct AsmArgs {
   const double* av;  // Newmark a (per dof), step mission only
   const double* bv;
   const double* scale;  // per dof or nullptr
-  double t;
-  double p0, p1, p2;
+  const double* sc;     // step constants: t, a1, a2, a3, b1, b2, b3
+  double p0;            // coefficient of ∂/∂X₀ (1)
   int mission;
   int* errflag;
 };
@@ -98,8 +98,8 @@ __global__ void __launch_bounds__(128) beam_kernel(int64_t nele, const int32_t* 
     for (int k = 0; k < 3; ++k) U[k] = __ldg(a.u + __ldg(uidx + k * nele + e));
   double R[12], K[144], rd[12];
   const bool step = DYN && a.mission == MGPU_ASM_STEP;
-  beam_element<DYN>(bc, X0, X1, X2, has_u ? U : nullptr, Perturb{a.p0, a.p1, a.p2}, av, bv, R, K, step ? rd : nullptr,
-                    nullptr);
+  const Perturb pt{a.p0, DYN ? a.sc[1] : 0.0, DYN ? a.sc[4] : 0.0};  // K + a1 C + b1 M
+  beam_element<DYN>(bc, X0, X1, X2, has_u ? U : nullptr, pt, av, bv, R, K, step ? rd : nullptr, nullptr);
   double s[12];
 #pragma unroll
   for (int i = 0; i < 12; ++i) s[i] = a.scale ? __ldg(a.scale + dof[i]) : 1.0;
@@ -145,7 +145,8 @@ __global__ void bar_kernel(int64_t nele, int nder, const int32_t* __restrict__ i
   if (has_u)
     for (int k = 0; k < 3; ++k) U[k] = __ldg(a.u + __ldg(uidx + k * nele + e));
   double R[6], K[36], rd[6];
-  bar_element(bc, nder, X0, X1, X2, has_u ? U : nullptr, a.t, a.p0, a.p1, a.p2, step ? av : nullptr,
+  bar_element(bc, nder, X0, X1, X2, has_u ? U : nullptr, a.sc[0], a.p0, nder > 1 ? a.sc[1] : 0.0,
+              nder > 1 ? a.sc[4] : 0.0, step ? av : nullptr,
               step ? bv : nullptr, R, K, rd, nullptr);
   double s[6];
   for (int i = 0; i < 6; ++i) s[i] = a.scale ? __ldg(a.scale + dof[i]) : 1.0;
@@ -225,13 +226,16 @@ __global__ void scatter_kernel(int64_t n, const uint32_t* __restrict__ seg, cons
   out[k] = s;
 }
 
-__global__ void newmark_ab_kernel(int64_t n, const double* x1, const double* x2, double a2, double a3, double b2,
-                                  double b3, double* av, double* bv) {
+__global__ void newmark_ab_kernel(int64_t n, const double* x1, const double* x2, const double* __restrict__ sc,
+                                  double* av, double* bv) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double a2 = sc[2], a3 = sc[3], b2 = sc[5], b3 = sc[6];
   av[i] = a2 * x1[i] + a3 * x2[i];
   bv[i] = b2 * x1[i] + b3 * x2[i];
 }
+
+__global__ void set_int_kernel(int* p, int v) { *p = v; }
 
 __global__ void fill_kernel(double* p, int64_t n, double v) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -241,7 +245,27 @@ __global__ void fill_kernel(double* p, int64_t n, double v) {
 static inline unsigned nblk(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 
 // ------------------------------------------------------------------ assembly
-int launch_assembly(mgpu_ctx* c, int mission, double t, const mgpu_newmark* nm, cudaEvent_t* ev_groups) {
+int upload_stepc(mgpu_ctx* c, double t, const mgpu_newmark* nm) {
+  const int k = c->stepc_slot;
+  c->stepc_slot = (k + 1) % kStepcSlots;
+  MG_CUDA(cudaEventSynchronize(c->stepc_ev[k]));  // the copy that last read this slot is done
+  double* h = c->hstepc + 8 * k;
+  h[0] = t;
+  h[1] = nm ? nm->a1 : 0.0;
+  h[2] = nm ? nm->a2 : 0.0;
+  h[3] = nm ? nm->a3 : 0.0;
+  h[4] = nm ? nm->b1 : 0.0;
+  h[5] = nm ? nm->b2 : 0.0;
+  h[6] = nm ? nm->b3 : 0.0;
+  h[7] = 0.0;
+  MG_CUDA(cudaMemcpyAsync(c->stepc, h, 8 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  MG_CUDA(cudaEventRecord(c->stepc_ev[k], c->stream));
+  return MGPU_OK;
+}
+
+void launch_reset_errflag(mgpu_ctx* c) { set_int_kernel<<<1, 1, 0, c->stream>>>(c->errflag, INT_MAX); }
+
+int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups) {
   const int64_t nX = c->nX;
   AsmArgs a;
   a.x0 = c->x;
@@ -252,17 +276,14 @@ int launch_assembly(mgpu_ctx* c, int mission, double t, const mgpu_newmark* nm, 
   a.av = c->ab;
   a.bv = c->ab + nX;
   a.scale = c->scale;
-  a.t = t;
+  a.sc = c->stepc;
   a.mission = mission;
   a.errflag = c->errflag;
   const bool dyn = mission != MGPU_ASM_STATIC;
   a.p0 = 1.0;
-  a.p1 = dyn ? nm->a1 : 0.0;
-  a.p2 = dyn ? nm->b1 : 0.0;
   if (dyn && c->nXder_resident != 3) return set_err(c, MGPU_ERR_ARG, "Newmark assembly needs X, X' and X''");
   if (mission == MGPU_ASM_STEP && nX > 0)
-    newmark_ab_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, a.x1, a.x2, nm->a2, nm->a3, nm->b2, nm->b3, c->ab,
-                                                             c->ab + nX);
+    newmark_ab_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, a.x1, a.x2, c->stepc, c->ab, c->ab + nX);
   int64_t gid0 = 0;
   for (size_t g = 0; g < c->groups.size(); ++g) {
     const DevGroup& G = c->groups[g];
@@ -310,9 +331,13 @@ int check_nan(mgpu_ctx* c) {
   int h[1];
   MG_CUDA(cudaMemcpyAsync(h, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   MG_CUDA(cudaStreamSynchronize(c->stream));
-  if (h[0] != INT_MAX) {
+  return nan_error(c, h[0]);
+}
+
+int nan_error(mgpu_ctx* c, int flag) {
+  if (flag != INT_MAX) {
     // locate type and element
-    int64_t gid = h[0], base = 0;
+    int64_t gid = flag, base = 0;
     for (size_t g = 0; g < c->groups.size(); ++g) {
       if (gid < base + c->groups[g].nele) {
         const char* names[] = {"?", "EulerBeam3D", "Bar3D", "DofConstraint", "DofLoad"};
@@ -330,8 +355,8 @@ int check_nan(mgpu_ctx* c) {
 }
 
 static int reset_errflag(mgpu_ctx* c) {
-  const int v = INT_MAX;
-  MG_CUDA(cudaMemcpyAsync(c->errflag, &v, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  launch_reset_errflag(c);
+  MG_CUDA(cudaGetLastError());
   return MGPU_OK;
 }
 
@@ -479,6 +504,10 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
   MG_CUDA(cudaMemset(c->tv, 0, std::max<int64_t>(c->ntval, 1) * sizeof(double)));
   MG_TRY(dalloc(c, &c->ab, 2 * c->nX));
   MG_TRY(dalloc(c, &c->errflag, 2));
+  MG_TRY(dalloc(c, &c->stepc, 8));
+  MG_CUDA(cudaMemset(c->stepc, 0, 8 * sizeof(double)));
+  MG_CUDA(cudaMallocHost(&c->hstepc, kStepcSlots * 8 * sizeof(double)));
+  for (int k = 0; k < kStepcSlots; ++k) MG_CUDA(cudaEventCreateWithFlags(&c->stepc_ev[k], cudaEventDisableTiming));
   if (d->scaleX) {
     bool ones = true;
     for (int64_t i = 0; i < d->nX; ++i) ones &= (d->scaleX[i] == 1.0);
@@ -504,8 +533,11 @@ extern "C" void mgpu_destroy(mgpu_ctx* c) {
     cudaFree(G.cdata);
   }
   void* ps[] = {c->kbuf, c->rbuf, c->mseg, c->msrc, c->vseg, c->vsrc, c->nzval, c->Ll, c->x,
-                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush};
+                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush, c->stepc};
   for (void* p : ps) cudaFree(p);
+  if (c->hstepc) cudaFreeHost(c->hstepc);
+  for (cudaEvent_t e : c->stepc_ev)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -551,7 +583,8 @@ extern "C" int mgpu_assemble_resident(mgpu_ctx* c, int32_t mission, double t, co
   if (!c || mission < 0 || mission > 2 || (mission != MGPU_ASM_STATIC && !nm))
     return set_err(c, MGPU_ERR_ARG, "mgpu_assemble_resident: bad arguments");
   MG_CUDA(cudaSetDevice(c->device));
-  return launch_assembly(c, mission, t, nm, nullptr);
+  MG_TRY(upload_stepc(c, t, mission != MGPU_ASM_STATIC ? nm : nullptr));
+  return launch_assembly(c, mission, nullptr);
 }
 
 extern "C" int mgpu_download(mgpu_ctx* c, double* Ll, double* nzval) {
@@ -581,6 +614,7 @@ extern "C" int mgpu_time_assemble(mgpu_ctx* c, int32_t mission, double t, const 
     MG_TRY(dalloc(c, reinterpret_cast<double**>(&c->flush), c->flush_bytes / 8));
   }
   MG_TRY(reset_errflag(c));
+  MG_TRY(upload_stepc(c, t, mission != MGPU_ASM_STATIC ? nm : nullptr));
   const int ng = int(c->groups.size());
   const int ne = ng + 2;  // start, one per group, end
   std::vector<cudaEvent_t> ev(size_t(ne) * reps);
@@ -590,7 +624,7 @@ extern "C" int mgpu_time_assemble(mgpu_ctx* c, int32_t mission, double t, const 
       fill_kernel<<<nblk(c->flush_bytes / 8, 256), 256, 0, c->stream>>>(c->flush, c->flush_bytes / 8, double(r));
     cudaEvent_t* E = &ev[size_t(ne) * r];
     MG_CUDA(cudaEventRecord(E[0], c->stream));
-    MG_TRY(launch_assembly(c, mission, t, nm, E + 1));
+    MG_TRY(launch_assembly(c, mission, E + 1));
     MG_CUDA(cudaEventRecord(E[ng + 1], c->stream));
   }
   MG_CUDA(cudaStreamSynchronize(c->stream));

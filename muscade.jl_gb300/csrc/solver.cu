@@ -31,6 +31,9 @@ using namespace mgpu;
 
 namespace mgpu {
 
+constexpr int kNormBlocks = 128;
+constexpr int kInfoSlots = 64;  // a captured step holds up to kInfoSlots-1 iterations
+
 enum SolverPath : int {
   PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
   PATH_F64ROWS = 1,  // row-band warp kernels in FP64
@@ -78,7 +81,11 @@ struct Solver {
   double* rdiag = nullptr;    // [nX] reciprocal pivots (block kernels)
   double* dx = nullptr;       // [nX] Δx in model order
   double* red = nullptr;      // [4] reductions: ΣΔx², ΣLλ²
-  int* info = nullptr;        // [1] first singular component+1 (0 = ok)
+  double* part = nullptr;     // [2 * kNormBlocks] partial sums of the reductions
+  int* info = nullptr;        // [kInfoSlots] first singular component+1 (0 = ok), one slot per iteration of a step
+  int32_t* cod = nullptr;     // [nX] component of each dof
+  int* frozen = nullptr;      // [ncomp] converged in this step (per-component convergence)
+  int* nactive = nullptr;     // [1] components still iterating
   double* hbuf = nullptr;     // pinned host: red[0..1], info
 };
 
@@ -293,7 +300,17 @@ static void analyse(mgpu_ctx* c, Solver& S) {
   good = good && cudaMalloc(&S.rdiag, n * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.dx, n * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.red, 4 * sizeof(double)) == cudaSuccess;
-  good = good && cudaMalloc(&S.info, sizeof(int)) == cudaSuccess;
+  good = good && cudaMalloc(&S.part, 2 * kNormBlocks * sizeof(double)) == cudaSuccess;
+  good = good && cudaMalloc(&S.info, kInfoSlots * sizeof(int)) == cudaSuccess &&
+         cudaMemset(S.info, 0, kInfoSlots * sizeof(int)) == cudaSuccess;
+  {
+    std::vector<int32_t> cod(n);
+    for (int64_t j = 0; j < n; ++j) cod[j] = comp[j];
+    good = good && up(&S.cod, cod);
+  }
+  good = good && cudaMalloc(&S.frozen, std::max(ncomp, 1) * sizeof(int)) == cudaSuccess &&
+         cudaMemset(S.frozen, 0, std::max(ncomp, 1) * sizeof(int)) == cudaSuccess;
+  good = good && cudaMalloc(&S.nactive, sizeof(int)) == cudaSuccess;
   good = good && cudaMallocHost(&S.hbuf, 8 * sizeof(double)) == cudaSuccess;
   if (!good) {
     S.why = "device allocation failed for the solver";
@@ -435,18 +452,19 @@ __global__ void __launch_bounds__(128) band_solve(const int64_t* cbase, const in
   for (int k = threadIdx.x; k < n; k += blockDim.x) dx[pm[k]] = b[k];
 }
 
-// Σ Δx², Σ Lλ² (deterministic: single block, fixed order of partial sums)
-__global__ void __launch_bounds__(1024) norms_kernel(int64_t n, const double* dx, const double* Ll, double* red) {
-  __shared__ double s1[1024], s2[1024];
+// Σ Δx², Σ Lλ²: kNormBlocks partial sums (fixed assignment and tree order), then
+// one block adds the partials in index order -- deterministic for a given n
+__global__ void __launch_bounds__(256) norms_partial(int64_t n, const double* dx, const double* Ll, double* part) {
+  __shared__ double s1[256], s2[256];
   double a = 0.0, b = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x; i < n; i += int64_t(gridDim.x) * 256) {
     a += dx[i] * dx[i];
     b += Ll[i] * Ll[i];
   }
   s1[threadIdx.x] = a;
   s2[threadIdx.x] = b;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+  for (int s = 128; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
       s1[threadIdx.x] += s1[threadIdx.x + s];
       s2[threadIdx.x] += s2[threadIdx.x + s];
@@ -454,16 +472,60 @@ __global__ void __launch_bounds__(1024) norms_kernel(int64_t n, const double* dx
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    red[0] = s1[0];
-    red[1] = s2[0];
+    part[2 * blockIdx.x] = s1[0];
+    part[2 * blockIdx.x + 1] = s2[0];
+  }
+}
+__global__ void norms_final(int nb, const double* part, double* red) {
+  if (threadIdx.x != 0) return;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k < nb; ++k) {
+    a += part[2 * k];
+    b += part[2 * k + 1];
+  }
+  red[0] = a;
+  red[1] = b;
+}
+
+// Per-component convergence for independent models solved together: ΣΔx² and
+// ΣLλ² over the component's dofs (one warp, fixed order); a component that
+// meets the test is frozen for the rest of the step, the others are counted.
+__global__ void __launch_bounds__(32) comp_converge(const int32_t* __restrict__ cn, const int32_t* __restrict__ cdof0,
+                                                    const int32_t* __restrict__ perm, const double* __restrict__ dx,
+                                                    const double* __restrict__ Ll, double cdx2, double cLl2,
+                                                    int* __restrict__ frozen, int* __restrict__ nactive) {
+  const int cc = blockIdx.x, lane = threadIdx.x;
+  if (frozen[cc]) return;
+  const int n = cn[cc];
+  const int32_t* pm = perm + cdof0[cc];
+  double a = 0.0, b = 0.0;
+  for (int k = lane; k < n; k += 32) {
+    const int d = pm[k];
+    a += dx[d] * dx[d];
+    b += Ll[d] * Ll[d];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    if (a <= cdx2 && b <= cLl2)
+      frozen[cc] = 1;
+    else
+      atomicAdd(nactive, 1);
   }
 }
 
 // Newmarkβdecrement!  (src/SweepX.jl:98-132, decrement! src/Assemble.jl:206-211)
-__global__ void decrement_kernel(int64_t n, int OX, int first, const double* dx, const double* scale, double a1,
-                                 double a2, double a3, double b1, double b2, double b3, double* x) {
+// (frozen, cod): dofs of converged components keep their state (per-component convergence)
+__global__ void decrement_kernel(int64_t n, int OX, int first, const double* dx, const double* scale,
+                                 const double* __restrict__ sc, double* x, const int* __restrict__ frozen,
+                                 const int32_t* __restrict__ cod) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (frozen && frozen[cod[i]]) return;
+  const double a1 = sc[1], a2 = sc[2], a3 = sc[3], b1 = sc[4], b2 = sc[5], b3 = sc[6];
   const double s = scale ? scale[i] : 1.0;
   const double d = dx[i];
   if (OX == 2) {
@@ -541,7 +603,8 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
   if (!S) return;
   void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx,
                 S->red, S->info, S->rbase, S->lbase, S->rbmap, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
-                S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag};
+                S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag, S->part, S->cod, S->frozen,
+                S->nactive};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -551,14 +614,15 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
 namespace mgpu {
 static unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 
-// one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device)
-static int factor_solve(mgpu_ctx* c) {
+// one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device);
+// a singular factorisation writes its component+1 to *info.  Capturable.
+static int factor_solve(mgpu_ctx* c, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
   if (S.path == PATH_BLOCK) {
     MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
     band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
-    band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.rdiag, S.info);
+    band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.rdiag, info);
     band_solve<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.perm, S.AB, S.ipiv, S.rdiag, c->Ll,
                                         S.rhs, S.dx);
   } else {
@@ -570,28 +634,182 @@ static int factor_solve(mgpu_ctx* c) {
     if (S.path == PATH_F32IR) {
       MG_CUDA(cudaMemsetAsync(S.flag, 0, S.ncomp * sizeof(int), st));
       if (S.wm == 32) {
-        rb_lu<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, S.info);
+        rb_lu<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, info);
         rb_solve<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC32, S.LM32, S.ipiv, c->Ll, S.bw, S.xw,
                                                     S.rw, S.tw32, S.dx, S.nref, RB_PRIMARY, S.flag, S.nsweep);
       } else {
-        rb_lu<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, S.info);
+        rb_lu<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, info);
         rb_solve<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC32, S.LM32, S.ipiv, c->Ll, S.bw, S.xw,
                                                     S.rw, S.tw32, S.dx, S.nref, RB_PRIMARY, S.flag, S.nsweep);
       }
     }
     // FP64: the whole solve (PATH_F64ROWS) or the components flagged above
     if (S.wm == 32) {
-      rb_lu<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, S.info);
+      rb_lu<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, info);
       rb_solve<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, c->Ll, S.bw, S.xw,
                                                    S.rw, S.tw64, S.dx, 0, mode64, S.flag, nullptr);
     } else {
-      rb_lu<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, S.info);
+      rb_lu<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, info);
       rb_solve<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, c->Ll, S.bw, S.xw,
                                                    S.rw, S.tw64, S.dx, 0, mode64, S.flag, nullptr);
     }
   }
-  norms_kernel<<<1, 1024, 0, st>>>(c->nX, S.dx, c->Ll, S.red);
+  norms_partial<<<kNormBlocks, 256, 0, st>>>(c->nX, S.dx, c->Ll, S.part);
+  norms_final<<<1, 32, 0, st>>>(kNormBlocks, S.part, S.red);
   MG_CUDA(cudaGetLastError());
+  return MGPU_OK;
+}
+}  // namespace mgpu
+
+namespace mgpu {
+static mgpu_newmark newmark_coefficients(double beta, double gamma, double dt) {
+  // Newmarkβcoefficients (src/SweepX.jl:3-15)
+  return mgpu_newmark{gamma / (beta * dt), gamma / beta, (gamma / (2 * beta) - 1) * dt, 1 / (beta * dt * dt),
+                      1 / (beta * dt), 1 / (2 * beta)};
+}
+
+static int singular_error(mgpu_ctx* c, mgpu_stats* stats, int64_t step, int it) {
+  stats->fail_step = int(step + 1);
+  stats->fail_iter = it;
+  char msg[128];
+  snprintf(msg, sizeof msg, "matrix factorization failed at step=%d, iiter=%d", int(step + 1), it);
+  return set_err(c, MGPU_ERR_SINGULAR, msg);
+}
+
+// Fixed-iteration steps replayed from one captured CUDA graph: per step the
+// host uploads t, the Newmark coefficients and the load values (pinned,
+// double-buffered), launches the graph, and queues the state and the error
+// flags back; it waits only at the end.  Errors are then reported for the
+// first failing step, with the states of the steps before it.
+static int sweep_graph(mgpu_ctx* c, int OX, int64_t nstep, const double* times, double t0, const double* tvals,
+                       const mgpu_sweep_opts* opts, double* states, mgpu_stats* stats) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  const int64_t n = c->nX;
+  const int nder = OX + 1, nit = opts->fixed_iter;
+  // steps with a positive time step (the reference stops at the first that is not)
+  int64_t nrun = nstep;
+  {
+    double told = t0;
+    for (int64_t k = 0; k < nstep; ++k) {
+      if (OX > 0 && !(times[k] - told > 0)) {
+        nrun = k;
+        break;
+      }
+      told = times[k];
+    }
+  }
+  const int64_t slot = 8 + c->ntval;
+  double* hbuf = nullptr;
+  int* hflags = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool registered = false;
+  int rc = MGPU_OK;
+  const size_t state_bytes = size_t(nstep) * nder * n * sizeof(double);
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(st);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    if (hbuf) cudaFreeHost(hbuf);
+    if (hflags) cudaFreeHost(hflags);
+    if (registered) cudaHostUnregister(states);
+    cudaGetLastError();
+  };
+#define MG_G(call)                                                                                        \
+  do {                                                                                                    \
+    cudaError_t e_ = (call);                                                                              \
+    if (e_ != cudaSuccess) {                                                                              \
+      rc = set_err(c, MGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+      cleanup();                                                                                          \
+      return rc;                                                                                          \
+    }                                                                                                     \
+  } while (0)
+  MG_G(cudaMallocHost(&hbuf, 2 * slot * sizeof(double)));
+  MG_G(cudaMallocHost(&hflags, std::max<int64_t>(nrun, 1) * (nit + 1) * sizeof(int)));
+  for (auto& e : ev) MG_G(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  if (state_bytes > 0) {
+    registered = cudaHostRegister(states, state_bytes, cudaHostRegisterDefault) == cudaSuccess;
+    if (!registered) cudaGetLastError();  // pageable copies still work, synchronously
+  }
+  // capture one step
+  MG_G(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  launch_reset_errflag(c);
+  cudaMemsetAsync(S.info, 0, kInfoSlots * sizeof(int), st);
+  for (int it = 1; it <= nit && rc == MGPU_OK; ++it) {
+    const int mission = OX == 0 ? MGPU_ASM_STATIC : (it == 1 ? MGPU_ASM_STEP : MGPU_ASM_ITER);
+    rc = launch_assembly(c, mission, nullptr);
+    if (rc == MGPU_OK) rc = factor_solve(c, S.info + it);
+    if (rc == MGPU_OK)
+      decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, it == 1, S.dx, c->scale, c->stepc, c->x, nullptr,
+                                                    nullptr);
+  }
+  {
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc != MGPU_OK) {
+      cleanup();
+      return rc;
+    }
+    MG_G(e);
+  }
+  MG_G(cudaGraphInstantiate(&exec, graph, 0));
+  double told = t0;
+  for (int64_t step = 0; step < nrun; ++step) {
+    const double t = times[step], dt = t - told;
+    told = t;
+    const mgpu_newmark nm = OX == 2 ? newmark_coefficients(opts->beta, opts->gamma, dt) : mgpu_newmark{0, 0, 0, 0, 0, 0};
+    const int k = int(step & 1);
+    MG_G(cudaEventSynchronize(ev[k]));  // the upload two steps back has read this slot
+    double* h = hbuf + k * slot;
+    const double v[8] = {t, nm.a1, nm.a2, nm.a3, nm.b1, nm.b2, nm.b3, 0.0};
+    for (int q = 0; q < 8; ++q) h[q] = v[q];
+    for (int64_t q = 0; q < c->ntval; ++q) h[8 + q] = tvals[step * c->ntval + q];
+    MG_G(cudaMemcpyAsync(c->stepc, h, 8 * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (c->ntval > 0) MG_G(cudaMemcpyAsync(c->tv, h + 8, c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
+    MG_G(cudaEventRecord(ev[k], st));
+    MG_G(cudaGraphLaunch(exec, st));
+    MG_G(cudaMemcpyAsync(states + step * nder * n, c->x, nder * n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int* f = hflags + step * (nit + 1);
+    MG_G(cudaMemcpyAsync(f, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_G(cudaMemcpyAsync(f + 1, S.info + 1, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
+  }
+  MG_G(cudaMemcpyAsync(S.hbuf, S.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MG_G(cudaStreamSynchronize(st));
+  stats->last_dx = std::sqrt(S.hbuf[0]);
+  stats->last_Ll = std::sqrt(S.hbuf[1]);
+  for (int64_t step = 0; step < nrun; ++step) {
+    const int* f = hflags + step * (nit + 1);
+    // within a step the NaN check of an iteration precedes its factorisation
+    int bad_it = 0;
+    for (int it = 1; it <= nit && !bad_it; ++it)
+      if (f[it] != 0) bad_it = it;
+    if (f[0] != INT_MAX || bad_it) {
+      stats->nstep_done = int(step);
+      stats->niter_total = int(step) * nit + (bad_it ? bad_it : 1);
+      if (f[0] != INT_MAX) {
+        stats->fail_step = int(step + 1);
+        stats->fail_iter = 0;
+        rc = nan_error(c, f[0]);
+      } else {
+        rc = singular_error(c, stats, step, bad_it);
+      }
+      cleanup();
+      return rc;
+    }
+  }
+  stats->nstep_done = int(nrun);
+  stats->niter_total = int(nrun) * nit;
+  cleanup();
+#undef MG_G
+  if (nrun < nstep) {
+    stats->fail_step = int(nrun + 1);
+    char msg[128];
+    snprintf(msg, sizeof msg, "Time step length not strictly positive at step=%3d", int(nrun + 1));
+    return set_err(c, MGPU_ERR_ARG, msg);
+  }
   return MGPU_OK;
 }
 }  // namespace mgpu
@@ -600,8 +818,10 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
                            const double* x0, const double* u, const double* tvals, const mgpu_sweep_opts* opts,
                            double* states, mgpu_stats* stats) {
   if (!c || !times || !opts || !states || !stats || !(OX == 0 || OX == 2) || nstep < 0 || nXder0 < 0 ||
-      nXder0 > OX + 1 || (nXder0 > 0 && !x0))
+      nXder0 > OX + 1 || (nXder0 > 0 && !x0) || (c->ntval > 0 && nstep > 0 && !tvals))
     return set_err(c, MGPU_ERR_ARG, "mgpu_sweepx: bad arguments");
+  if (opts->per_component && opts->fixed_iter > 0)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_sweepx: per_component needs the convergence test (fixed_iter = 0)");
   *stats = mgpu_stats{0, 0, 0, 0, 0.0, 0.0};
   Solver& S = *c->solver;
   if (!S.ok) return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why);
@@ -613,7 +833,10 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
   if (nXder0 > 0) MG_CUDA(cudaMemcpyAsync(c->x, x0, nXder0 * n * sizeof(double), cudaMemcpyHostToDevice, st));
   if (c->nU > 0 && u) MG_CUDA(cudaMemcpyAsync(c->u, u, c->nU * sizeof(double), cudaMemcpyHostToDevice, st));
   c->nXder_resident = OX + 1;
+  if (opts->fixed_iter > 0 && opts->fixed_iter < kInfoSlots && !opts->no_graph)
+    return sweep_graph(c, OX, nstep, times, t0, tvals, opts, states, stats);
   const int nder = OX + 1;
+  const bool percomp = opts->per_component != 0;
   const double cdx2 = opts->maxdx * opts->maxdx, cLl2 = opts->maxLl * opts->maxLl;
   double told = t0;
   for (int64_t step = 0; step < nstep; ++step) {
@@ -626,60 +849,66 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
       snprintf(msg, sizeof msg, "Time step length not strictly positive at step=%3d", int(step + 1));
       return set_err(c, MGPU_ERR_ARG, msg);
     }
-    mgpu_newmark nm{0, 0, 0, 0, 0, 0};
-    if (OX == 2) {
-      const double be = opts->beta, ga = opts->gamma;
-      nm = mgpu_newmark{ga / (be * dt), ga / be, (ga / (2 * be) - 1) * dt, 1 / (be * dt * dt), 1 / (be * dt),
-                        1 / (2 * be)};
-    }
+    const mgpu_newmark nm = OX == 2 ? newmark_coefficients(opts->beta, opts->gamma, dt) : mgpu_newmark{0, 0, 0, 0, 0, 0};
+    int rc = upload_stepc(c, t, OX == 2 ? &nm : nullptr);
+    if (rc) return rc;
     if (c->ntval > 0)
       MG_CUDA(cudaMemcpyAsync(c->tv, tvals + step * c->ntval, c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (percomp) MG_CUDA(cudaMemsetAsync(S.frozen, 0, std::max(S.ncomp, 1) * sizeof(int), st));
     const int itmax = opts->fixed_iter > 0 ? opts->fixed_iter : opts->maxiter;
     for (int it = 1; it <= itmax; ++it) {
       stats->niter_total++;
       const int first = it == 1;
       const int mission = OX == 0 ? MGPU_ASM_STATIC : (first ? MGPU_ASM_STEP : MGPU_ASM_ITER);
-      const int v = INT_MAX;
-      MG_CUDA(cudaMemcpyAsync(c->errflag, &v, sizeof(int), cudaMemcpyHostToDevice, st));
+      launch_reset_errflag(c);
       MG_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
-      int rc = launch_assembly(c, mission, t, &nm, nullptr);
+      rc = launch_assembly(c, mission, nullptr);
       if (rc) return rc;
-      rc = factor_solve(c);
+      rc = factor_solve(c, S.info);
       if (rc) return rc;
-      decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, first, S.dx, c->scale, nm.a1, nm.a2, nm.a3, nm.b1, nm.b2,
-                                                    nm.b3, c->x);
+      decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, first, S.dx, c->scale, c->stepc, c->x,
+                                                    percomp ? S.frozen : nullptr, S.cod);
+      if (percomp) {
+        MG_CUDA(cudaMemsetAsync(S.nactive, 0, sizeof(int), st));
+        comp_converge<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dx, c->Ll, cdx2, cLl2, S.frozen, S.nactive);
+      }
       MG_CUDA(cudaMemcpyAsync(S.hbuf, S.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-      MG_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(S.hbuf + 2), S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
-      MG_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(S.hbuf + 3), c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      int* hi = reinterpret_cast<int*>(S.hbuf + 2);
+      MG_CUDA(cudaMemcpyAsync(hi, S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      MG_CUDA(cudaMemcpyAsync(hi + 1, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      if (percomp) MG_CUDA(cudaMemcpyAsync(hi + 2, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
       MG_CUDA(cudaStreamSynchronize(st));
       const double dx2 = S.hbuf[0], Ll2 = S.hbuf[1];
-      const int info = *reinterpret_cast<int*>(S.hbuf + 2);
       stats->last_dx = std::sqrt(dx2);
       stats->last_Ll = std::sqrt(Ll2);
-      if (*reinterpret_cast<int*>(S.hbuf + 3) != INT_MAX) {
+      if (hi[1] != INT_MAX) {
         stats->fail_step = int(step + 1);
         stats->fail_iter = it;
-        return check_nan(c);
+        return nan_error(c, hi[1]);
       }
-      if (info != 0) {
-        stats->fail_step = int(step + 1);
-        stats->fail_iter = it;
-        char msg[128];
-        snprintf(msg, sizeof msg, "matrix factorization failed at step=%d, iiter=%d", int(step + 1), it);
-        return set_err(c, MGPU_ERR_SINGULAR, msg);
-      }
+      if (hi[0] != 0) return singular_error(c, stats, step, it);
       if (opts->fixed_iter > 0) {
         if (it == opts->fixed_iter) break;
         continue;
       }
-      if (dx2 <= cdx2 && Ll2 <= cLl2) break;
+      const bool done = percomp ? hi[2] == 0 : (dx2 <= cdx2 && Ll2 <= cLl2);
+      if (done) break;
       if (it == opts->maxiter) {
         stats->fail_step = int(step + 1);
         stats->fail_iter = it;
+        std::string which;
+        if (percomp) {
+          std::vector<int> fz(S.ncomp);
+          MG_CUDA(cudaMemcpy(fz.data(), S.frozen, S.ncomp * sizeof(int), cudaMemcpyDeviceToHost));
+          int first_open = 0;
+          while (first_open < S.ncomp && fz[first_open]) ++first_open;
+          which = " (" + std::to_string(hi[2]) + " components, the first is component " +
+                  std::to_string(first_open + 1) + ")";
+        }
         char msg[256];
         snprintf(msg, sizeof msg, "no convergence of step %3d after %3d iterations |Δx|=%g / %g, |Lλ|=%g / %g",
                  int(step + 1), it, std::sqrt(dx2), opts->maxdx, Ll2, opts->maxLl);
-        return set_err(c, MGPU_ERR_NOCONV, msg);
+        return set_err(c, MGPU_ERR_NOCONV, msg + which);
       }
     }
     MG_CUDA(cudaMemcpyAsync(states + step * nder * n, c->x, nder * n * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -170,14 +170,19 @@ class DeviceModel:
 
     # ---------------------------------------------------------------- solver
     def sweepx(self, OX, times, t0, X0, U=None, beta=0.25, gamma=0.5, maxiter=50, maxdx=1e-5, maxLl=math.inf,
-               fixed_iter=0):
+               fixed_iter=0, per_component=False, graph=True):
+        """Whole SweepX{OX} on the device.  fixed_iter > 0 runs exactly that many
+        Newton iterations per step (replayed from a captured CUDA graph unless
+        graph=False); per_component applies the convergence test to each
+        connected component (independent models) on its own."""
         times = np.ascontiguousarray(times, dtype=np.float64)
         nstep = len(times)
         X0 = [np.asarray(v, dtype=np.float64) for v in X0][: OX + 1]
         x0 = np.ascontiguousarray(np.concatenate(X0)) if X0 else np.zeros(0)
         u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
         tv = np.ascontiguousarray(np.stack([self.tvals(t) for t in times]) if self.ntval else np.zeros((nstep, 0)))
-        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, fixed_iter)
+        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, fixed_iter, int(bool(per_component)),
+                           int(not graph))
         states = np.zeros((nstep, OX + 1, self.nX))
         stats = L.Stats()
         rc = self.lib.mgpu_sweepx(self.ctx, OX, nstep, L.ptr(times), float(t0), len(X0), L.ptr(x0), L.ptr(u),

@@ -120,3 +120,88 @@ def risers(nriser=200, nel=250, length=1000.0, seed=2028, EA=5e9, EI=1e6, GJ=1e6
     m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t2",), lfield="λtop2", coeffs=[1.0], offset=zero, name="sway")
     m.addelement(DofConstraint, tops, xinod=(1,), xfield=("t3",), lfield="λtop3", coeffs=[1.0], offset=lift, name="lift")
     return m, 0.05 * np.arange(1, 2001)
+
+
+# ---------------------------------------------------------------- batched models
+def batched_params(nmodel=4096, nel_range=(10, 400), seed=2030, sigma=0.15):
+    """Parameters of independent models for one batched solve: half
+    cantilevers of the 10 m type above (tip DofLoad in t3), half portal frames
+    (two 5 m columns and a 10 m beam, both bases held in all six dofs,
+    mid-span DofLoad in -t3).  Element counts U{nel_range}; EA, EI2, EI3, GJ
+    the cantilever's times lognormal(0, sigma) per model; load Gumbel with mode
+    1e3 N and scale 200 N, ramped by t."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    portal = rng.random(nmodel) < 0.5
+    nel = rng.integers(nel_range[0], nel_range[1] + 1, nmodel)
+    ln = np.exp(rng.normal(0.0, sigma, (nmodel, 4)))
+    load = rng.gumbel(1e3, 200.0, nmodel)
+    return [dict(kind="portal" if portal[i] else "cantilever", nel=int(nel[i]), EA=EA0 * ln[i, 0], EI2=EI0 * ln[i, 1],
+                 EI3=EI0 * ln[i, 2], GJ=GJ0 * ln[i, 3], load=float(load[i])) for i in range(nmodel)]
+
+
+def _model_geometry(p):
+    """Node coordinates (local), beam connectivity (local, 1-based), held nodes, loaded node, load sign."""
+    nel = p["nel"]
+    if p["kind"] == "cantilever":
+        xs = np.linspace(0.0, 10.0, nel + 1)
+        xyz = np.stack([xs, np.zeros_like(xs), np.zeros_like(xs)], axis=1)
+        conn = np.stack([np.arange(1, nel + 1), np.arange(2, nel + 2)], axis=1)
+        return xyz, conn, [1], nel + 1, 1.0
+    H, B = 5.0, 10.0
+    ncol = max(1, nel // 4)
+    nbeam = nel - 2 * ncol
+    if nbeam % 2:  # even beam element count: a node at mid-span
+        ncol, nbeam = ncol + 1, nbeam - 1
+    if nbeam < 2:
+        ncol, nbeam = (nel - 2) // 2, 2 + (nel - 2) % 2
+    left = np.stack([np.zeros(ncol + 1), np.zeros(ncol + 1), np.linspace(0.0, H, ncol + 1)], axis=1)
+    top = np.stack([np.linspace(0.0, B, nbeam + 1)[1:], np.zeros(nbeam), np.full(nbeam, H)], axis=1)
+    right = np.stack([np.full(ncol, B), np.zeros(ncol), np.linspace(H, 0.0, ncol + 1)[1:]], axis=1)
+    xyz = np.concatenate([left, top, right])
+    nn = len(xyz)
+    conn = np.stack([np.arange(1, nn), np.arange(2, nn + 1)], axis=1)
+    mid = ncol + 1 + nbeam // 2
+    return xyz, conn, [1, nn], mid, -1.0
+
+
+def build_batched(params, spacing=30.0):
+    """One Model holding the given independent models (disjoint node sets, side
+    by side in y).  Returns (model, node_offset per model, load times)."""
+    m = Model("batched")
+    geo = [_model_geometry(p) for p in params]
+    xyz, conn, held, loaded, sign, offs = [], [], [], [], [], []
+    mats = {k: [] for k in ("EA", "EI2", "EI3", "GJ")}
+    off = 0
+    for i, (p, (x, c, h, ld, sg)) in enumerate(zip(params, geo)):
+        x = x.copy()
+        x[:, 1] += spacing * i
+        xyz.append(x)
+        conn.append(c + off)
+        held += [hh + off for hh in h]
+        loaded.append(ld + off)
+        sign.append(sg * p["load"])
+        for k in mats:
+            mats[k].append(np.full(len(c), p[k]))
+        offs.append(off)
+        off += len(x)
+    m.addnode(np.concatenate(xyz))
+    mat = BeamCrossSection(EA=np.concatenate(mats["EA"]), EI2=np.concatenate(mats["EI2"]),
+                           EI3=np.concatenate(mats["EI3"]), GJ=np.concatenate(mats["GJ"]), mu=MU0, iota1=IOTA0)
+    m.addelement(EulerBeam3D, np.concatenate(conn), mat=mat, orient2=(0.0, 1.0, 0.0))
+    held = np.asarray(held)[:, None]
+    for f in ("t1", "t2", "t3", "r1", "r2", "r3"):
+        m.addelement(Hold, held, field=f)
+    F = np.asarray(sign)
+
+    def ramp(t, F=F):
+        return F * t
+
+    m.addelement(DofLoad, np.asarray(loaded)[:, None], field="t3", value=ramp)
+    return m, np.asarray(offs), np.round(np.arange(1, 9) * 0.125, 12)
+
+
+def node_dofs(model, nodes):
+    """X-dof indices (0-based) of every X dof type at the given nodes, in dof-type order; -1 where absent."""
+    nodes = np.asarray(nodes, dtype=np.int64)
+    xt = [i for i, d in enumerate(model.doftyp) if d.cls == "X"]
+    return model._ndmap[nodes[:, None] - 1, np.asarray(xt)[None, :]] - 1

@@ -273,6 +273,55 @@ def test_fp32_refinement_falls_back_to_fp64_when_ill_conditioned():
     assert np.array_equal(a, b)
 
 
+def test_graph_replay_matches_kernel_by_kernel_launches():
+    """Fixed-iteration Newmark steps replayed from one captured CUDA graph give
+    the states of the same kernels launched one by one."""
+    m, times = W.risers(nriser=3, nel=16)
+    st = m.initialize(time=0.0)
+    dm = DeviceModel(m, st.dis)
+    rc1, a, s1 = dm.sweepx(2, times[:12], st.time, list(st.X), fixed_iter=3, graph=True)
+    rc2, b, s2 = dm.sweepx(2, times[:12], st.time, list(st.X), fixed_iter=3, graph=False)
+    dm.close()
+    assert rc1 == 0 and rc2 == 0 and s1.nstep_done == s2.nstep_done == 12 and s1.niter_total == 36
+    assert np.array_equal(a, b)
+
+
+def test_batched_models_follow_their_own_iterations():
+    """Independent models in one context with per-component convergence give,
+    bitwise, the states each model reaches when solved alone."""
+    params = W.batched_params(6, nel_range=(10, 30), seed=11)
+    mb, offs, times = W.build_batched(params)
+    sb = mb.initialize()
+    dm = DeviceModel(mb, sb.dis)
+    rc, xb, stats = dm.sweepx(0, times, sb.time, list(sb.X), maxdx=1e-9, maxLl=1e-5, per_component=True)
+    info = dm.linear_solver_info()
+    dm.close()
+    assert rc == 0 and info["ncomp"] == 6
+    for p, off in zip(params, offs):
+        mi, _, _ = W.build_batched([p])
+        si = mi.initialize()
+        dmi = DeviceModel(mi, si.dis)
+        rci, xi, _ = dmi.sweepx(0, times, si.time, list(si.X), maxdx=1e-9, maxLl=1e-5)
+        dmi.close()
+        assert rci == 0
+        nodes = np.arange(1, mi.nnod + 1)
+        di, db = W.node_dofs(mi, nodes), W.node_dofs(mb, nodes + off)
+        assert np.array_equal(di >= 0, db >= 0)
+        sel = di >= 0
+        assert np.array_equal(xi[:, 0, di[sel]], xb[:, 0, db[sel]]), p
+
+
+def test_sweepx0_portal_frame_matches_oracle():
+    from muscade_gpu import SweepXGPU, solve
+
+    p = next(q for q in W.batched_params(20, nel_range=(12, 24), seed=5) if q["kind"] == "portal")
+    m, _, times = W.build_batched([p])
+    st = m.initialize()
+    out = solve(SweepXGPU[0], st, times, maxdx=1e-9, maxLl=1e-5)
+    ref = REF.sweepx(m, st.dis, st, times, OX=0, maxdx=1e-9, maxLl=1e-5)
+    _compare_states(out, ref, 1, st.dis.fieldX)
+
+
 def test_nan_is_reported_like_the_reference():
     m, _ = W.cantilever()
     st = m.initialize()
