@@ -53,6 +53,9 @@ typedef struct {
   const int64_t *indexX; /* [nele][nX] 1-based model X-dof indices */
   const int64_t *indexU; /* [nele][nU] 1-based model U-dof indices (NULL if nU==0) */
   const double *edata;   /* [nele][ndata] element fields in the reference's declaration order */
+  const int64_t *indexA; /* [nele] 1-based A-dof of each element, NULL if none.  EULERBEAM3D only:
+                            the EI scale factor of the wrapper element EulerBeam3D{adof}
+                            (bending stiffnesses EI2, EI3 times the A-dof value) */
 } mgpu_group;
 
 typedef struct {
@@ -62,6 +65,7 @@ typedef struct {
   const mgpu_group *groups; /* [ngroup] */
   const double *scaleX;     /* [nX] dof scales (dis.scaleX), NULL for all ones */
   int32_t device;           /* CUDA device ordinal */
+  int64_t nA;               /* getndof(model,:A) */
 } mgpu_model_desc;
 
 /* Newmark-β coefficients (src/SweepX.jl:3-15) */
@@ -158,6 +162,29 @@ typedef struct {
 int mgpu_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, double t0, int32_t nXder0,
                 const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts, double *states,
                 mgpu_stats *stats);
+
+/* Values of the A-dofs, A[nA] (initially all 1: the nominal EI).  Copied; in
+ * effect for the following assemblies and solves. */
+int mgpu_set_A(mgpu_ctx *ctx, const double *A);
+
+/* Cost sensitivities of a SweepX{OX} run by the discrete adjoint (the
+ * analogue of DirectXUA's ∂C/∂A, src/DirectXUA.jl:438-513, for the Newmark
+ * time discretisation).  Runs the converged forward sweep (fixed_iter = 0,
+ * per_component = 0; opts as for mgpu_sweepx), keeping the state at the start
+ * of every segment of `ckpt` steps (ckpt <= 0: ⌈√nstep⌉), then walks the steps
+ * backwards, recomputing each segment from its checkpoint, and solves the
+ * transposed tangent of every step.  The cost is
+ *   C = Σ_n w_n Σ_s cost_w[s] (x_n[cost_dof[s]] − cost_y[n][s])²
+ * with w_n = t_n − t_{n−1} for OX = 2 (t_0 = t0) and 1 for OX = 0;
+ * cost_dof[ncost] are distinct 1-based X-dofs (SingleDofCost sensors).
+ * Outputs: *cost, dCdA[nA] (EI-scale A-dofs), and, when dCdtv != NULL,
+ * dCdtv[nstep][ntval]: the sensitivities to the load values F(t) of DofLoad
+ * elements and the gap offsets c(t) of DofConstraint elements, in the layout of
+ * tvals.  Needs the row-band solver for the transposed tangent. */
+int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, double t0, int32_t nXder0,
+                        const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts,
+                        int64_t ncost, const int64_t *cost_dof, const double *cost_w, const double *cost_y,
+                        int32_t ckpt, double *cost, double *dCdA, double *dCdtv, mgpu_stats *stats);
 
 /* Linear solver of the Newton loops (no counterpart in the reference, which
  * calls UMFPACK through lu/lu!/\ at src/SweepX.jl:207-210).  Every connected

@@ -1,0 +1,375 @@
+// Discrete adjoint of SweepX{OX} for cost sensitivities with respect to the
+// A-dofs and the time values of the loads.
+//
+// The reference obtains ∂C/∂A in DirectXUA as the A-block of the Lagrangian
+// gradient once the (Λ, X, U) blocks have converged (src/DirectXUA.jl:438-513),
+// over an all-steps system with finite differences in time.  Here the time
+// discretisation is the Newmark-β of SweepX (src/SweepX.jl:3-15, 98-132): the
+// cost
+//     C = Σ_n w_n Σ_s c_s (x_n[d_s] − y_{n,s})²,   w_n = Δt_n (OX = 2) or 1 (OX = 0),
+// is differentiated through the converged steps (the implicit-function adjoint
+// of R(x_n, v_n(x_n, S_{n-1}), a_n(x_n, S_{n-1}); A) = 0):
+//
+//   g_n      = x̄_n + a1 v̄_n + b1 ā_n            (x̄_n includes ∂C/∂x_n)
+//   J_nᵀ μ_n = g_n                               J_n = K + a1 C + b1 M at step n
+//   dC/dA   −= μ_nᵀ ∂R_n/∂A,   dC/dF_n = −μ_nᵀ ∂R_n/∂F_n
+//   p = v̄_n − C_nᵀ μ_n,   q = ā_n − M_nᵀ μ_n
+//   x̄_{n-1} = −a1 p − b1 q,  v̄_{n-1} = (1 − a2) p − b2 q,  ā_{n-1} = −a3 p + (1 − b3) q
+//
+// with a1..b3 the Newmark coefficients of step n.  With dof scaling the
+// device matrices are S J S and the residual S R: the solve uses S g and the
+// products S⁻¹ (S C S)ᵀ μ.  States are recomputed from √N checkpoints: the
+// forward pass keeps the state at the start of every segment of `ckpt` steps;
+// the reverse pass recomputes one segment (the same deterministic kernels, so
+// the same iterates bit for bit) and walks back through it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "beam_math.hpp"
+#include "solver.hpp"
+
+namespace mgpu {
+
+// Σ_s c_s (x[d_s] − y_s)², one block, fixed order
+__global__ void __launch_bounds__(256) adj_cost_value(int64_t ncost, const int32_t* __restrict__ dof,
+                                                      const double* __restrict__ cw, const double* __restrict__ y,
+                                                      const double* __restrict__ x, double* __restrict__ out) {
+  __shared__ double sm[256];
+  double a = 0.0;
+  for (int64_t s = threadIdx.x; s < ncost; s += 256) {
+    const double r = x[dof[s]] - y[s];
+    a += cw[s] * r * r;
+  }
+  sm[threadIdx.x] = a;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) sm[threadIdx.x] += sm[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0];
+}
+
+// x̄[d_s] += f · 2 c_s (x[d_s] − y_s)   (sensor dofs are distinct)
+__global__ void adj_cost_grad(int64_t ncost, const int32_t* __restrict__ dof, const double* __restrict__ cw,
+                              const double* __restrict__ y, const double* __restrict__ x, double f,
+                              double* __restrict__ xb) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s < ncost) xb[dof[s]] += f * 2.0 * cw[s] * (x[dof[s]] - y[s]);
+}
+
+// g = S (x̄ + a1 v̄ + b1 ā)
+__global__ void adj_rhs(int64_t n, int OX, double a1, double b1, const double* __restrict__ scale,
+                        const double* __restrict__ xb, const double* __restrict__ vb, const double* __restrict__ ab,
+                        double* __restrict__ g) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = xb[i];
+  if (OX == 2) v += a1 * vb[i] + b1 * ab[i];
+  g[i] = v * (scale ? scale[i] : 1.0);
+}
+
+// y_j = S⁻¹_j Σ_q nz[q] μ[row[q]] over column j (the transposed product, one thread per column)
+__global__ void adj_csc_tmatvec(int64_t n, const int64_t* __restrict__ colptr, const int32_t* __restrict__ rowval,
+                                const double* __restrict__ nz, const double* __restrict__ mu,
+                                const double* __restrict__ scale, double* __restrict__ y) {
+  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double s = 0.0;
+  for (int64_t q = colptr[j]; q < colptr[j + 1]; ++q) s += nz[q] * mu[rowval[q]];
+  y[j] = scale ? s / scale[j] : s;
+}
+
+__global__ void adj_propagate(int64_t n, double a1, double a2, double a3, double b1, double b2, double b3,
+                              const double* __restrict__ tC, const double* __restrict__ tM, double* __restrict__ xb,
+                              double* __restrict__ vb, double* __restrict__ ab) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p = vb[i] - tC[i], q = ab[i] - tM[i];
+  xb[i] = -a1 * p - b1 * q;
+  vb[i] = (1.0 - a2) * p - b2 * q;
+  ab[i] = -a3 * p + (1.0 - b3) * q;
+}
+
+// Per EI-scaled beam: contrib[e] = −μᵀ ∂(S R_e)/∂A_e.  R is linear in the
+// bending constants, so ∂R_e/∂A_e is the residual of the element with every
+// other stiffness, mass and load term set to zero (the state's bending forces).
+__global__ void __launch_bounds__(128) adj_beam_dRdA(int64_t nele, const int32_t* __restrict__ idx,
+                                                     const double* __restrict__ cdata, const double* __restrict__ x0,
+                                                     const double* __restrict__ mu,
+                                                     const double* __restrict__ scale, double* __restrict__ contrib) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  BeamConst bc;
+  double* d = reinterpret_cast<double*>(&bc);
+  for (int f = 0; f < int(sizeof(BeamConst) / sizeof(double)); ++f) d[f] = __ldg(cdata + f * nele + e);
+  bc.ke = 0.0;
+  bc.kt = 0.0;
+  bc.mu = 0.0;
+  bc.iota1 = 0.0;
+  bc.w = 0.0;
+  for (int k = 0; k < 3; ++k) bc.Ca[k] = bc.Cl[k] = bc.Cq[k] = 0.0;
+  int dof[12];
+  double X0[12], R[12], K[144];
+  for (int i = 0; i < 12; ++i) {
+    dof[i] = __ldg(idx + i * nele + e);
+    X0[i] = __ldg(x0 + dof[i]);
+  }
+  beam_element<false>(bc, X0, X0, X0, nullptr, Perturb{1.0, 0.0, 0.0}, nullptr, nullptr, R, K, nullptr, nullptr);
+  double s = 0.0;
+  for (int i = 0; i < 12; ++i) s += mu[dof[i]] * R[i] * (scale ? scale[dof[i]] : 1.0);
+  contrib[e] = -s;
+}
+
+// gradA[a] += Σ contrib over the elements of A-dof a (in element order)
+__global__ void adj_agrad(int64_t nA, const int64_t* __restrict__ aptr, const int32_t* __restrict__ aele,
+                          const double* __restrict__ contrib, double* __restrict__ gradA) {
+  const int64_t a = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (a >= nA) return;
+  double s = 0.0;
+  for (int64_t q = aptr[a]; q < aptr[a + 1]; ++q) s += contrib[aele[q]];
+  gradA[a] += s;
+}
+
+// dC/dF for DofLoad (R = −F s) and for the offset c of DofConstraint (R_λ = −(Σaᵢxᵢ − c) s_λ)
+__global__ void adj_dtv(int64_t nele, int nX, int sign, const int32_t* __restrict__ idx,
+                        const double* __restrict__ mu, const double* __restrict__ scale, double* __restrict__ out) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  const int d = __ldg(idx + int64_t(nX - 1) * nele + e);
+  out[e] = sign * mu[d] * (scale ? scale[d] : 1.0);
+}
+
+}  // namespace mgpu
+
+using namespace mgpu;
+
+extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double* times, double t0,
+                                   int32_t nXder0, const double* x0, const double* u, const double* tvals,
+                                   const mgpu_sweep_opts* opts, int64_t ncost, const int64_t* cost_dof,
+                                   const double* cost_w, const double* cost_y, int32_t ckpt, double* cost,
+                                   double* dCdA, double* dCdtv, mgpu_stats* stats) {
+  if (!c || !times || !opts || !stats || !cost || !(OX == 0 || OX == 2) || nstep < 1 || nXder0 < 0 ||
+      nXder0 > OX + 1 || (nXder0 > 0 && !x0) || ncost < 0 || (ncost > 0 && (!cost_dof || !cost_w || !cost_y)) ||
+      (c->ntval > 0 && !tvals) || (c->nA > 0 && !dCdA))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_adjoint_sweepx: bad arguments");
+  if (opts->fixed_iter > 0 || opts->per_component)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_adjoint_sweepx: the adjoint needs converged steps (fixed_iter = 0, "
+                                    "per_component = 0)");
+  *stats = mgpu_stats{0, 0, 0, 0, 0.0, 0.0};
+  Solver& S = *c->solver;
+  if (!S.ok) return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why);
+  if (!S.wmT)
+    return set_err(c, MGPU_ERR_UNSUPPORTED, "the adjoint needs the row-band solver (kl, ku <= 31, kl+ku+1 <= 64)");
+  const int64_t n = c->nX;
+  std::vector<int32_t> cdof(ncost);
+  {
+    std::vector<char> seen(n, 0);
+    for (int64_t s = 0; s < ncost; ++s) {
+      if (cost_dof[s] < 1 || cost_dof[s] > n) return set_err(c, MGPU_ERR_ARG, "cost dof out of range");
+      if (seen[cost_dof[s] - 1]++) return set_err(c, MGPU_ERR_ARG, "cost dofs must be distinct");
+      cdof[s] = int32_t(cost_dof[s] - 1);
+    }
+  }
+  MG_CUDA(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  if (ckpt <= 0) ckpt = int32_t(std::ceil(std::sqrt(double(nstep))));
+  ckpt = int32_t(std::min<int64_t>(ckpt, nstep));
+  const int64_t nseg = (nstep + ckpt - 1) / ckpt;
+  // A-dof -> beams (CSR over the EI-scaled beams of all groups, element order)
+  std::vector<int64_t> aptr(c->nA + 1, 0);
+  std::vector<int32_t> aele;
+  std::vector<int64_t> abase;  // per group: offset of its beams in contrib (-1 if none)
+  int64_t nbA = 0;
+  for (auto& G : c->groups) {
+    abase.push_back(G.aidx ? nbA : -1);
+    if (G.aidx) nbA += G.nele;
+  }
+  {
+    std::vector<std::vector<int32_t>> lists(c->nA);
+    for (size_t g = 0; g < c->groups.size(); ++g)
+      if (abase[g] >= 0)
+        for (int64_t e = 0; e < c->groups[g].nele; ++e)
+          lists[c->groups[g].h_indexA[e] - 1].push_back(int32_t(abase[g] + e));
+    for (int64_t a = 0; a < c->nA; ++a) {
+      aptr[a + 1] = aptr[a] + int64_t(lists[a].size());
+      aele.insert(aele.end(), lists[a].begin(), lists[a].end());
+    }
+  }
+  // device buffers
+  std::vector<void*> owned;
+  int rc = MGPU_OK;
+  auto alloc = [&](auto** p, size_t count) -> bool {
+    using T = typename std::remove_pointer<typename std::remove_reference<decltype(*p)>::type>::type;
+    if (cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return false;
+    owned.push_back(*p);
+    return true;
+  };
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(st);
+    for (void* p : owned) cudaFree(p);
+    cudaGetLastError();
+  };
+  const size_t ns = size_t(3) * n;
+  double *ck, *seg, *xb, *vb, *ab, *g, *mu, *tC, *tM, *costs, *cw, *cy, *gradA, *contrib, *dtv = nullptr;
+  int32_t *dcd, *aeled, *rowv;
+  int64_t *aptrd, *colp;
+  bool ok = alloc(&ck, nseg * ns) && alloc(&seg, size_t(ckpt) * ns) && alloc(&xb, n) && alloc(&vb, n) &&
+            alloc(&ab, n) && alloc(&g, n) && alloc(&mu, n) && alloc(&tC, n) && alloc(&tM, n) &&
+            alloc(&costs, nstep) && alloc(&cw, ncost) && alloc(&cy, size_t(nstep) * ncost) &&
+            alloc(&gradA, c->nA) && alloc(&contrib, nbA) && alloc(&dcd, ncost) && alloc(&aeled, aele.size()) &&
+            alloc(&aptrd, aptr.size()) && alloc(&colp, n + 1) && alloc(&rowv, c->pat.nnz);
+  if (ok && dCdtv && c->ntval > 0) ok = alloc(&dtv, size_t(nstep) * c->ntval);
+  if (!ok) {
+    cleanup();
+    return set_err(c, MGPU_ERR_NOMEM, "device allocation failed for the adjoint");
+  }
+  {
+    std::vector<int32_t> rv(c->pat.rowval.begin(), c->pat.rowval.end());
+    ok = cudaMemcpy(colp, c->pat.colptr.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(rowv, rv.data(), rv.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(dcd, cdof.data(), ncost * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(cw, cost_w, ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(cy, cost_y, size_t(nstep) * ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(aptrd, aptr.data(), aptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         (aele.empty() ||
+          cudaMemcpy(aeled, aele.data(), aele.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess) &&
+         cudaMemsetAsync(gradA, 0, std::max<int64_t>(c->nA, 1) * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(xb, 0, n * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(vb, 0, n * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(ab, 0, n * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(tC, 0, n * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(tM, 0, n * sizeof(double), st) == cudaSuccess;
+    if (!ok) {
+      cleanup();
+      return set_err(c, MGPU_ERR_CUDA, "adjoint: upload failed");
+    }
+  }
+#define ADJ_TRY(x)  \
+  do {              \
+    rc = (x);       \
+    if (rc) {       \
+      cleanup();    \
+      return rc;    \
+    }               \
+  } while (0)
+#define ADJ_CUDA(call)                                                                                  \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess) {                                                                            \
+      rc = set_err(c, MGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));               \
+      cleanup();                                                                                        \
+      return rc;                                                                                        \
+    }                                                                                                   \
+  } while (0)
+  // initial state
+  ADJ_CUDA(cudaMemsetAsync(c->x, 0, ns * sizeof(double), st));
+  if (nXder0 > 0) ADJ_CUDA(cudaMemcpyAsync(c->x, x0, nXder0 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (c->nU > 0 && u) ADJ_CUDA(cudaMemcpyAsync(c->u, u, c->nU * sizeof(double), cudaMemcpyHostToDevice, st));
+  c->nXder_resident = OX + 1;
+  auto tprev = [&](int64_t k) { return k == 0 ? t0 : times[k - 1]; };  // time of the state before step k+1
+  auto tvk = [&](int64_t k) { return c->ntval > 0 ? tvals + k * c->ntval : nullptr; };
+  // ---- forward pass: checkpoints and costs
+  for (int64_t k = 0; k < nstep; ++k) {
+    if (k % ckpt == 0) ADJ_CUDA(cudaMemcpyAsync(ck + (k / ckpt) * ns, c->x, ns * sizeof(double),
+                                               cudaMemcpyDeviceToDevice, st));
+    const double t = times[k], dt = t - tprev(k);
+    if (OX > 0 && !(dt > 0)) {
+      cleanup();
+      return set_err(c, MGPU_ERR_ARG, "Time step length not strictly positive at step=" + std::to_string(k + 1));
+    }
+    ADJ_TRY(newton_step(c, OX, k, t, dt, tvk(k), opts, stats));
+    stats->nstep_done = int(k + 1);
+    if (ncost > 0) adj_cost_value<<<1, 256, 0, st>>>(ncost, dcd, cw, cy + k * ncost, c->x, costs + k);
+  }
+  {
+    std::vector<double> hc(nstep, 0.0);
+    if (ncost > 0) ADJ_CUDA(cudaMemcpy(hc.data(), costs, nstep * sizeof(double), cudaMemcpyDeviceToHost));
+    double C = 0.0;
+    for (int64_t k = 0; k < nstep; ++k) C += (OX == 2 ? times[k] - tprev(k) : 1.0) * hc[k];
+    *cost = C;
+  }
+  // ---- reverse pass, segment by segment
+  mgpu_stats rstats{0, 0, 0, 0, 0.0, 0.0};
+  for (int64_t sgi = nseg - 1; sgi >= 0; --sgi) {
+    const int64_t k0 = sgi * ckpt, k1 = std::min<int64_t>(nstep, k0 + ckpt);
+    ADJ_CUDA(cudaMemcpyAsync(c->x, ck + sgi * ns, ns * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    for (int64_t k = k0; k < k1; ++k) {
+      ADJ_TRY(newton_step(c, OX, k, times[k], times[k] - tprev(k), tvk(k), opts, &rstats));
+      ADJ_CUDA(cudaMemcpyAsync(seg + (k - k0) * ns, c->x, ns * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+    for (int64_t k = k1 - 1; k >= k0; --k) {
+      const double t = times[k], dt = t - tprev(k), wk = OX == 2 ? dt : 1.0;
+      const mgpu_newmark nm = OX == 2 ? newmark_coefficients(opts->beta, opts->gamma, dt) : mgpu_newmark{0, 0, 0, 0, 0, 0};
+      ADJ_CUDA(cudaMemcpyAsync(c->x, seg + (k - k0) * ns, ns * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (c->ntval > 0)
+        ADJ_CUDA(cudaMemcpyAsync(c->tv, tvk(k), c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
+      if (ncost > 0)
+        adj_cost_grad<<<nb(ncost, 256), 256, 0, st>>>(ncost, dcd, cw, cy + k * ncost, c->x, wk, xb);
+      adj_rhs<<<nb(n, 256), 256, 0, st>>>(n, OX, nm.a1, nm.b1, c->scale, xb, vb, ab, g);
+      // μ = J⁻ᵀ S g
+      ADJ_TRY(upload_stepc(c, t, OX == 2 ? &nm : nullptr));
+      launch_reset_errflag(c);
+      ADJ_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
+      ADJ_TRY(launch_assembly(c, OX == 2 ? MGPU_ASM_ITER : MGPU_ASM_STATIC, nullptr, 1.0));
+      ADJ_TRY(factor_solve_T(c, g, mu, S.info));
+      // EI-scale sensitivities
+      for (size_t gi = 0; gi < c->groups.size(); ++gi)
+        if (abase[gi] >= 0 && c->groups[gi].nele > 0) {
+          const DevGroup& G = c->groups[gi];
+          adj_beam_dRdA<<<nb(G.nele, 128), 128, 0, st>>>(G.nele, G.idx, G.cdata, c->x, mu, c->scale,
+                                                         contrib + abase[gi]);
+        }
+      if (c->nA > 0) adj_agrad<<<nb(c->nA, 256), 256, 0, st>>>(c->nA, aptrd, aeled, contrib, gradA);
+      // load-value sensitivities
+      if (dtv) {
+        int64_t tvb = 0;
+        for (auto& G : c->groups) {
+          if (G.kind == MGPU_DOFLOAD && G.nele > 0)
+            adj_dtv<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, 1, 1, G.idx, mu, c->scale, dtv + k * c->ntval + tvb);
+          if (G.kind == MGPU_DOFCONSTRAINT_X && G.nele > 0)
+            adj_dtv<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, G.nX, -1, G.idx, mu, c->scale,
+                                                     dtv + k * c->ntval + tvb);
+          if (G.kind == MGPU_DOFLOAD || G.kind == MGPU_DOFCONSTRAINT_X) tvb += G.nele;
+        }
+      }
+      if (OX == 2) {
+        // Cᵀ μ and Mᵀ μ from the damping and mass matrices of the step
+        const mgpu_newmark onlyC{1.0, 0, 0, 0.0, 0, 0}, onlyM{0.0, 0, 0, 1.0, 0, 0};
+        ADJ_TRY(upload_stepc(c, t, &onlyC));
+        ADJ_TRY(launch_assembly(c, MGPU_ASM_ITER, nullptr, 0.0));
+        adj_csc_tmatvec<<<nb(n, 256), 256, 0, st>>>(n, colp, rowv, c->nzval, mu, c->scale, tC);
+        ADJ_TRY(upload_stepc(c, t, &onlyM));
+        ADJ_TRY(launch_assembly(c, MGPU_ASM_ITER, nullptr, 0.0));
+        adj_csc_tmatvec<<<nb(n, 256), 256, 0, st>>>(n, colp, rowv, c->nzval, mu, c->scale, tM);
+        adj_propagate<<<nb(n, 256), 256, 0, st>>>(n, nm.a1, nm.a2, nm.a3, nm.b1, nm.b2, nm.b3, tC, tM, xb, vb, ab);
+      } else {
+        ADJ_CUDA(cudaMemsetAsync(xb, 0, n * sizeof(double), st));
+      }
+      int hinfo = 0, hflag = INT_MAX;
+      ADJ_CUDA(cudaMemcpyAsync(&hinfo, S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      ADJ_CUDA(cudaMemcpyAsync(&hflag, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      ADJ_CUDA(cudaStreamSynchronize(st));
+      if (hflag != INT_MAX) {
+        rc = nan_error(c, hflag);
+        cleanup();
+        return rc;
+      }
+      if (hinfo != 0) {
+        cleanup();
+        return set_err(c, MGPU_ERR_SINGULAR, "adjoint: transposed factorization failed at step=" + std::to_string(k + 1));
+      }
+    }
+  }
+  if (c->nA > 0) ADJ_CUDA(cudaMemcpy(dCdA, gradA, c->nA * sizeof(double), cudaMemcpyDeviceToHost));
+  if (dtv) ADJ_CUDA(cudaMemcpy(dCdtv, dtv, size_t(nstep) * c->ntval * sizeof(double), cudaMemcpyDeviceToHost));
+  cleanup();
+#undef ADJ_TRY
+#undef ADJ_CUDA
+  return MGPU_OK;
+}

@@ -21,6 +21,8 @@ struct DevGroup {
   int64_t nele = 0;
   int32_t* idx = nullptr;   // [nX][nele] 0-based X dofs (entry-major)
   int32_t* uidx = nullptr;  // [nU][nele] 0-based U dofs
+  int32_t* aidx = nullptr;  // [nele] 0-based A-dof (EI scale) of each beam, or nullptr
+  std::vector<int64_t> h_indexA;  // host copy (1-based)
   double* cdata = nullptr;  // [nfield][nele] kernel constants (structure of arrays)
   int32_t nfield = 0;
   int64_t tval_base = -1;   // offset in the time-value vector (loads, constraints)
@@ -35,7 +37,8 @@ struct mgpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  int64_t nX = 0, nU = 0, ntval = 0;
+  int64_t nX = 0, nU = 0, ntval = 0, nA = 0;
+  double* Avec = nullptr;   // [nA] A-dof values
   std::vector<mgpu::DevGroup> groups;
   mgpu::Pattern pat;
   // device buffers
@@ -72,8 +75,11 @@ constexpr int kStepcSlots = 8;
 int upload_stepc(mgpu_ctx* c, double t, const mgpu_newmark* nm);
 // launches one complete assembly on ctx->stream from the resident state and
 // step constants; ev_groups (optional) receives an event after each element
-// type's kernel.  Enqueues no copy and no synchronisation (capturable).
-int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups);
+// type's kernel.  The matrix is p0 ∂R/∂X + a1 ∂R/∂X' + b1 ∂R/∂X'' with a1, b1
+// from the step constants (p0 = 1 in the Newton loops; 0 to assemble the
+// damping or mass matrix alone).  Enqueues no copy and no synchronisation
+// (capturable).
+int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0 = 1.0);
 // errflag <- INT_MAX on ctx->stream (capturable)
 void launch_reset_errflag(mgpu_ctx* c);
 int set_err(mgpu_ctx* c, int code, const std::string& msg);

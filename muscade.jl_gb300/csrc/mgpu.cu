@@ -67,15 +67,28 @@ __device__ __forceinline__ void flag_nan(int* errflag, int64_t gid, bool bad) {
 }
 
 // EulerBeam3D: one thread per element.  DYN selects the Newmark form.
+// EI-scale A-dof of the wrapper element EulerBeam3D{adof}: the bending
+// constants (EI2, EI3 times Gauss sums of the curvature shapes) scale with it
+__device__ __forceinline__ void scale_bending(BeamConst& bc, double s) {
+  bc.k3u *= s;
+  bc.k3uv *= s;
+  bc.k3v *= s;
+  bc.k2u *= s;
+  bc.k2uv *= s;
+  bc.k2v *= s;
+}
+
 template <bool DYN>
 __global__ void __launch_bounds__(128) beam_kernel(int64_t nele, const int32_t* __restrict__ idx,
                                                    const int32_t* __restrict__ uidx, const double* __restrict__ cdata,
+                                                   const int32_t* __restrict__ aidx, const double* __restrict__ Avec,
                                                    AsmArgs a, double* __restrict__ rout, double* __restrict__ kout,
                                                    int64_t gid0) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= nele) return;
   BeamConst bc;
   load_soa(bc, cdata, nele, e);
+  if (aidx) scale_bending(bc, __ldg(Avec + __ldg(aidx + e)));
   int dof[12];
   double X0[12], X1[12], X2[12], av[12], bv[12];
 #pragma unroll
@@ -265,7 +278,7 @@ int upload_stepc(mgpu_ctx* c, double t, const mgpu_newmark* nm) {
 
 void launch_reset_errflag(mgpu_ctx* c) { set_int_kernel<<<1, 1, 0, c->stream>>>(c->errflag, INT_MAX); }
 
-int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups) {
+int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0) {
   const int64_t nX = c->nX;
   AsmArgs a;
   a.x0 = c->x;
@@ -280,7 +293,7 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups) {
   a.mission = mission;
   a.errflag = c->errflag;
   const bool dyn = mission != MGPU_ASM_STATIC;
-  a.p0 = 1.0;
+  a.p0 = p0;
   if (dyn && c->nXder_resident != 3) return set_err(c, MGPU_ERR_ARG, "Newmark assembly needs X, X' and X''");
   if (mission == MGPU_ASM_STEP && nX > 0)
     newmark_ab_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, a.x1, a.x2, c->stepc, c->ab, c->ab + nX);
@@ -298,11 +311,11 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups) {
     switch (G.kind) {
       case MGPU_EULERBEAM3D:
         if (dyn)
-          beam_kernel<true><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, ag, rout, kout,
-                                                                      gid0);
+          beam_kernel<true><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, G.aidx,
+                                                                      c->Avec, ag, rout, kout, gid0);
         else
-          beam_kernel<false><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, ag, rout,
-                                                                       kout, gid0);
+          beam_kernel<false><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, G.aidx,
+                                                                       c->Avec, ag, rout, kout, gid0);
         break;
       case MGPU_BAR3D:
         bar_kernel<<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, dyn ? 3 : 1, G.idx, G.uidx, G.cdata, ag, rout,
@@ -416,6 +429,11 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
     if ((G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) && G.nU != 0)
       return set_err(c, MGPU_ERR_ARG, "constraints and loads have no U-dofs");
     if (G.nU > 0 && G.nele > 0 && !G.indexU) return set_err(c, MGPU_ERR_ARG, "missing indexU");
+    if (G.indexA && G.kind != MGPU_EULERBEAM3D)
+      return set_err(c, MGPU_ERR_UNSUPPORTED, "A-dofs are supported on EulerBeam3D (EI scale) only");
+    if (G.indexA)
+      for (int64_t k = 0; k < G.nele; ++k)
+        if (G.indexA[k] < 1 || G.indexA[k] > d->nA) return set_err(c, MGPU_ERR_ARG, "A-dof index out of range");
     for (int64_t k = 0; k < G.nele * G.nU; ++k)
       if (G.indexU[k] < 1 || G.indexU[k] > d->nU) return set_err(c, MGPU_ERR_ARG, "U-dof index out of range");
     shapes.push_back(GroupShape{G.nele, G.nX, G.indexX});
@@ -446,6 +464,13 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
         for (int i = 0; i < G.nU; ++i) uidx[size_t(i) * G.nele + e] = int32_t(G.indexU[e * G.nU + i] - 1);
       MG_TRY(dalloc(c, &D.uidx, uidx.size()));
       MG_CUDA(cudaMemcpy(D.uidx, uidx.data(), uidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
+    if (G.indexA && G.nele > 0) {
+      D.h_indexA.assign(G.indexA, G.indexA + G.nele);
+      std::vector<int32_t> aidx(G.nele);
+      for (int64_t e = 0; e < G.nele; ++e) aidx[e] = int32_t(G.indexA[e] - 1);
+      MG_TRY(dalloc(c, &D.aidx, aidx.size()));
+      MG_CUDA(cudaMemcpy(D.aidx, aidx.data(), aidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     }
     std::vector<double> cd;
     if (G.kind == MGPU_EULERBEAM3D) {
@@ -504,6 +529,12 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
   MG_CUDA(cudaMemset(c->tv, 0, std::max<int64_t>(c->ntval, 1) * sizeof(double)));
   MG_TRY(dalloc(c, &c->ab, 2 * c->nX));
   MG_TRY(dalloc(c, &c->errflag, 2));
+  c->nA = d->nA;
+  MG_TRY(dalloc(c, &c->Avec, std::max<int64_t>(c->nA, 1)));
+  {
+    std::vector<double> ones(std::max<int64_t>(c->nA, 1), 1.0);
+    MG_CUDA(cudaMemcpy(c->Avec, ones.data(), ones.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   MG_TRY(dalloc(c, &c->stepc, 8));
   MG_CUDA(cudaMemset(c->stepc, 0, 8 * sizeof(double)));
   MG_CUDA(cudaMallocHost(&c->hstepc, kStepcSlots * 8 * sizeof(double)));
@@ -530,16 +561,24 @@ extern "C" void mgpu_destroy(mgpu_ctx* c) {
   for (auto& G : c->groups) {
     cudaFree(G.idx);
     cudaFree(G.uidx);
+    cudaFree(G.aidx);
     cudaFree(G.cdata);
   }
   void* ps[] = {c->kbuf, c->rbuf, c->mseg, c->msrc, c->vseg, c->vsrc, c->nzval, c->Ll, c->x,
-                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush, c->stepc};
+                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush, c->stepc, c->Avec};
   for (void* p : ps) cudaFree(p);
   if (c->hstepc) cudaFreeHost(c->hstepc);
   for (cudaEvent_t e : c->stepc_ev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+extern "C" int mgpu_set_A(mgpu_ctx* c, const double* A) {
+  if (!c || (c->nA > 0 && !A)) return set_err(c, MGPU_ERR_ARG, "mgpu_set_A: bad arguments");
+  MG_CUDA(cudaSetDevice(c->device));
+  if (c->nA > 0) MG_CUDA(cudaMemcpy(c->Avec, A, c->nA * sizeof(double), cudaMemcpyHostToDevice));
+  return MGPU_OK;
 }
 
 extern "C" int64_t mgpu_nnz(const mgpu_ctx* c) { return c ? c->pat.nnz : -1; }
@@ -584,7 +623,7 @@ extern "C" int mgpu_assemble_resident(mgpu_ctx* c, int32_t mission, double t, co
     return set_err(c, MGPU_ERR_ARG, "mgpu_assemble_resident: bad arguments");
   MG_CUDA(cudaSetDevice(c->device));
   MG_TRY(upload_stepc(c, t, mission != MGPU_ASM_STATIC ? nm : nullptr));
-  return launch_assembly(c, mission, nullptr);
+  return launch_assembly(c, mission, nullptr, 1.0);
 }
 
 extern "C" int mgpu_download(mgpu_ctx* c, double* Ll, double* nzval) {
@@ -624,7 +663,7 @@ extern "C" int mgpu_time_assemble(mgpu_ctx* c, int32_t mission, double t, const 
       fill_kernel<<<nblk(c->flush_bytes / 8, 256), 256, 0, c->stream>>>(c->flush, c->flush_bytes / 8, double(r));
     cudaEvent_t* E = &ev[size_t(ne) * r];
     MG_CUDA(cudaEventRecord(E[0], c->stream));
-    MG_TRY(launch_assembly(c, mission, E + 1));
+    MG_TRY(launch_assembly(c, mission, E + 1, 1.0));
     MG_CUDA(cudaEventRecord(E[ng + 1], c->stream));
   }
   MG_CUDA(cudaStreamSynchronize(c->stream));

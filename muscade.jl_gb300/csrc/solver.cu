@@ -26,68 +26,12 @@
 
 #include "band_rows.cuh"
 #include "ctx.hpp"
+#include "solver.hpp"
 
 using namespace mgpu;
 
 namespace mgpu {
 
-constexpr int kNormBlocks = 128;
-constexpr int kInfoSlots = 64;  // a captured step holds up to kInfoSlots-1 iterations
-
-enum SolverPath : int {
-  PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
-  PATH_F64ROWS = 1,  // row-band warp kernels in FP64
-  PATH_BLOCK = 2   // gbtf2-layout block kernels in FP64 (any band width up to 256)
-};
-
-struct Solver {
-  bool ok = false;       // banded scheme applicable
-  int path = PATH_BLOCK;
-  int wm = 0;            // row-band register window (32 or 64), 0 if the row-band kernels do not apply
-  int nref = 8;          // refinement sweeps allowed on the FP32 path
-  // row-band layout
-  int64_t* rbase = nullptr;   // [ncomp] offset in RB / UC*
-  int64_t* lbase = nullptr;   // [ncomp] offset in LM*
-  int64_t* rbmap = nullptr;   // [nnz] position of each nnz in RB
-  int64_t rb_total = 0, lb_total = 0;
-  double* RB = nullptr;       // unfactorised rows (FP64)
-  float* RB32 = nullptr;      // the same in FP32
-  float* UC32 = nullptr;
-  float* LM32 = nullptr;
-  double* UC64 = nullptr;
-  double* LM64 = nullptr;
-  double* bw = nullptr;       // [nX] permuted right-hand side
-  double* xw = nullptr;       // [nX] solution (band order)
-  double* rw = nullptr;       // [nX] residual
-  float* tw32 = nullptr;      // [nX] substitution work
-  double* tw64 = nullptr;
-  int* flag = nullptr;        // [ncomp] FP64 fallback requested
-  int* nsweep = nullptr;      // [ncomp] refinement sweeps used
-  std::string why;       // reason when not
-  int ncomp = 0;
-  int64_t band_total = 0;
-  int maxkl = 0, maxku = 0;
-  // device
-  int64_t* cbase = nullptr;   // [ncomp] offset of component band storage
-  int32_t* cn = nullptr;      // [ncomp] component size
-  int32_t* ckl = nullptr;     // [ncomp]
-  int32_t* cku = nullptr;     // [ncomp]
-  int32_t* cdof0 = nullptr;   // [ncomp] offset into perm
-  int32_t* perm = nullptr;    // [nX] dofs of component c in band order: perm[cdof0[c] + k]
-  int64_t* bmap = nullptr;    // [nnz] band position of each nnz
-  double* AB = nullptr;       // band storage
-  int32_t* ipiv = nullptr;    // [nX] pivot offsets (band order)
-  double* rhs = nullptr;      // [nX] permuted right-hand side / solution
-  double* rdiag = nullptr;    // [nX] reciprocal pivots (block kernels)
-  double* dx = nullptr;       // [nX] Δx in model order
-  double* red = nullptr;      // [4] reductions: ΣΔx², ΣLλ²
-  double* part = nullptr;     // [2 * kNormBlocks] partial sums of the reductions
-  int* info = nullptr;        // [kInfoSlots] first singular component+1 (0 = ok), one slot per iteration of a step
-  int32_t* cod = nullptr;     // [nX] component of each dof
-  int* frozen = nullptr;      // [ncomp] converged in this step (per-component convergence)
-  int* nactive = nullptr;     // [1] components still iterating
-  double* hbuf = nullptr;     // pinned host: red[0..1], info
-};
 
 // ---------------------------------------------------------------- host analysis
 static void analyse(mgpu_ctx* c, Solver& S) {
@@ -261,21 +205,24 @@ static void analyse(mgpu_ctx* c, Solver& S) {
     for (int cc = 0; cc < ncomp; ++cc) {
       const int64_t nc = comp_start[cc + 1] - comp_start[cc];
       rb[cc + 1] = rb[cc] + nc * (kl[cc] + ku[cc] + 1);
-      lb[cc + 1] = lb[cc] + nc * kl[cc];
+      lb[cc + 1] = lb[cc] + nc * std::max(kl[cc], ku[cc]);  // room for the multipliers of Lλx and of its transpose
     }
     S.rb_total = rb[ncomp];
     S.lb_total = lb[ncomp];
-    std::vector<int64_t> rbmap(P.nnz);
+    std::vector<int64_t> rbmap(P.nnz), rbmapT(P.nnz);
     for (int64_t j = 0; j < n; ++j)
       for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
         const int64_t i = P.rowval[q];
         const int cc = comp[j];
         const int64_t kj = pos[j] - comp_start[cc], ki = pos[i] - comp_start[cc];
-        rbmap[q] = rb[cc] + ki * (kl[cc] + ku[cc] + 1) + (kj - ki + kl[cc]);
+        const int64_t w = kl[cc] + ku[cc] + 1;
+        rbmap[q] = rb[cc] + ki * w + (kj - ki + kl[cc]);
+        rbmapT[q] = rb[cc] + kj * w + (ki - kj + ku[cc]);  // entry (j, i) of the transpose: kl and ku exchange
       }
+    S.wmT = S.maxku <= 31 ? S.wm : 0;
     std::vector<int64_t> rbv(rb.begin(), rb.end() - 1), lbv(lb.begin(), lb.end() - 1);
     const size_t nr = std::max<int64_t>(S.rb_total, 1), nl = std::max<int64_t>(S.lb_total, 1);
-    good = good && up(&S.rbase, rbv) && up(&S.lbase, lbv) && up(&S.rbmap, rbmap);
+    good = good && up(&S.rbase, rbv) && up(&S.lbase, lbv) && up(&S.rbmap, rbmap) && up(&S.rbmapT, rbmapT);
     good = good && cudaMalloc(&S.RB, nr * sizeof(double)) == cudaSuccess &&
            cudaMemset(S.RB, 0, nr * sizeof(double)) == cudaSuccess;
     good = good && cudaMalloc(&S.RB32, nr * sizeof(float)) == cudaSuccess &&
@@ -602,7 +549,7 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
   Solver* S = c->solver;
   if (!S) return;
   void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx,
-                S->red, S->info, S->rbase, S->lbase, S->rbmap, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
+                S->red, S->info, S->rbase, S->lbase, S->rbmap, S->rbmapT, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
                 S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag, S->part, S->cod, S->frozen,
                 S->nactive};
   for (void* p : ps) cudaFree(p);
@@ -612,11 +559,11 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
 }
 
 namespace mgpu {
-static unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
+unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 
 // one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device);
 // a singular factorisation writes its component+1 to *info.  Capturable.
-static int factor_solve(mgpu_ctx* c, int* info) {
+int factor_solve(mgpu_ctx* c, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
   if (S.path == PATH_BLOCK) {
@@ -659,10 +606,31 @@ static int factor_solve(mgpu_ctx* c, int* info) {
   MG_CUDA(cudaGetLastError());
   return MGPU_OK;
 }
+
+int factor_solve_T(mgpu_ctx* c, const double* rhs, double* out, int* info) {
+  Solver& S = *c->solver;
+  if (!S.wmT)
+    return set_err(c, MGPU_ERR_UNSUPPORTED,
+                   "transposed solve needs the row-band kernels (kl, ku <= 31 and kl+ku+1 <= 64 in every component)");
+  cudaStream_t st = c->stream;
+  const RbComp cpT{S.rbase, S.lbase, S.cn, S.cku, S.ckl, S.cdof0};  // the transpose: kl and ku exchange
+  rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.rbmapT, c->nzval, S.RB, nullptr);
+  if (S.wmT == 32) {
+    rb_lu<double, 32><<<S.ncomp, 32, 0, st>>>(cpT, S.RB, S.UC64, S.LM64, S.ipiv, RB_PLAIN, S.flag, info);
+    rb_solve<double, 32><<<S.ncomp, 32, 0, st>>>(cpT, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, rhs, S.bw, S.xw, S.rw,
+                                                 S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
+  } else {
+    rb_lu<double, 64><<<S.ncomp, 32, 0, st>>>(cpT, S.RB, S.UC64, S.LM64, S.ipiv, RB_PLAIN, S.flag, info);
+    rb_solve<double, 64><<<S.ncomp, 32, 0, st>>>(cpT, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, rhs, S.bw, S.xw, S.rw,
+                                                 S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
+  }
+  MG_CUDA(cudaGetLastError());
+  return MGPU_OK;
+}
 }  // namespace mgpu
 
 namespace mgpu {
-static mgpu_newmark newmark_coefficients(double beta, double gamma, double dt) {
+mgpu_newmark newmark_coefficients(double beta, double gamma, double dt) {
   // Newmarkβcoefficients (src/SweepX.jl:3-15)
   return mgpu_newmark{gamma / (beta * dt), gamma / beta, (gamma / (2 * beta) - 1) * dt, 1 / (beta * dt * dt),
                       1 / (beta * dt), 1 / (2 * beta)};
@@ -674,6 +642,78 @@ static int singular_error(mgpu_ctx* c, mgpu_stats* stats, int64_t step, int it) 
   char msg[128];
   snprintf(msg, sizeof msg, "matrix factorization failed at step=%d, iiter=%d", int(step + 1), it);
   return set_err(c, MGPU_ERR_SINGULAR, msg);
+}
+
+int newton_step(mgpu_ctx* c, int OX, int64_t step, double t, double dt, const double* tvals_step,
+                const mgpu_sweep_opts* opts, mgpu_stats* stats) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  const int64_t n = c->nX;
+  const bool percomp = opts->per_component != 0;
+  const double cdx2 = opts->maxdx * opts->maxdx, cLl2 = opts->maxLl * opts->maxLl;
+  const mgpu_newmark nm = OX == 2 ? newmark_coefficients(opts->beta, opts->gamma, dt) : mgpu_newmark{0, 0, 0, 0, 0, 0};
+  int rc = upload_stepc(c, t, OX == 2 ? &nm : nullptr);
+  if (rc) return rc;
+  if (c->ntval > 0)
+    MG_CUDA(cudaMemcpyAsync(c->tv, tvals_step, c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (percomp) MG_CUDA(cudaMemsetAsync(S.frozen, 0, std::max(S.ncomp, 1) * sizeof(int), st));
+  const int itmax = opts->fixed_iter > 0 ? opts->fixed_iter : opts->maxiter;
+  for (int it = 1; it <= itmax; ++it) {
+    stats->niter_total++;
+    const int first = it == 1;
+    const int mission = OX == 0 ? MGPU_ASM_STATIC : (first ? MGPU_ASM_STEP : MGPU_ASM_ITER);
+    launch_reset_errflag(c);
+    MG_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
+    rc = launch_assembly(c, mission, nullptr);
+    if (rc) return rc;
+    rc = factor_solve(c, S.info);
+    if (rc) return rc;
+    decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, first, S.dx, c->scale, c->stepc, c->x,
+                                                  percomp ? S.frozen : nullptr, S.cod);
+    if (percomp) {
+      MG_CUDA(cudaMemsetAsync(S.nactive, 0, sizeof(int), st));
+      comp_converge<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dx, c->Ll, cdx2, cLl2, S.frozen, S.nactive);
+    }
+    MG_CUDA(cudaMemcpyAsync(S.hbuf, S.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int* hi = reinterpret_cast<int*>(S.hbuf + 2);
+    MG_CUDA(cudaMemcpyAsync(hi, S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaMemcpyAsync(hi + 1, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (percomp) MG_CUDA(cudaMemcpyAsync(hi + 2, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaStreamSynchronize(st));
+    const double dx2 = S.hbuf[0], Ll2 = S.hbuf[1];
+    stats->last_dx = std::sqrt(dx2);
+    stats->last_Ll = std::sqrt(Ll2);
+    if (hi[1] != INT_MAX) {
+      stats->fail_step = int(step + 1);
+      stats->fail_iter = it;
+      return nan_error(c, hi[1]);
+    }
+    if (hi[0] != 0) return singular_error(c, stats, step, it);
+    if (opts->fixed_iter > 0) {
+      if (it == opts->fixed_iter) break;
+      continue;
+    }
+    const bool done = percomp ? hi[2] == 0 : (dx2 <= cdx2 && Ll2 <= cLl2);
+    if (done) break;
+    if (it == opts->maxiter) {
+      stats->fail_step = int(step + 1);
+      stats->fail_iter = it;
+      std::string which;
+      if (percomp) {
+        std::vector<int> fz(S.ncomp);
+        MG_CUDA(cudaMemcpy(fz.data(), S.frozen, S.ncomp * sizeof(int), cudaMemcpyDeviceToHost));
+        int first_open = 0;
+        while (first_open < S.ncomp && fz[first_open]) ++first_open;
+        which = " (" + std::to_string(hi[2]) + " components, the first is component " + std::to_string(first_open + 1) +
+                ")";
+      }
+      char msg[256];
+      snprintf(msg, sizeof msg, "no convergence of step %3d after %3d iterations |Δx|=%g / %g, |Lλ|=%g / %g",
+               int(step + 1), it, std::sqrt(dx2), opts->maxdx, Ll2, opts->maxLl);
+      return set_err(c, MGPU_ERR_NOCONV, msg + which);
+    }
+  }
+  return MGPU_OK;
 }
 
 // Fixed-iteration steps replayed from one captured CUDA graph: per step the
@@ -836,8 +876,6 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
   if (opts->fixed_iter > 0 && opts->fixed_iter < kInfoSlots && !opts->no_graph)
     return sweep_graph(c, OX, nstep, times, t0, tvals, opts, states, stats);
   const int nder = OX + 1;
-  const bool percomp = opts->per_component != 0;
-  const double cdx2 = opts->maxdx * opts->maxdx, cLl2 = opts->maxLl * opts->maxLl;
   double told = t0;
   for (int64_t step = 0; step < nstep; ++step) {
     const double t = times[step];
@@ -849,68 +887,8 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
       snprintf(msg, sizeof msg, "Time step length not strictly positive at step=%3d", int(step + 1));
       return set_err(c, MGPU_ERR_ARG, msg);
     }
-    const mgpu_newmark nm = OX == 2 ? newmark_coefficients(opts->beta, opts->gamma, dt) : mgpu_newmark{0, 0, 0, 0, 0, 0};
-    int rc = upload_stepc(c, t, OX == 2 ? &nm : nullptr);
+    const int rc = newton_step(c, OX, step, t, dt, c->ntval > 0 ? tvals + step * c->ntval : nullptr, opts, stats);
     if (rc) return rc;
-    if (c->ntval > 0)
-      MG_CUDA(cudaMemcpyAsync(c->tv, tvals + step * c->ntval, c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
-    if (percomp) MG_CUDA(cudaMemsetAsync(S.frozen, 0, std::max(S.ncomp, 1) * sizeof(int), st));
-    const int itmax = opts->fixed_iter > 0 ? opts->fixed_iter : opts->maxiter;
-    for (int it = 1; it <= itmax; ++it) {
-      stats->niter_total++;
-      const int first = it == 1;
-      const int mission = OX == 0 ? MGPU_ASM_STATIC : (first ? MGPU_ASM_STEP : MGPU_ASM_ITER);
-      launch_reset_errflag(c);
-      MG_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
-      rc = launch_assembly(c, mission, nullptr);
-      if (rc) return rc;
-      rc = factor_solve(c, S.info);
-      if (rc) return rc;
-      decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, first, S.dx, c->scale, c->stepc, c->x,
-                                                    percomp ? S.frozen : nullptr, S.cod);
-      if (percomp) {
-        MG_CUDA(cudaMemsetAsync(S.nactive, 0, sizeof(int), st));
-        comp_converge<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dx, c->Ll, cdx2, cLl2, S.frozen, S.nactive);
-      }
-      MG_CUDA(cudaMemcpyAsync(S.hbuf, S.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-      int* hi = reinterpret_cast<int*>(S.hbuf + 2);
-      MG_CUDA(cudaMemcpyAsync(hi, S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
-      MG_CUDA(cudaMemcpyAsync(hi + 1, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
-      if (percomp) MG_CUDA(cudaMemcpyAsync(hi + 2, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
-      MG_CUDA(cudaStreamSynchronize(st));
-      const double dx2 = S.hbuf[0], Ll2 = S.hbuf[1];
-      stats->last_dx = std::sqrt(dx2);
-      stats->last_Ll = std::sqrt(Ll2);
-      if (hi[1] != INT_MAX) {
-        stats->fail_step = int(step + 1);
-        stats->fail_iter = it;
-        return nan_error(c, hi[1]);
-      }
-      if (hi[0] != 0) return singular_error(c, stats, step, it);
-      if (opts->fixed_iter > 0) {
-        if (it == opts->fixed_iter) break;
-        continue;
-      }
-      const bool done = percomp ? hi[2] == 0 : (dx2 <= cdx2 && Ll2 <= cLl2);
-      if (done) break;
-      if (it == opts->maxiter) {
-        stats->fail_step = int(step + 1);
-        stats->fail_iter = it;
-        std::string which;
-        if (percomp) {
-          std::vector<int> fz(S.ncomp);
-          MG_CUDA(cudaMemcpy(fz.data(), S.frozen, S.ncomp * sizeof(int), cudaMemcpyDeviceToHost));
-          int first_open = 0;
-          while (first_open < S.ncomp && fz[first_open]) ++first_open;
-          which = " (" + std::to_string(hi[2]) + " components, the first is component " +
-                  std::to_string(first_open + 1) + ")";
-        }
-        char msg[256];
-        snprintf(msg, sizeof msg, "no convergence of step %3d after %3d iterations |Δx|=%g / %g, |Lλ|=%g / %g",
-                 int(step + 1), it, std::sqrt(dx2), opts->maxdx, Ll2, opts->maxLl);
-        return set_err(c, MGPU_ERR_NOCONV, msg + which);
-      }
-    }
     MG_CUDA(cudaMemcpyAsync(states + step * nder * n, c->x, nder * n * sizeof(double), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaStreamSynchronize(st));
     stats->nstep_done = int(step + 1);

@@ -1,0 +1,87 @@
+// Linear solver state shared by the Newton drivers (solver.cu) and the
+// adjoint (adjoint.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "ctx.hpp"
+
+namespace mgpu {
+
+constexpr int kNormBlocks = 128;
+constexpr int kInfoSlots = 64;  // a captured step holds up to kInfoSlots-1 iterations
+
+enum SolverPath : int {
+  PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
+  PATH_F64ROWS = 1,  // row-band warp kernels in FP64
+  PATH_BLOCK = 2   // gbtf2-layout block kernels in FP64 (any band width up to 256)
+};
+
+struct Solver {
+  bool ok = false;       // banded scheme applicable
+  int path = PATH_BLOCK;
+  int wm = 0;            // row-band register window (32 or 64), 0 if the row-band kernels do not apply
+  int nref = 8;          // refinement sweeps allowed on the FP32 path
+  // row-band layout
+  int64_t* rbase = nullptr;   // [ncomp] offset in RB / UC*
+  int64_t* lbase = nullptr;   // [ncomp] offset in LM*
+  int64_t* rbmap = nullptr;   // [nnz] position of each nnz in RB
+  int64_t* rbmapT = nullptr;  // [nnz] position of each nnz in the rows of the transpose
+  int wmT = 0;                // as wm, for the transpose (0 when its kl = ku exceeds 31)
+  int64_t rb_total = 0, lb_total = 0;
+  double* RB = nullptr;       // unfactorised rows (FP64)
+  float* RB32 = nullptr;      // the same in FP32
+  float* UC32 = nullptr;
+  float* LM32 = nullptr;
+  double* UC64 = nullptr;
+  double* LM64 = nullptr;
+  double* bw = nullptr;       // [nX] permuted right-hand side
+  double* xw = nullptr;       // [nX] solution (band order)
+  double* rw = nullptr;       // [nX] residual
+  float* tw32 = nullptr;      // [nX] substitution work
+  double* tw64 = nullptr;
+  int* flag = nullptr;        // [ncomp] FP64 fallback requested
+  int* nsweep = nullptr;      // [ncomp] refinement sweeps used
+  std::string why;       // reason when not
+  int ncomp = 0;
+  int64_t band_total = 0;
+  int maxkl = 0, maxku = 0;
+  // device
+  int64_t* cbase = nullptr;   // [ncomp] offset of component band storage
+  int32_t* cn = nullptr;      // [ncomp] component size
+  int32_t* ckl = nullptr;     // [ncomp]
+  int32_t* cku = nullptr;     // [ncomp]
+  int32_t* cdof0 = nullptr;   // [ncomp] offset into perm
+  int32_t* perm = nullptr;    // [nX] dofs of component c in band order: perm[cdof0[c] + k]
+  int64_t* bmap = nullptr;    // [nnz] band position of each nnz
+  double* AB = nullptr;       // band storage
+  int32_t* ipiv = nullptr;    // [nX] pivot offsets (band order)
+  double* rhs = nullptr;      // [nX] permuted right-hand side / solution
+  double* rdiag = nullptr;    // [nX] reciprocal pivots (block kernels)
+  double* dx = nullptr;       // [nX] Δx in model order
+  double* red = nullptr;      // [4] reductions: ΣΔx², ΣLλ²
+  double* part = nullptr;     // [2 * kNormBlocks] partial sums of the reductions
+  int* info = nullptr;        // [kInfoSlots] first singular component+1 (0 = ok), one slot per iteration of a step
+  int32_t* cod = nullptr;     // [nX] component of each dof
+  int* frozen = nullptr;      // [ncomp] converged in this step (per-component convergence)
+  int* nactive = nullptr;     // [1] components still iterating
+  double* hbuf = nullptr;     // pinned host: red[0..1], info
+};
+
+// one Newton correction Δx = Lλx \ Lλ -> S.dx and its norms -> S.red; a
+// singular factorisation writes component+1 to *info.  Capturable.
+int factor_solve(mgpu_ctx* c, int* info);
+// out = Lλxᵀ⁻¹ rhs (both in model order) from the Lλx assembled in ctx->nzval,
+// with the FP64 row-band kernels; needs Solver::wmT.  Capturable.
+int factor_solve_T(mgpu_ctx* c, const double* rhs, double* out, int* info);
+// Newton loop of one SweepX step (src/SweepX.jl:190-224) on the resident
+// state: uploads the step constants and load values, iterates to convergence
+// (or fixed_iter times).  Errors carry the reference's messages.
+int newton_step(mgpu_ctx* c, int OX, int64_t step, double t, double dt, const double* tvals_step,
+                const mgpu_sweep_opts* opts, mgpu_stats* stats);
+unsigned nb(int64_t n, int b);
+mgpu_newmark newmark_coefficients(double beta, double gamma, double dt);
+
+}  // namespace mgpu

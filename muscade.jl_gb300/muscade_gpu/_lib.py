@@ -15,8 +15,9 @@ PKG = os.path.dirname(HERE)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
-SOURCES = ["mgpu.cu", "solver.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
-HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh"]
+SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
+HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh",
+           "solver.hpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes
@@ -60,13 +61,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
 class Group(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("nX", ctypes.c_int32), ("nU", ctypes.c_int32), ("ndata", ctypes.c_int32),
                 ("nele", ctypes.c_int64), ("indexX", ctypes.POINTER(ctypes.c_int64)),
-                ("indexU", ctypes.POINTER(ctypes.c_int64)), ("edata", ctypes.POINTER(ctypes.c_double))]
+                ("indexU", ctypes.POINTER(ctypes.c_int64)), ("edata", ctypes.POINTER(ctypes.c_double)),
+                ("indexA", ctypes.POINTER(ctypes.c_int64))]
 
 
 class ModelDesc(ctypes.Structure):
     _fields_ = [("nX", ctypes.c_int64), ("nU", ctypes.c_int64), ("ngroup", ctypes.c_int32),
                 ("groups", ctypes.POINTER(Group)), ("scaleX", ctypes.POINTER(ctypes.c_double)),
-                ("device", ctypes.c_int32)]
+                ("device", ctypes.c_int32), ("nA", ctypes.c_int64)]
 
 
 class Newmark(ctypes.Structure):
@@ -96,7 +98,8 @@ LINSOLVE_NAME = {v: k for k, v in LINSOLVE.items()}
 SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_get_pattern", "mgpu_get_asm",
            "mgpu_ntval", "mgpu_assemble", "mgpu_element_eval", "mgpu_upload_state", "mgpu_assemble_resident",
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
-           "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info"]
+           "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
+           "mgpu_adjoint_sweepx"]
 
 _lib = None
 
@@ -135,6 +138,9 @@ def load():
     L.mgpu_assemble_beams_noalloc.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp]
     L.mgpu_set_linear_solver.argtypes = [vp, i32]
     L.mgpu_linear_solver_info.argtypes = [vp, P(LinsolveInfo)]
+    L.mgpu_set_A.argtypes = [vp, pd]
+    L.mgpu_adjoint_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32, pd,
+                                      pd, pd, P(Stats)]
     for name in SYMBOLS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int and name not in ("mgpu_destroy",):

@@ -58,10 +58,18 @@ class DeviceModel:
             G.indexX = L.ptr(iX, ctypes.c_int64)
             G.indexU = L.ptr(iU, ctypes.c_int64) if G.nU else None
             G.edata = L.ptr(ed) if G.ndata else None
+            iA = np.ascontiguousarray(dg.index_A, dtype=np.int64)
+            if iA.size:
+                if kind != L.EULERBEAM3D or iA.shape[1] != 1:
+                    raise DeviceError(3, f"A-dofs of element type {g.key[0]} are not supported by the GPU path")
+                iA = np.ascontiguousarray(iA[:, 0])
+                self._keep.append(iA)
+                G.indexA = L.ptr(iA, ctypes.c_int64)
         self._groups = groups
         sc = np.ascontiguousarray(dis.scaleX, dtype=np.float64)
         self._keep.append(sc)
-        desc = L.ModelDesc(self.nX, self.nU, len(model.groups), groups, L.ptr(sc), device)
+        self.nA = model.ndof["A"]
+        desc = L.ModelDesc(self.nX, self.nU, len(model.groups), groups, L.ptr(sc), device, self.nA)
         self.ctx = ctypes.c_void_p()
         rc = self.lib.mgpu_create(ctypes.byref(self.ctx), ctypes.byref(desc))
         self._check(rc)
@@ -69,6 +77,40 @@ class DeviceModel:
         self.ntval = int(self.lib.mgpu_ntval(self.ctx))
         if linsolve != "auto":
             self.set_linear_solver(linsolve)
+
+    def set_A(self, A):
+        """A-dof values (the EI scale factors of EulerBeam3D{adof}); 1 until set."""
+        a = np.ascontiguousarray(A, dtype=np.float64)
+        if a.shape != (self.nA,):
+            raise ValueError(f"A must have {self.nA} values")
+        self._check(self.lib.mgpu_set_A(self.ctx, L.ptr(a)))
+
+    def adjoint(self, OX, times, t0, X0, cost_dof, cost_w, cost_y, U=None, beta=0.25, gamma=0.5, maxiter=50,
+                maxdx=1e-10, maxLl=math.inf, ckpt=0, load_gradient=False):
+        """Cost and its gradient with respect to the A-dofs (and, with
+        load_gradient, to the load values) by the discrete adjoint of a
+        converged SweepX{OX} sweep; see mgpu_adjoint_sweepx.  cost_dof are
+        1-based X-dofs, cost_y[nstep][ncost].  Returns (cost, dCdA, dCdtv, stats)."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        nstep = len(times)
+        X0 = [np.asarray(v, dtype=np.float64) for v in X0][: OX + 1]
+        x0 = np.ascontiguousarray(np.concatenate(X0)) if X0 else np.zeros(0)
+        u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
+        tv = np.ascontiguousarray(np.stack([self.tvals(t) for t in times]) if self.ntval else np.zeros((nstep, 0)))
+        cd = np.ascontiguousarray(cost_dof, dtype=np.int64)
+        cw = np.ascontiguousarray(np.broadcast_to(cost_w, cd.shape), dtype=np.float64)
+        cy = np.ascontiguousarray(cost_y, dtype=np.float64).reshape(nstep, len(cd))
+        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0)
+        cost = ctypes.c_double()
+        dA = np.zeros(max(self.nA, 1))
+        dtv = np.zeros((nstep, self.ntval)) if load_gradient and self.ntval else None
+        stats = L.Stats()
+        rc = self.lib.mgpu_adjoint_sweepx(self.ctx, OX, nstep, L.ptr(times), float(t0), len(X0), L.ptr(x0), L.ptr(u),
+                                          L.ptr(tv), ctypes.byref(opts), len(cd), L.ptr(cd, ctypes.c_int64), L.ptr(cw),
+                                          L.ptr(cy), int(ckpt), ctypes.byref(cost), L.ptr(dA),
+                                          L.ptr(dtv) if dtv is not None else None, ctypes.byref(stats))
+        self._check(rc)
+        return cost.value, dA[: self.nA], dtv, stats
 
     def set_linear_solver(self, kind: str):
         """'auto' | 'f32ir' (FP32 factors + FP64 refinement) | 'f64' | 'block'."""

@@ -55,24 +55,38 @@ def _coords(model, nod, col):
 
 
 class EulerBeam3D:
-    """Corotational 3D Euler beam, 2 nodes, 12 X-dofs (+3 U-dofs when `udof`)."""
+    """Corotational 3D Euler beam, 2 nodes, 12 X-dofs (+3 U-dofs when `udof`).
+
+    With `adof`, the element also has one A-dof, field "EIscale", on its last
+    node (node 3, or node 4 with `udof`): a factor on both bending stiffnesses
+    EI2 and EI3.  The reference's EulerBeam3D has no A-dofs
+    (toolbox/BeamElement.jl:109-118); this wrapper gives the stiffness
+    identification problem its parameters.  Its value is the factor itself, so
+    a State built by initialize() (A = 0) must have A set before solving.
+    """
 
     @staticmethod
     def doflist(key):
         udof = key[1]
+        adof = len(key) > 2 and key[2]
         inod = (1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2) + ((3, 3, 3) if udof else ())
         cls = ("X",) * 12 + (("U",) * 3 if udof else ())
         fld = ("t1", "t2", "t3", "r1", "r2", "r3") * 2 + (("t1", "t2", "t3") if udof else ())
+        if adof:
+            inod += (4 if udof else 3,)
+            cls += ("A",)
+            fld += ("EIscale",)
         return inod, cls, fld
 
     @staticmethod
-    def construct(model, nod, mat: BeamCrossSection, orient2=(0.0, 1.0, 0.0), udof=False):
+    def construct(model, nod, mat: BeamCrossSection, orient2=(0.0, 1.0, 0.0), udof=False, adof=False):
         n = nod.shape[0]
         c1 = _coords(model, nod, 0)
         c2 = _coords(model, nod, 1)
         o2 = np.broadcast_to(np.asarray(orient2, dtype=np.float64), (n, 3)).copy()
         ele = beam_fields(c1, c2, o2, mat.array(n))
-        return {"ele": ele}, ("EulerBeam3D", bool(udof))
+        key = ("EulerBeam3D", bool(udof), True) if adof else ("EulerBeam3D", bool(udof))
+        return {"ele": ele}, key
 
 
 def beam_fields(c1, c2, orient2, mat):

@@ -33,6 +33,8 @@ def solve(solver, initialstate: State, time, beta=0.25, gamma=0.5, maxiter=50, m
     model, dis = initialstate.model, initialstate.dis
     dm = devmodel or DeviceModel(model, dis, device=device, linsolve=linsolve)
     try:
+        if dm.nA:
+            dm.set_A(initialstate.A)
         X0 = list(initialstate.X)[: OX + 1]
         rc, states, stats = dm.sweepx(OX, np.asarray(time, dtype=np.float64), initialstate.time, X0,
                                       U=initialstate.U[0], beta=beta, gamma=gamma, maxiter=maxiter, maxdx=maxdx,

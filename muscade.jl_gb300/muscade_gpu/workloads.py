@@ -125,7 +125,10 @@ def risers(nriser=200, nel=250, length=1000.0, seed=2028, EA=5e9, EI=1e6, GJ=1e6
 # ---------------------------------------------------------------- batched models
 def batched_params(nmodel=4096, nel_range=(10, 400), seed=2030, sigma=0.15):
     """Parameters of independent models for one batched solve: half
-    cantilevers of the 10 m type above (tip DofLoad in t3), half portal frames
+    cantilevers with the section of the 10 m one above but 5 m long (tip
+    DofLoad in t3; with the full 10 m, plain Newton from the straight beam
+    diverges in the first load step for the finer meshes and larger loads,
+    in the oracle as on the device), half portal frames
     (two 5 m columns and a 10 m beam, both bases held in all six dofs,
     mid-span DofLoad in -t3).  Element counts U{nel_range}; EA, EI2, EI3, GJ
     the cantilever's times lognormal(0, sigma) per model; load Gumbel with mode
@@ -143,7 +146,7 @@ def _model_geometry(p):
     """Node coordinates (local), beam connectivity (local, 1-based), held nodes, loaded node, load sign."""
     nel = p["nel"]
     if p["kind"] == "cantilever":
-        xs = np.linspace(0.0, 10.0, nel + 1)
+        xs = np.linspace(0.0, 5.0, nel + 1)
         xyz = np.stack([xs, np.zeros_like(xs), np.zeros_like(xs)], axis=1)
         conn = np.stack([np.arange(1, nel + 1), np.arange(2, nel + 2)], axis=1)
         return xyz, conn, [1], nel + 1, 1.0
@@ -205,3 +208,60 @@ def node_dofs(model, nodes):
     nodes = np.asarray(nodes, dtype=np.int64)
     xt = [i for i, d in enumerate(model.doftyp) if d.cls == "X"]
     return model._ndmap[nodes[:, None] - 1, np.asarray(xt)[None, :]] - 1
+
+
+# ---------------------------------------------------------------- identification
+def adjoint_beam(nel=5000, nstep=500, dt=0.01, seed=2029, ele_len=0.1, EA=1e10, EI=1e8, GJ=1e8, mu=1e3, iota1=10.0,
+                 load_std=1e3, corr_x=10.0, corr_t=0.2, nfeat=64, sigma_A=0.2, sensor_frac=0.05):
+    """Simply supported beam for load and stiffness identification: nel
+    EulerBeam3D{adof} of ele_len along x, one EI-scale A-dof per element (on its
+    own parameter node), Hold t1, t2, t3 at both ends and r1 at the first node,
+    a DofLoad in t2 at every interior node whose values are a Gaussian process
+    in space (correlation length corr_x) and time (corr_t), drawn with nfeat
+    random Fourier features.  Returns a dict with the model, the time grid,
+    the load table, the true A (lognormal, sigma_A) and the sensor dofs
+    (a random sensor_frac of the free translational dofs, 1-based)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    m = Model("identification")
+    xs = np.arange(nel + 1) * ele_len
+    nodes = m.addnode(np.stack([xs, np.zeros_like(xs), np.zeros_like(xs)], axis=1))
+    pnodes = m.addnode(np.stack([(xs[:-1] + xs[1:]) / 2, np.full(nel, 1.0), np.zeros(nel)], axis=1))
+    mat = BeamCrossSection(EA=EA, EI2=EI, EI3=EI, GJ=GJ, mu=mu, iota1=iota1)
+    m.addelement(EulerBeam3D, np.stack([nodes[:-1], nodes[1:], pnodes], axis=1), mat=mat, orient2=(0.0, 1.0, 0.0),
+                 adof=True)
+    for f in ("t1", "t2", "t3"):
+        m.addelement(Hold, np.array([[nodes[0]], [nodes[-1]]]), field=f)
+    m.addelement(Hold, [nodes[0]], field="r1")
+    times = np.round(np.arange(1, nstep + 1) * dt, 12)
+    inner = nodes[1:-1]
+    wx = rng.normal(0.0, 1.0 / corr_x, nfeat)
+    wt = rng.normal(0.0, 1.0 / corr_t, nfeat)
+    ph = rng.uniform(0.0, 2 * math.pi, nfeat)
+    amp = load_std * math.sqrt(2.0 / nfeat)
+    xi = xs[1:-1]
+    table = np.zeros((nstep, len(inner)))
+    for k in range(nfeat):
+        table += amp * np.cos(wx[k] * xi[None, :] + wt[k] * times[:, None] + ph[k])
+
+    def load(t, table=table, dt=dt):
+        k = int(round(t / dt)) - 1
+        return table[k] if 0 <= k < len(table) else np.zeros(table.shape[1])
+
+    m.addelement(DofLoad, inner[:, None], field="t2", value=load)
+    A_true = np.exp(rng.normal(0.0, sigma_A, nel))
+    cand = node_dofs(m, nodes)[:, :3]  # t1, t2, t3 of the beam nodes
+    held = {(int(nodes[0]), 0), (int(nodes[0]), 1), (int(nodes[0]), 2), (int(nodes[-1]), 0), (int(nodes[-1]), 1),
+            (int(nodes[-1]), 2)}
+    free = [cand[i, j] for i in range(len(nodes)) for j in range(3) if (int(nodes[i]), j) not in held]
+    nsens = max(1, int(round(sensor_frac * len(free))))
+    sensors = np.sort(rng.choice(np.asarray(free), nsens, replace=False)) + 1
+    return dict(model=m, times=times, loads=table, A_true=A_true, sensors=sensors, nodes=nodes, seed=seed)
+
+
+def synthetic_measurements(states, sensors, noise=0.01, seed=2031):
+    """Sensor records from states[nstep][nder][nX] plus Gaussian noise at
+    `noise` times the RMS of the noise-free records."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    y = states[:, 0, np.asarray(sensors) - 1]
+    rms = math.sqrt(float(np.mean(y * y))) or 1.0
+    return y + rng.normal(0.0, noise * rms, y.shape), noise * rms

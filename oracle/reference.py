@@ -78,7 +78,7 @@ def group_kind(g):
     return g.key[0]
 
 
-def eval_group(model, g, dis_g, X, U, t, mode, c, scaleX=None):
+def eval_group(model, g, dis_g, X, U, t, mode, c, scaleX=None, A=None):
     """Residual (scaled) and partials of all elements of a group, in the
     seeding mode of oracle_api.cpp (1: SweepX{0}, 2: Newmark step, 3: iter).
     X: tuple of state vectors (X, X', X'').  Returns R (nele,nX), J (nele,nX,NJ)."""
@@ -90,6 +90,12 @@ def eval_group(model, g, dis_g, X, U, t, mode, c, scaleX=None):
     kind = group_kind(g)
     if kind in ("EulerBeam3D", "Bar3D"):
         ele = g.cat("ele")
+        if kind == "EulerBeam3D" and dis_g.index_A.size:
+            # EI-scale A-dof: factor on EI2, EI3 (fields 54, 55 of the 69-field record)
+            a = np.asarray(A)[dis_g.index_A[:, 0] - 1]
+            ele = ele.copy()
+            ele[:, 54] *= a
+            ele[:, 55] *= a
         Ue = U[0][dis_g.index_U - 1] if dis_g.index_U.size else None
         a = b = None
         if mode == 2:
@@ -133,8 +139,9 @@ class Prepared:
         return sp.csc_matrix((nzval, self.rowval - 1, self.colptr - 1), shape=(self.n, self.n))
 
 
-def assemble(prep, X, U, t, mission, c):
-    """assemble!{mission}: returns Lλ and nzval.  mission: 'static', 'step', 'iter'."""
+def assemble(prep, X, U, t, mission, c, A=None):
+    """assemble!{mission}: returns Lλ and nzval.  mission: 'static', 'step', 'iter'.
+    A: the A-dof values (EI-scale beams)."""
     model, dis = prep.model, prep.dis
     Ll = np.zeros(prep.n)
     nz = np.zeros(prep.nnz)
@@ -142,7 +149,7 @@ def assemble(prep, X, U, t, mission, c):
     for g, dg, a1, a2 in zip(model.groups, dis.dis, prep.asm1, prep.asm2):
         if g.nele == 0:
             continue
-        R, J = eval_group(model, g, dg, X, U, t, mode, c)
+        R, J = eval_group(model, g, dg, X, U, t, mode, c, A=A)
         nele, nX = R.shape
         np.add.at(Ll, a1.reshape(-1) - 1, R.reshape(-1))
         if mode == 2:  # add_∂!{1,:minus}(Lλ, ..., (Nx+1,))
@@ -173,6 +180,7 @@ def sweepx(model, dis, initialstate, time, OX=0, beta=0.25, gamma=0.5, maxiter=5
     nder = OX + 1
     X = [initialstate.X[i].copy() if i < len(initialstate.X) else np.zeros(n) for i in range(nder)]
     U = tuple(u.copy() for u in initialstate.U)
+    A = initialstate.A.copy()
     sX = dis.scaleX
     told = initialstate.time
     out = []
@@ -185,10 +193,10 @@ def sweepx(model, dis, initialstate, time, OX=0, beta=0.25, gamma=0.5, maxiter=5
         for it in range(1, maxiter + 1):
             first = it == 1
             mission = "static" if OX == 0 else ("step" if first else "iter")
-            Ll, nz = assemble(prep, tuple(X), U, t, mission, c)
-            A = prep.matrix(nz)
+            Ll, nz = assemble(prep, tuple(X), U, t, mission, c, A=A)
+            Kmat = prep.matrix(nz)
             try:
-                lu = spla.splu(A.tocsc())
+                lu = spla.splu(Kmat.tocsc())
                 dx = lu.solve(Ll)
             except RuntimeError as e:
                 raise RuntimeError(f"matrix factorization failed at step={step}, iiter={it}") from e

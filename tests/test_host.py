@@ -68,7 +68,7 @@ def test_beam_fields_match_oracle_constructor():
 def test_library_exports_every_declared_symbol():
     _lib.build()
     hdr = open(os.path.join(ROOT, "include", "muscade_gpu.h")).read()
-    declared = set(re.findall(r"\b(mgpu_[a-z_0-9]+)\s*\(", hdr))
+    declared = set(re.findall(r"\b(mgpu_[A-Za-z_0-9]+)\s*\(", hdr))
     L = ctypes.CDLL(_lib.LIB)
     missing = [s for s in sorted(declared) if not hasattr(L, s)]
     assert not missing, missing
