@@ -17,7 +17,7 @@ from oracle import reference as REF
 
 pytestmark = pytest.mark.gpu
 
-MAXDX = 1e-10
+MAXDX = 1e-7
 TOL_FD = 1e-6
 
 
