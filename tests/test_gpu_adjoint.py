@@ -79,9 +79,11 @@ def test_newmark_adjoint_matches_central_differences():
         fd.append((_cost(d, Ap) - _cost(d, Am)) / (2 * h))
     fd = np.array(fd)
     assert np.max(np.abs(gA[idx] - fd)) <= TOL_FD * np.max(np.abs(fd)), (gA[idx], fd)
-    # load values: perturb one entry of the load table (the DofLoad functions read it)
+    # load values: perturb one entry of the load table (the DofLoad functions read it);
+    # gF follows the tvals layout, where the Hold offsets come first
     dm.set_A(A0)
     tbl = d["loads"]
+    off = sum(g.nele for g in d["model"].groups if g.key[0] == "DofConstraint")
     checks = [(3, 5), (10, 12), (19, 20)]
     fdF, adF = [], []
     for k, j in checks:
@@ -92,7 +94,7 @@ def test_newmark_adjoint_matches_central_differences():
         cm = _cost(d, A0)
         tbl[k, j] += hF
         fdF.append((cp - cm) / (2 * hF))
-        adF.append(gF[k, j])
+        adF.append(gF[k, off + j])
     fdF, adF = np.array(fdF), np.array(adF)
     assert np.max(np.abs(adF - fdF)) <= TOL_FD * np.max(np.abs(fdF)), (adF, fdF)
     dm.close()
