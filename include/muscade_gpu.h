@@ -190,24 +190,30 @@ int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *
  * calls UMFPACK through lu/lu!/\ at src/SweepX.jl:207-210).  Every connected
  * component of Lλx is reordered (reverse Cuthill-McKee) and factorised as a
  * band with partial pivoting:
- *   MGPU_LINSOLVE_AUTO   F64 where every component has kl <= 31 and
- *                        kl+ku+1 <= 64, else BLOCK (the default)
+ *   MGPU_LINSOLVE_AUTO   TORN when some component has 512 dofs or more and
+ *                        max(kl, ku) <= 16, else F64 where every component
+ *                        has kl <= 31 and kl+ku+1 <= 64, else BLOCK (the default)
  *   MGPU_LINSOLVE_F32IR  FP32 factors, FP64 residuals and iterative refinement
  *                        until the correction is below 1e-12 of the solution;
  *                        a component that does not contract, or would need
  *                        more than 8 sweeps, is refactorised in FP64
  *   MGPU_LINSOLVE_F64    FP64 factors, one warp per component
  *   MGPU_LINSOLVE_BLOCK  FP64 factors, one thread block per component, bands up to 256
+ *   MGPU_LINSOLVE_TORN   FP64, long components cut into about √(n/s) interiors
+ *                        factorised in parallel and separators of s = max(kl, ku)
+ *                        dofs coupled through their banded Schur complement
+ *                        (pivoting within each interior and within the Schur band)
  * F64 and BLOCK give bitwise the same Δx.  Returns MGPU_ERR_UNSUPPORTED when
  * the bands are too wide for the requested kind. */
 #define MGPU_LINSOLVE_AUTO 0
 #define MGPU_LINSOLVE_F32IR 1
 #define MGPU_LINSOLVE_F64 2
 #define MGPU_LINSOLVE_BLOCK 3
+#define MGPU_LINSOLVE_TORN 4
 int mgpu_set_linear_solver(mgpu_ctx *ctx, int32_t kind);
 
 typedef struct {
-  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64 or _BLOCK in use */
+  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64, _BLOCK or _TORN in use */
   int32_t ncomp;         /* connected components of Lλx */
   int32_t max_kl;        /* widest lower / upper band after reordering */
   int32_t max_ku;

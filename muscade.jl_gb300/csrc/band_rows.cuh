@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(32) rb_solve(RbComp cp, const int32_t* __restr
 
 // unfactorised rows from the assembled CSC values (positions fixed at create),
 // in FP64 and, when A32 is given, in FP32 for the FP32 factorisation
-__global__ void rb_gather(int64_t nnz, const int64_t* __restrict__ map, const double* __restrict__ nzval,
+static __global__ void rb_gather(int64_t nnz, const int64_t* __restrict__ map, const double* __restrict__ nzval,
                           double* __restrict__ A, float* __restrict__ A32) {
   const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (q < nnz) {

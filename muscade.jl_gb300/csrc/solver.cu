@@ -240,6 +240,177 @@ static void analyse(mgpu_ctx* c, Solver& S) {
            cudaMemset(S.flag, 0, ncomp * sizeof(int)) == cudaSuccess &&
            cudaMalloc(&S.nsweep, ncomp * sizeof(int)) == cudaSuccess &&
            cudaMemset(S.nsweep, 0, ncomp * sizeof(int)) == cudaSuccess;
+    // ---- torn layout of the long components (needs s = max(kl, ku) <= 16 for the
+    // Schur-complement band 2s-1 <= 31)
+    std::vector<int> Pc(ncomp, 1), sc(ncomp, 0);
+    for (int cc = 0; cc < ncomp; ++cc) {
+      const int64_t nc = comp_start[cc + 1] - comp_start[cc];
+      const int sw = std::max(1, std::max(kl[cc], ku[cc]));
+      sc[cc] = sw;
+      if (sw > 16 || nc < kTornMinDofs) continue;
+      const int64_t mmin = std::max(2 * sw, 48);
+      const int64_t pmax = (nc + sw) / (mmin + sw);
+      const int64_t pc = std::llround(std::sqrt(double(nc) / sw));
+      Pc[cc] = int(std::max<int64_t>(1, std::min(pc, pmax)));
+      if (Pc[cc] > 1) S.tearable = 1;
+    }
+    if (S.tearable) {
+      std::vector<TornInt> ti, tiT;
+      std::vector<TornSep> ts;
+      std::vector<int64_t> irb, ilb, trb, tlb;
+      std::vector<int32_t> in_, ikl, iku, idof, tn, tkl, tdof;
+      int64_t orow = 0, oblk = 0, oy = 0, olm = 0, otr = 0, otl = 0, otv = 0;
+      // segment of each band position: >= 0 interior index (global), < 0 -(separator index + 1)
+      std::vector<int32_t> seg(n), loc(n);
+      int maxwI = 0;
+      for (int cc = 0; cc < ncomp; ++cc) {
+        const int64_t c0 = comp_start[cc], nc = comp_start[cc + 1] - c0;
+        const int P = Pc[cc], sw = sc[cc], w = kl[cc] + ku[cc] + 1;
+        maxwI = std::max(maxwI, w);
+        const int64_t tot = nc - int64_t(P - 1) * sw;
+        int64_t p0 = 0;
+        const int sep0 = int(ts.size()), int0 = int(ti.size());
+        const int64_t trow0 = otv;
+        for (int a = 0; a < P; ++a) {
+          const int64_t m = tot / P + (a < tot % P ? 1 : 0);
+          TornInt I{};
+          I.rbase = orow;
+          I.lbase = olm;
+          I.n = int32_t(m);
+          I.kl = kl[cc];
+          I.ku = ku[cc];
+          I.dof0 = int32_t(c0 + p0);
+          I.s = sw;
+          I.eL = I.eR = I.fL = I.fR = I.yL = I.yR = -1;
+          I.sepL = a > 0 ? sep0 + a - 1 : -1;
+          I.sepR = a < P - 1 ? sep0 + a : -1;
+          if (I.sepL >= 0) {
+            I.eL = oblk, oblk += int64_t(sw) * sw;
+            I.fL = oblk, oblk += int64_t(sw) * sw;
+            I.yL = oy, oy += m * sw;
+          }
+          if (I.sepR >= 0) {
+            I.eR = oblk, oblk += int64_t(sw) * sw;
+            I.fR = oblk, oblk += int64_t(sw) * sw;
+            I.yR = oy, oy += m * sw;
+          }
+          orow += m * w;
+          olm += m * std::max(kl[cc], ku[cc]);
+          for (int64_t q = 0; q < m; ++q) {
+            seg[c0 + p0 + q] = int32_t(ti.size());
+            loc[c0 + p0 + q] = int32_t(q);
+          }
+          irb.push_back(I.rbase), ilb.push_back(I.lbase), in_.push_back(I.n), ikl.push_back(I.kl),
+              iku.push_back(I.ku), idof.push_back(I.dof0);
+          ti.push_back(I);
+          TornInt IT = I;
+          std::swap(IT.kl, IT.ku);
+          tiT.push_back(IT);
+          p0 += m;
+          if (a < P - 1) {
+            TornSep Sp{};
+            Sp.s = sw;
+            Sp.dof0 = int32_t(c0 + p0);
+            Sp.d = oblk, oblk += int64_t(sw) * sw;
+            Sp.intL = int0 + a;
+            Sp.intR = int0 + a + 1;
+            Sp.trow = otv + int64_t(a) * sw;
+            Sp.first = a == 0;
+            Sp.last = a == P - 2;
+            for (int64_t q = 0; q < sw; ++q) {
+              seg[c0 + p0 + q] = -(int32_t(ts.size()) + 1);
+              loc[c0 + p0 + q] = int32_t(q);
+            }
+            ts.push_back(Sp);
+            p0 += sw;
+          }
+        }
+        if (P > 1) {
+          const int64_t nT = int64_t(P - 1) * sw;
+          const int klT = 2 * sw - 1, wT = 4 * sw - 1;
+          for (int k = sep0; k < int(ts.size()); ++k) {
+            ts[k].tbase = otr;
+            ts[k].tkl = klT;
+            ts[k].tw = wT;
+            ts[k].trow0 = trow0;
+          }
+          trb.push_back(otr), tlb.push_back(otl), tn.push_back(int32_t(nT)), tkl.push_back(klT),
+              tdof.push_back(int32_t(otv));
+          otr += nT * wT;
+          otl += nT * klT;
+          otv += nT;
+        }
+      }
+      S.nint = int(ti.size());
+      S.nsep = int(ts.size());
+      S.ntc = int(tn.size());
+      S.twmI = maxwI <= 32 ? 32 : 64;
+      int maxsT = 0;
+      for (int cc = 0; cc < ncomp; ++cc)
+        if (Pc[cc] > 1) maxsT = std::max(maxsT, sc[cc]);
+      S.twmT = 4 * maxsT - 1 <= 32 ? 32 : 64;
+      S.tb_rows = orow;
+      S.tb_blk = oblk;
+      S.tb_y = oy;
+      S.tb_lm = olm;
+      S.tb_trows = otr;
+      S.tb_tlm = otl;
+      S.tb_tvec = otv;
+      // every nnz to its place in TALL = [interior rows | blocks], for Lλx and for its transpose
+      std::vector<int64_t> tbmap(P.nnz), tbmapT(P.nnz);
+      auto place = [&](int64_t pi, int64_t pj, bool transposed) -> int64_t {
+        const int si = seg[pi], sj = seg[pj];
+        const int li = loc[pi], lj = loc[pj];
+        if (si >= 0 && sj >= 0) {  // same interior
+          if (si != sj) return -1;
+          const TornInt& I = ti[si];
+          const int w = I.kl + I.ku + 1, klx = transposed ? I.ku : I.kl;
+          return I.rbase + int64_t(li) * w + (lj - li + klx);
+        }
+        if (si >= 0) {  // interior row, separator column: E
+          const TornInt& I = ti[si];
+          const int k = -sj - 1;
+          if (k == I.sepL) return S.tb_rows + I.eL + int64_t(li) * I.s + lj;
+          return S.tb_rows + I.eR + int64_t(li - (I.n - I.s)) * I.s + lj;
+        }
+        if (sj >= 0) {  // separator row, interior column: F
+          const TornInt& I = ti[sj];
+          const int k = -si - 1;
+          if (k == I.sepL) return S.tb_rows + I.fL + int64_t(li) * I.s + lj;
+          return S.tb_rows + I.fR + int64_t(li) * I.s + (lj - (I.n - I.s));
+        }
+        if (si != sj) return -1;
+        return S.tb_rows + ts[-si - 1].d + int64_t(li) * ts[-si - 1].s + lj;  // same separator: D
+      };
+      for (int64_t j = 0; j < n; ++j)
+        for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+          const int64_t i = P.rowval[q];
+          tbmap[q] = place(pos[i], pos[j], false);
+          tbmapT[q] = place(pos[j], pos[i], true);
+          if (tbmap[q] < 0 || tbmapT[q] < 0) S.tearable = 0;  // an entry outside the bands (cannot happen)
+        }
+      std::vector<int32_t> tperm(std::max<int64_t>(otv, 1));
+      for (int64_t k = 0; k < otv; ++k) tperm[k] = int32_t(k);
+      auto upv = [&](auto** dst, const auto& v) -> bool { return v.empty() ? true : up(dst, v); };
+      good = good && upv(&S.d_ti, ti) && upv(&S.d_tiT, tiT) && upv(&S.d_ts, ts) && upv(&S.i_rbase, irb) &&
+             upv(&S.i_lbase, ilb) && upv(&S.i_n, in_) && upv(&S.i_kl, ikl) && upv(&S.i_ku, iku) &&
+             upv(&S.i_dof0, idof) && upv(&S.t_rbase, trb) && upv(&S.t_lbase, tlb) && upv(&S.t_n, tn) &&
+             upv(&S.t_kl, tkl) && upv(&S.t_dof0, tdof) && up(&S.t_perm, tperm) && up(&S.tbmap, tbmap) &&
+             up(&S.tbmapT, tbmapT);
+      const size_t nall = size_t(std::max<int64_t>(orow + oblk, 1));
+      good = good && cudaMalloc(&S.TALL, nall * sizeof(double)) == cudaSuccess &&
+             cudaMemset(S.TALL, 0, nall * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.TUC, std::max<int64_t>(orow, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.TLM, std::max<int64_t>(olm, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.TY, std::max<int64_t>(oy, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.TTR, std::max<int64_t>(otr, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.TTUC, std::max<int64_t>(otr, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.TTLM, std::max<int64_t>(otl, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.trhs, std::max<int64_t>(otv, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.txs, std::max<int64_t>(otv, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.tpiv, n * sizeof(int32_t)) == cudaSuccess &&
+             cudaMalloc(&S.ttpiv, std::max<int64_t>(otv, 1) * sizeof(int32_t)) == cudaSuccess;
+    }
   }
   good = good && cudaMalloc(&S.AB, std::max<int64_t>(S.band_total, 1) * sizeof(double)) == cudaSuccess;
   good = good && cudaMalloc(&S.ipiv, n * sizeof(int32_t)) == cudaSuccess;
@@ -499,9 +670,10 @@ extern "C" int mgpu_solver_create(mgpu_ctx* c) {
   cudaGetLastError();  // analysis errors are reported at solve time
   // default: the FP64 row-band kernels where they apply, else the FP64 block
   // kernels (mgpu_set_linear_solver changes it)
-  S.path = S.wm ? PATH_F64ROWS : PATH_BLOCK;
+  S.path = S.tearable ? PATH_TORN : S.wm ? PATH_F64ROWS : PATH_BLOCK;
   if (getenv("MGPU_VERBOSE")) {
-    static const char* names[] = {"row-band FP32 + FP64 refinement", "row-band FP64", "block FP64"};
+    static const char* names[] = {"row-band FP32 + FP64 refinement", "row-band FP64", "block FP64",
+                                  "partitioned FP64"};
     fprintf(stderr, "[muscade_gpu] solver: %s, %d components, max kl %d, max ku %d, %s\n",
             S.ok ? "banded" : S.why.c_str(), S.ncomp, S.maxkl, S.maxku, names[S.path]);
   }
@@ -509,14 +681,21 @@ extern "C" int mgpu_solver_create(mgpu_ctx* c) {
 }
 
 extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
-  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_BLOCK)
+  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_TORN)
     return set_err(c, MGPU_ERR_ARG, "mgpu_set_linear_solver: bad arguments");
   Solver& S = *c->solver;
+  if (kind == MGPU_LINSOLVE_TORN) {
+    if (!S.tearable)
+      return set_err(c, MGPU_ERR_UNSUPPORTED,
+                     "partitioned solve needs a component of at least 512 dofs with max(kl, ku) <= 16");
+    S.path = PATH_TORN;
+    return MGPU_OK;
+  }
   if ((kind == MGPU_LINSOLVE_F32IR || kind == MGPU_LINSOLVE_F64) && !S.wm)
     return set_err(c, MGPU_ERR_UNSUPPORTED,
                    "linear solver kind needs kl <= 31 and kl+ku+1 <= 64 in every component (kl=" +
                        std::to_string(S.maxkl) + ", ku=" + std::to_string(S.maxku) + ")");
-  S.path = kind == MGPU_LINSOLVE_AUTO ? (S.wm ? PATH_F64ROWS : PATH_BLOCK)
+  S.path = kind == MGPU_LINSOLVE_AUTO ? (S.tearable ? PATH_TORN : S.wm ? PATH_F64ROWS : PATH_BLOCK)
            : kind == MGPU_LINSOLVE_F32IR ? PATH_F32IR
            : kind == MGPU_LINSOLVE_F64   ? PATH_F64ROWS
                                          : PATH_BLOCK;
@@ -526,7 +705,10 @@ extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
 extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
   if (!c || !c->solver || !info) return set_err(c, MGPU_ERR_ARG, "mgpu_linear_solver_info: bad arguments");
   Solver& S = *c->solver;
-  info->kind = S.path == PATH_F32IR ? MGPU_LINSOLVE_F32IR : S.path == PATH_F64ROWS ? MGPU_LINSOLVE_F64 : MGPU_LINSOLVE_BLOCK;
+  info->kind = S.path == PATH_F32IR    ? MGPU_LINSOLVE_F32IR
+               : S.path == PATH_F64ROWS ? MGPU_LINSOLVE_F64
+               : S.path == PATH_TORN    ? MGPU_LINSOLVE_TORN
+                                        : MGPU_LINSOLVE_BLOCK;
   info->ncomp = S.ncomp;
   info->max_kl = S.maxkl;
   info->max_ku = S.maxku;
@@ -551,7 +733,9 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
   void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx,
                 S->red, S->info, S->rbase, S->lbase, S->rbmap, S->rbmapT, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
                 S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag, S->part, S->cod, S->frozen,
-                S->nactive};
+                S->nactive, S->d_ti, S->d_tiT, S->d_ts, S->i_rbase, S->i_lbase, S->i_n, S->i_kl, S->i_ku,
+                S->i_dof0, S->t_rbase, S->t_lbase, S->t_n, S->t_kl, S->t_dof0, S->t_perm, S->tbmap, S->tbmapT,
+                S->TALL, S->TUC, S->TLM, S->TY, S->TTR, S->TTUC, S->TTLM, S->trhs, S->txs, S->tpiv, S->ttpiv};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -563,10 +747,62 @@ unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 
 // one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device);
 // a singular factorisation writes its component+1 to *info.  Capturable.
+// Torn (partitioned) factorisation of Lλx or of its transpose and out = A⁻¹ rhs
+// (model order), FP64.  Capturable.
+static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int* info) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  const RbComp cpI = tr ? RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_ku, S.i_kl, S.i_dof0}
+                        : RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_kl, S.i_ku, S.i_dof0};
+  const RbComp cpT{S.t_rbase, S.t_lbase, S.t_n, S.t_kl, S.t_kl, S.t_dof0};
+  const TornInt* ti = tr ? S.d_tiT : S.d_ti;
+  rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, tr ? S.tbmapT : S.tbmap, c->nzval, S.TALL, nullptr);
+  const double* blk = S.TALL + S.tb_rows;
+  // interiors: factors, spikes; separators: Schur complement and its factors
+  if (S.twmI == 32)
+    rb_lu<double, 32><<<S.nint, 32, 0, st>>>(cpI, S.TALL, S.TUC, S.TLM, S.tpiv, RB_PLAIN, S.flag, info);
+  else
+    rb_lu<double, 64><<<S.nint, 32, 0, st>>>(cpI, S.TALL, S.TUC, S.TLM, S.tpiv, RB_PLAIN, S.flag, info);
+  if (S.nsep > 0) {
+    if (S.twmI == 32)
+      tb_spikes<32><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
+    else
+      tb_spikes<64><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
+    MG_CUDA(cudaMemsetAsync(S.TTR, 0, S.tb_trows * sizeof(double), st));
+    tb_schur<<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.TY, S.TTR);
+    if (S.twmT == 32)
+      rb_lu<double, 32><<<S.ntc, 32, 0, st>>>(cpT, S.TTR, S.TTUC, S.TTLM, S.ttpiv, RB_PLAIN, S.flag, info);
+    else
+      rb_lu<double, 64><<<S.ntc, 32, 0, st>>>(cpT, S.TTR, S.TTUC, S.TTLM, S.ttpiv, RB_PLAIN, S.flag, info);
+  }
+  // solve: interiors, separator right-hand sides, separators, back-substitution
+  if (S.twmI == 32)
+    rb_solve<double, 32><<<S.nint, 32, 0, st>>>(cpI, S.perm, S.TALL, S.TUC, S.TLM, S.tpiv, rhs, S.bw, S.xw, S.rw,
+                                                S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
+  else
+    rb_solve<double, 64><<<S.nint, 32, 0, st>>>(cpI, S.perm, S.TALL, S.TUC, S.TLM, S.tpiv, rhs, S.bw, S.xw, S.rw,
+                                                S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
+  if (S.nsep > 0) {
+    tb_sep_rhs<<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.perm, rhs, out, S.trhs);
+    if (S.twmT == 32)
+      rb_solve<double, 32><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, S.TTUC, S.TTLM, S.ttpiv, S.trhs, S.bw, S.xw,
+                                                 S.rw, S.tw64, S.txs, 0, RB_PLAIN, S.flag, nullptr);
+    else
+      rb_solve<double, 64><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, S.TTUC, S.TTLM, S.ttpiv, S.trhs, S.bw, S.xw,
+                                                 S.rw, S.tw64, S.txs, 0, RB_PLAIN, S.flag, nullptr);
+    tb_back<<<S.nint, 128, 0, st>>>(S.nint, ti, S.d_ts, S.TY, S.perm, S.txs, out);
+  }
+  MG_CUDA(cudaGetLastError());
+  return MGPU_OK;
+}
+
 int factor_solve(mgpu_ctx* c, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
-  if (S.path == PATH_BLOCK) {
+  if (S.path == PATH_TORN) {
+    const int rc = torn_solve(c, false, c->Ll, S.dx, info);
+    if (rc) return rc;
+  } else if (S.path == PATH_BLOCK) {
     MG_CUDA(cudaMemsetAsync(S.AB, 0, S.band_total * sizeof(double), st));
     band_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.bmap, c->nzval, S.AB);
     band_lu<<<S.ncomp, 128, 0, st>>>(S.cbase, S.cn, S.ckl, S.cku, S.cdof0, S.AB, S.ipiv, S.rdiag, info);
@@ -609,6 +845,7 @@ int factor_solve(mgpu_ctx* c, int* info) {
 
 int factor_solve_T(mgpu_ctx* c, const double* rhs, double* out, int* info) {
   Solver& S = *c->solver;
+  if (S.path == PATH_TORN) return torn_solve(c, true, rhs, out, info);
   if (!S.wmT)
     return set_err(c, MGPU_ERR_UNSUPPORTED,
                    "transposed solve needs the row-band kernels (kl, ku <= 31 and kl+ku+1 <= 64 in every component)");

@@ -6,17 +6,20 @@
 #include <cstdint>
 #include <string>
 
+#include "band_torn.cuh"
 #include "ctx.hpp"
 
 namespace mgpu {
 
 constexpr int kNormBlocks = 128;
+constexpr int64_t kTornMinDofs = 512;  // components shorter than this are factorised whole
 constexpr int kInfoSlots = 64;  // a captured step holds up to kInfoSlots-1 iterations
 
 enum SolverPath : int {
   PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
   PATH_F64ROWS = 1,  // row-band warp kernels in FP64
-  PATH_BLOCK = 2   // gbtf2-layout block kernels in FP64 (any band width up to 256)
+  PATH_BLOCK = 2,  // gbtf2-layout block kernels in FP64 (any band width up to 256)
+  PATH_TORN = 3    // long components cut into interiors and separators, FP64
 };
 
 struct Solver {
@@ -42,6 +45,24 @@ struct Solver {
   double* rw = nullptr;       // [nX] residual
   float* tw32 = nullptr;      // [nX] substitution work
   double* tw64 = nullptr;
+  // partitioned (torn) layout of long components: interiors factorised in
+  // parallel, separators coupled through a banded Schur complement
+  int tearable = 0;           // some component is long enough to be cut
+  int nint = 0, nsep = 0, ntc = 0;
+  int twmI = 0, twmT = 0;     // register windows of the interior and Schur-complement kernels
+  TornInt* d_ti = nullptr;    // [nint] interiors (bands of Lλx)
+  TornInt* d_tiT = nullptr;   // [nint] the same with kl and ku exchanged (the transpose)
+  TornSep* d_ts = nullptr;    // [nsep]
+  int64_t *i_rbase = nullptr, *i_lbase = nullptr;
+  int32_t *i_n = nullptr, *i_kl = nullptr, *i_ku = nullptr, *i_dof0 = nullptr;
+  int64_t *t_rbase = nullptr, *t_lbase = nullptr;
+  int32_t *t_n = nullptr, *t_kl = nullptr, *t_dof0 = nullptr, *t_perm = nullptr;
+  int64_t tb_rows = 0, tb_blk = 0, tb_y = 0, tb_lm = 0, tb_trows = 0, tb_tlm = 0, tb_tvec = 0;
+  int64_t* tbmap = nullptr;   // [nnz] position in TALL = [interior rows | blocks]
+  int64_t* tbmapT = nullptr;  // [nnz] the same for the transpose
+  double *TALL = nullptr, *TUC = nullptr, *TLM = nullptr, *TY = nullptr;
+  double *TTR = nullptr, *TTUC = nullptr, *TTLM = nullptr, *trhs = nullptr, *txs = nullptr;
+  int32_t *tpiv = nullptr, *ttpiv = nullptr;
   int* flag = nullptr;        // [ncomp] FP64 fallback requested
   int* nsweep = nullptr;      // [ncomp] refinement sweeps used
   std::string why;       // reason when not

@@ -17,7 +17,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
 SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
 HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh",
-           "solver.hpp"]
+           "band_torn.cuh", "solver.hpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes
@@ -91,7 +91,7 @@ class LinsolveInfo(ctypes.Structure):
                 ("max_ku", ctypes.c_int32), ("last_fallback", ctypes.c_int32), ("last_sweeps", ctypes.c_int32)]
 
 
-LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3}
+LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3, "torn": 4}
 LINSOLVE_NAME = {v: k for k, v in LINSOLVE.items()}
 
 # every symbol the header declares (checked by the CPU test suite)

@@ -322,6 +322,52 @@ def test_sweepx0_portal_frame_matches_oracle():
     _compare_states(out, ref, 1, st.dis.fieldX)
 
 
+def _rel_dev(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_partitioned_solver_matches_row_band_solver():
+    """Long risers (n = 606 per component) cut into interiors and separators:
+    the trajectory of the row-band solver within rounding (the pivoting is
+    restricted to the blocks, so not bitwise)."""
+    m, times = W.risers(nriser=3, nel=100)
+    st = m.initialize(time=0.0)
+    a, ia = _sweep(m, st, 2, times[:10], "torn", fixed_iter=3)
+    b, ib = _sweep(m, st, 2, times[:10], "f64", fixed_iter=3)
+    assert ia["kind"] == "torn" and ib["kind"] == "f64"
+    lam = np.array([str(f).startswith("λ") for f in st.dis.fieldX])
+    # the state tolerance: accelerations carry 1/(βΔt²) times the rounding of the positions
+    for d in range(3):
+        assert _rel_dev(a[:, d][:, ~lam], b[:, d][:, ~lam]) <= TOL_STATE, d
+    assert _rel_dev(a[:, 0][:, lam], b[:, 0][:, lam]) <= TOL_STATE
+
+
+def test_partitioned_solver_static_cantilever_matches_oracle():
+    from muscade_gpu import SweepXGPU, solve
+
+    m, _ = W.cantilever(nel=120, length=10.0, load=1e2)
+    st = m.initialize()
+    times = np.array([0.5, 1.0])
+    out = solve(SweepXGPU[0], st, times, maxdx=1e-8, maxiter=30, linsolve="torn")
+    ref = REF.sweepx(m, st.dis, st, times, OX=0, maxdx=1e-8, maxiter=30)
+    _compare_states(out, ref, 1, st.dis.fieldX)
+
+
+def test_partitioned_transposed_solve_gives_the_adjoint():
+    d = W.adjoint_beam(nel=120, nstep=8)
+    m = d["model"]
+    st = m.initialize(time=0.0)
+    y = np.zeros((8, len(d["sensors"])))
+    res = {}
+    for kind in ("torn", "f64"):
+        dm = DeviceModel(m, st.dis, linsolve=kind)
+        res[kind] = dm.adjoint(2, d["times"], st.time, list(st.X), d["sensors"], 1.0, y, maxdx=1e-7)
+        assert dm.linear_solver_info()["kind"] == kind
+        dm.close()
+    assert res["torn"][0] == pytest.approx(res["f64"][0], rel=1e-10)
+    assert _rel_dev(res["torn"][1], res["f64"][1]) <= 1e-9
+
+
 def test_nan_is_reported_like_the_reference():
     m, _ = W.cantilever()
     st = m.initialize()
