@@ -161,9 +161,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="60,60,20")
     ap.add_argument("--cpu-sample", type=int, default=int(os.environ.get("MGPU_CPU_SAMPLE", "60000")))
-    ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever", "batched"],
+    ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever", "batched", "adjoint"],
                     help="lattice: the headline assembly metric; risers/cantilever: whole SweepX solves; "
-                         "batched: independent cantilevers and portal frames solved together")
+                         "batched: independent cantilevers and portal frames solved together; "
+                         "adjoint: cost gradient of the stiffness identification beam")
+    ap.add_argument("--adj-nel", type=int, default=5000)
+    ap.add_argument("--adj-steps", type=int, default=500)
+    ap.add_argument("--fd-params", type=int, default=50, help="adjoint: A-dofs checked by central differences")
+    ap.add_argument("--fd-steps", type=int, default=50, help="adjoint: horizon of the finite-difference check")
     ap.add_argument("--models", type=int, default=4096, help="batched: number of models")
     ap.add_argument("--individual", type=int, default=16, help="batched: models also solved one by one")
     ap.add_argument("--no-graph", action="store_true", help="risers: launch kernel by kernel instead of replaying "
@@ -175,6 +180,8 @@ def main():
     rank, local_rank, ws, dist = dist_setup()
     if args.config == "batched":
         return bench_batched(args, rank, local_rank, ws, dist)
+    if args.config == "adjoint":
+        return bench_adjoint(args, rank, local_rank, ws, dist)
     if args.config != "lattice":
         return bench_solve(args, rank, local_rank, ws, dist)
     nx, ny, nz = (int(v) for v in args.grid.split(","))
@@ -460,6 +467,88 @@ def bench_batched(args, rank, local_rank, ws, dist):
                              "max_rel_state_dev_vs_fp64": worst, "linear_solver": info32,
                              "newton_iterations": stats32.niter_total},
             "gpu_launches": args.steps * iters * launches_per_iter, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
+def bench_adjoint(args, rank, local_rank, ws, dist):
+    """Stiffness identification: the gradient of the sensor misfit with
+    respect to one EI scale per beam by the discrete Newmark adjoint (one
+    forward sweep, √N checkpoints, a reverse sweep of transposed solves).  One
+    bench step is one gradient.  Replicas only: one beam per GPU."""
+    from muscade_gpu import _lib, workloads
+    from muscade_gpu.device import DeviceModel
+
+    _lib.build()
+    d = workloads.adjoint_beam(nel=args.adj_nel, nstep=args.adj_steps)
+    m = d["model"]
+    st = m.initialize(time=0.0)
+    dm = DeviceModel(m, st.dis, device=local_rank)
+    X0 = list(st.X)
+    tol = 1e-7
+    dm.set_A(d["A_true"])
+    rc, truth, _ = dm.sweepx(2, d["times"], st.time, X0, maxdx=tol)
+    if rc != 0:
+        raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
+    y, sd = workloads.synthetic_measurements(truth, d["sensors"])
+    w = 1.0 / sd**2
+    A0 = np.ones(dm.nA)
+    dm.set_A(A0)
+    # one forward sweep alone (the unit of a finite-difference gradient)
+    t0 = time.perf_counter()
+    dm.sweepx(2, d["times"], st.time, X0, maxdx=tol)
+    t_fwd = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        dm.adjoint(2, d["times"], st.time, X0, d["sensors"], w, y, maxdx=tol)
+    if dist:
+        dist.barrier()
+    with Clocks(local_rank) as ck:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            C, gA, _, stats = dm.adjoint(2, d["times"], st.time, X0, d["sensors"], w, y, maxdx=tol)
+        dt = (time.perf_counter() - t0) / args.steps
+    clocks = ck.summary()
+    dt = reduce_max(dist, dt)
+    if rank != 0:
+        dm.close()
+        return
+    # central differences on the first fd_steps steps at fd_params random A-dofs
+    nfd = min(args.fd_steps, len(d["times"]))
+    tf, yf = d["times"][:nfd], y[:nfd]
+    Cf, gf, _, _ = dm.adjoint(2, tf, st.time, X0, d["sensors"], w, yf, maxdx=tol)
+
+    def cost(A):
+        dm.set_A(A)
+        rc, s, _ = dm.sweepx(2, tf, st.time, X0, maxdx=tol)
+        r = s[:, 0, d["sensors"] - 1] - yf
+        return float(np.sum(np.diff(np.concatenate([[st.time], tf])) * np.sum(w * r * r, axis=1)))
+
+    idx = np.random.Generator(np.random.PCG64(2032)).choice(dm.nA, min(args.fd_params, dm.nA), replace=False)
+    h = 1e-4
+    fd = np.array([(cost(A0 + h * np.eye(1, dm.nA, i)[0]) - cost(A0 - h * np.eye(1, dm.nA, i)[0])) / (2 * h)
+                   for i in idx])
+    fd_err = float(np.max(np.abs(gf[idx] - fd)) / np.max(np.abs(fd)))
+    dm.set_A(A0)
+    info = dm.linear_solver_info()
+    dm.close()
+    nst = len(d["times"])
+    line = {"metric": "adjoint gradients/s (dC/dA, stiffness identification)", "value": ws / dt,
+            "unit": "gradients/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded GP loads, lognormal true EI scales, 1 % sensor noise)",
+            "config": {"workload": f"simply supported beam, {args.adj_nel} EulerBeam3D with EI-scale A-dofs, "
+                                   f"{nst} Newmark steps of 0.01 s", "beams": args.adj_nel, "dofs": m.ndof["X"],
+                       "A_dofs": dm.nA, "sensors": int(len(d["sensors"])), "checkpoints": "sqrt(N)",
+                       "newton_iterations_forward": stats.niter_total, "linear_solver": info},
+            "cost": C, "grad_norm": float(np.linalg.norm(gA)),
+            "fd_check": {"params": int(len(idx)), "steps": int(nfd), "h": h, "max_rel_err": fd_err},
+            "forward_sweep_s": t_fwd,
+            "speedup_vs_finite_differences": 2 * dm.nA * t_fwd / dt,
+            "e2e": {"value": ws / dt, "unit": "gradients/s", "h2d_bytes_per_step": 8 * (nst * (dm.ntval + 1 + len(d["sensors"])) + dm.nA),
+                    "d2h_bytes_per_step": 8 * (dm.nA + nst),
+                    "note": "the whole mgpu_adjoint_sweepx call with host loads, records and gradient"},
+            # per Newton iteration ~20 launches (element kernels, scatters, partitioned solve,
+            # decrement, norms), forward and recomputation; per reverse step ~31
+            "gpu_launches": args.steps * (2 * stats.niter_total * 20 + nst * 31), "clocks": clocks}
     print(json.dumps(line), flush=True)
 
 

@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
                                                 double* __restrict__ Y) {
   __shared__ __align__(16) double sU[32 * WM];
   __shared__ __align__(16) double sL[32 * 31];
+  __shared__ __align__(16) double sYin[32 * 33];  // backward: the chunk's incoming rows, one column per lane
   __shared__ int sP[32];
   const int a = blockIdx.x, lane = threadIdx.x;
   if (a >= nint) return;
@@ -142,6 +143,13 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
     const int k0 = c * 32, k1 = min(m, k0 + 32);
     __syncwarp();
     for (int e = lane; e < (k1 - k0) * w; e += 32) sU[e] = U[int64_t(k0) * w + e];
+    // rows k-1-kv entering the window during this chunk (forward results, this lane's column):
+    // read once per chunk instead of one dependent global load per row
+#pragma unroll 4
+    for (int q = 0; q < 32; ++q) {
+      const int i = k0 + q - 1 - kv;
+      sYin[q * 33 + lane] = (act && i >= 0 && q < k1 - k0) ? Yout[int64_t(i) * s + col] : 0.0;
+    }
     __syncwarp();
     for (int k = k1 - 1; k >= k0; --k) {
       const double* uk = sU + (k - k0) * w;
@@ -151,8 +159,7 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
 #pragma unroll
       for (int p = 1; p < WM; ++p)
         if (p <= pm) zw[p] = fma(-uk[p], xk, zw[p]);
-      const int inew = k - 1 - kv;
-      const double nx = (act && inew >= 0) ? Yout[int64_t(inew) * s + col] : 0.0;
+      const double nx = sYin[(k - k0) * 33 + lane];
 #pragma unroll
       for (int p = 0; p < WM - 1; ++p) zw[p] = (p < kv) ? zw[p + 1] : zw[p];
 #pragma unroll
