@@ -63,8 +63,9 @@ struct TornSep {
 // entries for the forward substitution (L with the interchanges), kv+1 for
 // the backward one (U).  L, U and the pivots stream through shared memory in
 // chunks of 32 columns.  FP64: kl + kv FMA instructions per row, one lane per
-// right-hand side.
-template <int WM>
+// right-hand side.  KLW >= kl+1 sizes the forward window (16 or 32), WM >= kv+1
+// the backward one.
+template <int WM, int KLW>
 __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restrict__ ti,
                                                 const double* __restrict__ UC, const double* __restrict__ LM,
                                                 const int32_t* __restrict__ ipiv, const double* __restrict__ blk,
@@ -93,9 +94,9 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
   };
   double* Yout = Y + (isL ? I.yL : I.yR);  // only dereferenced when act
   // ---- forward: window rows k..k+kl
-  double yw[32];
+  double yw[KLW];
 #pragma unroll
-  for (int p = 0; p < 32; ++p) yw[p] = (p <= kl) ? rhs(p) : 0.0;
+  for (int p = 0; p < KLW; ++p) yw[p] = (p <= kl) ? rhs(p) : 0.0;
   const int nch = (m + 31) >> 5;
   for (int c = 0; c < nch; ++c) {
     const int k0 = c * 32, k1 = min(m, k0 + 32);
@@ -109,26 +110,24 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
       if (jp != 0) {
         double v = yw[0];
 #pragma unroll
-        for (int p = 1; p < 32; ++p) v = (p == jp) ? yw[p] : v;
+        for (int p = 1; p < KLW; ++p) v = (p == jp) ? yw[p] : v;
         const double y0 = yw[0];
         yw[0] = v;
 #pragma unroll
-        for (int p = 1; p < 32; ++p) yw[p] = (p == jp) ? y0 : yw[p];
+        for (int p = 1; p < KLW; ++p) yw[p] = (p == jp) ? y0 : yw[p];
       }
       const double yk = yw[0];
       if (act) Yout[int64_t(k) * s + col] = yk;
       const double* lk = sL + (k - k0) * kl;
 #pragma unroll
-      for (int p = 1; p < 32; ++p)
+      for (int p = 1; p < KLW; ++p)
         if (p <= km) yw[p] = fma(-lk[p - 1], yk, yw[p]);
       const double nx = rhs(k + 1 + kl);
 #pragma unroll
-      for (int p = 0; p < 31; ++p) yw[p] = (p < kl) ? yw[p + 1] : yw[p];
-      if (kl <= 31) {
+      for (int p = 0; p < KLW - 1; ++p) yw[p] = (p < kl) ? yw[p + 1] : yw[p];
 #pragma unroll
-        for (int p = 0; p < 32; ++p)
-          if (p == kl) yw[p] = nx;
-      }
+      for (int p = 0; p < KLW; ++p)
+        if (p == kl) yw[p] = nx;
     }
   }
   __syncwarp();

@@ -349,6 +349,9 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       for (int cc = 0; cc < ncomp; ++cc)
         if (Pc[cc] > 1) maxsT = std::max(maxsT, sc[cc]);
       S.twmT = 4 * maxsT - 1 <= 32 ? 32 : 64;
+      int maxs = 0;
+      for (int cc = 0; cc < ncomp; ++cc) maxs = std::max(maxs, std::max(kl[cc], ku[cc]));
+      S.tmaxs = maxs;
       S.tb_rows = orow;
       S.tb_blk = oblk;
       S.tb_y = oy;
@@ -764,10 +767,16 @@ static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int*
   else
     rb_lu<double, 64><<<S.nint, 32, 0, st>>>(cpI, S.TALL, S.TUC, S.TLM, S.tpiv, RB_PLAIN, S.flag, info);
   if (S.nsep > 0) {
-    if (S.twmI == 32)
-      tb_spikes<32><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
+    // forward window: kl+1 of the matrix being factorised (ku for the transpose); both <= s <= 16
+    const bool narrow = S.tmaxs <= 15;
+    if (S.twmI == 32 && narrow)
+      tb_spikes<32, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
+    else if (S.twmI == 32)
+      tb_spikes<32, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
+    else if (narrow)
+      tb_spikes<64, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
     else
-      tb_spikes<64><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
+      tb_spikes<64, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
     MG_CUDA(cudaMemsetAsync(S.TTR, 0, S.tb_trows * sizeof(double), st));
     tb_schur<<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.TY, S.TTR);
     if (S.twmT == 32)

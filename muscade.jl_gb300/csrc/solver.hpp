@@ -50,6 +50,7 @@ struct Solver {
   int tearable = 0;           // some component is long enough to be cut
   int nint = 0, nsep = 0, ntc = 0;
   int twmI = 0, twmT = 0;     // register windows of the interior and Schur-complement kernels
+  int tmaxs = 0;              // largest max(kl, ku) over all components
   TornInt* d_ti = nullptr;    // [nint] interiors (bands of Lλx)
   TornInt* d_tiT = nullptr;   // [nint] the same with kl and ku exchanged (the transpose)
   TornSep* d_ts = nullptr;    // [nsep]
