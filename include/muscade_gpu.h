@@ -203,6 +203,10 @@ int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *
  *                        factorised in parallel and separators of s = max(kl, ku)
  *                        dofs coupled through their banded Schur complement
  *                        (pivoting within each interior and within the Schur band)
+ *   MGPU_LINSOLVE_TORN32 the partitioned factorisation in FP32 inside 4 sweeps of
+ *                        FP64 iterative refinement; a component whose last
+ *                        correction is not below 1e-10 of its solution is solved
+ *                        again with the FP64 partitioned factorisation
  * F64 and BLOCK give bitwise the same Δx.  Returns MGPU_ERR_UNSUPPORTED when
  * the bands are too wide for the requested kind. */
 #define MGPU_LINSOLVE_AUTO 0
@@ -210,15 +214,16 @@ int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *
 #define MGPU_LINSOLVE_F64 2
 #define MGPU_LINSOLVE_BLOCK 3
 #define MGPU_LINSOLVE_TORN 4
+#define MGPU_LINSOLVE_TORN32 5
 int mgpu_set_linear_solver(mgpu_ctx *ctx, int32_t kind);
 
 typedef struct {
-  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64, _BLOCK or _TORN in use */
+  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64, _BLOCK, _TORN or _TORN32 in use */
   int32_t ncomp;         /* connected components of Lλx */
   int32_t max_kl;        /* widest lower / upper band after reordering */
   int32_t max_ku;
-  int32_t last_fallback; /* F32IR: components refactorised in FP64 in the last solve */
-  int32_t last_sweeps;   /* F32IR: most refinement sweeps any component needed in the last solve */
+  int32_t last_fallback; /* F32IR, TORN32: components refactorised in FP64 in the last solve */
+  int32_t last_sweeps;   /* F32IR, TORN32: refinement sweeps in the last solve */
 } mgpu_linsolve_info;
 int mgpu_linear_solver_info(mgpu_ctx *ctx, mgpu_linsolve_info *info);
 

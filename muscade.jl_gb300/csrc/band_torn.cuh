@@ -40,6 +40,7 @@ struct TornInt {
   int64_t eL, eR, fL, fR;  // offsets of E^L, E^R, F^L, F^R in the block array, -1 if absent
   int64_t yL, yR;          // offsets of Y^L, Y^R (m x s), -1 if absent
   int32_t sepL, sepR;      // global index of the left / right separator, -1 if absent
+  int32_t comp;            // connected component it belongs to
 };
 
 // per separator
@@ -54,7 +55,12 @@ struct TornSep {
   int64_t trow0;    // first row of that T component in the T vector
   int32_t first;    // 1 when this is the first separator of its component
   int32_t last;     // 1 when it is the last
+  int32_t comp;     // connected component it belongs to
 };
+
+// only[comp] == 0 skips the component (FP64 fallback after an FP32 factorisation);
+// only == nullptr runs all
+__device__ __forceinline__ bool tb_skip(const int* only, int comp) { return only && only[comp] == 0; }
 
 // ---------------------------------------------------------------- spikes
 // One warp per interior with at least one separator.  Lane r < s computes
@@ -65,38 +71,39 @@ struct TornSep {
 // chunks of 32 columns.  FP64: kl + kv FMA instructions per row, one lane per
 // right-hand side.  KLW >= kl+1 sizes the forward window (16 or 32), WM >= kv+1
 // the backward one.
-template <int WM, int KLW>
+template <typename T, int WM, int KLW>
 __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restrict__ ti,
-                                                const double* __restrict__ UC, const double* __restrict__ LM,
-                                                const int32_t* __restrict__ ipiv, const double* __restrict__ blk,
-                                                double* __restrict__ Y) {
-  __shared__ __align__(16) double sU[32 * WM];
-  __shared__ __align__(16) double sL[32 * 31];
-  __shared__ __align__(16) double sYin[32 * 33];  // backward: the chunk's incoming rows, one column per lane
+                                                const T* __restrict__ UC, const T* __restrict__ LM,
+                                                const int32_t* __restrict__ ipiv, const T* __restrict__ blk,
+                                                T* __restrict__ Y, const int* __restrict__ only) {
+  __shared__ __align__(16) T sU[32 * WM];
+  __shared__ __align__(16) T sL[32 * 31];
+  __shared__ __align__(16) T sYin[32 * 33];  // backward: the chunk's incoming rows, one column per lane
   __shared__ int sP[32];
   const int a = blockIdx.x, lane = threadIdx.x;
   if (a >= nint) return;
   const TornInt I = ti[a];
   if (I.sepL < 0 && I.sepR < 0) return;
+  if (tb_skip(only, I.comp)) return;
   const int m = I.n, kl = I.kl, kv = I.kl + I.ku, w = kv + 1, s = I.s;
-  const double* U = UC + I.rbase;
-  const double* L = LM + I.lbase;
+  const T* U = UC + I.rbase;
+  const T* L = LM + I.lbase;
   const int32_t* piv = ipiv + I.dof0;
   const bool isL = lane < s, isR = lane >= s && lane < 2 * s;
   const bool act = (isL && I.sepL >= 0) || (isR && I.sepR >= 0);
   const int col = isL ? lane : lane - s;
   // right-hand side entry of this lane's column at row i
-  auto rhs = [&](int i) -> double {
-    if (!act || i < 0 || i >= m) return 0.0;
-    if (isL) return i < s ? blk[I.eL + int64_t(i) * s + col] : 0.0;
+  auto rhs = [&](int i) -> T {
+    if (!act || i < 0 || i >= m) return T(0);
+    if (isL) return i < s ? blk[I.eL + int64_t(i) * s + col] : T(0);
     const int r = i - (m - s);
-    return r >= 0 ? blk[I.eR + int64_t(r) * s + col] : 0.0;
+    return r >= 0 ? blk[I.eR + int64_t(r) * s + col] : T(0);
   };
-  double* Yout = Y + (isL ? I.yL : I.yR);  // only dereferenced when act
+  T* Yout = Y + (isL ? I.yL : I.yR);  // only dereferenced when act
   // ---- forward: window rows k..k+kl
-  double yw[KLW];
+  T yw[KLW];
 #pragma unroll
-  for (int p = 0; p < KLW; ++p) yw[p] = (p <= kl) ? rhs(p) : 0.0;
+  for (int p = 0; p < KLW; ++p) yw[p] = (p <= kl) ? rhs(p) : T(0);
   const int nch = (m + 31) >> 5;
   for (int c = 0; c < nch; ++c) {
     const int k0 = c * 32, k1 = min(m, k0 + 32);
@@ -108,21 +115,21 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
       const int km = min(kl, m - 1 - k);
       const int jp = sP[k - k0];
       if (jp != 0) {
-        double v = yw[0];
+        T v = yw[0];
 #pragma unroll
         for (int p = 1; p < KLW; ++p) v = (p == jp) ? yw[p] : v;
-        const double y0 = yw[0];
+        const T y0 = yw[0];
         yw[0] = v;
 #pragma unroll
         for (int p = 1; p < KLW; ++p) yw[p] = (p == jp) ? y0 : yw[p];
       }
-      const double yk = yw[0];
+      const T yk = yw[0];
       if (act) Yout[int64_t(k) * s + col] = yk;
-      const double* lk = sL + (k - k0) * kl;
+      const T* lk = sL + (k - k0) * kl;
 #pragma unroll
       for (int p = 1; p < KLW; ++p)
         if (p <= km) yw[p] = fma(-lk[p - 1], yk, yw[p]);
-      const double nx = rhs(k + 1 + kl);
+      const T nx = rhs(k + 1 + kl);
 #pragma unroll
       for (int p = 0; p < KLW - 1; ++p) yw[p] = (p < kl) ? yw[p + 1] : yw[p];
 #pragma unroll
@@ -132,11 +139,11 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
   }
   __syncwarp();
   // ---- backward: window rows k-kv..k (zw[p] holds row k-p)
-  double zw[WM];
+  T zw[WM];
 #pragma unroll
   for (int p = 0; p < WM; ++p) {
     const int i = m - 1 - p;
-    zw[p] = (act && p <= kv && i >= 0) ? Yout[int64_t(i) * s + col] : 0.0;
+    zw[p] = (act && p <= kv && i >= 0) ? Yout[int64_t(i) * s + col] : T(0);
   }
   for (int c = nch - 1; c >= 0; --c) {
     const int k0 = c * 32, k1 = min(m, k0 + 32);
@@ -147,18 +154,18 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
 #pragma unroll 4
     for (int q = 0; q < 32; ++q) {
       const int i = k0 + q - 1 - kv;
-      sYin[q * 33 + lane] = (act && i >= 0 && q < k1 - k0) ? Yout[int64_t(i) * s + col] : 0.0;
+      sYin[q * 33 + lane] = (act && i >= 0 && q < k1 - k0) ? Yout[int64_t(i) * s + col] : T(0);
     }
     __syncwarp();
     for (int k = k1 - 1; k >= k0; --k) {
-      const double* uk = sU + (k - k0) * w;
-      const double xk = zw[0] * uk[0];  // 1/U(k,k)
+      const T* uk = sU + (k - k0) * w;
+      const T xk = zw[0] * uk[0];  // 1/U(k,k)
       if (act) Yout[int64_t(k) * s + col] = xk;
       const int pm = min(kv, k);
 #pragma unroll
       for (int p = 1; p < WM; ++p)
         if (p <= pm) zw[p] = fma(-uk[p], xk, zw[p]);
-      const double nx = sYin[(k - k0) * 33 + lane];
+      const T nx = sYin[(k - k0) * 33 + lane];
 #pragma unroll
       for (int p = 0; p < WM - 1; ++p) zw[p] = (p < kv) ? zw[p + 1] : zw[p];
 #pragma unroll
@@ -171,25 +178,28 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
 // ---------------------------------------------------------------- Schur complement
 // One warp per separator k: its block row of T (T_kk, T_k,k+1, T_k+1,k) into
 // the row-band storage of its T component (kl = ku = 2s-1).
-static __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restrict__ ts,
-                                               const TornInt* __restrict__ ti, const double* __restrict__ blk,
-                                               const double* __restrict__ Y, double* __restrict__ TR) {
+template <typename T>
+__global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restrict__ ts,
+                                               const TornInt* __restrict__ ti, const T* __restrict__ blk,
+                                               const T* __restrict__ Y, T* __restrict__ TR,
+                                               const int* __restrict__ only) {
   const int k = blockIdx.x, lane = threadIdx.x;
   if (k >= nsep) return;
   const TornSep S = ts[k];
+  if (tb_skip(only, S.comp)) return;
   const int s = S.s;
   const TornInt IL = ti[S.intL], IR = ti[S.intR];
   const int64_t r0 = S.trow - S.trow0;  // first row of this separator in its T component
-  auto put = [&](int64_t i, int64_t j, double v) { TR[S.tbase + i * S.tw + (j - i + S.tkl)] = v; };
+  auto put = [&](int64_t i, int64_t j, T v) { TR[S.tbase + i * S.tw + (j - i + S.tkl)] = v; };
   for (int e = lane; e < s * s; e += 32) {
     const int i = e / s, j = e % s;
     // T_kk = D - F^R_{left} Y^R_{left}[last s rows] - F^L_{right} Y^L_{right}[first s rows]
-    double v = blk[S.d + e];
-    const double* FR = blk + IL.fR;
-    const double* YR = Y + IL.yR + int64_t(IL.n - s) * s;
-    const double* FL = blk + IR.fL;
-    const double* YL = Y + IR.yL;
-    double a1 = 0.0, a2 = 0.0;
+    T v = blk[S.d + e];
+    const T* FR = blk + IL.fR;
+    const T* YR = Y + IL.yR + int64_t(IL.n - s) * s;
+    const T* FL = blk + IR.fL;
+    const T* YL = Y + IR.yL;
+    T a1 = T(0), a2 = T(0);
     for (int q = 0; q < s; ++q) {
       a1 = fma(FR[i * s + q], YR[q * s + j], a1);
       a2 = fma(FL[i * s + q], YL[q * s + j], a2);
@@ -197,10 +207,10 @@ static __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* _
     put(r0 + i, r0 + j, v - a1 - a2);
     if (!S.last) {
       // T_k,k+1 = -F^L_{right} Y^R_{right}[first s rows];  T_k+1,k = -F^R_{right} Y^L_{right}[last s rows]
-      const double* YRr = Y + IR.yR;
-      const double* FRr = blk + IR.fR;
-      const double* YLr = Y + IR.yL + int64_t(IR.n - s) * s;
-      double b1 = 0.0, b2 = 0.0;
+      const T* YRr = Y + IR.yR;
+      const T* FRr = blk + IR.fR;
+      const T* YLr = Y + IR.yL + int64_t(IR.n - s) * s;
+      T b1 = T(0), b2 = T(0);
       for (int q = 0; q < s; ++q) {
         b1 = fma(FL[i * s + q], YRr[q * s + j], b1);
         b2 = fma(FRr[i * s + q], YLr[q * s + j], b2);
@@ -214,31 +224,36 @@ static __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* _
 // ---------------------------------------------------------------- solve
 // separator right-hand sides: r = b_S - F^R_{left} ỹ_{left}[last s] - F^L_{right} ỹ_{right}[first s]
 // (b and ỹ in model order; ỹ of the interiors is already in x)
-static __global__ void tb_sep_rhs(int nsep, const TornSep* __restrict__ ts, const TornInt* __restrict__ ti,
-                           const double* __restrict__ blk, const int32_t* __restrict__ perm,
-                           const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ tr) {
+template <typename T>
+__global__ void tb_sep_rhs(int nsep, const TornSep* __restrict__ ts, const TornInt* __restrict__ ti,
+                           const T* __restrict__ blk, const int32_t* __restrict__ perm,
+                           const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ tr,
+                           const int* __restrict__ only) {
   const int k = blockIdx.x, lane = threadIdx.x;
   if (k >= nsep) return;
   const TornSep S = ts[k];
+  if (tb_skip(only, S.comp)) return;
   const int s = S.s;
   const TornInt IL = ti[S.intL], IR = ti[S.intR];
   for (int i = lane; i < s; i += 32) {
     double v = b[perm[S.dof0 + i]];
     for (int q = 0; q < s; ++q) {
-      v -= blk[IL.fR + i * s + q] * x[perm[IL.dof0 + IL.n - s + q]];
-      v -= blk[IR.fL + i * s + q] * x[perm[IR.dof0 + q]];
+      v -= double(blk[IL.fR + i * s + q]) * x[perm[IL.dof0 + IL.n - s + q]];
+      v -= double(blk[IR.fL + i * s + q]) * x[perm[IR.dof0 + q]];
     }
     tr[S.trow + i] = v;
   }
 }
 
 // x_a -= Y^L_a x_S_a + Y^R_a x_S_a+1 (interior dofs), x_S = T solution (separator dofs)
-static __global__ void tb_back(int nint, const TornInt* __restrict__ ti, const TornSep* __restrict__ ts,
-                        const double* __restrict__ Y, const int32_t* __restrict__ perm,
-                        const double* __restrict__ txs, double* __restrict__ x) {
+template <typename T>
+__global__ void tb_back(int nint, const TornInt* __restrict__ ti, const TornSep* __restrict__ ts,
+                        const T* __restrict__ Y, const int32_t* __restrict__ perm,
+                        const double* __restrict__ txs, double* __restrict__ x, const int* __restrict__ only) {
   const int a = blockIdx.x;
   if (a >= nint) return;
   const TornInt I = ti[a];
+  if (tb_skip(only, I.comp)) return;
   const int s = I.s;
   const double* xl = I.sepL >= 0 ? txs + ts[I.sepL].trow : nullptr;
   const double* xr = I.sepR >= 0 ? txs + ts[I.sepR].trow : nullptr;
@@ -246,14 +261,73 @@ static __global__ void tb_back(int nint, const TornInt* __restrict__ ti, const T
     for (int i = threadIdx.x; i < I.n; i += blockDim.x) {
       double v = x[perm[I.dof0 + i]];
       for (int q = 0; q < s; ++q) {
-        if (xl) v -= Y[I.yL + int64_t(i) * s + q] * xl[q];
-        if (xr) v -= Y[I.yR + int64_t(i) * s + q] * xr[q];
+        if (xl) v -= double(Y[I.yL + int64_t(i) * s + q]) * xl[q];
+        if (xr) v -= double(Y[I.yR + int64_t(i) * s + q]) * xr[q];
       }
       x[perm[I.dof0 + i]] = v;
     }
   if (I.sepR >= 0) {
     const TornSep S = ts[I.sepR];
     for (int i = threadIdx.x; i < s; i += blockDim.x) x[perm[S.dof0 + i]] = txs[S.trow + i];
+  }
+}
+
+// per-virtual-component flags (interiors, Schur components) from per-component ones
+static __global__ void tb_expand_flags(int n, const int32_t* __restrict__ comp_of, const int* __restrict__ cflag,
+                                int* __restrict__ vflag) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) vflag[v] = cflag[comp_of[v]];
+}
+
+// r = b - A x, FP64, one thread per row; A given by columns (CSC) with a row
+// index (rptr, rq = CSC position, rc = column) for A x, or used as is for Aᵀ x
+static __global__ void tb_residual(int64_t n, int transposed, const int64_t* __restrict__ rptr,
+                            const int64_t* __restrict__ rq, const int32_t* __restrict__ rc,
+                            const int64_t* __restrict__ colptr, const int32_t* __restrict__ rowval,
+                            const double* __restrict__ nz, const double* __restrict__ b,
+                            const double* __restrict__ x, double* __restrict__ r) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = b[i];
+  if (transposed)
+    for (int64_t q = colptr[i]; q < colptr[i + 1]; ++q) s = fma(-nz[q], x[rowval[q]], s);
+  else
+    for (int64_t q = rptr[i]; q < rptr[i + 1]; ++q) s = fma(-nz[rq[q]], x[rc[q]], s);
+  r[i] = s;
+}
+
+static __global__ void tb_axpy(int64_t n, const double* __restrict__ d, double* __restrict__ x) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += d[i];
+}
+
+// refinement check per component: flag[c] = 1 unless max|d| <= 1e-10 max|x| (NaN fails);
+// *nbad counts the flagged components
+static __global__ void __launch_bounds__(32) tb_ir_check(const int32_t* __restrict__ cn, const int32_t* __restrict__ cdof0,
+                                                  const int32_t* __restrict__ perm, const double* __restrict__ d,
+                                                  const double* __restrict__ x, int* __restrict__ flag,
+                                                  int* __restrict__ nbad) {
+  const int c = blockIdx.x, lane = threadIdx.x;
+  const int n = cn[c];
+  const int32_t* pm = perm + cdof0[c];
+  double dn = 0.0, xn = 0.0;
+  bool finite = true;
+  for (int k = lane; k < n; k += 32) {
+    const double dv = d[pm[k]], xv = x[pm[k]];
+    finite = finite && isfinite(dv) && isfinite(xv);
+    dn = fmax(dn, fabs(dv));
+    xn = fmax(xn, fabs(xv));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    dn = fmax(dn, __shfl_xor_sync(0xffffffffu, dn, o));
+    xn = fmax(xn, __shfl_xor_sync(0xffffffffu, xn, o));
+  }
+  finite = __all_sync(0xffffffffu, finite);
+  if (lane == 0) {
+    const int bad = !(finite && dn <= 1e-10 * xn);
+    flag[c] = bad;
+    if (bad) atomicAdd(nbad, 1);
   }
 }
 

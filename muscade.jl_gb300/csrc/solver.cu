@@ -258,7 +258,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       std::vector<TornInt> ti, tiT;
       std::vector<TornSep> ts;
       std::vector<int64_t> irb, ilb, trb, tlb;
-      std::vector<int32_t> in_, ikl, iku, idof, tn, tkl, tdof;
+      std::vector<int32_t> in_, ikl, iku, idof, tn, tkl, tdof, tcomp, icomp;
       int64_t orow = 0, oblk = 0, oy = 0, olm = 0, otr = 0, otl = 0, otv = 0;
       // segment of each band position: >= 0 interior index (global), < 0 -(separator index + 1)
       std::vector<int32_t> seg(n), loc(n);
@@ -284,6 +284,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
           I.eL = I.eR = I.fL = I.fR = I.yL = I.yR = -1;
           I.sepL = a > 0 ? sep0 + a - 1 : -1;
           I.sepR = a < P - 1 ? sep0 + a : -1;
+          I.comp = cc;
           if (I.sepL >= 0) {
             I.eL = oblk, oblk += int64_t(sw) * sw;
             I.fL = oblk, oblk += int64_t(sw) * sw;
@@ -301,7 +302,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
             loc[c0 + p0 + q] = int32_t(q);
           }
           irb.push_back(I.rbase), ilb.push_back(I.lbase), in_.push_back(I.n), ikl.push_back(I.kl),
-              iku.push_back(I.ku), idof.push_back(I.dof0);
+              iku.push_back(I.ku), idof.push_back(I.dof0), icomp.push_back(cc);
           ti.push_back(I);
           TornInt IT = I;
           std::swap(IT.kl, IT.ku);
@@ -317,6 +318,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
             Sp.trow = otv + int64_t(a) * sw;
             Sp.first = a == 0;
             Sp.last = a == P - 2;
+            Sp.comp = cc;
             for (int64_t q = 0; q < sw; ++q) {
               seg[c0 + p0 + q] = -(int32_t(ts.size()) + 1);
               loc[c0 + p0 + q] = int32_t(q);
@@ -336,6 +338,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
           }
           trb.push_back(otr), tlb.push_back(otl), tn.push_back(int32_t(nT)), tkl.push_back(klT),
               tdof.push_back(int32_t(otv));
+          tcomp.push_back(cc);
           otr += nT * wT;
           otl += nT * klT;
           otv += nT;
@@ -413,6 +416,37 @@ static void analyse(mgpu_ctx* c, Solver& S) {
              cudaMalloc(&S.txs, std::max<int64_t>(otv, 1) * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&S.tpiv, n * sizeof(int32_t)) == cudaSuccess &&
              cudaMalloc(&S.ttpiv, std::max<int64_t>(otv, 1) * sizeof(int32_t)) == cudaSuccess;
+      // FP32 factorisation and FP64 refinement
+      auto fal = [&](float** p, int64_t cnt) {
+        return cudaMalloc(p, std::max<int64_t>(cnt, 1) * sizeof(float)) == cudaSuccess;
+      };
+      good = good && fal(&S.TALL32, orow + oblk) &&
+             cudaMemset(S.TALL32, 0, std::max<int64_t>(orow + oblk, 1) * sizeof(float)) == cudaSuccess &&
+             fal(&S.TUC32, orow) && fal(&S.TLM32, olm) && fal(&S.TY32, oy) && fal(&S.TTR32, otr) &&
+             fal(&S.TTUC32, otr) && fal(&S.TTLM32, otl);
+      good = good && upv(&S.i_comp, icomp) && upv(&S.t_comp, tcomp) &&
+             cudaMalloc(&S.iflag, std::max(S.nint, 1) * sizeof(int)) == cudaSuccess &&
+             cudaMalloc(&S.tflag, std::max(S.ntc, 1) * sizeof(int)) == cudaSuccess &&
+             cudaMalloc(&S.nbad, sizeof(int)) == cudaSuccess && cudaMalloc(&S.info32, sizeof(int)) == cudaSuccess &&
+             cudaMalloc(&S.dtmp, n * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.rtmp, n * sizeof(double)) == cudaSuccess;
+      {
+        // rows of the pattern: CSC positions and columns, row by row
+        std::vector<int64_t> rptr(n + 1, 0), rq(P.nnz);
+        std::vector<int32_t> rcol(P.nnz);
+        for (int64_t q = 0; q < P.nnz; ++q) rptr[P.rowval[q] + 1]++;
+        for (int64_t i = 0; i < n; ++i) rptr[i + 1] += rptr[i];
+        std::vector<int64_t> fill(rptr.begin(), rptr.end() - 1);
+        for (int64_t j = 0; j < n; ++j)
+          for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+            const int64_t at = fill[P.rowval[q]]++;
+            rq[at] = q;
+            rcol[at] = int32_t(j);
+          }
+        std::vector<int32_t> rv(P.rowval.begin(), P.rowval.end());
+        good = good && up(&S.rptr, rptr) && up(&S.rq, rq) && up(&S.rcol, rcol) && up(&S.dcolptr, P.colptr) &&
+               up(&S.drowval, rv);
+      }
     }
   }
   good = good && cudaMalloc(&S.AB, std::max<int64_t>(S.band_total, 1) * sizeof(double)) == cudaSuccess;
@@ -676,7 +710,7 @@ extern "C" int mgpu_solver_create(mgpu_ctx* c) {
   S.path = S.tearable ? PATH_TORN : S.wm ? PATH_F64ROWS : PATH_BLOCK;
   if (getenv("MGPU_VERBOSE")) {
     static const char* names[] = {"row-band FP32 + FP64 refinement", "row-band FP64", "block FP64",
-                                  "partitioned FP64"};
+                                  "partitioned FP64", "partitioned FP32 + FP64 refinement"};
     fprintf(stderr, "[muscade_gpu] solver: %s, %d components, max kl %d, max ku %d, %s\n",
             S.ok ? "banded" : S.why.c_str(), S.ncomp, S.maxkl, S.maxku, names[S.path]);
   }
@@ -684,14 +718,14 @@ extern "C" int mgpu_solver_create(mgpu_ctx* c) {
 }
 
 extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
-  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_TORN)
+  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_TORN32)
     return set_err(c, MGPU_ERR_ARG, "mgpu_set_linear_solver: bad arguments");
   Solver& S = *c->solver;
-  if (kind == MGPU_LINSOLVE_TORN) {
+  if (kind == MGPU_LINSOLVE_TORN || kind == MGPU_LINSOLVE_TORN32) {
     if (!S.tearable)
       return set_err(c, MGPU_ERR_UNSUPPORTED,
                      "partitioned solve needs a component of at least 512 dofs with max(kl, ku) <= 16");
-    S.path = PATH_TORN;
+    S.path = kind == MGPU_LINSOLVE_TORN ? PATH_TORN : PATH_TORN32;
     return MGPU_OK;
   }
   if ((kind == MGPU_LINSOLVE_F32IR || kind == MGPU_LINSOLVE_F64) && !S.wm)
@@ -711,13 +745,14 @@ extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
   info->kind = S.path == PATH_F32IR    ? MGPU_LINSOLVE_F32IR
                : S.path == PATH_F64ROWS ? MGPU_LINSOLVE_F64
                : S.path == PATH_TORN    ? MGPU_LINSOLVE_TORN
+               : S.path == PATH_TORN32  ? MGPU_LINSOLVE_TORN32
                                         : MGPU_LINSOLVE_BLOCK;
   info->ncomp = S.ncomp;
   info->max_kl = S.maxkl;
   info->max_ku = S.maxku;
   info->last_fallback = 0;
   info->last_sweeps = 0;
-  if (S.path == PATH_F32IR && S.ncomp > 0 && S.flag) {
+  if ((S.path == PATH_F32IR || S.path == PATH_TORN32) && S.ncomp > 0 && S.flag) {
     std::vector<int> f(S.ncomp), w(S.ncomp);
     MG_CUDA(cudaStreamSynchronize(c->stream));
     MG_CUDA(cudaMemcpy(f.data(), S.flag, S.ncomp * sizeof(int), cudaMemcpyDeviceToHost));
@@ -726,6 +761,7 @@ extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
       info->last_fallback += f[i] != 0;
       info->last_sweeps = std::max(info->last_sweeps, w[i]);
     }
+    if (S.path == PATH_TORN32) info->last_sweeps = S.nrefine;
   }
   return MGPU_OK;
 }
@@ -738,7 +774,10 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
                 S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag, S->part, S->cod, S->frozen,
                 S->nactive, S->d_ti, S->d_tiT, S->d_ts, S->i_rbase, S->i_lbase, S->i_n, S->i_kl, S->i_ku,
                 S->i_dof0, S->t_rbase, S->t_lbase, S->t_n, S->t_kl, S->t_dof0, S->t_perm, S->tbmap, S->tbmapT,
-                S->TALL, S->TUC, S->TLM, S->TY, S->TTR, S->TTUC, S->TTLM, S->trhs, S->txs, S->tpiv, S->ttpiv};
+                S->TALL, S->TUC, S->TLM, S->TY, S->TTR, S->TTUC, S->TTLM, S->trhs, S->txs, S->tpiv, S->ttpiv,
+                S->TALL32, S->TUC32, S->TLM32, S->TY32, S->TTR32, S->TTUC32, S->TTLM32, S->i_comp, S->t_comp,
+                S->iflag, S->tflag, S->nbad, S->info32, S->dtmp, S->rtmp, S->rptr, S->rq, S->rcol, S->dcolptr,
+                S->drowval};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -750,57 +789,121 @@ unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 
 // one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device);
 // a singular factorisation writes its component+1 to *info.  Capturable.
-// Torn (partitioned) factorisation of Lλx or of its transpose and out = A⁻¹ rhs
-// (model order), FP64.  Capturable.
-static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int* info) {
+// Buffers of the partitioned factorisation in one precision.
+template <typename T>
+struct TornBufs {
+  T *rows, *uc, *lm, *y, *ttr, *ttuc, *ttlm;
+};
+static TornBufs<double> torn_bufs(Solver& S, double*) {
+  return {S.TALL, S.TUC, S.TLM, S.TY, S.TTR, S.TTUC, S.TTLM};
+}
+static TornBufs<float> torn_bufs(Solver& S, float*) {
+  return {S.TALL32, S.TUC32, S.TLM32, S.TY32, S.TTR32, S.TTUC32, S.TTLM32};
+}
+
+// Partitioned factorisation of Lλx or of its transpose, already gathered into
+// TALL (and TALL32).  cflag: only the components with cflag[c] != 0 (their
+// interiors and Schur components flagged in iflag/tflag), or all when null.
+template <typename T>
+static void torn_factor(mgpu_ctx* c, bool tr, const int* cflag, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
+  const TornBufs<T> B = torn_bufs(S, static_cast<T*>(nullptr));
   const RbComp cpI = tr ? RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_ku, S.i_kl, S.i_dof0}
                         : RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_kl, S.i_ku, S.i_dof0};
   const RbComp cpT{S.t_rbase, S.t_lbase, S.t_n, S.t_kl, S.t_kl, S.t_dof0};
   const TornInt* ti = tr ? S.d_tiT : S.d_ti;
-  rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, tr ? S.tbmapT : S.tbmap, c->nzval, S.TALL, nullptr);
-  const double* blk = S.TALL + S.tb_rows;
-  // interiors: factors, spikes; separators: Schur complement and its factors
+  const int mode = cflag ? RB_FALLBACK : RB_PLAIN;
+  const T* blk = B.rows + S.tb_rows;
   if (S.twmI == 32)
-    rb_lu<double, 32><<<S.nint, 32, 0, st>>>(cpI, S.TALL, S.TUC, S.TLM, S.tpiv, RB_PLAIN, S.flag, info);
+    rb_lu<T, 32><<<S.nint, 32, 0, st>>>(cpI, B.rows, B.uc, B.lm, S.tpiv, mode, S.iflag, info);
   else
-    rb_lu<double, 64><<<S.nint, 32, 0, st>>>(cpI, S.TALL, S.TUC, S.TLM, S.tpiv, RB_PLAIN, S.flag, info);
-  if (S.nsep > 0) {
-    // forward window: kl+1 of the matrix being factorised (ku for the transpose); both <= s <= 16
-    const bool narrow = S.tmaxs <= 15;
-    if (S.twmI == 32 && narrow)
-      tb_spikes<32, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
-    else if (S.twmI == 32)
-      tb_spikes<32, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
-    else if (narrow)
-      tb_spikes<64, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
-    else
-      tb_spikes<64, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, S.TUC, S.TLM, S.tpiv, blk, S.TY);
-    MG_CUDA(cudaMemsetAsync(S.TTR, 0, S.tb_trows * sizeof(double), st));
-    tb_schur<<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.TY, S.TTR);
-    if (S.twmT == 32)
-      rb_lu<double, 32><<<S.ntc, 32, 0, st>>>(cpT, S.TTR, S.TTUC, S.TTLM, S.ttpiv, RB_PLAIN, S.flag, info);
-    else
-      rb_lu<double, 64><<<S.ntc, 32, 0, st>>>(cpT, S.TTR, S.TTUC, S.TTLM, S.ttpiv, RB_PLAIN, S.flag, info);
-  }
-  // solve: interiors, separator right-hand sides, separators, back-substitution
+    rb_lu<T, 64><<<S.nint, 32, 0, st>>>(cpI, B.rows, B.uc, B.lm, S.tpiv, mode, S.iflag, info);
+  if (S.nsep == 0) return;
+  // forward window: kl+1 of the matrix being factorised (ku for the transpose); both <= s <= 16
+  const bool narrow = S.tmaxs <= 15;
+  if (S.twmI == 32 && narrow)
+    tb_spikes<T, 32, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, B.uc, B.lm, S.tpiv, blk, B.y, cflag);
+  else if (S.twmI == 32)
+    tb_spikes<T, 32, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, B.uc, B.lm, S.tpiv, blk, B.y, cflag);
+  else if (narrow)
+    tb_spikes<T, 64, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, B.uc, B.lm, S.tpiv, blk, B.y, cflag);
+  else
+    tb_spikes<T, 64, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, B.uc, B.lm, S.tpiv, blk, B.y, cflag);
+  cudaMemsetAsync(B.ttr, 0, S.tb_trows * sizeof(T), st);  // band positions outside the blocks stay zero
+  tb_schur<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, B.y, B.ttr, cflag);
+  if (S.twmT == 32)
+    rb_lu<T, 32><<<S.ntc, 32, 0, st>>>(cpT, B.ttr, B.ttuc, B.ttlm, S.ttpiv, mode, S.tflag, info);
+  else
+    rb_lu<T, 64><<<S.ntc, 32, 0, st>>>(cpT, B.ttr, B.ttuc, B.ttlm, S.ttpiv, mode, S.tflag, info);
+}
+
+// out = A⁻¹ rhs (model order, FP64 in and out) with the factors of torn_factor<T>
+template <typename T>
+static void torn_apply(mgpu_ctx* c, bool tr, const double* rhs, double* out, const int* cflag) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  const TornBufs<T> B = torn_bufs(S, static_cast<T*>(nullptr));
+  const RbComp cpI = tr ? RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_ku, S.i_kl, S.i_dof0}
+                        : RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_kl, S.i_ku, S.i_dof0};
+  const RbComp cpT{S.t_rbase, S.t_lbase, S.t_n, S.t_kl, S.t_kl, S.t_dof0};
+  const TornInt* ti = tr ? S.d_tiT : S.d_ti;
+  const int mode = cflag ? RB_FALLBACK : RB_PLAIN;
+  const T* blk = B.rows + S.tb_rows;
+  T* tw = sizeof(T) == 4 ? reinterpret_cast<T*>(S.tw32) : reinterpret_cast<T*>(S.tw64);
   if (S.twmI == 32)
-    rb_solve<double, 32><<<S.nint, 32, 0, st>>>(cpI, S.perm, S.TALL, S.TUC, S.TLM, S.tpiv, rhs, S.bw, S.xw, S.rw,
-                                                S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
+    rb_solve<T, 32><<<S.nint, 32, 0, st>>>(cpI, S.perm, S.TALL, B.uc, B.lm, S.tpiv, rhs, S.bw, S.xw, S.rw, tw, out, 0,
+                                           mode, S.iflag, nullptr);
   else
-    rb_solve<double, 64><<<S.nint, 32, 0, st>>>(cpI, S.perm, S.TALL, S.TUC, S.TLM, S.tpiv, rhs, S.bw, S.xw, S.rw,
-                                                S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
-  if (S.nsep > 0) {
-    tb_sep_rhs<<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.perm, rhs, out, S.trhs);
-    if (S.twmT == 32)
-      rb_solve<double, 32><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, S.TTUC, S.TTLM, S.ttpiv, S.trhs, S.bw, S.xw,
-                                                 S.rw, S.tw64, S.txs, 0, RB_PLAIN, S.flag, nullptr);
-    else
-      rb_solve<double, 64><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, S.TTUC, S.TTLM, S.ttpiv, S.trhs, S.bw, S.xw,
-                                                 S.rw, S.tw64, S.txs, 0, RB_PLAIN, S.flag, nullptr);
-    tb_back<<<S.nint, 128, 0, st>>>(S.nint, ti, S.d_ts, S.TY, S.perm, S.txs, out);
+    rb_solve<T, 64><<<S.nint, 32, 0, st>>>(cpI, S.perm, S.TALL, B.uc, B.lm, S.tpiv, rhs, S.bw, S.xw, S.rw, tw, out, 0,
+                                           mode, S.iflag, nullptr);
+  if (S.nsep == 0) return;
+  tb_sep_rhs<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.perm, rhs, out, S.trhs, cflag);
+  if (S.twmT == 32)
+    rb_solve<T, 32><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, B.ttuc, B.ttlm, S.ttpiv, S.trhs, S.bw, S.xw, S.rw,
+                                          tw, S.txs, 0, mode, S.tflag, nullptr);
+  else
+    rb_solve<T, 64><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, B.ttuc, B.ttlm, S.ttpiv, S.trhs, S.bw, S.xw, S.rw,
+                                          tw, S.txs, 0, mode, S.tflag, nullptr);
+  tb_back<T><<<S.nint, 128, 0, st>>>(S.nint, ti, S.d_ts, B.y, S.perm, S.txs, out, cflag);
+}
+
+// Partitioned solve of Lλx (or its transpose) x = rhs.  FP64 directly, or
+// (PATH_TORN32) FP32 factors inside S.nrefine sweeps of FP64 iterative
+// refinement, then the FP64 factorisation for the components whose last
+// correction is not below 1e-10 of their solution.  Capturable (no host
+// decision).
+static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int* info) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  const int64_t n = c->nX;
+  const bool mixed = S.path == PATH_TORN32;
+  rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, tr ? S.tbmapT : S.tbmap, c->nzval, S.TALL,
+                                                 mixed ? S.TALL32 : nullptr);
+  if (!mixed) {
+    torn_factor<double>(c, tr, nullptr, info);
+    torn_apply<double>(c, tr, rhs, out, nullptr);
+    MG_CUDA(cudaGetLastError());
+    return MGPU_OK;
   }
+  torn_factor<float>(c, tr, nullptr, S.info32);
+  MG_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), st));
+  const double* r = rhs;
+  for (int sweep = 0; sweep < S.nrefine; ++sweep) {
+    torn_apply<float>(c, tr, r, S.dtmp, nullptr);
+    tb_axpy<<<nb(n, 256), 256, 0, st>>>(n, S.dtmp, out);
+    if (sweep + 1 < S.nrefine) {
+      tb_residual<<<nb(n, 256), 256, 0, st>>>(n, tr ? 1 : 0, S.rptr, S.rq, S.rcol, S.dcolptr, S.drowval, c->nzval,
+                                               rhs, out, S.rtmp);
+      r = S.rtmp;
+    }
+  }
+  MG_CUDA(cudaMemsetAsync(S.nbad, 0, sizeof(int), st));
+  tb_ir_check<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dtmp, out, S.flag, S.nbad);
+  tb_expand_flags<<<nb(S.nint, 256), 256, 0, st>>>(S.nint, S.i_comp, S.flag, S.iflag);
+  if (S.ntc > 0) tb_expand_flags<<<nb(S.ntc, 256), 256, 0, st>>>(S.ntc, S.t_comp, S.flag, S.tflag);
+  torn_factor<double>(c, tr, S.flag, info);
+  torn_apply<double>(c, tr, rhs, out, S.flag);
   MG_CUDA(cudaGetLastError());
   return MGPU_OK;
 }
@@ -808,7 +911,7 @@ static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int*
 int factor_solve(mgpu_ctx* c, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
-  if (S.path == PATH_TORN) {
+  if (S.path == PATH_TORN || S.path == PATH_TORN32) {
     const int rc = torn_solve(c, false, c->Ll, S.dx, info);
     if (rc) return rc;
   } else if (S.path == PATH_BLOCK) {
@@ -854,7 +957,7 @@ int factor_solve(mgpu_ctx* c, int* info) {
 
 int factor_solve_T(mgpu_ctx* c, const double* rhs, double* out, int* info) {
   Solver& S = *c->solver;
-  if (S.path == PATH_TORN) return torn_solve(c, true, rhs, out, info);
+  if (S.path == PATH_TORN || S.path == PATH_TORN32) return torn_solve(c, true, rhs, out, info);
   if (!S.wmT)
     return set_err(c, MGPU_ERR_UNSUPPORTED,
                    "transposed solve needs the row-band kernels (kl, ku <= 31 and kl+ku+1 <= 64 in every component)");

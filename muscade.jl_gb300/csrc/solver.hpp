@@ -19,7 +19,8 @@ enum SolverPath : int {
   PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
   PATH_F64ROWS = 1,  // row-band warp kernels in FP64
   PATH_BLOCK = 2,  // gbtf2-layout block kernels in FP64 (any band width up to 256)
-  PATH_TORN = 3    // long components cut into interiors and separators, FP64
+  PATH_TORN = 3,   // long components cut into interiors and separators, FP64
+  PATH_TORN32 = 4  // the same with FP32 factors inside FP64 iterative refinement, FP64 fallback per component
 };
 
 struct Solver {
@@ -64,6 +65,19 @@ struct Solver {
   double *TALL = nullptr, *TUC = nullptr, *TLM = nullptr, *TY = nullptr;
   double *TTR = nullptr, *TTUC = nullptr, *TTLM = nullptr, *trhs = nullptr, *txs = nullptr;
   int32_t *tpiv = nullptr, *ttpiv = nullptr;
+  // FP32 copies of the partitioned factorisation (refined in FP64)
+  float *TALL32 = nullptr, *TUC32 = nullptr, *TLM32 = nullptr, *TY32 = nullptr;
+  float *TTR32 = nullptr, *TTUC32 = nullptr, *TTLM32 = nullptr;
+  int32_t *i_comp = nullptr, *t_comp = nullptr;  // component of each interior / Schur component
+  int *iflag = nullptr, *tflag = nullptr;        // fallback flags per interior / Schur component
+  int* nbad = nullptr;                           // components whose FP32 refinement fell short
+  int* info32 = nullptr;                         // zero pivots of the FP32 factorisation (caught by the check)
+  double *dtmp = nullptr, *rtmp = nullptr;       // refinement correction and residual
+  int64_t *rptr = nullptr, *rq = nullptr;        // rows of Lλx: CSC positions ...
+  int32_t* rcol = nullptr;                       // ... and columns
+  int64_t* dcolptr = nullptr;                    // the CSC pattern on the device
+  int32_t* drowval = nullptr;
+  int nrefine = 4;                               // FP64 refinement sweeps around the FP32 factors
   int* flag = nullptr;        // [ncomp] FP64 fallback requested
   int* nsweep = nullptr;      // [ncomp] refinement sweeps used
   std::string why;       // reason when not

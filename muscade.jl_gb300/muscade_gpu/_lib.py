@@ -91,7 +91,7 @@ class LinsolveInfo(ctypes.Structure):
                 ("max_ku", ctypes.c_int32), ("last_fallback", ctypes.c_int32), ("last_sweeps", ctypes.c_int32)]
 
 
-LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3, "torn": 4}
+LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3, "torn": 4, "torn32": 5}
 LINSOLVE_NAME = {v: k for k, v in LINSOLVE.items()}
 
 # every symbol the header declares (checked by the CPU test suite)

@@ -342,6 +342,31 @@ def test_partitioned_solver_matches_row_band_solver():
     assert _rel_dev(a[:, 0][:, lam], b[:, 0][:, lam]) <= TOL_STATE
 
 
+def test_partitioned_fp32_refined_matches_fp64():
+    """FP32 partitioned factors inside FP64 refinement: the FP64 trajectory to
+    the state tolerance, no fallback on the (well-conditioned) risers."""
+    m, times = W.risers(nriser=3, nel=100)
+    st = m.initialize(time=0.0)
+    a, ia = _sweep(m, st, 2, times[:10], "torn32", fixed_iter=3)
+    b, _ = _sweep(m, st, 2, times[:10], "torn", fixed_iter=3)
+    assert ia["kind"] == "torn32" and ia["last_fallback"] == 0
+    lam = np.array([str(f).startswith("λ") for f in st.dis.fieldX])
+    for d in range(3):
+        assert _rel_dev(a[:, d][:, ~lam], b[:, d][:, ~lam]) <= TOL_STATE, d
+
+
+def test_partitioned_fp32_falls_back_on_an_ill_conditioned_chain():
+    """A static 600-element cantilever is beyond FP32 refinement: its component
+    is solved again in FP64 and the result is the FP64 one."""
+    m, _ = W.cantilever(nel=600, length=300.0, load=1e-4)
+    st = m.initialize()
+    times = np.array([0.5, 1.0])
+    a, ia = _sweep(m, st, 0, times, "torn32", fixed_iter=2)
+    b, _ = _sweep(m, st, 0, times, "torn", fixed_iter=2)
+    assert ia["last_fallback"] == 1
+    assert np.array_equal(a, b)
+
+
 def test_partitioned_solver_static_cantilever_matches_oracle():
     from muscade_gpu import SweepXGPU, solve
 
@@ -359,13 +384,14 @@ def test_partitioned_transposed_solve_gives_the_adjoint():
     st = m.initialize(time=0.0)
     y = np.zeros((8, len(d["sensors"])))
     res = {}
-    for kind in ("torn", "f64"):
+    for kind in ("torn", "torn32", "f64"):
         dm = DeviceModel(m, st.dis, linsolve=kind)
         res[kind] = dm.adjoint(2, d["times"], st.time, list(st.X), d["sensors"], 1.0, y, maxdx=1e-7)
         assert dm.linear_solver_info()["kind"] == kind
         dm.close()
-    assert res["torn"][0] == pytest.approx(res["f64"][0], rel=1e-10)
-    assert _rel_dev(res["torn"][1], res["f64"][1]) <= 1e-9
+    for kind in ("torn", "torn32"):
+        assert res[kind][0] == pytest.approx(res["f64"][0], rel=1e-10)
+        assert _rel_dev(res[kind][1], res["f64"][1]) <= 1e-9
 
 
 def test_nan_is_reported_like_the_reference():
