@@ -174,7 +174,7 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="risers: launch kernel by kernel instead of replaying "
                                                               "a captured CUDA graph per step")
     ap.add_argument("--risers", type=int, default=200)
-    ap.add_argument("--linsolve", default="auto", choices=["auto", "f32ir", "f64", "block"],
+    ap.add_argument("--linsolve", default="auto", choices=["auto", "f32ir", "f64", "block", "torn", "torn32"],
                     help="device linear solver of the whole-solve modes")
     args = ap.parse_args()
     rank, local_rank, ws, dist = dist_setup()
@@ -482,7 +482,7 @@ def bench_adjoint(args, rank, local_rank, ws, dist):
     d = workloads.adjoint_beam(nel=args.adj_nel, nstep=args.adj_steps)
     m = d["model"]
     st = m.initialize(time=0.0)
-    dm = DeviceModel(m, st.dis, device=local_rank)
+    dm = DeviceModel(m, st.dis, device=local_rank, linsolve=args.linsolve)
     X0 = list(st.X)
     tol = 1e-7
     dm.set_A(d["A_true"])
