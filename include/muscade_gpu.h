@@ -190,9 +190,11 @@ int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *
  * calls UMFPACK through lu/lu!/\ at src/SweepX.jl:207-210).  Every connected
  * component of Lλx is reordered (reverse Cuthill-McKee) and factorised as a
  * band with partial pivoting:
- *   MGPU_LINSOLVE_AUTO   TORN when some component has 512 dofs or more and
- *                        max(kl, ku) <= 16, else F64 where every component
- *                        has kl <= 31 and kl+ku+1 <= 64, else BLOCK (the default)
+ *   MGPU_LINSOLVE_AUTO   TORN32 when some component has 512 dofs or more and
+ *                        max(kl, ku) <= 16 -- switching to TORN for the rest of
+ *                        the context's life after the first solve that needs the
+ *                        FP64 fallback -- else F64 where every component has
+ *                        kl <= 31 and kl+ku+1 <= 64, else BLOCK (the default)
  *   MGPU_LINSOLVE_F32IR  FP32 factors, FP64 residuals and iterative refinement
  *                        until the correction is below 1e-12 of the solution;
  *                        a component that does not contract, or would need

@@ -707,7 +707,8 @@ extern "C" int mgpu_solver_create(mgpu_ctx* c) {
   cudaGetLastError();  // analysis errors are reported at solve time
   // default: the FP64 row-band kernels where they apply, else the FP64 block
   // kernels (mgpu_set_linear_solver changes it)
-  S.path = S.tearable ? PATH_TORN : S.wm ? PATH_F64ROWS : PATH_BLOCK;
+  S.path = S.tearable ? PATH_TORN32 : S.wm ? PATH_F64ROWS : PATH_BLOCK;
+  S.adaptive = S.tearable;
   if (getenv("MGPU_VERBOSE")) {
     static const char* names[] = {"row-band FP32 + FP64 refinement", "row-band FP64", "block FP64",
                                   "partitioned FP64", "partitioned FP32 + FP64 refinement"};
@@ -726,13 +727,15 @@ extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
       return set_err(c, MGPU_ERR_UNSUPPORTED,
                      "partitioned solve needs a component of at least 512 dofs with max(kl, ku) <= 16");
     S.path = kind == MGPU_LINSOLVE_TORN ? PATH_TORN : PATH_TORN32;
+    S.adaptive = false;
     return MGPU_OK;
   }
   if ((kind == MGPU_LINSOLVE_F32IR || kind == MGPU_LINSOLVE_F64) && !S.wm)
     return set_err(c, MGPU_ERR_UNSUPPORTED,
                    "linear solver kind needs kl <= 31 and kl+ku+1 <= 64 in every component (kl=" +
                        std::to_string(S.maxkl) + ", ku=" + std::to_string(S.maxku) + ")");
-  S.path = kind == MGPU_LINSOLVE_AUTO ? (S.tearable ? PATH_TORN : S.wm ? PATH_F64ROWS : PATH_BLOCK)
+  S.adaptive = kind == MGPU_LINSOLVE_AUTO && S.tearable;
+  S.path = kind == MGPU_LINSOLVE_AUTO ? (S.tearable ? PATH_TORN32 : S.wm ? PATH_F64ROWS : PATH_BLOCK)
            : kind == MGPU_LINSOLVE_F32IR ? PATH_F32IR
            : kind == MGPU_LINSOLVE_F64   ? PATH_F64ROWS
                                          : PATH_BLOCK;
@@ -1028,7 +1031,9 @@ int newton_step(mgpu_ctx* c, int OX, int64_t step, double t, double dt, const do
     MG_CUDA(cudaMemcpyAsync(hi, S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaMemcpyAsync(hi + 1, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
     if (percomp) MG_CUDA(cudaMemcpyAsync(hi + 2, S.nactive, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (S.path == PATH_TORN32) MG_CUDA(cudaMemcpyAsync(hi + 3, S.nbad, sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaStreamSynchronize(st));
+    if (S.path == PATH_TORN32 && hi[3] > 0 && S.adaptive) S.path = PATH_TORN;  // FP32 refinement falls short here
     const double dx2 = S.hbuf[0], Ll2 = S.hbuf[1];
     stats->last_dx = std::sqrt(dx2);
     stats->last_Ll = std::sqrt(Ll2);
@@ -1166,9 +1171,12 @@ static int sweep_graph(mgpu_ctx* c, int OX, int64_t nstep, const double* times, 
     MG_G(cudaMemcpyAsync(f + 1, S.info + 1, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
   }
   MG_G(cudaMemcpyAsync(S.hbuf, S.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (S.path == PATH_TORN32)
+    MG_G(cudaMemcpyAsync(reinterpret_cast<int*>(S.hbuf + 2), S.nbad, sizeof(int), cudaMemcpyDeviceToHost, st));
   MG_G(cudaStreamSynchronize(st));
   stats->last_dx = std::sqrt(S.hbuf[0]);
   stats->last_Ll = std::sqrt(S.hbuf[1]);
+  if (S.path == PATH_TORN32 && *reinterpret_cast<int*>(S.hbuf + 2) > 0 && S.adaptive) S.path = PATH_TORN;
   for (int64_t step = 0; step < nrun; ++step) {
     const int* f = hflags + step * (nit + 1);
     // within a step the NaN check of an iteration precedes its factorisation

@@ -78,6 +78,7 @@ struct Solver {
   int64_t* dcolptr = nullptr;                    // the CSC pattern on the device
   int32_t* drowval = nullptr;
   int nrefine = 4;                               // FP64 refinement sweeps around the FP32 factors
+  bool adaptive = false;                         // AUTO: leave the FP32 path after its first fallback
   int* flag = nullptr;        // [ncomp] FP64 fallback requested
   int* nsweep = nullptr;      // [ncomp] refinement sweeps used
   std::string why;       // reason when not
