@@ -242,6 +242,14 @@ static void analyse(mgpu_ctx* c, Solver& S) {
            cudaMemset(S.nsweep, 0, ncomp * sizeof(int)) == cudaSuccess;
     // ---- torn layout of the long components (needs s = max(kl, ku) <= 16 for the
     // Schur-complement band 2s-1 <= 31)
+    // P interiors per component: about sqrt(n/s) (balances an interior's length
+    // against the Schur band's), but no more than needed to give every SM
+    // sub-partition ~4 warps: with many components (batched models) the GPU is
+    // already full and cutting only adds work
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm <= 0) nsm = 152;
+    const int64_t target_warps = int64_t(16) * nsm;
+    const int64_t pcap = std::max<int64_t>(1, (target_warps + ncomp - 1) / std::max(ncomp, 1));
     std::vector<int> Pc(ncomp, 1), sc(ncomp, 0);
     for (int cc = 0; cc < ncomp; ++cc) {
       const int64_t nc = comp_start[cc + 1] - comp_start[cc];
@@ -249,7 +257,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       sc[cc] = sw;
       if (sw > 16 || nc < kTornMinDofs) continue;
       const int64_t mmin = std::max(2 * sw, 48);
-      const int64_t pmax = (nc + sw) / (mmin + sw);
+      const int64_t pmax = std::min((nc + sw) / (mmin + sw), pcap);
       const int64_t pc = std::llround(std::sqrt(double(nc) / sw));
       Pc[cc] = int(std::max<int64_t>(1, std::min(pc, pmax)));
       if (Pc[cc] > 1) S.tearable = 1;
