@@ -435,7 +435,8 @@ def bench_batched(args, rank, local_rank, ws, dist):
     for i in pick:
         mi, _, _ = workloads.build_batched([params[i]])
         si = mi.initialize()
-        di = DeviceModel(mi, si.dis, device=local_rank)
+        # the batch's linear solver (one model alone would be partitioned, another pivoting order)
+        di = DeviceModel(mi, si.dis, device=local_rank, linsolve=info64["kind"])
         di.sweepx(0, times, si.time, list(si.X), maxdx=1e-9, maxLl=math.inf)  # warm
         t0 = time.perf_counter()
         rci, xi, _ = di.sweepx(0, times, si.time, list(si.X), maxdx=1e-9, maxLl=math.inf)

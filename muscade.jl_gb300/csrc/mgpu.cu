@@ -78,8 +78,14 @@ __device__ __forceinline__ void scale_bending(BeamConst& bc, double s) {
   bc.k2v *= s;
 }
 
+// Minimum resident blocks per SM for the Newmark form (bounds its registers);
+// the static form keeps the compiler's choice.
+#ifndef MGPU_BEAM_DYN_MINB
+#define MGPU_BEAM_DYN_MINB 1
+#endif
+
 template <bool DYN>
-__global__ void __launch_bounds__(128) beam_kernel(int64_t nele, const int32_t* __restrict__ idx,
+__global__ void __launch_bounds__(128, DYN ? MGPU_BEAM_DYN_MINB : 1) beam_kernel(int64_t nele, const int32_t* __restrict__ idx,
                                                    const int32_t* __restrict__ uidx, const double* __restrict__ cdata,
                                                    const int32_t* __restrict__ aidx, const double* __restrict__ Avec,
                                                    AsmArgs a, double* __restrict__ rout, double* __restrict__ kout,
