@@ -255,6 +255,12 @@ int mgpu_assemble_beams_noalloc(int64_t nele, int64_t nX, int64_t nnz, const dou
                                 const int64_t *asm1, const int64_t *asm2, const double *x, double *Ll,
                                 double *nzval, void *stream);
 
+/* Page-lock a caller's host buffer (cudaHostRegister) so that the copies of
+ * the calls above run at full host-device bandwidth and without staging;
+ * optional.  Unregister before freeing the buffer. */
+int mgpu_host_register(void *ptr, int64_t bytes);
+int mgpu_host_unregister(void *ptr);
+
 /* Measurement utility (no counterpart in the reference): FP64 FMA throughput
  * of `device` in TFLOP/s, from independent DFMA chains timed with CUDA events;
  * the roofline denominator of the FP64-bound element kernels. */

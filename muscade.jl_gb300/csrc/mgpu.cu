@@ -580,6 +580,16 @@ extern "C" void mgpu_destroy(mgpu_ctx* c) {
   delete c;
 }
 
+extern "C" int mgpu_host_register(void* ptr, int64_t bytes) {
+  if (!ptr || bytes <= 0) return MGPU_ERR_ARG;
+  return cudaHostRegister(ptr, size_t(bytes), cudaHostRegisterDefault) == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+}
+
+extern "C" int mgpu_host_unregister(void* ptr) {
+  if (!ptr) return MGPU_ERR_ARG;
+  return cudaHostUnregister(ptr) == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
+}
+
 extern "C" int mgpu_set_A(mgpu_ctx* c, const double* A) {
   if (!c || (c->nA > 0 && !A)) return set_err(c, MGPU_ERR_ARG, "mgpu_set_A: bad arguments");
   MG_CUDA(cudaSetDevice(c->device));

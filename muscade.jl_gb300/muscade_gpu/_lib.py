@@ -99,7 +99,7 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_ntval", "mgpu_assemble", "mgpu_element_eval", "mgpu_upload_state", "mgpu_assemble_resident",
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
-           "mgpu_adjoint_sweepx"]
+           "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister"]
 
 _lib = None
 
@@ -139,6 +139,8 @@ def load():
     L.mgpu_set_linear_solver.argtypes = [vp, i32]
     L.mgpu_linear_solver_info.argtypes = [vp, P(LinsolveInfo)]
     L.mgpu_set_A.argtypes = [vp, pd]
+    L.mgpu_host_register.argtypes = [vp, i64]
+    L.mgpu_host_unregister.argtypes = [vp]
     L.mgpu_adjoint_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32, pd,
                                       pd, pd, P(Stats)]
     for name in SYMBOLS:

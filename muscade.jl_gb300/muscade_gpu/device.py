@@ -34,6 +34,7 @@ class DeviceModel:
 
     def __init__(self, model, dis, device: int = 0, linsolve: str = "auto"):
         self.lib = L.load()
+        self._registered = []
         self.model, self.dis = model, dis
         self.nX, self.nU = model.ndof["X"], model.ndof["U"]
         self._keep = []
@@ -129,6 +130,9 @@ class DeviceModel:
             raise DeviceError(rc, msg)
 
     def close(self):
+        for buf in getattr(self, "_registered", []):
+            self.lib.mgpu_host_unregister(buf.ctypes.data_as(ctypes.c_void_p))
+        self._registered = []
         if getattr(self, "ctx", None):
             self.lib.mgpu_destroy(self.ctx)
             self.ctx = None
@@ -164,15 +168,36 @@ class DeviceModel:
         return np.ascontiguousarray(np.concatenate(out) if out else np.zeros(0))
 
     # ---------------------------------------------------------------- assembly
-    def assemble(self, X, U=None, t=0.0, mission=L.ASM_STATIC, c=None, want=(True, True)):
+    def _pinned(self, name, n):
+        """A host array kept for the life of the model and page-locked for the device copies."""
+        buf = getattr(self, name, None)
+        if buf is None or buf.size != n:
+            buf = np.zeros(max(n, 1))
+            if self.lib.mgpu_host_register(buf.ctypes.data_as(ctypes.c_void_p), buf.nbytes) == L.MGPU_OK:
+                self._registered.append(buf)
+            setattr(self, name, buf)
+        return buf[:n]
+
+    def assemble(self, X, U=None, t=0.0, mission=L.ASM_STATIC, c=None, want=(True, True), reuse=False):
+        """One assembly with host buffers (mgpu_assemble).  With reuse, the state
+        goes through and the outputs come back in page-locked arrays kept by the
+        model: the returned arrays are overwritten by the next reuse call."""
         X = [np.ascontiguousarray(x, dtype=np.float64) for x in X]
         nXder = len(X)
-        x = np.ascontiguousarray(np.concatenate(X))
+        if reuse:
+            x = self._pinned("_xin", nXder * self.nX)
+            np.concatenate(X, out=x)
+        else:
+            x = np.ascontiguousarray(np.concatenate(X))
         u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
         tv = self.tvals(t)
         nm = L.Newmark(**(c or {})) if c else L.Newmark()
-        Ll = np.zeros(self.nX) if want[0] else None
-        nz = np.zeros(self.nnz) if want[1] else None
+        if reuse:
+            Ll = self._pinned("_Lout", self.nX) if want[0] else None
+            nz = self._pinned("_nzout", self.nnz) if want[1] else None
+        else:
+            Ll = np.zeros(self.nX) if want[0] else None
+            nz = np.zeros(self.nnz) if want[1] else None
         rc = self.lib.mgpu_assemble(self.ctx, mission, nXder, L.ptr(x), L.ptr(u), float(t), L.ptr(tv),
                                     ctypes.byref(nm), L.ptr(Ll), L.ptr(nz))
         self._check(rc)

@@ -148,9 +148,11 @@ def test_assembly_parity(name, model):
     Ll, nz = dm.assemble(X, t=0.4)
     Lr, nr = REF.assemble(prep, tuple(X), U, 0.4, "static", REF.newmark_coefficients(0, 1, 0.25, 0.5))
     assert relerr(Ll, Lr) <= TOL_ASM and relerr(nz, nr) <= TOL_ASM
-    # determinism: bitwise identical on repeat
+    # determinism: bitwise identical on repeat, and through the page-locked reused buffers
     Ll2, nz2 = dm.assemble(X, t=0.4)
     assert np.array_equal(Ll, Ll2) and np.array_equal(nz, nz2)
+    Ll3, nz3 = dm.assemble(X, t=0.4, reuse=True)
+    assert np.array_equal(Ll, Ll3) and np.array_equal(nz, nz3)
     # Newmark forms
     X3 = _state(model, 8, 3)
     c = REF.newmark_coefficients(2, 0.05, 0.25, 0.5)
