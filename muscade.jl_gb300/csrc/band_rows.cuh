@@ -93,6 +93,7 @@ struct RbComp {
   const int32_t* ckl;    // [ncomp]
   const int32_t* cku;    // [ncomp]
   const int32_t* cdof0;  // [ncomp] offset in perm / piv / vectors
+  const int32_t* list = nullptr;  // components of this launch (block b does list[b]); nullptr: block b does b
 };
 
 // ---------------------------------------------------------------- factorisation
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(32) rb_lu(RbComp cp, const T* __restrict__ Aro
                                            T* __restrict__ LM, int32_t* __restrict__ ipiv, int mode,
                                            int* __restrict__ flag, int* __restrict__ info) {
   __shared__ __align__(16) T sR[2][32 * WM];
-  const int cc = blockIdx.x, lane = threadIdx.x;
+  const int cc = cp.list ? cp.list[blockIdx.x] : int(blockIdx.x), lane = threadIdx.x;
   if (mode == RB_FALLBACK && flag[cc] == 0) return;
   const int n = cp.cn[cc], kl = cp.ckl[cc], kv = kl + cp.cku[cc], w = kv + 1;
   const T* Ac = Arows + cp.rbase[cc];
@@ -340,7 +341,7 @@ __global__ void __launch_bounds__(32) rb_solve(RbComp cp, const int32_t* __restr
                                               double* __restrict__ dx, int nref, int mode, int* __restrict__ flag,
                                               int* __restrict__ nsweep) {
   __shared__ __align__(16) unsigned char smem[RbSmem<T, WM>::bytes];
-  const int cc = blockIdx.x, lane = threadIdx.x;
+  const int cc = cp.list ? cp.list[blockIdx.x] : int(blockIdx.x), lane = threadIdx.x;
   if (mode == RB_FALLBACK && flag[cc] == 0) return;
   if (mode == RB_PRIMARY && flag[cc] != 0) return;  // zero pivot in the primary factorisation
   const int n = cp.cn[cc], kl = cp.ckl[cc], kv = kl + cp.cku[cc], w = kv + 1;

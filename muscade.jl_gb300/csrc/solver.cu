@@ -201,6 +201,14 @@ static void analyse(mgpu_ctx* c, Solver& S) {
   for (int cc = 0; cc < ncomp; ++cc) maxw = std::max(maxw, kl[cc] + ku[cc] + 1);
   if (S.maxkl <= 31 && maxw <= 64) {
     S.wm = maxw <= 32 ? 32 : 64;
+    {
+      std::vector<int32_t> l32, l64;
+      for (int cc = 0; cc < ncomp; ++cc) (kl[cc] + ku[cc] + 1 <= 32 ? l32 : l64).push_back(cc);
+      S.n32 = int(l32.size());
+      S.n64 = int(l64.size());
+      if (!l32.empty()) good = good && up(&S.list32, l32);
+      if (!l64.empty()) good = good && up(&S.list64, l64);
+    }
     std::vector<int64_t> rb(ncomp + 1, 0), lb(ncomp + 1, 0);
     for (int cc = 0; cc < ncomp; ++cc) {
       const int64_t nc = comp_start[cc + 1] - comp_start[cc];
@@ -788,7 +796,7 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
                 S->TALL, S->TUC, S->TLM, S->TY, S->TTR, S->TTUC, S->TTLM, S->trhs, S->txs, S->tpiv, S->ttpiv,
                 S->TALL32, S->TUC32, S->TLM32, S->TY32, S->TTR32, S->TTUC32, S->TTLM32, S->i_comp, S->t_comp,
                 S->iflag, S->tflag, S->nbad, S->info32, S->dtmp, S->rtmp, S->rptr, S->rq, S->rcol, S->dcolptr,
-                S->drowval};
+                S->drowval, S->list32, S->list64};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -800,6 +808,27 @@ unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 
 // one Newton correction: factor Lλx, Δx = Lλx \ Lλ, norms -> S.red (device);
 // a singular factorisation writes its component+1 to *info.  Capturable.
+// Row-band factorisation and solve of all components: those whose band fits a
+// 32-wide register window (kl+ku+1 <= 32) in one launch of the 32-wide
+// kernels, the others in one of the 64-wide ones (a window wider than the band
+// costs predicated FP64 instructions in every column).
+template <typename T>
+static void rb_launch(Solver& S, RbComp cp, cudaStream_t st, const T* rows, T* uc, T* lm, const double* rhs, T* tw,
+                      double* out, int nref, int mode, int* nsweep, int* info) {
+  if (S.n32 > 0) {
+    cp.list = S.list32;
+    rb_lu<T, 32><<<S.n32, 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
+    rb_solve<T, 32><<<S.n32, 32, 0, st>>>(cp, S.perm, S.RB, uc, lm, S.ipiv, rhs, S.bw, S.xw, S.rw, tw, out, nref, mode,
+                                          S.flag, nsweep);
+  }
+  if (S.n64 > 0) {
+    cp.list = S.list64;
+    rb_lu<T, 64><<<S.n64, 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
+    rb_solve<T, 64><<<S.n64, 32, 0, st>>>(cp, S.perm, S.RB, uc, lm, S.ipiv, rhs, S.bw, S.xw, S.rw, tw, out, nref, mode,
+                                          S.flag, nsweep);
+  }
+}
+
 // Buffers of the partitioned factorisation in one precision.
 template <typename T>
 struct TornBufs {
@@ -939,26 +968,10 @@ int factor_solve(mgpu_ctx* c, int* info) {
     const int mode64 = S.path == PATH_F32IR ? RB_FALLBACK : RB_PLAIN;
     if (S.path == PATH_F32IR) {
       MG_CUDA(cudaMemsetAsync(S.flag, 0, S.ncomp * sizeof(int), st));
-      if (S.wm == 32) {
-        rb_lu<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, info);
-        rb_solve<float, 32><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC32, S.LM32, S.ipiv, c->Ll, S.bw, S.xw,
-                                                    S.rw, S.tw32, S.dx, S.nref, RB_PRIMARY, S.flag, S.nsweep);
-      } else {
-        rb_lu<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB32, S.UC32, S.LM32, S.ipiv, RB_PRIMARY, S.flag, info);
-        rb_solve<float, 64><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC32, S.LM32, S.ipiv, c->Ll, S.bw, S.xw,
-                                                    S.rw, S.tw32, S.dx, S.nref, RB_PRIMARY, S.flag, S.nsweep);
-      }
+      rb_launch<float>(S, cp, st, S.RB32, S.UC32, S.LM32, c->Ll, S.tw32, S.dx, S.nref, RB_PRIMARY, S.nsweep, info);
     }
     // FP64: the whole solve (PATH_F64ROWS) or the components flagged above
-    if (S.wm == 32) {
-      rb_lu<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, info);
-      rb_solve<double, 32><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, c->Ll, S.bw, S.xw,
-                                                   S.rw, S.tw64, S.dx, 0, mode64, S.flag, nullptr);
-    } else {
-      rb_lu<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.RB, S.UC64, S.LM64, S.ipiv, mode64, S.flag, info);
-      rb_solve<double, 64><<<S.ncomp, 32, 0, st>>>(cp, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, c->Ll, S.bw, S.xw,
-                                                   S.rw, S.tw64, S.dx, 0, mode64, S.flag, nullptr);
-    }
+    rb_launch<double>(S, cp, st, S.RB, S.UC64, S.LM64, c->Ll, S.tw64, S.dx, 0, mode64, nullptr, info);
   }
   norms_partial<<<kNormBlocks, 256, 0, st>>>(c->nX, S.dx, c->Ll, S.part);
   norms_final<<<1, 32, 0, st>>>(kNormBlocks, S.part, S.red);
@@ -975,15 +988,7 @@ int factor_solve_T(mgpu_ctx* c, const double* rhs, double* out, int* info) {
   cudaStream_t st = c->stream;
   const RbComp cpT{S.rbase, S.lbase, S.cn, S.cku, S.ckl, S.cdof0};  // the transpose: kl and ku exchange
   rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, S.rbmapT, c->nzval, S.RB, nullptr);
-  if (S.wmT == 32) {
-    rb_lu<double, 32><<<S.ncomp, 32, 0, st>>>(cpT, S.RB, S.UC64, S.LM64, S.ipiv, RB_PLAIN, S.flag, info);
-    rb_solve<double, 32><<<S.ncomp, 32, 0, st>>>(cpT, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, rhs, S.bw, S.xw, S.rw,
-                                                 S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
-  } else {
-    rb_lu<double, 64><<<S.ncomp, 32, 0, st>>>(cpT, S.RB, S.UC64, S.LM64, S.ipiv, RB_PLAIN, S.flag, info);
-    rb_solve<double, 64><<<S.ncomp, 32, 0, st>>>(cpT, S.perm, S.RB, S.UC64, S.LM64, S.ipiv, rhs, S.bw, S.xw, S.rw,
-                                                 S.tw64, out, 0, RB_PLAIN, S.flag, nullptr);
-  }
+  rb_launch<double>(S, cpT, st, S.RB, S.UC64, S.LM64, rhs, S.tw64, out, 0, RB_PLAIN, nullptr, info);
   MG_CUDA(cudaGetLastError());
   return MGPU_OK;
 }
