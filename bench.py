@@ -173,6 +173,8 @@ def main():
     ap.add_argument("--individual", type=int, default=16, help="batched: models also solved one by one")
     ap.add_argument("--no-graph", action="store_true", help="risers: launch kernel by kernel instead of replaying "
                                                               "a captured CUDA graph per step")
+    ap.add_argument("--autotune", action="store_true",
+                    help="risers/batched: pick element block size and linear solver by timing them first")
     ap.add_argument("--risers", type=int, default=200)
     ap.add_argument("--linsolve", default="auto", choices=["auto", "f32ir", "f64", "block", "torn", "torn32"],
                     help="device linear solver of the whole-solve modes")
@@ -329,6 +331,15 @@ def bench_solve(args, rank, local_rank, ws, dist):
         nbeam = model.groups[0].nele
     dm = DeviceModel(model, st.dis, device=local_rank, linsolve=args.linsolve)
     X0 = list(st.X)[: OX + 1]
+    tune = None
+    if args.autotune:
+        nX = model.ndof["X"]
+        dm.upload_state([st.X[0]] + [np.zeros(nX)] * OX, t=float(times[0]))
+        nm = None
+        if OX == 2:
+            a1, b1 = 0.5 / (0.25 * 0.05), 1 / (0.25 * 0.05**2)
+            nm = dict(a1=a1, a2=2.0, a3=0.0, b1=b1, b2=1 / (0.25 * 0.05), b3=2.0)
+        tune = dm.autotune(2 if OX == 2 else 0, nm)
     T = np.asarray(times[: nstep_w + nstep], dtype=np.float64)
     if args.config == "risers" and nstep_w:
         dm.sweepx(OX, T[:nstep_w], st.time, X0, **kw)
@@ -368,7 +379,7 @@ def bench_solve(args, rank, local_rank, ws, dist):
             "value": ms_step, "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": steps_run,
             "warmup": nstep_w, "ms_per_step": ms_step, "dtype": "f64", "data": "synthetic",
             "config": {"workload": args.config, "beams": nbeam, "dofs": model.ndof["X"], "newton_iterations": iters,
-                       "cuda_graph": bool(kw.get("graph", False)),
+                       "cuda_graph": bool(kw.get("graph", False)), "autotune": tune,
                        "linear_solver": dm.linear_solver_info()},
             "beam_assemblies_per_s": value, "e2e": {"value": ms_step, "unit": "ms", "note": "whole solve incl. copies"},
             "cpu_baseline": {"value": cpu_rate, "unit": "beam assemblies/s", "kind": "port", "sample": sample,
@@ -394,8 +405,12 @@ def bench_batched(args, rank, local_rank, ws, dist):
     # maxLλ = ∞ (the reference's default): with the finer meshes the residual
     # levels off near 1e-4 N from rounding, while Δx still reaches 1e-9
     kw = dict(maxdx=1e-9, maxLl=math.inf, per_component=True)
-    dm = DeviceModel(model, st.dis, device=local_rank)
+    dm = DeviceModel(model, st.dis, device=local_rank, linsolve=args.linsolve)
     X0 = list(st.X)
+    tune = None
+    if args.autotune:
+        dm.upload_state([st.X[0]], t=float(times[0]))
+        tune = dm.autotune(0)
     for _ in range(args.warmup):
         dm.sweepx(0, times, st.time, X0, **kw)
     if dist:
@@ -458,7 +473,7 @@ def bench_batched(args, rank, local_rank, ws, dist):
             "data": "synthetic (seeded cantilevers and portal frames, lognormal sections, Gumbel loads)",
             "config": {"workload": f"batched uneven models: {len(params)} models, {nbeam} beams, "
                                    f"{model.ndof['X']} dofs", "models": len(params), "beams": nbeam,
-                       "dofs": model.ndof["X"], "newton_iterations": iters, "linear_solver": info64,
+                       "dofs": model.ndof["X"], "newton_iterations": iters, "linear_solver": info64, "autotune": tune,
                        "l2": "inputs larger than L2 (nzval alone is several hundred MB)"},
             "beam_assemblies_per_s": ws * nbeam * iters / dt,
             "e2e": {"value": value, "unit": "models/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -229,6 +229,20 @@ typedef struct {
 } mgpu_linsolve_info;
 int mgpu_linear_solver_info(mgpu_ctx *ctx, mgpu_linsolve_info *info);
 
+/* Autotuner (no counterpart in the reference): on the resident state (after
+ * mgpu_upload_state) times one assembly of `mission` with 64, 128 and 256
+ * threads per block of the element kernels, and then the factorisation and
+ * solve of the assembled matrix with every applicable linear solver kind, and
+ * keeps the fastest of each for the following assemblies and solves.  Timings
+ * are means of 3 runs after one warm-up, CUDA events on the context stream. */
+typedef struct {
+  int32_t elem_block;     /* chosen threads per block */
+  int32_t linsolve;       /* chosen MGPU_LINSOLVE_* */
+  double ms_elem[3];      /* assembly with 64, 128, 256 threads per block */
+  double ms_linsolve[6];  /* factorisation + solve by MGPU_LINSOLVE_* index, < 0 when not applicable */
+} mgpu_tune_report;
+int mgpu_autotune(mgpu_ctx *ctx, int32_t mission, const mgpu_newmark *c, mgpu_tune_report *rep);
+
 /* Beam assembly that allocates nothing (no counterpart in the reference).
  * For callers that cannot call cudaMalloc where they assemble -- inside a
  * captured CUDA graph, in a loop whose device memory was fixed beforehand, or

@@ -59,6 +59,7 @@ struct mgpu_ctx {
   double* flush = nullptr;  // L2 flush buffer
   size_t flush_bytes = 0;
   int nXder_resident = 1;
+  int elem_block = 128;     // threads per block of the beam and bar kernels (mgpu_autotune)
   mgpu::Solver* solver = nullptr;
   // constants of the current step, read by the kernels from device memory so
   // that a captured step replays with new values: t, a1, a2, a3, b1, b2, b3

@@ -78,14 +78,10 @@ __device__ __forceinline__ void scale_bending(BeamConst& bc, double s) {
   bc.k2v *= s;
 }
 
-// Minimum resident blocks per SM for the Newmark form (bounds its registers);
-// the static form keeps the compiler's choice.
-#ifndef MGPU_BEAM_DYN_MINB
-#define MGPU_BEAM_DYN_MINB 1
-#endif
-
+// Launched with 64, 128 (default) or 256 threads per block (mgpu_autotune
+// picks); the bound of 256 leaves the register cap at 255 either way.
 template <bool DYN>
-__global__ void __launch_bounds__(128, DYN ? MGPU_BEAM_DYN_MINB : 1) beam_kernel(int64_t nele, const int32_t* __restrict__ idx,
+__global__ void __launch_bounds__(256) beam_kernel(int64_t nele, const int32_t* __restrict__ idx,
                                                    const int32_t* __restrict__ uidx, const double* __restrict__ cdata,
                                                    const int32_t* __restrict__ aidx, const double* __restrict__ Avec,
                                                    AsmArgs a, double* __restrict__ rout, double* __restrict__ kout,
@@ -317,14 +313,14 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0)
     switch (G.kind) {
       case MGPU_EULERBEAM3D:
         if (dyn)
-          beam_kernel<true><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, G.aidx,
+          beam_kernel<true><<<nblk(G.nele, c->elem_block), c->elem_block, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, G.aidx,
                                                                       c->Avec, ag, rout, kout, gid0);
         else
-          beam_kernel<false><<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, G.aidx,
+          beam_kernel<false><<<nblk(G.nele, c->elem_block), c->elem_block, 0, c->stream>>>(G.nele, G.idx, G.uidx, G.cdata, G.aidx,
                                                                        c->Avec, ag, rout, kout, gid0);
         break;
       case MGPU_BAR3D:
-        bar_kernel<<<nblk(G.nele, 128), 128, 0, c->stream>>>(G.nele, dyn ? 3 : 1, G.idx, G.uidx, G.cdata, ag, rout,
+        bar_kernel<<<nblk(G.nele, c->elem_block), c->elem_block, 0, c->stream>>>(G.nele, dyn ? 3 : 1, G.idx, G.uidx, G.cdata, ag, rout,
                                                              kout, gid0);
         break;
       case MGPU_DOFCONSTRAINT_X:

@@ -785,6 +785,86 @@ extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
   return MGPU_OK;
 }
 
+extern "C" int mgpu_autotune(mgpu_ctx* c, int32_t mission, const mgpu_newmark* nm, mgpu_tune_report* rep) {
+  if (!c || !c->solver || !rep || mission < 0 || mission > 2 || (mission != MGPU_ASM_STATIC && !nm))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_autotune: bad arguments");
+  Solver& S = *c->solver;
+  MG_CUDA(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  cudaEvent_t e0, e1;
+  MG_CUDA(cudaEventCreate(&e0));
+  MG_CUDA(cudaEventCreate(&e1));
+  int rc = upload_stepc(c, 0.0, mission != MGPU_ASM_STATIC ? nm : nullptr);
+  auto time3 = [&](auto&& f) -> double {  // mean of 3 after one warm-up, -1 on failure
+    if (f() != MGPU_OK) return -1.0;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 3; ++r)
+      if (f() != MGPU_OK) return -1.0;
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / 3.0;
+  };
+  // element kernels
+  const int blocks[3] = {64, 128, 256};
+  int best_b = c->elem_block;
+  double best_t = 1e300;
+  for (int k = 0; k < 3 && rc == MGPU_OK; ++k) {
+    c->elem_block = blocks[k];
+    launch_reset_errflag(c);
+    const double t = time3([&] { return launch_assembly(c, mission, nullptr); });
+    rep->ms_elem[k] = t;
+    if (t >= 0 && t < best_t) best_t = t, best_b = blocks[k];
+  }
+  c->elem_block = best_b;
+  rep->elem_block = best_b;
+  // linear solvers on the assembled matrix
+  for (double& t : rep->ms_linsolve) t = -1.0;
+  if (rc == MGPU_OK) rc = launch_assembly(c, mission, nullptr);
+  const int saved_path = S.path;
+  const bool saved_adaptive = S.adaptive;
+  int best_k = -1;
+  best_t = 1e300;
+  if (rc == MGPU_OK && S.ok) {
+    for (int kind = MGPU_LINSOLVE_F32IR; kind <= MGPU_LINSOLVE_TORN32; ++kind) {
+      const bool applicable = (kind == MGPU_LINSOLVE_F32IR || kind == MGPU_LINSOLVE_F64) ? S.wm != 0
+                              : (kind == MGPU_LINSOLVE_TORN || kind == MGPU_LINSOLVE_TORN32) ? S.tearable != 0
+                                                                                             : true;
+      if (!applicable) continue;
+      S.path = kind == MGPU_LINSOLVE_F32IR ? PATH_F32IR
+               : kind == MGPU_LINSOLVE_F64 ? PATH_F64ROWS
+               : kind == MGPU_LINSOLVE_BLOCK ? PATH_BLOCK
+               : kind == MGPU_LINSOLVE_TORN ? PATH_TORN
+                                            : PATH_TORN32;
+      S.adaptive = false;
+      MG_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
+      const double t = time3([&] { return factor_solve(c, S.info); });
+      int hinfo = 0;
+      MG_CUDA(cudaMemcpy(&hinfo, S.info, sizeof(int), cudaMemcpyDeviceToHost));
+      rep->ms_linsolve[kind] = hinfo == 0 ? t : -1.0;
+      if (hinfo == 0 && t >= 0 && t < best_t) best_t = t, best_k = kind;
+    }
+  }
+  if (best_k < 0) {
+    S.path = saved_path;
+    S.adaptive = saved_adaptive;
+  } else {
+    S.path = best_k == MGPU_LINSOLVE_F32IR ? PATH_F32IR
+             : best_k == MGPU_LINSOLVE_F64 ? PATH_F64ROWS
+             : best_k == MGPU_LINSOLVE_BLOCK ? PATH_BLOCK
+             : best_k == MGPU_LINSOLVE_TORN ? PATH_TORN
+                                            : PATH_TORN32;
+    S.adaptive = best_k == MGPU_LINSOLVE_TORN32;  // still leaves FP32 after a fallback
+  }
+  rep->linsolve = best_k < 0 ? MGPU_LINSOLVE_AUTO : best_k;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  launch_reset_errflag(c);
+  MG_CUDA(cudaStreamSynchronize(st));
+  return rc;
+}
+
 extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
   Solver* S = c->solver;
   if (!S) return;

@@ -91,6 +91,11 @@ class LinsolveInfo(ctypes.Structure):
                 ("max_ku", ctypes.c_int32), ("last_fallback", ctypes.c_int32), ("last_sweeps", ctypes.c_int32)]
 
 
+class TuneReport(ctypes.Structure):
+    _fields_ = [("elem_block", ctypes.c_int32), ("linsolve", ctypes.c_int32), ("ms_elem", ctypes.c_double * 3),
+                ("ms_linsolve", ctypes.c_double * 6)]
+
+
 LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3, "torn": 4, "torn32": 5}
 LINSOLVE_NAME = {v: k for k, v in LINSOLVE.items()}
 
@@ -99,7 +104,7 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_ntval", "mgpu_assemble", "mgpu_element_eval", "mgpu_upload_state", "mgpu_assemble_resident",
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
-           "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister"]
+           "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune"]
 
 _lib = None
 
@@ -140,6 +145,7 @@ def load():
     L.mgpu_linear_solver_info.argtypes = [vp, P(LinsolveInfo)]
     L.mgpu_set_A.argtypes = [vp, pd]
     L.mgpu_host_register.argtypes = [vp, i64]
+    L.mgpu_autotune.argtypes = [vp, i32, P(Newmark), P(TuneReport)]
     L.mgpu_host_unregister.argtypes = [vp]
     L.mgpu_adjoint_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32, pd,
                                       pd, pd, P(Stats)]

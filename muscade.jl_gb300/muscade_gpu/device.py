@@ -113,6 +113,16 @@ class DeviceModel:
         self._check(rc)
         return cost.value, dA[: self.nA], dtv, stats
 
+    def autotune(self, mission=L.ASM_STATIC, c=None):
+        """Time the element kernels' block sizes and the applicable linear solvers on
+        the resident state (see upload_state) and keep the fastest (mgpu_autotune)."""
+        nm = L.Newmark(**(c or {})) if c else L.Newmark()
+        rep = L.TuneReport()
+        self._check(self.lib.mgpu_autotune(self.ctx, mission, ctypes.byref(nm), ctypes.byref(rep)))
+        return {"elem_block": rep.elem_block, "linsolve": L.LINSOLVE_NAME[rep.linsolve],
+                "ms_elem": dict(zip((64, 128, 256), list(rep.ms_elem))),
+                "ms_linsolve": {L.LINSOLVE_NAME[k]: rep.ms_linsolve[k] for k in range(1, 6) if rep.ms_linsolve[k] >= 0}}
+
     def set_linear_solver(self, kind: str):
         """'auto' | 'f32ir' (FP32 factors + FP64 refinement) | 'f64' | 'block'."""
         self._check(self.lib.mgpu_set_linear_solver(self.ctx, L.LINSOLVE[kind]))

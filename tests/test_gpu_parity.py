@@ -396,6 +396,25 @@ def test_partitioned_transposed_solve_gives_the_adjoint():
         assert _rel_dev(res[kind][1], res["f64"][1]) <= 1e-9
 
 
+def test_autotune_keeps_a_faster_configuration_with_the_same_results():
+    m, times = W.risers(nriser=3, nel=100)
+    st = m.initialize(time=0.0)
+    ref, _ = _sweep(m, st, 2, times[:6], "auto", fixed_iter=3)
+    dm = DeviceModel(m, st.dis)
+    dm.upload_state([st.X[0], np.zeros(m.ndof["X"]), np.zeros(m.ndof["X"])], t=times[0])
+    c = REF.newmark_coefficients(2, 0.05, 0.25, 0.5)
+    rep = dm.autotune(_lib.ASM_ITER, {k: c[k] for k in ("a1", "a2", "a3", "b1", "b2", "b3")})
+    assert rep["elem_block"] in (64, 128, 256) and set(rep["ms_elem"]) == {64, 128, 256}
+    assert rep["linsolve"] in rep["ms_linsolve"] and {"f64", "torn", "torn32", "block"} <= set(rep["ms_linsolve"])
+    assert rep["ms_linsolve"][rep["linsolve"]] == min(rep["ms_linsolve"].values())
+    rc, a, _ = dm.sweepx(2, times[:6], st.time, list(st.X), fixed_iter=3)
+    dm.close()
+    assert rc == 0
+    lam = np.array([str(f).startswith("λ") for f in st.dis.fieldX])
+    for d in range(3):
+        assert _rel_dev(a[:, d][:, ~lam], ref[:, d][:, ~lam]) <= TOL_STATE, d
+
+
 def test_nan_is_reported_like_the_reference():
     m, _ = W.cantilever()
     st = m.initialize()
