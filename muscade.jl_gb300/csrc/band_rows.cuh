@@ -162,11 +162,10 @@ __global__ void __launch_bounds__(32) rb_lu(RbComp cp, const T* __restrict__ Aro
     for (int s = 0; s < NS; ++s) cap[s] = T(0);
 #pragma unroll
     for (int j = 1; j < WM; ++j) {
-      if (j <= kv) {
-        const T u = __shfl_sync(RB_FULL, a[j], pl);
-        if ((j & 31) == lane) cap[j >> 5] = u;
-        a[j] = fma(-le, u, a[j]);
-      }
+      if (j > kv) break;  // uniform: jump past the columns beyond the band instead of predicating them
+      const T u = __shfl_sync(RB_FULL, a[j], pl);
+      if ((j & 31) == lane) cap[j >> 5] = u;
+      a[j] = fma(-le, u, a[j]);
     }
 #pragma unroll
     for (int s = 0; s < NS; ++s) {

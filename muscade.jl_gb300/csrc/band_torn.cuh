@@ -127,8 +127,10 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
       if (act) Yout[int64_t(k) * s + col] = yk;
       const T* lk = sL + (k - k0) * kl;
 #pragma unroll
-      for (int p = 1; p < KLW; ++p)
-        if (p <= km) yw[p] = fma(-lk[p - 1], yk, yw[p]);
+      for (int p = 1; p < KLW; ++p) {
+        if (p > km) break;  // uniform
+        yw[p] = fma(-lk[p - 1], yk, yw[p]);
+      }
       const T nx = rhs(k + 1 + kl);
 #pragma unroll
       for (int p = 0; p < KLW - 1; ++p) yw[p] = (p < kl) ? yw[p + 1] : yw[p];
@@ -163,8 +165,10 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
       if (act) Yout[int64_t(k) * s + col] = xk;
       const int pm = min(kv, k);
 #pragma unroll
-      for (int p = 1; p < WM; ++p)
-        if (p <= pm) zw[p] = fma(-uk[p], xk, zw[p]);
+      for (int p = 1; p < WM; ++p) {
+        if (p > pm) break;  // uniform
+        zw[p] = fma(-uk[p], xk, zw[p]);
+      }
       const T nx = sYin[(k - k0) * 33 + lane];
 #pragma unroll
       for (int p = 0; p < WM - 1; ++p) zw[p] = (p < kv) ? zw[p + 1] : zw[p];
