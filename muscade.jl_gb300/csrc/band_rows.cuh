@@ -150,13 +150,19 @@ __global__ void __launch_bounds__(32) rb_lu(RbComp cp, const T* __restrict__ Aro
       pos = jp;
     const bool zero = (pv == T(0));
     singular = singular || zero;
-    const T rp = zero ? T(0) : T(1) / pv;
+    T rp = T(0);  // correctly rounded 1/pv (the value of T(1)/pv, without the general division)
+    if (!zero) {
+      if constexpr (sizeof(T) == 8)
+        rp = __drcp_rn(pv);
+      else
+        rp = __frcp_rn(pv);
+    }
     const bool act = !zero && pos >= 1 && pos <= km;
     const T l = act ? a[0] * rp : a[0];
     if (pos >= 1 && pos <= km) L[int64_t(k) * kl + pos - 1] = l;
     const T le = act ? l : T(0);  // rows outside the update subtract 0*u: no branch per column entry
     // U row k (the pivot row) goes out by columns; rank-1 update of the other rows
-    constexpr int NS = WM / 32;
+    constexpr int NS = (WM + 31) / 32;
     T cap[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) cap[s] = T(0);

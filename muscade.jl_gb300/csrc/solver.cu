@@ -202,12 +202,20 @@ static void analyse(mgpu_ctx* c, Solver& S) {
   if (S.maxkl <= 31 && maxw <= 64) {
     S.wm = maxw <= 32 ? 32 : 64;
     {
-      std::vector<int32_t> l32, l64;
-      for (int cc = 0; cc < ncomp; ++cc) (kl[cc] + ku[cc] + 1 <= 32 ? l32 : l64).push_back(cc);
+      std::vector<int32_t> l32, l64, lu[4];
+      for (int cc = 0; cc < ncomp; ++cc) {
+        const int w = kl[cc] + ku[cc] + 1;
+        (w <= 32 ? l32 : l64).push_back(cc);
+        lu[w <= 32 ? 0 : w <= 40 ? 1 : w <= 48 ? 2 : 3].push_back(cc);
+      }
       S.n32 = int(l32.size());
       S.n64 = int(l64.size());
       if (!l32.empty()) good = good && up(&S.list32, l32);
       if (!l64.empty()) good = good && up(&S.list64, l64);
+      for (int q = 0; q < 4; ++q) {
+        S.nlu[q] = int(lu[q].size());
+        if (!lu[q].empty()) good = good && up(&S.lulist[q], lu[q]);
+      }
     }
     std::vector<int64_t> rb(ncomp + 1, 0), lb(ncomp + 1, 0);
     for (int cc = 0; cc < ncomp; ++cc) {
@@ -876,7 +884,7 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
                 S->TALL, S->TUC, S->TLM, S->TY, S->TTR, S->TTUC, S->TTLM, S->trhs, S->txs, S->tpiv, S->ttpiv,
                 S->TALL32, S->TUC32, S->TLM32, S->TY32, S->TTR32, S->TTUC32, S->TTLM32, S->i_comp, S->t_comp,
                 S->iflag, S->tflag, S->nbad, S->info32, S->dtmp, S->rtmp, S->rptr, S->rq, S->rcol, S->dcolptr,
-                S->drowval, S->list32, S->list64};
+                S->drowval, S->list32, S->list64, S->lulist[0], S->lulist[1], S->lulist[2], S->lulist[3]};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -895,15 +903,31 @@ unsigned nb(int64_t n, int b) { return unsigned((n + b - 1) / b); }
 template <typename T>
 static void rb_launch(Solver& S, RbComp cp, cudaStream_t st, const T* rows, T* uc, T* lm, const double* rhs, T* tw,
                       double* out, int nref, int mode, int* nsweep, int* info) {
+  // factorisation: windows of 32, 40, 48 or 64 (registers, and so resident warps, follow the window)
+  if (S.nlu[0] > 0) {
+    cp.list = S.lulist[0];
+    rb_lu<T, 32><<<S.nlu[0], 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
+  }
+  if (S.nlu[1] > 0) {
+    cp.list = S.lulist[1];
+    rb_lu<T, 40><<<S.nlu[1], 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
+  }
+  if (S.nlu[2] > 0) {
+    cp.list = S.lulist[2];
+    rb_lu<T, 48><<<S.nlu[2], 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
+  }
+  if (S.nlu[3] > 0) {
+    cp.list = S.lulist[3];
+    rb_lu<T, 64><<<S.nlu[3], 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
+  }
+  // substitution: circular windows of 32 or 64 (a power of two)
   if (S.n32 > 0) {
     cp.list = S.list32;
-    rb_lu<T, 32><<<S.n32, 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
     rb_solve<T, 32><<<S.n32, 32, 0, st>>>(cp, S.perm, S.RB, uc, lm, S.ipiv, rhs, S.bw, S.xw, S.rw, tw, out, nref, mode,
                                           S.flag, nsweep);
   }
   if (S.n64 > 0) {
     cp.list = S.list64;
-    rb_lu<T, 64><<<S.n64, 32, 0, st>>>(cp, rows, uc, lm, S.ipiv, mode, S.flag, info);
     rb_solve<T, 64><<<S.n64, 32, 0, st>>>(cp, S.perm, S.RB, uc, lm, S.ipiv, rhs, S.bw, S.xw, S.rw, tw, out, nref, mode,
                                           S.flag, nsweep);
   }

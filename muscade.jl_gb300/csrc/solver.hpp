@@ -27,8 +27,10 @@ struct Solver {
   bool ok = false;       // banded scheme applicable
   int path = PATH_BLOCK;
   int wm = 0;            // row-band register window (32 or 64), 0 if the row-band kernels do not apply
-  int n32 = 0, n64 = 0;  // components whose band fits a 32- / needs a 64-wide window
+  int n32 = 0, n64 = 0;  // components whose band fits a 32- / needs a 64-wide window (substitution)
   int32_t *list32 = nullptr, *list64 = nullptr;
+  int nlu[4] = {0, 0, 0, 0};  // components by factorisation window: 32, 40, 48, 64
+  int32_t* lulist[4] = {nullptr, nullptr, nullptr, nullptr};
   int nref = 8;          // refinement sweeps allowed on the FP32 path
   // row-band layout
   int64_t* rbase = nullptr;   // [ncomp] offset in RB / UC*
