@@ -227,7 +227,9 @@ def main():
     _lib.build()
     device = local_rank
     fp64_peak = fp64_peak_tflops(device) if rank == 0 else None
+    t_create = time.perf_counter()
     dm = DeviceModel(model, st.dis, device=device)
+    t_create = time.perf_counter() - t_create
     dm.upload_state(X, t=t)
     # warm-up
     dm.time_assemble(reps=max(args.warmup, 1), t=t, flush_l2=True)
@@ -303,6 +305,7 @@ def main():
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{min(args.cpu_sample, nbeam)} beams (oracle nested-dual R and K + residual scatter)"},
         "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
+        "create_s": t_create,
     }
     print(json.dumps(line), flush=True)
     dm.close()
@@ -405,7 +408,9 @@ def bench_batched(args, rank, local_rank, ws, dist):
     # maxLλ = ∞ (the reference's default): with the finer meshes the residual
     # levels off near 1e-4 N from rounding, while Δx still reaches 1e-9
     kw = dict(maxdx=1e-9, maxLl=math.inf, per_component=True)
+    t_create = time.perf_counter()
     dm = DeviceModel(model, st.dis, device=local_rank, linsolve=args.linsolve)
+    t_create = time.perf_counter() - t_create
     X0 = list(st.X)
     tune = None
     if args.autotune:
@@ -483,7 +488,7 @@ def bench_batched(args, rank, local_rank, ws, dist):
             "fp32_refined": {"models_per_s": len(params) / dt32 if rc32 == 0 else None, "rc": rc32,
                              "max_rel_state_dev_vs_fp64": worst, "linear_solver": info32,
                              "newton_iterations": stats32.niter_total},
-            "gpu_launches": args.steps * iters * launches_per_iter, "clocks": clocks}
+            "gpu_launches": args.steps * iters * launches_per_iter, "clocks": clocks, "create_s": t_create}
     print(json.dumps(line), flush=True)
 
 

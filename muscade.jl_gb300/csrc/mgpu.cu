@@ -15,8 +15,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -441,8 +444,10 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
     shapes.push_back(GroupShape{G.nele, G.nX, G.indexX});
     if (G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) ntv += G.nele;
   }
+  const auto t_pat0 = std::chrono::steady_clock::now();
   std::string perr = build_pattern(d->nX, shapes, c->pat);
   if (!perr.empty()) return set_err(c, MGPU_ERR_ARG, perr);
+  const auto t_pat1 = std::chrono::steady_clock::now();
   c->ntval = ntv;
   // ---- per-group device data
   int64_t tvb = 0;
@@ -550,7 +555,14 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
     }
   }
   MG_TRY(reset_errflag(c));
+  const auto t_sol0 = std::chrono::steady_clock::now();
   MG_TRY(mgpu_solver_create(c));
+  if (getenv("MGPU_VERBOSE")) {
+    const auto t_sol1 = std::chrono::steady_clock::now();
+    auto sec = [](auto a, auto b) { return std::chrono::duration<double>(b - a).count(); };
+    fprintf(stderr, "[muscade_gpu] create: pattern %.3f s (nnz %lld), solver analysis %.3f s\n", sec(t_pat0, t_pat1),
+            (long long)c->pat.nnz, sec(t_sol0, t_sol1));
+  }
   MG_CUDA(cudaStreamSynchronize(c->stream));
   return MGPU_OK;
 }
