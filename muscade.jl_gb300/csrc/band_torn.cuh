@@ -15,10 +15,11 @@
 // s columns, F^R_a = A[S_{a+1}, I_a] in the last s columns).  A solve is
 //     ỹ_a = A_a^-1 b_a,   r_k = b_S_k - F^R_{k-1} ỹ_{k-1} - F^L_k ỹ_k,
 //     x_S = T^-1 r,       x_a = ỹ_a - Y^L_a x_S_a - Y^R_a x_S_{a+1}.
-// The interiors and T are factorised by the row-band kernels (band_rows.cuh)
-// with partial pivoting inside each block; the P interiors of every component
-// run in parallel, which is the point: a chain of 30,000 dofs becomes ~50
-// independent chains and one band of ~50 s.
+// The interiors are factorised by the row-band kernels (band_rows.cuh), all P
+// of every component in parallel, and T by block cyclic reduction
+// (band_bcr.cuh), log2(P) parallel levels; pivoting is partial within each
+// interior and within each s x s block.  A chain of 30,000 dofs becomes
+// hundreds of short independent chains and nine reduction levels.
 //
 // The blocks E, F, D are stored dense, s x s, row-major, each at its own
 // offset (-1 when absent); Y^L_a, Y^R_a as m_a x s row-major.
@@ -27,6 +28,7 @@
 
 #include <cstdint>
 
+#include "band_bcr.cuh"
 #include "band_rows.cuh"
 
 namespace mgpu {
@@ -49,10 +51,7 @@ struct TornSep {
   int32_t dof0;     // offset of its dofs in perm
   int64_t d;        // offset of D in the block array
   int32_t intL, intR;  // interiors on its left / right
-  int64_t trow;     // first row of this separator in the T vector
-  int64_t tbase;    // row-band storage offset of the T component holding it
-  int32_t tkl, tw;  // bands of that T component: kl = ku = 2s-1, w = 4s-1
-  int64_t trow0;    // first row of that T component in the T vector
+  int64_t trow;     // first row of this separator in the separator vector
   int32_t first;    // 1 when this is the first separator of its component
   int32_t last;     // 1 when it is the last
   int32_t comp;     // connected component it belongs to
@@ -180,12 +179,13 @@ __global__ void __launch_bounds__(32) tb_spikes(int nint, const TornInt* __restr
 }
 
 // ---------------------------------------------------------------- Schur complement
-// One warp per separator k: its block row of T (T_kk, T_k,k+1, T_k+1,k) into
-// the row-band storage of its T component (kl = ku = 2s-1).
+// One warp per separator k: its blocks of T (D_k = T_kk, U_k = T_k,k+1 and
+// L_k+1 = T_k+1,k) into level 0 of the block cyclic reduction storage
+// (band_bcr.cuh: [level][separator][D, L, U][16 x 16]).
 template <typename T>
 __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restrict__ ts,
                                                const TornInt* __restrict__ ti, const T* __restrict__ blk,
-                                               const T* __restrict__ Y, T* __restrict__ TR,
+                                               const T* __restrict__ Y, T* __restrict__ DLU,
                                                const int* __restrict__ only) {
   const int k = blockIdx.x, lane = threadIdx.x;
   if (k >= nsep) return;
@@ -193,12 +193,12 @@ __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restri
   if (tb_skip(only, S.comp)) return;
   const int s = S.s;
   const TornInt IL = ti[S.intL], IR = ti[S.intR];
-  const int64_t r0 = S.trow - S.trow0;  // first row of this separator in its T component
-  auto put = [&](int64_t i, int64_t j, T v) { TR[S.tbase + i * S.tw + (j - i + S.tkl)] = v; };
+  T* Dk = DLU + 3 * int64_t(k) * BCR_SS;
+  T* Uk = Dk + 2 * BCR_SS;
+  T* Lk1 = DLU + (3 * int64_t(k + 1) + 1) * BCR_SS;  // L of the next separator (only when !S.last)
   for (int e = lane; e < s * s; e += 32) {
     const int i = e / s, j = e % s;
     // T_kk = D - F^R_{left} Y^R_{left}[last s rows] - F^L_{right} Y^L_{right}[first s rows]
-    T v = blk[S.d + e];
     const T* FR = blk + IL.fR;
     const T* YR = Y + IL.yR + int64_t(IL.n - s) * s;
     const T* FL = blk + IR.fL;
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restri
       a1 = fma(FR[i * s + q], YR[q * s + j], a1);
       a2 = fma(FL[i * s + q], YL[q * s + j], a2);
     }
-    put(r0 + i, r0 + j, v - a1 - a2);
+    Dk[i * BCR_S + j] = blk[S.d + e] - a1 - a2;
     if (!S.last) {
       // T_k,k+1 = -F^L_{right} Y^R_{right}[first s rows];  T_k+1,k = -F^R_{right} Y^L_{right}[last s rows]
       const T* YRr = Y + IR.yR;
@@ -219,8 +219,8 @@ __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restri
         b1 = fma(FL[i * s + q], YRr[q * s + j], b1);
         b2 = fma(FRr[i * s + q], YLr[q * s + j], b2);
       }
-      put(r0 + i, r0 + s + j, -b1);
-      put(r0 + s + i, r0 + j, -b2);
+      Uk[i * BCR_S + j] = -b1;
+      Lk1[i * BCR_S + j] = -b2;
     }
   }
 }

@@ -258,10 +258,11 @@ static void analyse(mgpu_ctx* c, Solver& S) {
            cudaMemset(S.nsweep, 0, ncomp * sizeof(int)) == cudaSuccess;
     // ---- torn layout of the long components (needs s = max(kl, ku) <= 16 for the
     // Schur-complement band 2s-1 <= 31)
-    // P interiors per component: about sqrt(n/s) (balances an interior's length
-    // against the Schur band's), but no more than needed to give every SM
-    // sub-partition ~4 warps: with many components (batched models) the GPU is
-    // already full and cutting only adds work
+    // P interiors per component: as many as keep interiors of at least
+    // max(2s, 48) dofs (the separators cost log2(P) cyclic-reduction levels),
+    // but no more than needed to give every SM sub-partition ~4 warps: with
+    // many components (batched models) the GPU is already full and cutting only
+    // adds work
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nsm <= 0) nsm = 152;
     const int64_t target_warps = int64_t(16) * nsm;
@@ -274,16 +275,16 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       if (sw > 16 || nc < kTornMinDofs) continue;
       const int64_t mmin = std::max(2 * sw, 48);
       const int64_t pmax = std::min((nc + sw) / (mmin + sw), pcap);
-      const int64_t pc = std::llround(std::sqrt(double(nc) / sw));
-      Pc[cc] = int(std::max<int64_t>(1, std::min(pc, pmax)));
+      Pc[cc] = int(std::max<int64_t>(1, pmax));
       if (Pc[cc] > 1) S.tearable = 1;
     }
     if (S.tearable) {
       std::vector<TornInt> ti, tiT;
       std::vector<TornSep> ts;
-      std::vector<int64_t> irb, ilb, trb, tlb;
-      std::vector<int32_t> in_, ikl, iku, idof, tn, tkl, tdof, tcomp, icomp;
-      int64_t orow = 0, oblk = 0, oy = 0, olm = 0, otr = 0, otl = 0, otv = 0;
+      std::vector<int64_t> irb, ilb, brow;
+      std::vector<int32_t> in_, ikl, iku, idof, icomp;
+      std::vector<BcrSep> bsep;
+      int64_t orow = 0, oblk = 0, oy = 0, olm = 0, otv = 0;
       // segment of each band position: >= 0 interior index (global), < 0 -(separator index + 1)
       std::vector<int32_t> seg(n), loc(n);
       int maxwI = 0;
@@ -294,7 +295,6 @@ static void analyse(mgpu_ctx* c, Solver& S) {
         const int64_t tot = nc - int64_t(P - 1) * sw;
         int64_t p0 = 0;
         const int sep0 = int(ts.size()), int0 = int(ti.size());
-        const int64_t trow0 = otv;
         for (int a = 0; a < P; ++a) {
           const int64_t m = tot / P + (a < tot % P ? 1 : 0);
           TornInt I{};
@@ -352,30 +352,28 @@ static void analyse(mgpu_ctx* c, Solver& S) {
           }
         }
         if (P > 1) {
-          const int64_t nT = int64_t(P - 1) * sw;
-          const int klT = 2 * sw - 1, wT = 4 * sw - 1;
+          // block cyclic reduction of this component's N = P-1 separator blocks
+          const int N = P - 1;
+          int nlev = 0;
+          while ((1 << nlev) < N) ++nlev;
           for (int k = sep0; k < int(ts.size()); ++k) {
-            ts[k].tbase = otr;
-            ts[k].tkl = klT;
-            ts[k].tw = wT;
-            ts[k].trow0 = trow0;
+            BcrSep B{};
+            B.comp = cc;
+            B.kloc = k - sep0;
+            B.N = N;
+            B.s = sw;
+            B.sep0 = sep0;
+            B.nlev = nlev;
+            bsep.push_back(B);
+            brow.push_back(ts[k].trow);
           }
-          trb.push_back(otr), tlb.push_back(otl), tn.push_back(int32_t(nT)), tkl.push_back(klT),
-              tdof.push_back(int32_t(otv));
-          tcomp.push_back(cc);
-          otr += nT * wT;
-          otl += nT * klT;
-          otv += nT;
+          S.bcr_levels = std::max(S.bcr_levels, nlev);
+          otv += int64_t(N) * sw;
         }
       }
       S.nint = int(ti.size());
       S.nsep = int(ts.size());
-      S.ntc = int(tn.size());
       S.twmI = maxwI <= 32 ? 32 : 64;
-      int maxsT = 0;
-      for (int cc = 0; cc < ncomp; ++cc)
-        if (Pc[cc] > 1) maxsT = std::max(maxsT, sc[cc]);
-      S.twmT = 4 * maxsT - 1 <= 32 ? 32 : 64;
       int maxs = 0;
       for (int cc = 0; cc < ncomp; ++cc) maxs = std::max(maxs, std::max(kl[cc], ku[cc]));
       S.tmaxs = maxs;
@@ -383,8 +381,6 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       S.tb_blk = oblk;
       S.tb_y = oy;
       S.tb_lm = olm;
-      S.tb_trows = otr;
-      S.tb_tlm = otl;
       S.tb_tvec = otv;
       // every nnz to its place in TALL = [interior rows | blocks], for Lλx and for its transpose
       std::vector<int64_t> tbmap(P.nnz), tbmapT(P.nnz);
@@ -419,38 +415,40 @@ static void analyse(mgpu_ctx* c, Solver& S) {
           tbmapT[q] = place(pos[j], pos[i], true);
           if (tbmap[q] < 0 || tbmapT[q] < 0) S.tearable = 0;  // an entry outside the bands (cannot happen)
         }
-      std::vector<int32_t> tperm(std::max<int64_t>(otv, 1));
-      for (int64_t k = 0; k < otv; ++k) tperm[k] = int32_t(k);
       auto upv = [&](auto** dst, const auto& v) -> bool { return v.empty() ? true : up(dst, v); };
       good = good && upv(&S.d_ti, ti) && upv(&S.d_tiT, tiT) && upv(&S.d_ts, ts) && upv(&S.i_rbase, irb) &&
              upv(&S.i_lbase, ilb) && upv(&S.i_n, in_) && upv(&S.i_kl, ikl) && upv(&S.i_ku, iku) &&
-             upv(&S.i_dof0, idof) && upv(&S.t_rbase, trb) && upv(&S.t_lbase, tlb) && upv(&S.t_n, tn) &&
-             upv(&S.t_kl, tkl) && upv(&S.t_dof0, tdof) && up(&S.t_perm, tperm) && up(&S.tbmap, tbmap) &&
+             upv(&S.i_dof0, idof) && upv(&S.d_bsep, bsep) && upv(&S.d_brow, brow) && up(&S.tbmap, tbmap) &&
              up(&S.tbmapT, tbmapT);
+      // cyclic-reduction storage: levels 0..L of D, L, U per separator, factors and W per separator
+      const size_t nblk = size_t(std::max(S.nsep, 1)) * BCR_SS;
+      const size_t ndlu = size_t(S.bcr_levels + 1) * 3 * nblk;
       const size_t nall = size_t(std::max<int64_t>(orow + oblk, 1));
       good = good && cudaMalloc(&S.TALL, nall * sizeof(double)) == cudaSuccess &&
              cudaMemset(S.TALL, 0, nall * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&S.TUC, std::max<int64_t>(orow, 1) * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&S.TLM, std::max<int64_t>(olm, 1) * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&S.TY, std::max<int64_t>(oy, 1) * sizeof(double)) == cudaSuccess &&
-             cudaMalloc(&S.TTR, std::max<int64_t>(otr, 1) * sizeof(double)) == cudaSuccess &&
-             cudaMalloc(&S.TTUC, std::max<int64_t>(otr, 1) * sizeof(double)) == cudaSuccess &&
-             cudaMalloc(&S.TTLM, std::max<int64_t>(otl, 1) * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.DLU, ndlu * sizeof(double)) == cudaSuccess &&
+             cudaMemset(S.DLU, 0, ndlu * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.FA, nblk * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.WL, nblk * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.WU, nblk * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&S.PV, size_t(std::max(S.nsep, 1)) * BCR_S * sizeof(int)) == cudaSuccess &&
              cudaMalloc(&S.trhs, std::max<int64_t>(otv, 1) * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&S.txs, std::max<int64_t>(otv, 1) * sizeof(double)) == cudaSuccess &&
-             cudaMalloc(&S.tpiv, n * sizeof(int32_t)) == cudaSuccess &&
-             cudaMalloc(&S.ttpiv, std::max<int64_t>(otv, 1) * sizeof(int32_t)) == cudaSuccess;
+             cudaMalloc(&S.tpiv, n * sizeof(int32_t)) == cudaSuccess;
       // FP32 factorisation and FP64 refinement
       auto fal = [&](float** p, int64_t cnt) {
         return cudaMalloc(p, std::max<int64_t>(cnt, 1) * sizeof(float)) == cudaSuccess;
       };
       good = good && fal(&S.TALL32, orow + oblk) &&
              cudaMemset(S.TALL32, 0, std::max<int64_t>(orow + oblk, 1) * sizeof(float)) == cudaSuccess &&
-             fal(&S.TUC32, orow) && fal(&S.TLM32, olm) && fal(&S.TY32, oy) && fal(&S.TTR32, otr) &&
-             fal(&S.TTUC32, otr) && fal(&S.TTLM32, otl);
-      good = good && upv(&S.i_comp, icomp) && upv(&S.t_comp, tcomp) &&
+             fal(&S.TUC32, orow) && fal(&S.TLM32, olm) && fal(&S.TY32, oy) && fal(&S.DLU32, int64_t(ndlu)) &&
+             cudaMemset(S.DLU32, 0, ndlu * sizeof(float)) == cudaSuccess && fal(&S.FA32, int64_t(nblk)) &&
+             fal(&S.WL32, int64_t(nblk)) && fal(&S.WU32, int64_t(nblk));
+      good = good && upv(&S.i_comp, icomp) &&
              cudaMalloc(&S.iflag, std::max(S.nint, 1) * sizeof(int)) == cudaSuccess &&
-             cudaMalloc(&S.tflag, std::max(S.ntc, 1) * sizeof(int)) == cudaSuccess &&
              cudaMalloc(&S.nbad, sizeof(int)) == cudaSuccess && cudaMalloc(&S.info32, sizeof(int)) == cudaSuccess &&
              cudaMalloc(&S.dtmp, n * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&S.rtmp, n * sizeof(double)) == cudaSuccess;
@@ -880,10 +878,10 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
                 S->red, S->info, S->rbase, S->lbase, S->rbmap, S->rbmapT, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
                 S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag, S->part, S->cod, S->frozen,
                 S->nactive, S->d_ti, S->d_tiT, S->d_ts, S->i_rbase, S->i_lbase, S->i_n, S->i_kl, S->i_ku,
-                S->i_dof0, S->t_rbase, S->t_lbase, S->t_n, S->t_kl, S->t_dof0, S->t_perm, S->tbmap, S->tbmapT,
-                S->TALL, S->TUC, S->TLM, S->TY, S->TTR, S->TTUC, S->TTLM, S->trhs, S->txs, S->tpiv, S->ttpiv,
-                S->TALL32, S->TUC32, S->TLM32, S->TY32, S->TTR32, S->TTUC32, S->TTLM32, S->i_comp, S->t_comp,
-                S->iflag, S->tflag, S->nbad, S->info32, S->dtmp, S->rtmp, S->rptr, S->rq, S->rcol, S->dcolptr,
+                S->i_dof0, S->d_bsep, S->d_brow, S->tbmap, S->tbmapT, S->TALL, S->TUC, S->TLM, S->TY, S->DLU,
+                S->FA, S->WL, S->WU, S->PV, S->trhs, S->txs, S->tpiv, S->TALL32, S->TUC32, S->TLM32, S->TY32,
+                S->DLU32, S->FA32, S->WL32, S->WU32, S->i_comp,
+                S->iflag, S->nbad, S->info32, S->dtmp, S->rtmp, S->rptr, S->rq, S->rcol, S->dcolptr,
                 S->drowval, S->list32, S->list64, S->lulist[0], S->lulist[1], S->lulist[2], S->lulist[3]};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
@@ -936,13 +934,13 @@ static void rb_launch(Solver& S, RbComp cp, cudaStream_t st, const T* rows, T* u
 // Buffers of the partitioned factorisation in one precision.
 template <typename T>
 struct TornBufs {
-  T *rows, *uc, *lm, *y, *ttr, *ttuc, *ttlm;
+  T *rows, *uc, *lm, *y, *dlu, *fa, *wl, *wu;
 };
 static TornBufs<double> torn_bufs(Solver& S, double*) {
-  return {S.TALL, S.TUC, S.TLM, S.TY, S.TTR, S.TTUC, S.TTLM};
+  return {S.TALL, S.TUC, S.TLM, S.TY, S.DLU, S.FA, S.WL, S.WU};
 }
 static TornBufs<float> torn_bufs(Solver& S, float*) {
-  return {S.TALL32, S.TUC32, S.TLM32, S.TY32, S.TTR32, S.TTUC32, S.TTLM32};
+  return {S.TALL32, S.TUC32, S.TLM32, S.TY32, S.DLU32, S.FA32, S.WL32, S.WU32};
 }
 
 // Partitioned factorisation of Lλx or of its transpose, already gathered into
@@ -955,7 +953,6 @@ static void torn_factor(mgpu_ctx* c, bool tr, const int* cflag, int* info) {
   const TornBufs<T> B = torn_bufs(S, static_cast<T*>(nullptr));
   const RbComp cpI = tr ? RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_ku, S.i_kl, S.i_dof0}
                         : RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_kl, S.i_ku, S.i_dof0};
-  const RbComp cpT{S.t_rbase, S.t_lbase, S.t_n, S.t_kl, S.t_kl, S.t_dof0};
   const TornInt* ti = tr ? S.d_tiT : S.d_ti;
   const int mode = cflag ? RB_FALLBACK : RB_PLAIN;
   const T* blk = B.rows + S.tb_rows;
@@ -974,12 +971,12 @@ static void torn_factor(mgpu_ctx* c, bool tr, const int* cflag, int* info) {
     tb_spikes<T, 64, 16><<<S.nint, 32, 0, st>>>(S.nint, ti, B.uc, B.lm, S.tpiv, blk, B.y, cflag);
   else
     tb_spikes<T, 64, 32><<<S.nint, 32, 0, st>>>(S.nint, ti, B.uc, B.lm, S.tpiv, blk, B.y, cflag);
-  cudaMemsetAsync(B.ttr, 0, S.tb_trows * sizeof(T), st);  // band positions outside the blocks stay zero
-  tb_schur<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, B.y, B.ttr, cflag);
-  if (S.twmT == 32)
-    rb_lu<T, 32><<<S.ntc, 32, 0, st>>>(cpT, B.ttr, B.ttuc, B.ttlm, S.ttpiv, mode, S.tflag, info);
-  else
-    rb_lu<T, 64><<<S.ntc, 32, 0, st>>>(cpT, B.ttr, B.ttuc, B.ttlm, S.ttpiv, mode, S.tflag, info);
+  tb_schur<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, B.y, B.dlu, cflag);
+  for (int l = 0; l < S.bcr_levels; ++l) {
+    bcr_eliminate<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, l, B.dlu, B.fa, S.PV, B.wl, B.wu, cflag, info);
+    bcr_update<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, l, B.dlu, B.wl, B.wu, cflag);
+  }
+  bcr_root<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, B.dlu, B.fa, S.PV, cflag, info);
 }
 
 // out = A⁻¹ rhs (model order, FP64 in and out) with the factors of torn_factor<T>
@@ -990,7 +987,6 @@ static void torn_apply(mgpu_ctx* c, bool tr, const double* rhs, double* out, con
   const TornBufs<T> B = torn_bufs(S, static_cast<T*>(nullptr));
   const RbComp cpI = tr ? RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_ku, S.i_kl, S.i_dof0}
                         : RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_kl, S.i_ku, S.i_dof0};
-  const RbComp cpT{S.t_rbase, S.t_lbase, S.t_n, S.t_kl, S.t_kl, S.t_dof0};
   const TornInt* ti = tr ? S.d_tiT : S.d_ti;
   const int mode = cflag ? RB_FALLBACK : RB_PLAIN;
   const T* blk = B.rows + S.tb_rows;
@@ -1003,12 +999,14 @@ static void torn_apply(mgpu_ctx* c, bool tr, const double* rhs, double* out, con
                                            mode, S.iflag, nullptr);
   if (S.nsep == 0) return;
   tb_sep_rhs<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_ts, ti, blk, S.perm, rhs, out, S.trhs, cflag);
-  if (S.twmT == 32)
-    rb_solve<T, 32><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, B.ttuc, B.ttlm, S.ttpiv, S.trhs, S.bw, S.xw, S.rw,
-                                          tw, S.txs, 0, mode, S.tflag, nullptr);
-  else
-    rb_solve<T, 64><<<S.ntc, 32, 0, st>>>(cpT, S.t_perm, S.TTR, B.ttuc, B.ttlm, S.ttpiv, S.trhs, S.bw, S.xw, S.rw,
-                                          tw, S.txs, 0, mode, S.tflag, nullptr);
+  // separators: block cyclic reduction (trhs reduced in place, txs receives z and then x)
+  for (int l = 0; l < S.bcr_levels; ++l) {
+    bcr_fwd_elim<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, l, B.fa, S.PV, S.d_brow, S.trhs, S.txs, cflag);
+    bcr_fwd_keep<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, l, B.dlu, S.d_brow, S.trhs, S.txs, cflag);
+  }
+  bcr_root_solve<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, B.fa, S.PV, S.d_brow, S.trhs, S.txs, cflag);
+  for (int l = S.bcr_levels - 1; l >= 0; --l)
+    bcr_back<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, l, B.wl, B.wu, S.d_brow, S.txs, cflag);
   tb_back<T><<<S.nint, 128, 0, st>>>(S.nint, ti, S.d_ts, B.y, S.perm, S.txs, out, cflag);
 }
 
@@ -1045,7 +1043,6 @@ static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int*
   MG_CUDA(cudaMemsetAsync(S.nbad, 0, sizeof(int), st));
   tb_ir_check<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dtmp, out, S.flag, S.nbad);
   tb_expand_flags<<<nb(S.nint, 256), 256, 0, st>>>(S.nint, S.i_comp, S.flag, S.iflag);
-  if (S.ntc > 0) tb_expand_flags<<<nb(S.ntc, 256), 256, 0, st>>>(S.ntc, S.t_comp, S.flag, S.tflag);
   torn_factor<double>(c, tr, S.flag, info);
   torn_apply<double>(c, tr, rhs, out, S.flag);
   MG_CUDA(cudaGetLastError());

@@ -53,27 +53,30 @@ struct Solver {
   // partitioned (torn) layout of long components: interiors factorised in
   // parallel, separators coupled through a banded Schur complement
   int tearable = 0;           // some component is long enough to be cut
-  int nint = 0, nsep = 0, ntc = 0;
-  int twmI = 0, twmT = 0;     // register windows of the interior and Schur-complement kernels
+  int nint = 0, nsep = 0;
+  int twmI = 0;               // register window of the interior kernels
+  int bcr_levels = 0;         // cyclic-reduction levels of the longest separator chain
   int tmaxs = 0;              // largest max(kl, ku) over all components
   TornInt* d_ti = nullptr;    // [nint] interiors (bands of Lλx)
   TornInt* d_tiT = nullptr;   // [nint] the same with kl and ku exchanged (the transpose)
   TornSep* d_ts = nullptr;    // [nsep]
   int64_t *i_rbase = nullptr, *i_lbase = nullptr;
   int32_t *i_n = nullptr, *i_kl = nullptr, *i_ku = nullptr, *i_dof0 = nullptr;
-  int64_t *t_rbase = nullptr, *t_lbase = nullptr;
-  int32_t *t_n = nullptr, *t_kl = nullptr, *t_dof0 = nullptr, *t_perm = nullptr;
-  int64_t tb_rows = 0, tb_blk = 0, tb_y = 0, tb_lm = 0, tb_trows = 0, tb_tlm = 0, tb_tvec = 0;
+  BcrSep* d_bsep = nullptr;   // [nsep] cyclic-reduction roles
+  int64_t* d_brow = nullptr;  // [nsep] first row of each separator in the separator vectors
+  int64_t tb_rows = 0, tb_blk = 0, tb_y = 0, tb_lm = 0, tb_tvec = 0;
   int64_t* tbmap = nullptr;   // [nnz] position in TALL = [interior rows | blocks]
   int64_t* tbmapT = nullptr;  // [nnz] the same for the transpose
   double *TALL = nullptr, *TUC = nullptr, *TLM = nullptr, *TY = nullptr;
-  double *TTR = nullptr, *TTUC = nullptr, *TTLM = nullptr, *trhs = nullptr, *txs = nullptr;
-  int32_t *tpiv = nullptr, *ttpiv = nullptr;
+  double *DLU = nullptr, *FA = nullptr, *WL = nullptr, *WU = nullptr;  // cyclic reduction (band_bcr.cuh)
+  int* PV = nullptr;
+  double *trhs = nullptr, *txs = nullptr;
+  int32_t* tpiv = nullptr;
   // FP32 copies of the partitioned factorisation (refined in FP64)
   float *TALL32 = nullptr, *TUC32 = nullptr, *TLM32 = nullptr, *TY32 = nullptr;
-  float *TTR32 = nullptr, *TTUC32 = nullptr, *TTLM32 = nullptr;
-  int32_t *i_comp = nullptr, *t_comp = nullptr;  // component of each interior / Schur component
-  int *iflag = nullptr, *tflag = nullptr;        // fallback flags per interior / Schur component
+  float *DLU32 = nullptr, *FA32 = nullptr, *WL32 = nullptr, *WU32 = nullptr;
+  int32_t* i_comp = nullptr;                     // component of each interior
+  int* iflag = nullptr;                          // fallback flags per interior
   int* nbad = nullptr;                           // components whose FP32 refinement fell short
   int* info32 = nullptr;                         // zero pivots of the FP32 factorisation (caught by the check)
   double *dtmp = nullptr, *rtmp = nullptr;       // refinement correction and residual

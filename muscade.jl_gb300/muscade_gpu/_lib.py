@@ -17,7 +17,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
 SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
 HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh",
-           "band_torn.cuh", "solver.hpp"]
+           "band_torn.cuh", "band_bcr.cuh", "solver.hpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes
