@@ -237,65 +237,150 @@ __global__ void __launch_bounds__(32) bcr_root(int nsep, const BcrSep* __restric
   if (lane == 0 && sing && info) atomicCAS(info, 0, B.comp + 1);
 }
 
-// ---- solve: r (FP64, per separator s entries at row r0 + kloc*s) -> x in place of r
-// forward, level l: eliminated z_k = D_k^-1 r_k (into z), kept r_e -= U_e z_{e+h} + L_e z_{e-h}
+// ---- solve: r (FP64, per separator s entries at row0[k]) -> x, stored in FP64
+// and computed in the factors' type (with FP32 factors the solve is a
+// refinement correction).  One warp per block; the per-block steps are device
+// functions shared by the level-by-level kernels below and by the fused
+// per-component solve (band_torn.cuh).
+
+// shared scratch of one warp
+template <typename T>
+struct BcrWarp {
+  T A[BCR_SS];
+  T B[BCR_SS];
+  T v[BCR_S];
+  T w[BCR_S];
+  int p[BCR_S];
+};
+
+// v <- (LU)^-1 P v for one block: F and v in shared memory, the triangular
+// sweeps lane-parallel over rows (one column step per warp-synchronous step)
+template <typename T>
+__device__ void bcr_block_solve(const T* F, const int* piv, T* v, int s, int lane) {
+  if (lane == 0)
+    for (int j = 0; j < s; ++j)
+      if (piv[j] != j) {
+        const T t = v[j];
+        v[j] = v[piv[j]];
+        v[piv[j]] = t;
+      }
+  __syncwarp();
+  for (int j = 0; j < s; ++j) {  // unit lower
+    if (lane > j && lane < s) v[lane] = fma(-F[lane * BCR_S + j], v[j], v[lane]);
+    __syncwarp();
+  }
+  for (int j = s - 1; j >= 0; --j) {  // upper
+    if (lane == j) v[j] /= F[j * BCR_S + j];
+    __syncwarp();
+    if (lane < j) v[lane] = fma(-F[lane * BCR_S + j], v[j], v[lane]);
+    __syncwarp();
+  }
+}
+
+template <typename T>
+__device__ void bcr_stage(T* dst, const T* src, int lane) {
+  for (int e = lane; e < BCR_SS; e += 32) dst[e] = src[e];
+}
+
+// z_k = D_k^-1 r_k with the factors FA[k] (an eliminated block at its level, or the root)
+template <typename T>
+__device__ void bcr_diag_solve_warp(const BcrSep& B, int k, const T* __restrict__ FA, const int* __restrict__ PV,
+                                    const int64_t* __restrict__ row0, const double* r, double* z,
+                                    BcrWarp<T>* sw, int lane) {
+  const int s = B.s;
+  const int64_t o = row0[k];
+  bcr_stage(sw->A, FA + int64_t(k) * BCR_SS, lane);
+  if (lane < s) {
+    sw->v[lane] = T(r[o + lane]);
+    sw->p[lane] = PV[int64_t(k) * BCR_S + lane];
+  }
+  __syncwarp();
+  bcr_block_solve(sw->A, sw->p, sw->v, s, lane);
+  if (lane < s) z[o + lane] = double(sw->v[lane]);
+  __syncwarp();
+}
+
+// kept block e at level l: r_e -= U_e z_{e+h} + L_e z_{e-h}
+template <typename T>
+__device__ void bcr_keep_warp(const BcrSep& B, int k, int l, int nsep, const T* __restrict__ DLU,
+                              const int64_t* __restrict__ row0, double* r, const double* z, BcrWarp<T>* sw,
+                              int lane) {
+  const int s = B.s, h = 1 << l;
+  const T* cur = DLU + (int64_t(l) * nsep * 3 + 3 * int64_t(k)) * BCR_SS;
+  const bool up = B.kloc + h < B.N, dn = B.kloc >= h;
+  if (up) bcr_stage(sw->B, cur + 2 * BCR_SS, lane);
+  if (dn) bcr_stage(sw->A, cur + BCR_SS, lane);
+  if (lane < s) {
+    sw->v[lane] = up ? T(z[row0[k + h] + lane]) : T(0);
+    sw->w[lane] = dn ? T(z[row0[k - h] + lane]) : T(0);
+  }
+  __syncwarp();
+  if (lane < s) {
+    const int64_t o = row0[k];
+    T v = T(r[o + lane]);
+    for (int q = 0; q < s; ++q) {
+      if (up) v = fma(-sw->B[lane * BCR_S + q], sw->v[q], v);
+      if (dn) v = fma(-sw->A[lane * BCR_S + q], sw->w[q], v);
+    }
+    r[o + lane] = double(v);
+  }
+  __syncwarp();
+}
+
+// eliminated block k at level l: x_k = z_k - W_L(k) x_{k-h} - W_U(k) x_{k+h}  (z holds z_k and the kept x)
+template <typename T>
+__device__ void bcr_back_warp(const BcrSep& B, int k, int l, const T* __restrict__ WL, const T* __restrict__ WU,
+                              const int64_t* __restrict__ row0, double* z, BcrWarp<T>* sw, int lane) {
+  const int s = B.s, h = 1 << l;
+  const bool up = B.kloc + h < B.N;
+  const int64_t o = row0[k];
+  bcr_stage(sw->A, WL + int64_t(k) * BCR_SS, lane);
+  if (up) bcr_stage(sw->B, WU + int64_t(k) * BCR_SS, lane);
+  if (lane < s) {
+    sw->w[lane] = T(z[row0[k - h] + lane]);
+    sw->v[lane] = up ? T(z[row0[k + h] + lane]) : T(0);
+  }
+  __syncwarp();
+  if (lane < s) {
+    T a = T(z[o + lane]);
+    for (int q = 0; q < s; ++q) {
+      a = fma(-sw->A[lane * BCR_S + q], sw->w[q], a);
+      if (up) a = fma(-sw->B[lane * BCR_S + q], sw->v[q], a);
+    }
+    z[o + lane] = double(a);
+  }
+  __syncwarp();
+}
+
+// level-by-level kernels: one warp per separator of every component
+// forward, level l: eliminated z_k = D_k^-1 r_k
 template <typename T>
 __global__ void __launch_bounds__(32) bcr_fwd_elim(int nsep, const BcrSep* __restrict__ bs, int l,
                                                    const T* __restrict__ FA, const int* __restrict__ PV,
                                                    const int64_t* __restrict__ row0, const double* __restrict__ r,
                                                    double* __restrict__ z, const int* __restrict__ only) {
-  const int k = blockIdx.x, lane = threadIdx.x;
-  if (k >= nsep || lane != 0) return;
+  __shared__ BcrWarp<T> sw;
+  const int k = blockIdx.x;
+  if (k >= nsep) return;
   const BcrSep B = bs[k];
   if (only && only[B.comp] == 0) return;
   if (!(l < B.nlev && bcr_role(B.kloc, B.N, l) == 1)) return;
-  const int s = B.s;
-  const T* F = FA + int64_t(k) * BCR_SS;
-  const int* piv = PV + int64_t(k) * BCR_S;
-  double v[BCR_S];
-  const int64_t o = row0[k];
-  for (int i = 0; i < s; ++i) v[i] = r[o + i];
-  for (int j = 0; j < s; ++j)
-    if (piv[j] != j) {
-      const double t = v[j];
-      v[j] = v[piv[j]];
-      v[piv[j]] = t;
-    }
-  for (int i = 1; i < s; ++i)
-    for (int j = 0; j < i; ++j) v[i] = fma(-double(F[i * BCR_S + j]), v[j], v[i]);
-  for (int i = s - 1; i >= 0; --i) {
-    for (int j = i + 1; j < s; ++j) v[i] = fma(-double(F[i * BCR_S + j]), v[j], v[i]);
-    v[i] /= double(F[i * BCR_S + i]);
-  }
-  for (int i = 0; i < s; ++i) z[o + i] = v[i];
+  bcr_diag_solve_warp(B, k, FA, PV, row0, r, z, &sw, threadIdx.x);
 }
 
+// forward, level l: kept r_e -= U_e z_{e+h} + L_e z_{e-h}
 template <typename T>
 __global__ void __launch_bounds__(32) bcr_fwd_keep(int nsep, const BcrSep* __restrict__ bs, int l,
                                                    const T* __restrict__ DLU, const int64_t* __restrict__ row0,
                                                    double* __restrict__ r, const double* __restrict__ z,
                                                    const int* __restrict__ only) {
-  const int k = blockIdx.x, lane = threadIdx.x;
+  __shared__ BcrWarp<T> sw;
+  const int k = blockIdx.x;
   if (k >= nsep) return;
   const BcrSep B = bs[k];
   if (only && only[B.comp] == 0) return;
   if (!(l < B.nlev && bcr_role(B.kloc, B.N, l) == 2)) return;
-  const int s = B.s, h = 1 << l;
-  const T* cur = DLU + (int64_t(l) * nsep * 3 + 3 * int64_t(k)) * BCR_SS;
-  const bool up = B.kloc + h < B.N, dn = B.kloc >= h;
-  const int64_t o = row0[k];
-  for (int i = lane; i < s; i += 32) {
-    double v = r[o + i];
-    if (up) {
-      const int64_t ou = row0[k + h];
-      for (int q = 0; q < s; ++q) v = fma(-double(cur[2 * BCR_SS + i * BCR_S + q]), z[ou + q], v);
-    }
-    if (dn) {
-      const int64_t od = row0[k - h];
-      for (int q = 0; q < s; ++q) v = fma(-double(cur[BCR_SS + i * BCR_S + q]), z[od + q], v);
-    }
-    r[o + i] = v;
-  }
+  bcr_keep_warp(B, k, l, nsep, DLU, row0, r, z, &sw, threadIdx.x);
 }
 
 // root: x_0 = D_0^-1 r_0 (into z, which then holds x for every block as the back-substitution proceeds)
@@ -304,60 +389,27 @@ __global__ void __launch_bounds__(32) bcr_root_solve(int nsep, const BcrSep* __r
                                                      const T* __restrict__ FA, const int* __restrict__ PV,
                                                      const int64_t* __restrict__ row0, const double* __restrict__ r,
                                                      double* __restrict__ z, const int* __restrict__ only) {
-  const int k = blockIdx.x, lane = threadIdx.x;
-  if (k >= nsep || lane != 0) return;
+  __shared__ BcrWarp<T> sw;
+  const int k = blockIdx.x;
+  if (k >= nsep) return;
   const BcrSep B = bs[k];
   if (B.kloc != 0 || (only && only[B.comp] == 0)) return;
-  const int s = B.s;
-  const T* F = FA + int64_t(k) * BCR_SS;
-  const int* piv = PV + int64_t(k) * BCR_S;
-  double v[BCR_S];
-  const int64_t o = row0[k];
-  for (int i = 0; i < s; ++i) v[i] = r[o + i];
-  for (int j = 0; j < s; ++j)
-    if (piv[j] != j) {
-      const double t = v[j];
-      v[j] = v[piv[j]];
-      v[piv[j]] = t;
-    }
-  for (int i = 1; i < s; ++i)
-    for (int j = 0; j < i; ++j) v[i] = fma(-double(F[i * BCR_S + j]), v[j], v[i]);
-  for (int i = s - 1; i >= 0; --i) {
-    for (int j = i + 1; j < s; ++j) v[i] = fma(-double(F[i * BCR_S + j]), v[j], v[i]);
-    v[i] /= double(F[i * BCR_S + i]);
-  }
-  for (int i = 0; i < s; ++i) z[o + i] = v[i];
+  bcr_diag_solve_warp(B, k, FA, PV, row0, r, z, &sw, threadIdx.x);
 }
 
-// backward, level l: eliminated x_k = z_k - W_L(k) x_{k-h} - W_U(k) x_{k+h}  (z holds z_k and, for kept blocks, x)
+// backward, level l
 template <typename T>
 __global__ void __launch_bounds__(32) bcr_back(int nsep, const BcrSep* __restrict__ bs, int l,
                                                const T* __restrict__ WL, const T* __restrict__ WU,
                                                const int64_t* __restrict__ row0, double* __restrict__ z,
                                                const int* __restrict__ only) {
-  const int k = blockIdx.x, lane = threadIdx.x;
+  __shared__ BcrWarp<T> sw;
+  const int k = blockIdx.x;
   if (k >= nsep) return;
   const BcrSep B = bs[k];
   if (only && only[B.comp] == 0) return;
   if (!(l < B.nlev && bcr_role(B.kloc, B.N, l) == 1)) return;
-  const int s = B.s, h = 1 << l;
-  const bool up = B.kloc + h < B.N;
-  const int64_t o = row0[k], od = row0[k - h];
-  const T* wl = WL + int64_t(k) * BCR_SS;
-  const T* wu = WU + int64_t(k) * BCR_SS;
-  double v[BCR_S];
-  for (int i = 0; i < s; ++i) {
-    double a = z[o + i];
-    for (int q = 0; q < s; ++q) a = fma(-double(wl[i * BCR_S + q]), z[od + q], a);
-    if (up) {
-      const int64_t ou = row0[k + h];
-      for (int q = 0; q < s; ++q) a = fma(-double(wu[i * BCR_S + q]), z[ou + q], a);
-    }
-    v[i] = a;
-  }
-  __syncwarp();
-  if (lane == 0)
-    for (int i = 0; i < s; ++i) z[o + i] = v[i];
+  bcr_back_warp(B, k, l, WL, WU, row0, z, &sw, threadIdx.x);
 }
 
 }  // namespace mgpu

@@ -227,52 +227,393 @@ __global__ void __launch_bounds__(32) tb_schur(int nsep, const TornSep* __restri
 
 // ---------------------------------------------------------------- solve
 // separator right-hand sides: r = b_S - F^R_{left} ỹ_{left}[last s] - F^L_{right} ỹ_{right}[first s]
-// (b and ỹ in model order; ỹ of the interiors is already in x)
+// (b and ỹ in model order; ỹ of the interiors is already in x); arithmetic in
+// the factors' type, stored in FP64.  One warp; yl, yr: s entries of scratch.
 template <typename T>
-__global__ void tb_sep_rhs(int nsep, const TornSep* __restrict__ ts, const TornInt* __restrict__ ti,
-                           const T* __restrict__ blk, const int32_t* __restrict__ perm,
-                           const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ tr,
-                           const int* __restrict__ only) {
-  const int k = blockIdx.x, lane = threadIdx.x;
+__device__ void tb_sep_rhs_warp(const TornSep& S, const TornInt* __restrict__ ti, const T* __restrict__ blk,
+                                const int32_t* __restrict__ perm, const double* b, const double* x, double* tr,
+                                T* yl, T* yr, int lane) {
+  const int s = S.s;
+  const TornInt IL = ti[S.intL], IR = ti[S.intR];
+  if (lane < s) {
+    yl[lane] = T(x[perm[IL.dof0 + IL.n - s + lane]]);
+    yr[lane] = T(x[perm[IR.dof0 + lane]]);
+  }
+  __syncwarp();
+  if (lane < s) {
+    T v = T(b[perm[S.dof0 + lane]]);
+    for (int q = 0; q < s; ++q) {
+      v -= blk[IL.fR + lane * s + q] * yl[q];
+      v -= blk[IR.fL + lane * s + q] * yr[q];
+    }
+    tr[S.trow + lane] = double(v);
+  }
+  __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) tb_sep_rhs(int nsep, const TornSep* __restrict__ ts,
+                                                 const TornInt* __restrict__ ti, const T* __restrict__ blk,
+                                                 const int32_t* __restrict__ perm, const double* __restrict__ b,
+                                                 const double* __restrict__ x, double* __restrict__ tr,
+                                                 const int* __restrict__ only) {
+  __shared__ T yl[BCR_S], yr[BCR_S];
+  const int k = blockIdx.x;
   if (k >= nsep) return;
   const TornSep S = ts[k];
   if (tb_skip(only, S.comp)) return;
-  const int s = S.s;
-  const TornInt IL = ti[S.intL], IR = ti[S.intR];
-  for (int i = lane; i < s; i += 32) {
-    double v = b[perm[S.dof0 + i]];
-    for (int q = 0; q < s; ++q) {
-      v -= double(blk[IL.fR + i * s + q]) * x[perm[IL.dof0 + IL.n - s + q]];
-      v -= double(blk[IR.fL + i * s + q]) * x[perm[IR.dof0 + q]];
-    }
-    tr[S.trow + i] = v;
-  }
+  tb_sep_rhs_warp(S, ti, blk, perm, b, x, tr, yl, yr, threadIdx.x);
 }
 
-// x_a -= Y^L_a x_S_a + Y^R_a x_S_a+1 (interior dofs), x_S = T solution (separator dofs)
+// x_a -= Y^L_a x_S_a + Y^R_a x_S_a+1 (interior dofs), x_S = T solution (separator dofs);
+// arithmetic in the factors' type (with FP32 factors this is a refinement
+// correction).  One warp; xl, xr: s entries of scratch.
 template <typename T>
-__global__ void tb_back(int nint, const TornInt* __restrict__ ti, const TornSep* __restrict__ ts,
-                        const T* __restrict__ Y, const int32_t* __restrict__ perm,
-                        const double* __restrict__ txs, double* __restrict__ x, const int* __restrict__ only) {
+__device__ void tb_back_warp(const TornInt& I, const TornSep* __restrict__ ts, const T* __restrict__ Y,
+                             const int32_t* __restrict__ perm, const double* txs, double* x, T* xl, T* xr,
+                             int lane) {
+  const int s = I.s;
+  const bool hl = I.sepL >= 0, hr = I.sepR >= 0;
+  if (!(hl || hr)) return;
+  if (lane < s) {
+    xl[lane] = hl ? T(txs[ts[I.sepL].trow + lane]) : T(0);
+    xr[lane] = hr ? T(txs[ts[I.sepR].trow + lane]) : T(0);
+  }
+  __syncwarp();
+  for (int i = lane; i < I.n; i += 32) {
+    T v = T(x[perm[I.dof0 + i]]);
+    for (int q = 0; q < s; ++q) {
+      if (hl) v -= Y[I.yL + int64_t(i) * s + q] * xl[q];
+      if (hr) v -= Y[I.yR + int64_t(i) * s + q] * xr[q];
+    }
+    x[perm[I.dof0 + i]] = double(v);
+  }
+  if (hr) {
+    const TornSep S = ts[I.sepR];
+    if (lane < s) x[perm[S.dof0 + lane]] = txs[S.trow + lane];
+  }
+  __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32) tb_back(int nint, const TornInt* __restrict__ ti,
+                                              const TornSep* __restrict__ ts, const T* __restrict__ Y,
+                                              const int32_t* __restrict__ perm, const double* __restrict__ txs,
+                                              double* __restrict__ x, const int* __restrict__ only) {
+  __shared__ T xl[BCR_S], xr[BCR_S];
   const int a = blockIdx.x;
   if (a >= nint) return;
   const TornInt I = ti[a];
   if (tb_skip(only, I.comp)) return;
-  const int s = I.s;
-  const double* xl = I.sepL >= 0 ? txs + ts[I.sepL].trow : nullptr;
-  const double* xr = I.sepR >= 0 ? txs + ts[I.sepR].trow : nullptr;
-  if (xl || xr)
-    for (int i = threadIdx.x; i < I.n; i += blockDim.x) {
-      double v = x[perm[I.dof0 + i]];
-      for (int q = 0; q < s; ++q) {
-        if (xl) v -= double(Y[I.yL + int64_t(i) * s + q]) * xl[q];
-        if (xr) v -= double(Y[I.yR + int64_t(i) * s + q]) * xr[q];
-      }
-      x[perm[I.dof0 + i]] = v;
+  tb_back_warp(I, ts, Y, perm, txs, x, xl, xr, threadIdx.x);
+}
+
+// ---------------------------------------------------------------- fused per-component solve
+// Everything of one solve of one component in one block, for layouts whose
+// components have few interiors (many components, e.g. independent risers):
+// W warps take the component's interiors and separators in turn, and the
+// cyclic-reduction levels, the back-substitution and (with nref > 1) the
+// sweeps of FP64 iterative refinement follow one another behind block
+// barriers instead of kernel boundaries.  All vectors stay in the band order
+// of the factorisation (contiguous per interior and separator); the
+// right-hand side is gathered from model order once and the result scattered
+// back once.
+//   b = P rhs
+//   sweep: t = A~^-1 r  (interiors, separator right-hand sides, cyclic
+//          reduction, back-substitution; r = b on the first sweep)
+//          x += t (x = t on the first sweep); stop when max|t| <= tol_stop max|x|
+//          r = b - A x (FP64, from the unfactorised interior rows and the
+//          E, F, D blocks)
+//   out = P^T x
+// At the end flag[c] = 1 unless max|t| <= tol_ok max|x| and all finite (for
+// the FP64 fallback), nsweep[c] = sweeps.  With nref = 1 it is a plain
+// solve.  only[c] == 0 skips the component.
+struct TbFusedArgs {
+  int ncomp;
+  const int32_t* cint0;  // [ncomp+1] first interior of each component
+  const int32_t* csep0;  // [ncomp+1] first separator of each component
+  RbComp cpI;            // interiors as row-band components (bands exchanged for the transpose)
+  const TornInt* ti;
+  const TornSep* ts;
+  const BcrSep* bs;
+  int nsep;
+  const int32_t* perm;
+  const int32_t* tpiv;
+  const int64_t* brow;
+  const double* tall;    // unfactorised interior rows, then the blocks at tall + tb_rows (FP64)
+  int64_t tb_rows;
+  double* bw;    // [nX] band-order right-hand side
+  double* xw;    // [nX] band-order solution
+  double* rw;    // [nX] band-order residual
+  double* trhs;  // separator vectors
+  double* txs;
+  const double* rhs;  // model order
+  double* out;        // model order
+  const int32_t* ccn;    // [ncomp] component sizes
+  const int32_t* ccdof0; // [ncomp] component offsets in perm
+  int nref;
+  double tol_stop, tol_ok;
+  const int* only;
+  int* flag;
+  int* nsweep;
+  int* nbad;  // incremented per flagged component
+};
+
+template <typename T>
+struct TbFusedFactors {
+  const T *UC, *LM, *blk, *Y, *FA, *DLU, *WL, *WU;
+  const int* PV;
+  T* tw;  // [nX] band-order correction
+};
+
+template <typename T, int WM>
+__host__ __device__ constexpr int tb_fused_warp_bytes() {
+  return ((RbSmem<T, WM>::bytes > int(sizeof(BcrWarp<T>)) ? RbSmem<T, WM>::bytes : int(sizeof(BcrWarp<T>))) + 15) /
+         16 * 16;
+}
+
+// separator right-hand side in band order: r_S = b_S - F^R_{left} t_{left}[last s] - F^L_{right} t_{right}[first s]
+template <typename T>
+__device__ void tb_sep_rhs_band(const TornSep& S, const TornInt* __restrict__ ti, const T* __restrict__ blk,
+                                const double* b, const T* t, double* tr, int lane) {
+  const int s = S.s;
+  if (lane < s) {
+    const TornInt IL = ti[S.intL], IR = ti[S.intR];
+    const T* yl = t + IL.dof0 + IL.n - s;
+    const T* yr = t + IR.dof0;
+    T v = T(b[S.dof0 + lane]);
+    for (int q = 0; q < s; ++q) {
+      v -= blk[IL.fR + lane * s + q] * yl[q];
+      v -= blk[IR.fL + lane * s + q] * yr[q];
     }
-  if (I.sepR >= 0) {
-    const TornSep S = ts[I.sepR];
-    for (int i = threadIdx.x; i < s; i += blockDim.x) x[perm[S.dof0 + i]] = txs[S.trow + i];
+    tr[S.trow + lane] = double(v);
+  }
+}
+
+// back-substitution in band order: t_a -= Y^L_a x_S_a + Y^R_a x_S_a+1, t_S = x_S.
+// One warp; the rows of Y go through shared memory 32 at a time (contiguous
+// loads), each lane then takes one row.  sc: scratch of 2*32*16 + 32 T.
+template <typename T>
+__device__ void tb_back_band(const TornInt& I, const TornSep* __restrict__ ts, const T* __restrict__ Y,
+                             const double* txs, T* t, T* sc, int lane) {
+  const int s = I.s;
+  const bool hl = I.sepL >= 0, hr = I.sepR >= 0;
+  if (!(hl || hr)) return;
+  T* yl = sc;
+  T* yr = sc + 32 * BCR_S;
+  T* xl = sc + 64 * BCR_S;
+  T* xr = xl + BCR_S;
+  if (lane < s) {
+    xl[lane] = hl ? T(txs[ts[I.sepL].trow + lane]) : T(0);
+    xr[lane] = hr ? T(txs[ts[I.sepR].trow + lane]) : T(0);
+  }
+#pragma unroll 1
+  for (int i0 = 0; i0 < I.n; i0 += 32) {
+    const int m = min(32, I.n - i0);
+    __syncwarp();
+    if (hl)
+      for (int e = lane; e < m * s; e += 32) yl[e] = Y[I.yL + int64_t(i0) * s + e];
+    if (hr)
+      for (int e = lane; e < m * s; e += 32) yr[e] = Y[I.yR + int64_t(i0) * s + e];
+    __syncwarp();
+    if (lane < m) {
+      T v = t[I.dof0 + i0 + lane];
+      for (int q = 0; q < s; ++q) {
+        if (hl) v -= yl[lane * s + q] * xl[q];
+        if (hr) v -= yr[lane * s + q] * xr[q];
+      }
+      t[I.dof0 + i0 + lane] = v;
+    }
+  }
+  if (hr && lane < s) t[ts[I.sepR].dof0 + lane] = xr[lane];
+  __syncwarp();
+}
+
+// v - sum_{j < s} a[j] b[j] (s <= 16), ascending j; the loads issued 8 at a time
+__device__ __forceinline__ double tb_dot16_sub(const double* a, const double* b, int s, double v) {
+#pragma unroll
+  for (int jb = 0; jb < 16; jb += 8) {
+    if (jb >= s) break;
+    double av[8], bv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool ok = jb + u < s;
+      av[u] = ok ? a[jb + u] : 0.0;
+      bv[u] = ok ? b[jb + u] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (jb + u < s) v = fma(-av[u], bv[u], v);
+  }
+  return v;
+}
+
+template <typename T, int WM>
+__global__ void __launch_bounds__(416, 2) tb_fused(TbFusedArgs A, TbFusedFactors<T> F) {
+  extern __shared__ __align__(16) unsigned char tb_dyn[];
+  __shared__ double red[2][32];
+  __shared__ int fin[32];
+  const int cc = blockIdx.x;
+  if (cc >= A.ncomp) return;
+  if (A.only && A.only[cc] == 0) return;
+  const int W = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* my = tb_dyn + size_t(w) * tb_fused_warp_bytes<T, WM>();
+  BcrWarp<T>* sw = reinterpret_cast<BcrWarp<T>*>(my);
+  const int a0 = A.cint0[cc], a1 = A.cint0[cc + 1], k0 = A.csep0[cc], k1 = A.csep0[cc + 1];
+  const int nc = A.ccn[cc];
+  const int64_t q0 = A.ccdof0[cc];
+  const int32_t* pm = A.perm + q0;
+  const int nlev = k1 > k0 ? A.bs[k0].nlev : 0;
+  const double* blk64 = A.tall + A.tb_rows;
+  T* t = F.tw;
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) A.bw[q0 + k] = A.rhs[pm[k]];
+  __syncthreads();
+  const double* in = A.bw;
+  double dn = 0.0, xn = 0.0;
+  bool finite = true;
+  int sweeps = 0;
+  for (int it = 0; it < A.nref; ++it) {
+    // interiors: t = A_a^-1 in
+    for (int a = a0 + w; a < a1; a += W) {
+      const int n = A.cpI.cn[a], kl = A.cpI.ckl[a], kv = kl + A.cpI.cku[a];
+      const int64_t d0 = A.cpI.cdof0[a];
+      rb_fb<T, WM>(n, kl, kv, kv + 1, F.UC + A.cpI.rbase[a], F.LM + A.cpI.lbase[a], A.tpiv + d0, in + d0, t + d0,
+                   my, lane);
+      __syncwarp();
+    }
+    __syncthreads();
+    if (k1 > k0) {
+      for (int k = k0 + w; k < k1; k += W) tb_sep_rhs_band(A.ts[k], A.ti, F.blk, in, t, A.trhs, lane);
+      __syncthreads();
+      for (int l = 0; l < nlev; ++l) {
+        for (int k = k0 + w; k < k1; k += W) {
+          const BcrSep B = A.bs[k];
+          if (bcr_role(B.kloc, B.N, l) == 1) bcr_diag_solve_warp(B, k, F.FA, F.PV, A.brow, A.trhs, A.txs, sw, lane);
+        }
+        __syncthreads();
+        for (int k = k0 + w; k < k1; k += W) {
+          const BcrSep B = A.bs[k];
+          if (bcr_role(B.kloc, B.N, l) == 2) bcr_keep_warp(B, k, l, A.nsep, F.DLU, A.brow, A.trhs, A.txs, sw, lane);
+        }
+        __syncthreads();
+      }
+      if (w == 0) bcr_diag_solve_warp(A.bs[k0], k0, F.FA, F.PV, A.brow, A.trhs, A.txs, sw, lane);
+      __syncthreads();
+      for (int l = nlev - 1; l >= 0; --l) {
+        for (int k = k0 + w; k < k1; k += W) {
+          const BcrSep B = A.bs[k];
+          if (bcr_role(B.kloc, B.N, l) == 1) bcr_back_warp(B, k, l, F.WL, F.WU, A.brow, A.txs, sw, lane);
+        }
+        __syncthreads();
+      }
+      for (int a = a0 + w; a < a1; a += W) tb_back_band(A.ti[a], A.ts, F.Y, A.txs, t, reinterpret_cast<T*>(my), lane);
+      __syncthreads();
+    }
+    ++sweeps;
+    if (A.nref == 1) break;
+    // x += t and the max norms
+    dn = 0.0;
+    xn = 0.0;
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+      const int64_t q = q0 + k;
+      const double dv = double(t[q]);
+      const double xv = it == 0 ? dv : A.xw[q] + dv;
+      A.xw[q] = xv;
+      finite = finite && isfinite(dv) && isfinite(xv);
+      dn = fmax(dn, fabs(dv));
+      xn = fmax(xn, fabs(xv));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dn = fmax(dn, __shfl_xor_sync(0xffffffffu, dn, o));
+      xn = fmax(xn, __shfl_xor_sync(0xffffffffu, xn, o));
+    }
+    const bool wfin = __all_sync(0xffffffffu, finite);
+    if (lane == 0) {
+      red[0][w] = dn;
+      red[1][w] = xn;
+      fin[w] = wfin;
+    }
+    __syncthreads();
+    dn = 0.0;
+    xn = 0.0;
+    finite = true;
+    for (int q = 0; q < W; ++q) {
+      dn = fmax(dn, red[0][q]);
+      xn = fmax(xn, red[1][q]);
+      finite = finite && fin[q];
+    }
+    __syncthreads();  // red / fin are rewritten by the next sweep
+    if (it + 1 == A.nref || !finite || dn <= A.tol_stop * xn) break;
+    // r = b - A x: interior rows (band storage and the E blocks), separator rows
+    // (F and D blocks).  The band rows go through the warp's shared scratch 32
+    // rows at a time (contiguous loads), each lane then sums one row in
+    // ascending column order; its x entries are consecutive across lanes.
+    for (int a = a0 + w; a < a1; a += W) {
+      const TornInt I = A.ti[a];
+      const int n = I.n, kl = I.kl, kv = I.kl + I.ku, wd = kv + 1, s = I.s;
+      const double* rows = A.tall + I.rbase;
+      const double* xl = I.sepL >= 0 ? A.xw + A.ts[I.sepL].dof0 : nullptr;
+      const double* xr = I.sepR >= 0 ? A.xw + A.ts[I.sepR].dof0 : nullptr;
+      double* sm = reinterpret_cast<double*>(my);
+#pragma unroll 1
+      for (int i0 = 0; i0 < n; i0 += 32) {
+        const int m = min(32, n - i0);
+        __syncwarp();
+        for (int e = lane; e < m * wd; e += 32) sm[e] = rows[int64_t(i0) * wd + e];
+        __syncwarp();
+        if (lane < m) {
+          const int i = i0 + lane;
+          const int64_t q = I.dof0 + i;
+          double v = A.bw[q];
+          const int c0 = max(0, kl - i), c1 = min(kv, n - 1 - i + kl);
+          const double* row = sm + lane * wd;
+          const double* xx = A.xw + q - kl;
+#pragma unroll 1
+          for (int cb = 0; cb <= c1; cb += 8) {
+            double xv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = cb + u;
+              xv[u] = (c >= c0 && c <= c1) ? xx[c] : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+              if (cb + u >= c0 && cb + u <= c1) v = fma(-row[cb + u], xv[u], v);
+          }
+          if (xl && i < s) v = tb_dot16_sub(blk64 + I.eL + int64_t(i) * s, xl, s, v);
+          if (xr && i >= n - s) v = tb_dot16_sub(blk64 + I.eR + int64_t(i - (n - s)) * s, xr, s, v);
+          A.rw[q] = v;
+        }
+      }
+    }
+#pragma unroll 1
+    for (int k = k0 + w; k < k1; k += W) {
+      const TornSep S = A.ts[k];
+      const int s = S.s;
+      if (lane < s) {
+        const TornInt IL = A.ti[S.intL], IR = A.ti[S.intR];
+        const int64_t q = S.dof0 + lane;
+        double v = A.bw[q];
+        v = tb_dot16_sub(blk64 + IL.fR + lane * s, A.xw + IL.dof0 + IL.n - s, s, v);
+        v = tb_dot16_sub(blk64 + S.d + lane * s, A.xw + S.dof0, s, v);
+        v = tb_dot16_sub(blk64 + IR.fL + lane * s, A.xw + IR.dof0, s, v);
+        A.rw[q] = v;
+      }
+    }
+    __syncthreads();
+    in = A.rw;
+  }
+  if (A.nref == 1) {
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) A.out[pm[k]] = double(t[q0 + k]);
+  } else {
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) A.out[pm[k]] = A.xw[q0 + k];
+    if (threadIdx.x == 0) {
+      const int bad = !(finite && dn <= A.tol_ok * xn);
+      if (A.flag) A.flag[cc] = bad;
+      if (A.nbad && bad) atomicAdd(A.nbad, 1);
+      if (A.nsweep) A.nsweep[cc] = sweeps;
+    }
   }
 }
 

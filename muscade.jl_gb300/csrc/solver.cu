@@ -288,9 +288,13 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       // segment of each band position: >= 0 interior index (global), < 0 -(separator index + 1)
       std::vector<int32_t> seg(n), loc(n);
       int maxwI = 0;
+      std::vector<int32_t> cint0(ncomp + 1, 0), csep0(ncomp + 1, 0);
       for (int cc = 0; cc < ncomp; ++cc) {
         const int64_t c0 = comp_start[cc], nc = comp_start[cc + 1] - c0;
         const int P = Pc[cc], sw = sc[cc], w = kl[cc] + ku[cc] + 1;
+        cint0[cc] = int32_t(ti.size());
+        csep0[cc] = int32_t(ts.size());
+        S.maxP = std::max(S.maxP, P);
         maxwI = std::max(maxwI, w);
         const int64_t tot = nc - int64_t(P - 1) * sw;
         int64_t p0 = 0;
@@ -373,7 +377,29 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       }
       S.nint = int(ti.size());
       S.nsep = int(ts.size());
+      cint0[ncomp] = S.nint;
+      csep0[ncomp] = S.nsep;
       S.twmI = maxwI <= 32 ? 32 : 64;
+      // fused per-component solve (one block per component) when every component has
+      // few interiors; warps per block bounded by ~112 KB of shared memory (two blocks per SM)
+      {
+        const char* fe = getenv("MGPU_TORN_FUSED");
+        const bool allow = !(fe && fe[0] == '0');
+        const int b32 = S.twmI == 32 ? tb_fused_warp_bytes<float, 32>() : tb_fused_warp_bytes<float, 64>();
+        const int b64 = S.twmI == 32 ? tb_fused_warp_bytes<double, 32>() : tb_fused_warp_bytes<double, 64>();
+        const int budget = 112 * 1024;
+        if (allow && S.maxP <= kFusedMaxP) {
+          S.fuseW32 = std::max(1, std::min({S.maxP, budget / b32, kFusedMaxW}));
+          S.fuseW64 = std::max(1, std::min({S.maxP, budget / b64, kFusedMaxW}));
+          if (S.twmI == 32) {
+            cudaFuncSetAttribute(tb_fused<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, S.fuseW32 * b32);
+            cudaFuncSetAttribute(tb_fused<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, S.fuseW64 * b64);
+          } else {
+            cudaFuncSetAttribute(tb_fused<float, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, S.fuseW32 * b32);
+            cudaFuncSetAttribute(tb_fused<double, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, S.fuseW64 * b64);
+          }
+        }
+      }
       int maxs = 0;
       for (int cc = 0; cc < ncomp; ++cc) maxs = std::max(maxs, std::max(kl[cc], ku[cc]));
       S.tmaxs = maxs;
@@ -419,7 +445,7 @@ static void analyse(mgpu_ctx* c, Solver& S) {
       good = good && upv(&S.d_ti, ti) && upv(&S.d_tiT, tiT) && upv(&S.d_ts, ts) && upv(&S.i_rbase, irb) &&
              upv(&S.i_lbase, ilb) && upv(&S.i_n, in_) && upv(&S.i_kl, ikl) && upv(&S.i_ku, iku) &&
              upv(&S.i_dof0, idof) && upv(&S.d_bsep, bsep) && upv(&S.d_brow, brow) && up(&S.tbmap, tbmap) &&
-             up(&S.tbmapT, tbmapT);
+             up(&S.tbmapT, tbmapT) && up(&S.c_int0, cint0) && up(&S.c_sep0, csep0);
       // cyclic-reduction storage: levels 0..L of D, L, U per separator, factors and W per separator
       const size_t nblk = size_t(std::max(S.nsep, 1)) * BCR_SS;
       const size_t ndlu = size_t(S.bcr_levels + 1) * 3 * nblk;
@@ -786,7 +812,7 @@ extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
       info->last_fallback += f[i] != 0;
       info->last_sweeps = std::max(info->last_sweeps, w[i]);
     }
-    if (S.path == PATH_TORN32) info->last_sweeps = S.nrefine;
+    if (S.path == PATH_TORN32 && !S.fuseW32) info->last_sweeps = S.nrefine;
   }
   return MGPU_OK;
 }
@@ -882,7 +908,7 @@ extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
                 S->FA, S->WL, S->WU, S->PV, S->trhs, S->txs, S->tpiv, S->TALL32, S->TUC32, S->TLM32, S->TY32,
                 S->DLU32, S->FA32, S->WL32, S->WU32, S->i_comp,
                 S->iflag, S->nbad, S->info32, S->dtmp, S->rtmp, S->rptr, S->rq, S->rcol, S->dcolptr,
-                S->drowval, S->list32, S->list64, S->lulist[0], S->lulist[1], S->lulist[2], S->lulist[3]};
+                S->drowval, S->c_int0, S->c_sep0, S->list32, S->list64, S->lulist[0], S->lulist[1], S->lulist[2], S->lulist[3]};
   for (void* p : ps) cudaFree(p);
   if (S->hbuf) cudaFreeHost(S->hbuf);
   delete S;
@@ -1007,7 +1033,64 @@ static void torn_apply(mgpu_ctx* c, bool tr, const double* rhs, double* out, con
   bcr_root_solve<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, B.fa, S.PV, S.d_brow, S.trhs, S.txs, cflag);
   for (int l = S.bcr_levels - 1; l >= 0; --l)
     bcr_back<T><<<S.nsep, 32, 0, st>>>(S.nsep, S.d_bsep, l, B.wl, B.wu, S.d_brow, S.txs, cflag);
-  tb_back<T><<<S.nint, 128, 0, st>>>(S.nint, ti, S.d_ts, B.y, S.perm, S.txs, out, cflag);
+  tb_back<T><<<S.nint, 32, 0, st>>>(S.nint, ti, S.d_ts, B.y, S.perm, S.txs, out, cflag);
+}
+
+// Fused per-component partitioned solve (band_torn.cuh tb_fused): nref
+// sweeps of refinement around the factors of torn_factor<T> (nref = 1 with
+// d == x: a plain solve).
+template <typename T>
+static void torn_fused(mgpu_ctx* c, bool tr, const double* rhs, double* out, int nref, const int* only, int* flag,
+                       int* nsweep, int* nbad) {
+  Solver& S = *c->solver;
+  const TornBufs<T> B = torn_bufs(S, static_cast<T*>(nullptr));
+  TbFusedArgs A{};
+  A.ncomp = S.ncomp;
+  A.cint0 = S.c_int0;
+  A.csep0 = S.c_sep0;
+  A.cpI = tr ? RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_ku, S.i_kl, S.i_dof0}
+             : RbComp{S.i_rbase, S.i_lbase, S.i_n, S.i_kl, S.i_ku, S.i_dof0};
+  A.ti = tr ? S.d_tiT : S.d_ti;
+  A.ts = S.d_ts;
+  A.bs = S.d_bsep;
+  A.nsep = S.nsep;
+  A.perm = S.perm;
+  A.tpiv = S.tpiv;
+  A.brow = S.d_brow;
+  A.tall = S.TALL;
+  A.tb_rows = S.tb_rows;
+  A.bw = S.bw;
+  A.xw = S.xw;
+  A.rw = S.rw;
+  A.trhs = S.trhs;
+  A.txs = S.txs;
+  A.rhs = rhs;
+  A.out = out;
+  A.ccn = S.cn;
+  A.ccdof0 = S.cdof0;
+  A.nref = nref;
+  A.tol_stop = 1e-12;
+  A.tol_ok = 1e-10;
+  A.only = only;
+  A.flag = flag;
+  A.nsweep = nsweep;
+  A.nbad = nbad;
+  TbFusedFactors<T> F{};
+  F.UC = B.uc;
+  F.LM = B.lm;
+  F.blk = B.rows + S.tb_rows;
+  F.Y = B.y;
+  F.FA = B.fa;
+  F.DLU = B.dlu;
+  F.WL = B.wl;
+  F.WU = B.wu;
+  F.PV = S.PV;
+  F.tw = sizeof(T) == 4 ? reinterpret_cast<T*>(S.tw32) : reinterpret_cast<T*>(S.tw64);
+  const int W = sizeof(T) == 4 ? S.fuseW32 : S.fuseW64;
+  if (S.twmI == 32)
+    tb_fused<T, 32><<<S.ncomp, 32 * W, size_t(W) * tb_fused_warp_bytes<T, 32>(), c->stream>>>(A, F);
+  else
+    tb_fused<T, 64><<<S.ncomp, 32 * W, size_t(W) * tb_fused_warp_bytes<T, 64>(), c->stream>>>(A, F);
 }
 
 // Partitioned solve of Lλx (or its transpose) x = rhs.  FP64 directly, or
@@ -1022,13 +1105,27 @@ static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int*
   const bool mixed = S.path == PATH_TORN32;
   rb_gather<<<nb(c->pat.nnz, 256), 256, 0, st>>>(c->pat.nnz, tr ? S.tbmapT : S.tbmap, c->nzval, S.TALL,
                                                  mixed ? S.TALL32 : nullptr);
+  const bool fused = S.fuseW32 > 0;
   if (!mixed) {
     torn_factor<double>(c, tr, nullptr, info);
-    torn_apply<double>(c, tr, rhs, out, nullptr);
+    if (fused)
+      torn_fused<double>(c, tr, rhs, out, 1, nullptr, nullptr, nullptr, nullptr);
+    else
+      torn_apply<double>(c, tr, rhs, out, nullptr);
     MG_CUDA(cudaGetLastError());
     return MGPU_OK;
   }
   torn_factor<float>(c, tr, nullptr, S.info32);
+  if (fused) {
+    // sweeps with an early stop per component, the check, then FP64 for the flagged components
+    MG_CUDA(cudaMemsetAsync(S.nbad, 0, sizeof(int), st));
+    torn_fused<float>(c, tr, rhs, out, S.nrefine, nullptr, S.flag, S.nsweep, S.nbad);
+    tb_expand_flags<<<nb(S.nint, 256), 256, 0, st>>>(S.nint, S.i_comp, S.flag, S.iflag);
+    torn_factor<double>(c, tr, S.flag, info);
+    torn_fused<double>(c, tr, rhs, out, 1, S.flag, nullptr, nullptr, nullptr);
+    MG_CUDA(cudaGetLastError());
+    return MGPU_OK;
+  }
   MG_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), st));
   const double* r = rhs;
   for (int sweep = 0; sweep < S.nrefine; ++sweep) {

@@ -14,6 +14,8 @@ namespace mgpu {
 constexpr int kNormBlocks = 128;
 constexpr int64_t kTornMinDofs = 512;  // components shorter than this are factorised whole
 constexpr int kInfoSlots = 64;  // a captured step holds up to kInfoSlots-1 iterations
+constexpr int kFusedMaxP = 32;  // the fused per-component partitioned solve takes components of up to 32 interiors
+constexpr int kFusedMaxW = 13;  // and runs at most 13 warps per block (two blocks per SM at <= 78 registers)
 
 enum SolverPath : int {
   PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
@@ -76,6 +78,9 @@ struct Solver {
   float *TALL32 = nullptr, *TUC32 = nullptr, *TLM32 = nullptr, *TY32 = nullptr;
   float *DLU32 = nullptr, *FA32 = nullptr, *WL32 = nullptr, *WU32 = nullptr;
   int32_t* i_comp = nullptr;                     // component of each interior
+  int32_t *c_int0 = nullptr, *c_sep0 = nullptr;  // [ncomp+1] first interior / separator of each component
+  int maxP = 0;                                  // most interiors in one component
+  int fuseW32 = 0, fuseW64 = 0;                  // warps per block of the fused per-component solve, 0: off
   int* iflag = nullptr;                          // fallback flags per interior
   int* nbad = nullptr;                           // components whose FP32 refinement fell short
   int* info32 = nullptr;                         // zero pivots of the FP32 factorisation (caught by the check)

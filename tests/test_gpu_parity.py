@@ -369,6 +369,45 @@ def test_partitioned_fp32_falls_back_on_an_ill_conditioned_chain():
     assert np.array_equal(a, b)
 
 
+def test_fused_partitioned_solve_is_bitwise_the_level_by_level_one(monkeypatch):
+    """Components of few interiors are solved by one block each (interiors,
+    cyclic reduction and back-substitution behind block barriers); the
+    arithmetic is that of the one-launch-per-level kernels, bit for bit, for
+    Lλx and for its transpose."""
+    m, times = W.risers(nriser=3, nel=100)
+    st = m.initialize(time=0.0)
+    a, _ = _sweep(m, st, 2, times[:6], "torn", fixed_iter=3)
+    d = W.adjoint_beam(nel=120, nstep=6)
+    ma = d["model"]
+    sa = ma.initialize(time=0.0)
+    y = np.zeros((6, len(d["sensors"])))
+
+    def adj():
+        dm = DeviceModel(ma, sa.dis, linsolve="torn")
+        r = dm.adjoint(2, d["times"], sa.time, list(sa.X), d["sensors"], 1.0, y, maxdx=1e-7)
+        dm.close()
+        return r
+
+    ga = adj()
+    monkeypatch.setenv("MGPU_TORN_FUSED", "0")
+    b, _ = _sweep(m, st, 2, times[:6], "torn", fixed_iter=3)
+    gb = adj()
+    assert np.array_equal(a, b)
+    assert ga[0] == gb[0] and np.array_equal(ga[1], gb[1])
+
+
+def test_fused_partitioned_fp32_falls_back_on_an_ill_conditioned_chain():
+    """The fused FP32 refinement flags a component it cannot refine (a slender
+    cantilever, about 20 interiors); its FP64 solve is the FP64 one."""
+    m, _ = W.cantilever(nel=200, length=300.0, load=1e-4)
+    st = m.initialize()
+    times = np.array([0.5, 1.0])
+    a, ia = _sweep(m, st, 0, times, "torn32", fixed_iter=2)
+    b, _ = _sweep(m, st, 0, times, "torn", fixed_iter=2)
+    assert ia["last_fallback"] == 1
+    assert np.array_equal(a, b)
+
+
 def test_partitioned_solver_static_cantilever_matches_oracle():
     from muscade_gpu import SweepXGPU, solve
 
