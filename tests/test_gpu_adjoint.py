@@ -136,3 +136,28 @@ def test_static_adjoint_matches_central_differences():
     fd = np.array(fd)
     assert np.max(np.abs(gA[idx] - fd)) <= TOL_FD * np.max(np.abs(fd)), (gA[idx], fd)
     dm.close()
+
+
+def test_static_adjoint_matches_directxua():
+    """The device static adjoint against the DirectXUA restatement
+    (oracle/directxua.py): both are the stationarity conditions of
+    Σ cost + Λ·R with the loads given and A held, so the gradients agree to
+    rounding.  DirectXUA's Lagrangian carries Δt per step, the static adjoint
+    weight 1."""
+    from oracle import directxua as DX
+    from test_directxua import MAXDX as MAXDX_DX
+    from test_directxua import _problem as dx_problem
+
+    d = dx_problem()
+    m, st = d["model"], d["st"]
+    A0 = np.ones(len(st.A))
+    s = st.copy()
+    s.A = A0.copy()
+    C_dx, g_dx, X_dx = DX.directxua_static(m, s.dis, s, d["times"], d["sensors"], d["w"], d["y"], maxdx=MAXDX_DX,
+                                          maxdl=np.inf)
+    dm = DeviceModel(m, st.dis)
+    dm.set_A(A0)
+    C, gA, _, _ = dm.adjoint(0, d["times"], s.time, list(s.X), d["sensors"], d["w"], d["y"], maxdx=MAXDX_DX)
+    dm.close()
+    assert d["dt"] * C == pytest.approx(C_dx, rel=1e-9)
+    assert np.max(np.abs(d["dt"] * gA - g_dx)) <= 1e-8 * np.max(np.abs(g_dx))
