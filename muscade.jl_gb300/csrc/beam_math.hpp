@@ -95,7 +95,7 @@ MG_HD void scac_derivs(real x, real f[4]) {
 // Rodrigues(v) = I + sinc1(θ) S + ½ sinc1(θ/2)² S²,  θ = norm3(v)   (Rotations.jl:131-135)
 template <bool D>
 MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
-  const TJ<D> s2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const TJ<D> s2 = tj_dot3(v, v);
   TJ<D> A, B;
   const real th = sqrt(s2.v);
   if (th < 1e-14) {  // norm3 returns an exact zero: sinc1 terms become constants
@@ -107,16 +107,19 @@ MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
     const TJ<D> t = tj_apply(s2, th, 0.5 * r, -0.25 * r * r * r, 0.375 * r * r * r * r * r);
     A = tj_apply(t, sinc1_0(th), sinc1_1(th), sinc1_2(th), sinc1_3(th));
     const real h = 0.5 * th;
-    const TJ<D> sh = tj_apply(t, sinc1_0(h), 0.5 * sinc1_1(h), 0.25 * sinc1_2(h), 0.125 * sinc1_3(h));
-    B = (sh * sh) * 0.5;
+    // B = ½ sh² with sh = sinc1(θ/2); the ½ is taken into sh as 1/√2
+    const real k = 0.70710678118654752440;
+    const TJ<D> sh = tj_apply(t, k * sinc1_0(h), k * 0.5 * sinc1_1(h), k * 0.25 * sinc1_2(h), k * 0.125 * sinc1_3(h));
+    B = sh * sh;
   }
   // S = spin(v): S[2,1]=v3, S[3,1]=-v2, S[1,2]=-v3, S[3,2]=v1, S[1,3]=v2, S[2,3]=-v1
   // S² = v vᵀ - |v|² I  (spin², Rotations.jl:114-122)
   const TJ<D> ab = v[0] * v[1], ca = v[2] * v[0], bc = v[1] * v[2];
   const TJ<D> aa = v[0] * v[0], bb = v[1] * v[1], cc = v[2] * v[2];
-  R[0] = B * (-(bb + cc)) + 1.0;
-  R[4] = B * (-(aa + cc)) + 1.0;
-  R[8] = B * (-(aa + bb)) + 1.0;
+  const TJ<D> one = tj_const<D>(1.0);
+  R[0] = tj_fnma(B, bb + cc, one);
+  R[4] = tj_fnma(B, aa + cc, one);
+  R[8] = tj_fnma(B, aa + bb, one);
   const TJ<D> Bab = B * ab, Bca = B * ca, Bbc = B * bc;
   const TJ<D> Av0 = A * v[0], Av1 = A * v[1], Av2 = A * v[2];
   R[1] = Av2 + Bab;   // [2,1]
@@ -129,35 +132,39 @@ MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
 
 // Rodrigues⁻¹(m) = spin⁻¹(m) / scac((tr m − 1)/2)   (Rotations.jl:105)
 template <bool D>
-MG_HD void rodrigues_inv(const TJ<D> m[9], TJ<D> w[3]) {
+MG_HD void rodrigues_inv(const TJ<D> m[9], TJ<D> w[3], real scale = 1.0) {
   const TJ<D> c = (m[0] + m[4] + m[8] + (-1.0)) * 0.5;
   real f[4];
   scac_derivs(c.v, f);
   const TJ<D> s = tj_apply(c, f[0], f[1], f[2], f[3]);
   const real iv = 1.0 / s.v;
-  const TJ<D> is = tj_apply(s, iv, -iv * iv, 2.0 * iv * iv * iv, -6.0 * iv * iv * iv * iv);
-  w[0] = ((m[5] - m[7]) * 0.5) * is;  // (m32 - m23)/2
-  w[1] = ((m[6] - m[2]) * 0.5) * is;  // (m13 - m31)/2
-  w[2] = ((m[1] - m[3]) * 0.5) * is;  // (m21 - m12)/2
+  // ½ scale / s, the ½ of spin⁻¹ and the caller's scale taken into the composition
+  const real q = 0.5 * scale;
+  const TJ<D> is = tj_apply(s, q * iv, -q * iv * iv, q * 2.0 * iv * iv * iv, -q * 6.0 * iv * iv * iv * iv);
+  w[0] = (m[5] - m[7]) * is;  // (m32 - m23)/2
+  w[1] = (m[6] - m[2]) * is;  // (m13 - m31)/2
+  w[2] = (m[1] - m[3]) * is;  // (m21 - m12)/2
 }
 
 // C = A Bᵀ  (both Taylor)
 template <bool D>
 MG_HD void mul_abt(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) C[i + 3 * j] = A[i] * B[j] + A[i + 3] * B[j + 3] + A[i + 6] * B[j + 6];
+    for (int j = 0; j < 3; ++j) C[i + 3 * j] = tj_fma(A[i + 6], B[j + 6], tj_fma(A[i + 3], B[j + 3], A[i] * B[j]));
 }
 // C = A B
 template <bool D>
 MG_HD void mul_ab(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[1 + 3 * j] + A[i + 6] * B[2 + 3 * j];
+    for (int j = 0; j < 3; ++j)
+      C[i + 3 * j] = tj_fma(A[i + 6], B[2 + 3 * j], tj_fma(A[i + 3], B[1 + 3 * j], A[i] * B[3 * j]));
 }
 // C = A M with M a constant matrix
 template <bool D>
 MG_HD void mul_ac(const TJ<D> A[9], const double M[9], TJ<D> C[9]) {
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) C[i + 3 * j] = A[i] * M[3 * j] + A[i + 3] * M[1 + 3 * j] + A[i + 6] * M[2 + 3 * j];
+    for (int j = 0; j < 3; ++j)
+      C[i + 3 * j] = tj_fma(A[i + 6], real(M[2 + 3 * j]), tj_fma(A[i + 3], real(M[1 + 3 * j]), A[i] * real(M[3 * j])));
 }
 
 // ---- per-element constants, precomputed at create time ----------------------
@@ -213,9 +220,7 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
     rodrigues(v1, r1);
     rodrigues(v2, r2);
     mul_abt(r2, r1, Q);
-    TJ<D> wv[3];
-    rodrigues_inv(Q, wv);
-    for (int i = 0; i < 3; ++i) dv[i] = wv[i] * 0.5;
+    rodrigues_inv(Q, dv, 0.5);  // Δv = ½ Rodrigues⁻¹(r₂r₁ᵀ)
   }
   {
     TJ<D> rD[9], rs[9];
@@ -239,9 +244,9 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   const real eps = dn * 2.0 / c.L - 1.0;
 
   // ---- strain measures
-  const TJ<D> th_t = dot3(t, dv), th_n = dot3(n, dv), th_b = dot3(b, dv);
-  const TJ<D> w_n = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
-  const TJ<D> w_b = b[0] * d[0] + b[1] * d[1] + b[2] * d[2];
+  const TJ<D> th_t = tj_dot3(t, dv), th_n = tj_dot3(n, dv), th_b = tj_dot3(b, dv);
+  const TJ<D> w_n = tj_dot3(n, d);
+  const TJ<D> w_b = tj_dot3(b, d);
   // frozen stresses σ = ∂Π/∂q
   const real s_e = c.ke * eps;
   const real s_t = c.kt * th_t.v;
@@ -259,12 +264,12 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
       dT[i].vtt = 0.5 * dd2[i];
     }
   }
-  const TJ<D> td = dot3(t, dT);
+  const TJ<D> td = tj_dot3(t, dT);
   TJ<D> mv[3], wv[3];  // m = (t·d) t,  w = Δv × t
   for (int i = 0; i < 3; ++i) mv[i] = td * t[i];
-  wv[0] = dv[1] * t[2] - dv[2] * t[1];
-  wv[1] = dv[2] * t[0] - dv[0] * t[2];
-  wv[2] = dv[0] * t[1] - dv[1] * t[0];
+  wv[0] = tj_fnma(dv[2], t[1], dv[1] * t[2]);
+  wv[1] = tj_fnma(dv[0], t[2], dv[2] * t[0]);
+  wv[2] = tj_fnma(dv[1], t[0], dv[0] * t[1]);
 
   // ---- loads per Gauss point (frozen) and their sums
   real fg[4][3];
@@ -335,16 +340,17 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
     for (int i = 0; i < 3; ++i) me[i] = c.S0 * c.iota1 * vi21 * r0[i];
 
   // ---- Φ_v: scalar with frozen multipliers, Taylor in the rotation dofs
-  TJ<D> Phi = th_t * s_t + th_n * s_n + th_b * s_b + w_n * s_wn + w_b * s_wb;
+  TJ<D> Phi = tj_fma(w_b, s_wb, tj_fma(w_n, s_wn, tj_fma(th_b, s_b, tj_fma(th_n, s_n, th_t * s_t))));
   {
-    const TJ<D> tAa = t[0] * Aa[0] + t[1] * Aa[1] + t[2] * Aa[2];
-    const TJ<D> tdv = t[0] * d[0] + t[1] * d[1] + t[2] * d[2];
-    Phi = Phi + tdv * tAa + (wv[0] * Av[0] + wv[1] * Av[1] + wv[2] * Av[2]);
-    if (rotinertia) Phi = Phi + (vsm[0] * me[0] + vsm[1] * me[1] + vsm[2] * me[2]);
+    const TJ<D> tAa = tj_dot3(t, Aa);
+    const TJ<D> tdv = tj_dot3(t, d);
+    Phi = tj_fma(tdv, tAa, Phi);
+    Phi = tj_fma(wv[2], Av[2], tj_fma(wv[1], Av[1], tj_fma(wv[0], Av[0], Phi)));
+    if (rotinertia) Phi = tj_fma(vsm[2], me[2], tj_fma(vsm[1], me[1], tj_fma(vsm[0], me[0], Phi)));
     // P = ∂Φ/∂d (value and rotation gradient)
     TJ<D> P[3];
     for (int i = 0; i < 3; ++i)
-      P[i] = n[i] * s_wn + b[i] * s_wb + tAa * t[i] + (s_e * 2.0 / c.L * dh[i] + Au[i]);
+      P[i] = tj_fma(n[i], s_wn, tj_fma(b[i], s_wb, tAa * t[i])) + (s_e * 2.0 / c.L * dh[i] + Au[i]);
     // residual
     for (int i = 0; i < 3; ++i) {
       R[i] = to_d(-0.5 * P[i].v + 0.5 * A0[i]);
