@@ -107,6 +107,19 @@ int64_t mgpu_ntval(const mgpu_ctx *ctx);
 int mgpu_assemble(mgpu_ctx *ctx, int32_t mission, int32_t nXder, const double *x, const double *u, double t,
                   const double *tvals, const mgpu_newmark *c, double *Ll, double *nzval);
 
+/* The same assembly, pipelined: enqueues it and returns a ticket.  The inputs
+ * are copied before the call returns (the caller may reuse x, u, tvals at
+ * once).  Ll and nzval receive the outputs by the time mgpu_assemble_wait
+ * returns for that ticket; until then the caller must leave them alone.  At
+ * most two assemblies are in flight: a third call first waits for the copies
+ * of the oldest.  The outputs of one call are copied back while the next one
+ * computes, so a loop of calls costs the larger of the two, not their sum.
+ * mgpu_assemble_wait takes one of the last two tickets and reports a NaN in
+ * that assembly with the same message as mgpu_assemble. */
+int mgpu_assemble_async(mgpu_ctx *ctx, int32_t mission, int32_t nXder, const double *x, const double *u, double t,
+                        const double *tvals, const mgpu_newmark *c, double *Ll, double *nzval, int64_t *ticket);
+int mgpu_assemble_wait(mgpu_ctx *ctx, int64_t ticket);
+
 /* Element-level evaluation like diffed_residual (src/Diagnostic.jl:929-965)
  * for the elements of group `igroup`:  X[nele][nXder][nX], U[nele][nU].
  * Returns R[nele][nX] and, per element, dR[nele][nX][nX] (column-major per

@@ -67,6 +67,18 @@ struct mgpu_ctx {
   double* hstepc = nullptr;  // pinned upload ring [kStepcSlots][8]
   cudaEvent_t stepc_ev[8] = {};
   int stepc_slot = 0;
+  // pipelined assembly (mgpu_assemble_async): two slots of device outputs and
+  // host input staging; a copy stream returns each slot's outputs while the
+  // next slot computes
+  cudaStream_t cstream = nullptr;
+  double* anz[2] = {nullptr, nullptr};   // [nnz] device outputs per slot
+  double* aLl[2] = {nullptr, nullptr};   // [nX]
+  int* aerr = nullptr;                   // [2] device NaN flags per slot
+  int* haerr = nullptr;                  // [2] pinned host copies
+  double* astage[2] = {nullptr, nullptr};  // pinned host staging: x [3nX], u [nU], tvals [ntval]
+  cudaEvent_t a_h2d[2] = {}, a_comp[2] = {}, a_d2h[2] = {};
+  bool a_used[2] = {false, false};
+  int64_t aticket = 0;
 };
 
 namespace mgpu {

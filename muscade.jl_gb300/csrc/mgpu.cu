@@ -578,10 +578,19 @@ extern "C" void mgpu_destroy(mgpu_ctx* c) {
     cudaFree(G.aidx);
     cudaFree(G.cdata);
   }
+  if (c->cstream) cudaStreamSynchronize(c->cstream);
   void* ps[] = {c->kbuf, c->rbuf, c->mseg, c->msrc, c->vseg, c->vsrc, c->nzval, c->Ll, c->x,
-                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush, c->stepc, c->Avec};
+                c->u,    c->tv,   c->ab,   c->scale, c->errflag, c->flush, c->stepc, c->Avec,
+                c->anz[0], c->anz[1], c->aLl[0], c->aLl[1], c->aerr};
   for (void* p : ps) cudaFree(p);
   if (c->hstepc) cudaFreeHost(c->hstepc);
+  for (double* h : c->astage)
+    if (h) cudaFreeHost(h);
+  if (c->haerr) cudaFreeHost(c->haerr);
+  for (int k = 0; k < 2; ++k)
+    for (cudaEvent_t e : {c->a_h2d[k], c->a_comp[k], c->a_d2h[k]})
+      if (e) cudaEventDestroy(e);
+  if (c->cstream) cudaStreamDestroy(c->cstream);
   for (cudaEvent_t e : c->stepc_ev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -666,6 +675,85 @@ extern "C" int mgpu_assemble(mgpu_ctx* c, int32_t mission, int32_t nXder, const 
   MG_TRY(mgpu_upload_state(c, nXder, x, u, tvals));
   MG_TRY(mgpu_assemble_resident(c, mission, t, nm));
   return mgpu_download(c, Ll, nzval);
+}
+
+// Pipelined assembly.  Slot s = ticket mod 2 owns a device copy of the outputs
+// (nzval, Lλ, NaN flag) and a page-locked staging area for the inputs.  The
+// compute stream uploads the staged inputs into the resident state, assembles
+// into the slot's outputs and records a_comp[s]; the copy stream then returns
+// them to the caller's buffers and records a_d2h[s].  Slot s is reused two calls
+// later, after its copies are done (host wait on a_h2d[s] before restaging,
+// stream wait on a_d2h[s] before assembling into it again).
+static int async_setup(mgpu_ctx* c) {
+  if (c->cstream) return MGPU_OK;
+  MG_CUDA(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking));
+  const size_t nst = size_t(3 * c->nX + c->nU + c->ntval);
+  for (int k = 0; k < 2; ++k) {
+    MG_CUDA(cudaMalloc(&c->anz[k], std::max<int64_t>(c->pat.nnz, 1) * sizeof(double)));
+    MG_CUDA(cudaMalloc(&c->aLl[k], std::max<int64_t>(c->nX, 1) * sizeof(double)));
+    MG_CUDA(cudaMallocHost(&c->astage[k], std::max<size_t>(nst, 1) * sizeof(double)));
+    MG_CUDA(cudaEventCreateWithFlags(&c->a_h2d[k], cudaEventDisableTiming));
+    MG_CUDA(cudaEventCreateWithFlags(&c->a_comp[k], cudaEventDisableTiming));
+    MG_CUDA(cudaEventCreateWithFlags(&c->a_d2h[k], cudaEventDisableTiming));
+  }
+  MG_CUDA(cudaMalloc(&c->aerr, 2 * sizeof(int)));
+  MG_CUDA(cudaMallocHost(&c->haerr, 2 * sizeof(int)));
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_assemble_async(mgpu_ctx* c, int32_t mission, int32_t nXder, const double* x, const double* u,
+                                   double t, const double* tvals, const mgpu_newmark* nm, double* Ll, double* nzval,
+                                   int64_t* ticket) {
+  if (!c || !x || nXder < 1 || nXder > 3 || mission < 0 || mission > 2 || (mission != MGPU_ASM_STATIC && !nm))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_assemble_async: bad arguments");
+  MG_CUDA(cudaSetDevice(c->device));
+  MG_TRY(async_setup(c));
+  const int64_t tk = c->aticket++;
+  const int s = int(tk & 1);
+  // the staging area and the outputs of this slot are free once its previous copies are done
+  if (c->a_used[s]) MG_CUDA(cudaEventSynchronize(c->a_h2d[s]));
+  double* st = c->astage[s];
+  std::memcpy(st, x, size_t(nXder) * c->nX * sizeof(double));
+  double* su = st + 3 * c->nX;
+  double* stv = su + c->nU;
+  if (c->nU > 0 && u) std::memcpy(su, u, c->nU * sizeof(double));
+  if (c->ntval > 0 && tvals) std::memcpy(stv, tvals, c->ntval * sizeof(double));
+  if (c->a_used[s]) MG_CUDA(cudaStreamWaitEvent(c->stream, c->a_d2h[s], 0));
+  MG_TRY(mgpu_upload_state(c, nXder, st, (c->nU > 0 && u) ? su : nullptr, (c->ntval > 0 && tvals) ? stv : nullptr));
+  MG_CUDA(cudaEventRecord(c->a_h2d[s], c->stream));
+  MG_TRY(upload_stepc(c, t, mission != MGPU_ASM_STATIC ? nm : nullptr));
+  // assemble into this slot's outputs (the kernels take the pointers at launch)
+  double* nz0 = c->nzval;
+  double* Ll0 = c->Ll;
+  int* err0 = c->errflag;
+  c->nzval = c->anz[s];
+  c->Ll = c->aLl[s];
+  c->errflag = c->aerr + s;
+  launch_reset_errflag(c);
+  const int rc = launch_assembly(c, mission, nullptr, 1.0);
+  c->nzval = nz0;
+  c->Ll = Ll0;
+  c->errflag = err0;
+  if (rc) return rc;
+  MG_CUDA(cudaEventRecord(c->a_comp[s], c->stream));
+  MG_CUDA(cudaStreamWaitEvent(c->cstream, c->a_comp[s], 0));
+  if (Ll) MG_CUDA(cudaMemcpyAsync(Ll, c->aLl[s], c->nX * sizeof(double), cudaMemcpyDeviceToHost, c->cstream));
+  if (nzval)
+    MG_CUDA(cudaMemcpyAsync(nzval, c->anz[s], c->pat.nnz * sizeof(double), cudaMemcpyDeviceToHost, c->cstream));
+  MG_CUDA(cudaMemcpyAsync(c->haerr + s, c->aerr + s, sizeof(int), cudaMemcpyDeviceToHost, c->cstream));
+  MG_CUDA(cudaEventRecord(c->a_d2h[s], c->cstream));
+  c->a_used[s] = true;
+  if (ticket) *ticket = tk;
+  return MGPU_OK;
+}
+
+extern "C" int mgpu_assemble_wait(mgpu_ctx* c, int64_t ticket) {
+  if (!c || ticket < 0 || ticket >= c->aticket || ticket < c->aticket - 2)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_assemble_wait: ticket is not one of the last two assemblies");
+  MG_CUDA(cudaSetDevice(c->device));
+  const int s = int(ticket & 1);
+  MG_CUDA(cudaEventSynchronize(c->a_d2h[s]));
+  return nan_error(c, c->haerr[s]);
 }
 
 extern "C" int mgpu_time_assemble(mgpu_ctx* c, int32_t mission, double t, const mgpu_newmark* nm, int32_t reps,

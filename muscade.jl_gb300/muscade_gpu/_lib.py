@@ -104,7 +104,8 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_ntval", "mgpu_assemble", "mgpu_element_eval", "mgpu_upload_state", "mgpu_assemble_resident",
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
-           "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune"]
+           "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune",
+           "mgpu_assemble_async", "mgpu_assemble_wait"]
 
 _lib = None
 
@@ -133,6 +134,8 @@ def load():
     L.mgpu_get_pattern.argtypes = [vp, pi64, pi64]
     L.mgpu_get_asm.argtypes = [vp, i32, pi64, pi64]
     L.mgpu_assemble.argtypes = [vp, i32, i32, pd, pd, d, pd, P(Newmark), pd, pd]
+    L.mgpu_assemble_async.argtypes = [vp, i32, i32, pd, pd, d, pd, P(Newmark), pd, pd, pi64]
+    L.mgpu_assemble_wait.argtypes = [vp, i64]
     L.mgpu_element_eval.argtypes = [vp, i32, i32, pd, pd, d, d, d, d, pd, pd, pd]
     L.mgpu_upload_state.argtypes = [vp, i32, pd, pd, pd]
     L.mgpu_assemble_resident.argtypes = [vp, i32, d, P(Newmark)]

@@ -35,6 +35,7 @@ class DeviceModel:
     def __init__(self, model, dis, device: int = 0, linsolve: str = "auto"):
         self.lib = L.load()
         self._registered = []
+        self._aticket = 0
         self.model, self.dis = model, dis
         self.nX, self.nU = model.ndof["X"], model.ndof["U"]
         self._keep = []
@@ -212,6 +213,30 @@ class DeviceModel:
                                     ctypes.byref(nm), L.ptr(Ll), L.ptr(nz))
         self._check(rc)
         return Ll, nz
+
+    def assemble_async(self, X, U=None, t=0.0, mission=L.ASM_STATIC, c=None, want=(True, True)):
+        """Pipelined assembly (mgpu_assemble_async): enqueues one assembly and
+        returns (ticket, Lλ, nzval) without waiting.  The arrays are page-locked
+        buffers of the ticket's slot (two slots, alternating), valid after
+        assemble_wait(ticket) and overwritten two calls later."""
+        X = [np.ascontiguousarray(x, dtype=np.float64) for x in X]
+        x = X[0] if len(X) == 1 else np.concatenate(X)
+        u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
+        tv = self.tvals(t)
+        nm = L.Newmark(**(c or {})) if c else L.Newmark()
+        slot = self._aticket & 1
+        Ll = self._pinned(f"_aLout{slot}", self.nX) if want[0] else None
+        nz = self._pinned(f"_anzout{slot}", self.nnz) if want[1] else None
+        tk = ctypes.c_int64()
+        rc = self.lib.mgpu_assemble_async(self.ctx, mission, len(X), L.ptr(x), L.ptr(u), float(t), L.ptr(tv),
+                                          ctypes.byref(nm), L.ptr(Ll), L.ptr(nz), ctypes.byref(tk))
+        self._check(rc)
+        self._aticket = tk.value + 1
+        return tk.value, Ll, nz
+
+    def assemble_wait(self, ticket):
+        """Waits for the outputs of a pipelined assembly (one of the last two tickets)."""
+        self._check(self.lib.mgpu_assemble_wait(self.ctx, int(ticket)))
 
     def element_eval(self, ig, X, U=None, t=0.0, p=(1.0, 0.0, 0.0)):
         """diffed_residual-like evaluation of all elements of group ig.

@@ -454,6 +454,39 @@ def test_autotune_keeps_a_faster_configuration_with_the_same_results():
         assert _rel_dev(a[:, d][:, ~lam], ref[:, d][:, ~lam]) <= TOL_STATE, d
 
 
+def test_pipelined_assembly_is_bitwise_the_synchronous_one():
+    """mgpu_assemble_async/wait: five steps of different states and times with
+    two in flight (both slots reused) give the synchronous call's Lλ and nzval
+    bit for bit, static and Newmark; a NaN is reported at the wait."""
+    m, _ = W.lattice(6, 5, 4)
+    st = m.initialize()
+    dm = DeviceModel(m, st.dis)
+    c = REF.newmark_coefficients(2, 0.05, 0.25, 0.5)
+    cases = [(_state(m, 20 + k, 1), 0.2 * (k + 1), _lib.ASM_STATIC, None) for k in range(3)]
+    cases += [(_state(m, 30 + k, 3), 0.3 + 0.05 * k, mis, c) for k, mis in enumerate((_lib.ASM_STEP, _lib.ASM_ITER))]
+    ref = [tuple(a.copy() for a in dm.assemble(X, t=t, mission=mis, c=cc)) for X, t, mis, cc in cases]
+    got, pending = [], []
+    for X, t, mis, cc in cases:
+        tk, Ll, nz = dm.assemble_async(X, t=t, mission=mis, c=cc)
+        pending.append((tk, Ll, nz))
+        if len(pending) == 2:
+            tk0, Ll0, nz0 = pending.pop(0)
+            dm.assemble_wait(tk0)
+            got.append((Ll0.copy(), nz0.copy()))
+    tk0, Ll0, nz0 = pending.pop(0)
+    dm.assemble_wait(tk0)
+    got.append((Ll0.copy(), nz0.copy()))
+    for (La, na), (Lb, nb) in zip(got, ref):
+        assert np.array_equal(La, Lb) and np.array_equal(na, nb)
+    x = np.zeros(m.ndof["X"])
+    x[7] = np.nan
+    tk, _, _ = dm.assemble_async([x], t=0.1)
+    with pytest.raises(DeviceError) as e:
+        dm.assemble_wait(tk)
+    assert e.value.kind == "nan" and "returned NaN" in str(e.value)
+    dm.close()
+
+
 def test_nan_is_reported_like_the_reference():
     m, _ = W.cantilever()
     st = m.initialize()
