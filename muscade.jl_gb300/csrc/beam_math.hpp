@@ -546,7 +546,8 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
         double* col = (j < 12) ? (K + 12 * j) : rdir;
         if (j == 12 && g == 0)
           for (int a = 0; a < 12; ++a) rdir[a] = 0.0;
-        for (int a = 0; a < 12; ++a) col[a] += to_d(wq * (Jx[0][a] * df[0] + Jx[1][a] * df[1] + Jx[2][a] * df[2]));
+        const real w0 = wq * df[0], w1 = wq * df[1], w2 = wq * df[2];
+        for (int a = 0; a < 12; ++a) col[a] = to_d(fma(Jx[2][a], w2, fma(Jx[1][a], w1, fma(Jx[0][a], w0, real(col[a])))));
       }
     }
   }
