@@ -93,35 +93,35 @@ MG_HD void scac_derivs(real x, real f[4]) {
 
 // ---- rotations in Taylor arithmetic ----------------------------------------
 // Rodrigues(v) = I + sinc1(θ) S + ½ sinc1(θ/2)² S²,  θ = norm3(v)   (Rotations.jl:131-135)
-template <bool D>
-MG_HD void rodrigues(const TJ<D> v[3], TJ<D> R[9]) {
-  const TJ<D> s2 = tj_dot3(v, v);
-  TJ<D> A, B;
+template <bool D, int N>
+MG_HD void rodrigues(const TJ<D, N> v[3], TJ<D, N> R[9]) {
+  const TJ<D, N> s2 = tj_dot3(v, v);
+  TJ<D, N> A, B;
   const real th = sqrt(s2.v);
   if (th < 1e-14) {  // norm3 returns an exact zero: sinc1 terms become constants
-    A = tj_const<D>(1.0);
-    B = tj_const<D>(0.5);
+    A = tj_const<D, N>(1.0);
+    B = tj_const<D, N>(0.5);
   } else {
     const real r = 1.0 / th;
     // θ = √s2
-    const TJ<D> t = tj_apply(s2, th, 0.5 * r, -0.25 * r * r * r, 0.375 * r * r * r * r * r);
+    const TJ<D, N> t = tj_apply(s2, th, 0.5 * r, -0.25 * r * r * r, 0.375 * r * r * r * r * r);
     A = tj_apply(t, sinc1_0(th), sinc1_1(th), sinc1_2(th), sinc1_3(th));
     const real h = 0.5 * th;
     // B = ½ sh² with sh = sinc1(θ/2); the ½ is taken into sh as 1/√2
     const real k = 0.70710678118654752440;
-    const TJ<D> sh = tj_apply(t, k * sinc1_0(h), k * 0.5 * sinc1_1(h), k * 0.25 * sinc1_2(h), k * 0.125 * sinc1_3(h));
+    const TJ<D, N> sh = tj_apply(t, k * sinc1_0(h), k * 0.5 * sinc1_1(h), k * 0.25 * sinc1_2(h), k * 0.125 * sinc1_3(h));
     B = sh * sh;
   }
   // S = spin(v): S[2,1]=v3, S[3,1]=-v2, S[1,2]=-v3, S[3,2]=v1, S[1,3]=v2, S[2,3]=-v1
   // S² = v vᵀ - |v|² I  (spin², Rotations.jl:114-122)
-  const TJ<D> ab = v[0] * v[1], ca = v[2] * v[0], bc = v[1] * v[2];
-  const TJ<D> aa = v[0] * v[0], bb = v[1] * v[1], cc = v[2] * v[2];
-  const TJ<D> one = tj_const<D>(1.0);
+  const TJ<D, N> ab = v[0] * v[1], ca = v[2] * v[0], bc = v[1] * v[2];
+  const TJ<D, N> aa = v[0] * v[0], bb = v[1] * v[1], cc = v[2] * v[2];
+  const TJ<D, N> one = tj_const<D, N>(1.0);
   R[0] = tj_fnma(B, bb + cc, one);
   R[4] = tj_fnma(B, aa + cc, one);
   R[8] = tj_fnma(B, aa + bb, one);
-  const TJ<D> Bab = B * ab, Bca = B * ca, Bbc = B * bc;
-  const TJ<D> Av0 = A * v[0], Av1 = A * v[1], Av2 = A * v[2];
+  const TJ<D, N> Bab = B * ab, Bca = B * ca, Bbc = B * bc;
+  const TJ<D, N> Av0 = A * v[0], Av1 = A * v[1], Av2 = A * v[2];
   R[1] = Av2 + Bab;   // [2,1]
   R[3] = Bab - Av2;   // [1,2]
   R[2] = Bca - Av1;   // [3,1]
@@ -158,6 +158,24 @@ MG_HD void mul_ab(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j)
       C[i + 3 * j] = tj_fma(A[i + 6], B[2 + 3 * j], tj_fma(A[i + 3], B[1 + 3 * j], A[i] * B[3 * j]));
+}
+// C = B Aᵀ with A over node 1's variables and B over node 2's (r₂ r₁ᵀ)
+template <bool D>
+MG_HD void mul_abt_nodes(const TJ<D, 3> B[9], const TJ<D, 3> A[9], TJ<D> C[9]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const TJ<D> z = tj_cross<false>(A[j], B[i], C[0]);  // C[0] is not read without ACC
+      C[i + 3 * j] = tj_cross<true>(A[j + 6], B[i + 6], tj_cross<true>(A[j + 3], B[i + 3], z));
+    }
+}
+// C = A B with B over node 1's variables (r_Δ r₁)
+template <bool D>
+MG_HD void mul_ab_node1(const TJ<D> A[9], const TJ<D, 3> B[9], TJ<D> C[9]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const TJ<D> z = tj_mixA<false>(A[i], B[3 * j], C[0]);
+      C[i + 3 * j] = tj_mixA<true>(A[i + 6], B[2 + 3 * j], tj_mixA<true>(A[i + 3], B[1 + 3 * j], z));
+    }
 }
 // C = A M with M a constant matrix
 template <bool D>
@@ -204,28 +222,31 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
                         Perturb pt, const double* av, const double* bv, double* R, double* K, double* rdir,
                         double* H) {
   // ---- rotation core
-  TJ<D> v1[3], v2[3];
+  // the nodal rotations depend on their own node's three dofs only
+  TJ<D, 3> v1[3], v2[3];
   for (int i = 0; i < 3; ++i) {
     if constexpr (D) {
-      v1[i] = tj_var<D>(X0[3 + i], i, X1[3 + i], X2[3 + i]);
-      v2[i] = tj_var<D>(X0[9 + i], 3 + i, X1[9 + i], X2[9 + i]);
+      v1[i] = tj_var<D, 3>(X0[3 + i], i, X1[3 + i], X2[3 + i]);
+      v2[i] = tj_var<D, 3>(X0[9 + i], i, X1[9 + i], X2[9 + i]);
     } else {
-      v1[i] = tj_var<D>(X0[3 + i], i);
-      v2[i] = tj_var<D>(X0[9 + i], 3 + i);
+      v1[i] = tj_var<D, 3>(X0[3 + i], i);
+      v2[i] = tj_var<D, 3>(X0[9 + i], i);
     }
   }
-  TJ<D> r1[9], rsm[9], dv[3];
+  TJ<D, 3> r1[9];
+  TJ<D> rsm[9], dv[3];
   {
-    TJ<D> r2[9], Q[9];
+    TJ<D, 3> r2[9];
+    TJ<D> Q[9];
     rodrigues(v1, r1);
     rodrigues(v2, r2);
-    mul_abt(r2, r1, Q);
+    mul_abt_nodes(r2, r1, Q);
     rodrigues_inv(Q, dv, 0.5);  // Δv = ½ Rodrigues⁻¹(r₂r₁ᵀ)
   }
   {
     TJ<D> rD[9], rs[9];
     rodrigues(dv, rD);
-    mul_ab(rD, r1, rs);
+    mul_ab_node1(rD, r1, rs);
     mul_ac(rs, c.rm, rsm);
   }
   const TJ<D>* t = rsm;      // first column
