@@ -107,10 +107,10 @@ MG_HD void rodrigues(const TJ<D, N> v[3], TJ<D, N> R[9]) {
     const TJ<D, N> t = tj_apply(s2, th, 0.5 * r, -0.25 * r * r * r, 0.375 * r * r * r * r * r);
     A = tj_apply(t, sinc1_0(th), sinc1_1(th), sinc1_2(th), sinc1_3(th));
     const real h = 0.5 * th;
-    // B = ½ sh² with sh = sinc1(θ/2); the ½ is taken into sh as 1/√2
-    const real k = 0.70710678118654752440;
-    const TJ<D, N> sh = tj_apply(t, k * sinc1_0(h), k * 0.5 * sinc1_1(h), k * 0.25 * sinc1_2(h), k * 0.125 * sinc1_3(h));
-    B = sh * sh;
+    // B(θ) = ½ s(θ/2)² with s = sinc1, composed from its derivatives in θ:
+    // B′ = ½ s s′, B″ = ¼ (s′² + s s″), B‴ = ⅛ (3 s′ s″ + s s‴)
+    const real s0 = sinc1_0(h), s1 = sinc1_1(h), s2d = sinc1_2(h), s3 = sinc1_3(h);
+    B = tj_apply(t, 0.5 * s0 * s0, 0.5 * s0 * s1, 0.25 * fma(s1, s1, s0 * s2d), 0.125 * fma(3.0 * s1, s2d, s0 * s3));
   }
   // S = spin(v): S[2,1]=v3, S[3,1]=-v2, S[1,2]=-v3, S[3,2]=v1, S[1,3]=v2, S[2,3]=-v1
   // S² = v vᵀ - |v|² I  (spin², Rotations.jl:114-122)
@@ -178,8 +178,8 @@ MG_HD void mul_ab_node1(const TJ<D> A[9], const TJ<D, 3> B[9], TJ<D> C[9]) {
     }
 }
 // C = A M with M a constant matrix
-template <bool D>
-MG_HD void mul_ac(const TJ<D> A[9], const double M[9], TJ<D> C[9]) {
+template <bool D, int N>
+MG_HD void mul_ac(const TJ<D, N> A[9], const double M[9], TJ<D, N> C[9]) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j)
       C[i + 3 * j] = tj_fma(A[i + 6], real(M[2 + 3 * j]), tj_fma(A[i + 3], real(M[1 + 3 * j]), A[i] * real(M[3 * j])));
@@ -244,10 +244,12 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
     rodrigues_inv(Q, dv, 0.5);  // Δv = ½ Rodrigues⁻¹(r₂r₁ᵀ)
   }
   {
-    TJ<D> rD[9], rs[9];
+    // rₛₘ = r_Δ (r₁ rₘ): the constant frame goes into the node-1 value first
+    TJ<D> rD[9];
+    TJ<D, 3> r1m[9];
+    mul_ac(r1, c.rm, r1m);
     rodrigues(dv, rD);
-    mul_ab_node1(rD, r1, rs);
-    mul_ac(rs, c.rm, rsm);
+    mul_ab_node1(rD, r1m, rsm);
   }
   const TJ<D>* t = rsm;      // first column
   const TJ<D>* n = rsm + 3;  // second column
@@ -412,7 +414,11 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
         K[(6 + k) + 12 * l] -= to_d(h);
       }
   }
-  // ---- material part Gᵀ D G over q = (ε, θt, θn, θb, wn, wb)
+  // ---- material part Gᵀ D G over q = (ε, θt, θn, θb, wn, wb).  Row 0 of G (ε)
+  // is zero on the rotation dofs and rows 1-3 (θ) on the translation dofs, and
+  // D is symmetric: the upper triangle is summed over the rows that are nonzero
+  // at its row dof (3 at a translation dof, 5 at a rotation dof), p0 taken
+  // into D G, and mirrored.
   {
     real G[6][12];
     for (int q = 0; q < 6; ++q)
@@ -433,18 +439,41 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
       G[4][a] = w_n.g[j];
       G[5][a] = w_b.g[j];
     }
-    // DG rows
     const real p0 = pt.p0;
+    real DG[6][12];
+#pragma unroll
     for (int j = 0; j < 12; ++j) {
-      const real DG0 = c.ke * G[0][j];
-      const real DG1 = c.kt * G[1][j];
-      const real DG2 = c.k2v * G[2][j] - c.k2uv * G[5][j];
-      const real DG3 = c.k3v * G[3][j] + c.k3uv * G[4][j];
-      const real DG4 = c.k3uv * G[3][j] + c.k3u * G[4][j];
-      const real DG5 = -c.k2uv * G[2][j] + c.k2u * G[5][j];
-      for (int i = 0; i < 12; ++i)
-        K[i + 12 * j] += to_d(p0 * (G[0][i] * DG0 + G[1][i] * DG1 + G[2][i] * DG2 + G[3][i] * DG3 +
-                                    G[4][i] * DG4 + G[5][i] * DG5));
+      const bool tr = j < 3 || (j >= 6 && j < 9);
+      if (tr) {
+        DG[0][j] = p0 * (c.ke * G[0][j]);
+        DG[1][j] = 0.0;
+        DG[2][j] = p0 * (-c.k2uv * G[5][j]);
+        DG[3][j] = p0 * (c.k3uv * G[4][j]);
+        DG[4][j] = p0 * (c.k3u * G[4][j]);
+        DG[5][j] = p0 * (c.k2u * G[5][j]);
+      } else {
+        DG[0][j] = 0.0;
+        DG[1][j] = p0 * (c.kt * G[1][j]);
+        DG[2][j] = p0 * fma(c.k2v, G[2][j], -c.k2uv * G[5][j]);
+        DG[3][j] = p0 * fma(c.k3v, G[3][j], c.k3uv * G[4][j]);
+        DG[4][j] = p0 * fma(c.k3uv, G[3][j], c.k3u * G[4][j]);
+        DG[5][j] = p0 * fma(-c.k2uv, G[2][j], c.k2u * G[5][j]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      const bool tr = i < 3 || (i >= 6 && i < 9);
+#pragma unroll
+      for (int j = i; j < 12; ++j) {
+        real v;
+        if (tr)
+          v = fma(G[0][i], DG[0][j], fma(G[4][i], DG[4][j], G[5][i] * DG[5][j]));
+        else
+          v = fma(G[1][i], DG[1][j],
+                  fma(G[2][i], DG[2][j], fma(G[3][i], DG[3][j], fma(G[4][i], DG[4][j], G[5][i] * DG[5][j]))));
+        K[i + 12 * j] += to_d(v);
+        if (j != i) K[j + 12 * i] += to_d(v);
+      }
     }
   }
 
