@@ -279,15 +279,9 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   const real s_n = -c.k2uv * w_b.v + c.k2v * th_n.v;
 
   // ---- Gauss point positions: x = yᵤ d + (yₐ−yᵤ) m + yᵥ w + ½(u₁+u₂) + cₘ
-  TJ<D> dT[3];
-  for (int i = 0; i < 3; ++i) {
-    dT[i] = tj_const<D>(d[i]);
-    if constexpr (D) {
-      dT[i].vt = dd1[i];
-      dT[i].vtt = 0.5 * dd2[i];
-    }
-  }
-  const TJ<D> td = tj_dot3(t, dT);
+  real d2h[3];
+  for (int i = 0; i < 3; ++i) d2h[i] = 0.5 * dd2[i];
+  const TJ<D> td = tj_dot3_time(t, d, dd1, d2h);  // t·d with d's time jet
   TJ<D> mv[3], wv[3];  // m = (t·d) t,  w = Δv × t
   for (int i = 0; i < 3; ++i) mv[i] = td * t[i];
   wv[0] = tj_fnma(dv[2], t[1], dv[1] * t[2]);
@@ -579,20 +573,25 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
             }
           }
         }
-        // δ(local components):  δ(r₀ᵀy) = δr₀ᵀ y + r₀ᵀ δy
+        // δ(local components):  δ(r₀ᵀy) = δr₀ᵀ y + r₀ᵀ δy  (δr₀ = 0 along the
+        // translation directions and δr)
+        const bool rotdir = j < 12 && rot_index(j) >= 0;
         real dl1[3], dl2[3];
         for (int k = 0; k < 3; ++k) {
-          dl1[k] = dr0[3 * k] * xd[g][0] + dr0[3 * k + 1] * xd[g][1] + dr0[3 * k + 2] * xd[g][2] +
-                   r0[3 * k] * dx1[0] + r0[3 * k + 1] * dx1[1] + r0[3 * k + 2] * dx1[2];
-          dl2[k] = dr0[3 * k] * xdd[g][0] + dr0[3 * k + 1] * xdd[g][1] + dr0[3 * k + 2] * xdd[g][2] +
-                   r0[3 * k] * dx2[0] + r0[3 * k + 1] * dx2[1] + r0[3 * k + 2] * dx2[2];
+          dl1[k] = r0[3 * k] * dx1[0] + r0[3 * k + 1] * dx1[1] + r0[3 * k + 2] * dx1[2];
+          dl2[k] = r0[3 * k] * dx2[0] + r0[3 * k + 1] * dx2[1] + r0[3 * k + 2] * dx2[2];
+          if (rotdir) {
+            dl1[k] += dr0[3 * k] * xd[g][0] + dr0[3 * k + 1] * xd[g][1] + dr0[3 * k + 2] * xd[g][2];
+            dl2[k] += dr0[3 * k] * xdd[g][0] + dr0[3 * k + 1] * xdd[g][1] + dr0[3 * k + 2] * xdd[g][2];
+          }
         }
         real dfl[3];
         for (int k = 0; k < 3; ++k) dfl[k] = c.Ca[k] * dl2[k] + dfl1[k] * dl1[k];
         real df[3];
-        for (int i = 0; i < 3; ++i)
-          df[i] = c.mu * dx2[i] + dr0[i] * fl[0] + dr0[i + 3] * fl[1] + dr0[i + 6] * fl[2] + r0[i] * dfl[0] +
-                  r0[i + 3] * dfl[1] + r0[i + 6] * dfl[2];
+        for (int i = 0; i < 3; ++i) {
+          df[i] = c.mu * dx2[i] + r0[i] * dfl[0] + r0[i + 3] * dfl[1] + r0[i + 6] * dfl[2];
+          if (rotdir) df[i] += dr0[i] * fl[0] + dr0[i + 3] * fl[1] + dr0[i + 6] * fl[2];
+        }
         double* col = (j < 12) ? (K + 12 * j) : rdir;
         if (j == 12 && g == 0)
           for (int a = 0; a < 12; ++a) rdir[a] = 0.0;

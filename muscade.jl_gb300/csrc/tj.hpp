@@ -309,6 +309,26 @@ MG_HD TJ<DYN, N> tj_dot3(const TJ<DYN, N> a[3], const real x[3]) {
   return tj_fma(a[2], x[2], tj_fma(a[1], x[1], a[0] * x[0]));
 }
 
+// Σ a[i] y_i with y_i(τ) = y0_i + y1_i τ + y2_i τ² independent of ε (a time jet
+// without gradient): the products skip y's zero gradient and Hessian
+template <bool DYN>
+MG_HD TJ<DYN> tj_dot3_time(const TJ<DYN> a[3], const real y0[3], const real y1[3], const real y2[3]) {
+  TJ<DYN> r = tj_dot3(a, y0);
+  if constexpr (DYN) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      r.vtt = fma(a[k].vt, y1[k], fma(a[k].v, y2[k], r.vtt));
+      r.vt = fma(a[k].v, y1[k], r.vt);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        r.gtt[i] = fma(a[k].gt[i], y1[k], fma(a[k].g[i], y2[k], r.gtt[i]));
+        r.gt[i] = fma(a[k].g[i], y1[k], r.gt[i]);
+      }
+    }
+  }
+  return r;
+}
+
 // ---- block products of the two-node structure (six variables = node 1's
 // three, then node 2's three).  ACC: accumulate into c, else c is not read.
 template <bool ACC>
