@@ -1,0 +1,72 @@
+"""The device element code (csrc/beam_math.hpp, the body of beam_kernel)
+compiled for the host and compared with the oracle's nested-dual evaluation
+of the same elements: R and the Newton matrix of SweepX{0} (K) and of a
+Newmark iteration (K + a₁C + b₁M) within the assembly tolerance, on the
+models of the GPU assembly tests.  No GPU needed."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from muscade_gpu import workloads as W
+from oracle import reference as REF
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "muscade.jl_gb300", "csrc")
+TOL = 1e-12  # relative to the largest entry, as the assembly parity tests
+
+
+@pytest.fixture(scope="module")
+def host_eval(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    exe = str(tmp_path_factory.mktemp("beam") / "beam_host_eval")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", CSRC, os.path.join(HERE, "beam_host_eval.cpp"), "-o", exe],
+                   check=True, capture_output=True)
+
+    def run(fields, X0, X1, X2, mode, a1=0.0, b1=0.0):
+        lines = [f"{len(fields)} {mode} {a1!r} {b1!r}"]
+        for f, x0, x1, x2 in zip(fields, X0, X1, X2):
+            lines.append(" ".join(repr(float(v)) for v in np.concatenate([f, x0, x1, x2])))
+        out = subprocess.run([exe], input="\n".join(lines) + "\n", check=True, capture_output=True, text=True).stdout
+        a = np.array([[float(v) for v in ln.split()] for ln in out.strip().splitlines()])
+        return a[:, :12], a[:, 12:].reshape(-1, 12, 12).transpose(0, 2, 1)  # K[e][i][j]
+
+    return run
+
+
+def _relerr(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+MODELS = {"cantilever": lambda: W.cantilever()[0], "lattice": lambda: W.lattice(5, 4, 3)[0],
+          "risers": lambda: W.risers(nriser=2, nel=10)[0]}
+
+
+@pytest.mark.parametrize("name", list(MODELS))
+def test_device_element_code_matches_the_oracle(name, host_eval):
+    m = MODELS[name]()
+    st = m.initialize()
+    rng = np.random.default_rng(11)
+    n = m.ndof["X"]
+    X = [rng.normal(size=n) * 0.05 for _ in range(3)]
+    U = (np.zeros(m.ndof["U"]),)
+    c = REF.newmark_coefficients(2, 0.05, 0.25, 0.5)
+    checked = 0
+    for g, dg in zip(m.groups, st.dis.dis):
+        if REF.group_kind(g) != "EulerBeam3D" or g.nele == 0:
+            continue
+        idx = dg.index_X - 1
+        Xe = [x[idx] for x in X]
+        fields = g.cat("ele")
+        for mode, mref, cc in ((1, "static", REF.newmark_coefficients(0, 1.0, 0.25, 0.5)), (3, "iter", c)):
+            Xs = (X[0],) if mode == 1 else tuple(X)
+            Rr, Jr = REF.eval_group(m, g, dg, Xs, U, 0.3, mode, cc)
+            Rh, Kh = host_eval(fields, Xe[0], Xe[1], Xe[2], mode, cc.get("a1", 0.0), cc.get("b1", 0.0))
+            assert _relerr(Rh, Rr) <= TOL, (name, mref)
+            assert _relerr(Kh, Jr[:, :, :12]) <= TOL, (name, mref)
+            checked += 1
+    assert checked >= 2
