@@ -146,34 +146,23 @@ MG_HD void rodrigues_inv(const TJ<D> m[9], TJ<D> w[3], real scale = 1.0) {
   w[2] = (m[1] - m[3]) * is;  // (m21 - m12)/2
 }
 
-// C = A Bᵀ  (both Taylor)
-template <bool D>
-MG_HD void mul_abt(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) C[i + 3 * j] = tj_fma(A[i + 6], B[j + 6], tj_fma(A[i + 3], B[j + 3], A[i] * B[j]));
-}
-// C = A B
-template <bool D>
-MG_HD void mul_ab(const TJ<D> A[9], const TJ<D> B[9], TJ<D> C[9]) {
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j)
-      C[i + 3 * j] = tj_fma(A[i + 6], B[2 + 3 * j], tj_fma(A[i + 3], B[1 + 3 * j], A[i] * B[3 * j]));
-}
 // C = B Aᵀ with A over node 1's variables and B over node 2's (r₂ r₁ᵀ)
 template <bool D>
 MG_HD void mul_abt_nodes(const TJ<D, 3> B[9], const TJ<D, 3> A[9], TJ<D> C[9]) {
+  const TJ<D> zero = tj_const<D>(0.0);  // not accumulated into (ACC = false)
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      const TJ<D> z = tj_cross<false>(A[j], B[i], C[0]);  // C[0] is not read without ACC
+      const TJ<D> z = tj_cross<false>(A[j], B[i], zero);
       C[i + 3 * j] = tj_cross<true>(A[j + 6], B[i + 6], tj_cross<true>(A[j + 3], B[i + 3], z));
     }
 }
 // C = A B with B over node 1's variables (r_Δ r₁)
 template <bool D>
 MG_HD void mul_ab_node1(const TJ<D> A[9], const TJ<D, 3> B[9], TJ<D> C[9]) {
+  const TJ<D> zero = tj_const<D>(0.0);  // not accumulated into (ACC = false)
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      const TJ<D> z = tj_mixA<false>(A[i], B[3 * j], C[0]);
+      const TJ<D> z = tj_mixA<false>(A[i], B[3 * j], zero);
       C[i + 3 * j] = tj_mixA<true>(A[i + 6], B[2 + 3 * j], tj_mixA<true>(A[i + 3], B[1 + 3 * j], z));
     }
 }
@@ -203,11 +192,6 @@ struct BeamConst {
 struct Perturb {
   double p0, p1, p2;
 };
-
-template <class T>
-MG_HD T dot3(const T a[3], const T b[3]) {
-  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-}
 
 // rotation-dof index (0..5) of element dof j, or -1 for translations
 MG_HD int rot_index(int j) { return (j >= 3 && j < 6) ? j - 3 : (j >= 9 ? j - 6 : -1); }

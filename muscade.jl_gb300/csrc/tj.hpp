@@ -452,9 +452,4 @@ MG_HD TJ<DYN, N> tj_apply(const TJ<DYN, N>& a, real f0, real f1, real f2, real f
   return r;
 }
 
-template <bool DYN, int N>
-MG_HD bool tj_is_zero_value(const TJ<DYN, N>& a) {
-  return a.v == 0.0;
-}
-
 }  // namespace mgpu
