@@ -93,10 +93,9 @@ MG_HD void scac_derivs(real x, real f[4]) {
 
 // ---- rotations in Taylor arithmetic ----------------------------------------
 // Rodrigues(v) = I + sinc1(θ) S + ½ sinc1(θ/2)² S²,  θ = norm3(v)   (Rotations.jl:131-135)
+// A = sinc1(θ) and B = ½ sinc1(θ/2)² as compositions of s2 = |v|²
 template <bool D, int N>
-MG_HD void rodrigues(const TJ<D, N> v[3], TJ<D, N> R[9]) {
-  const TJ<D, N> s2 = tj_dot3(v, v);
-  TJ<D, N> A, B;
+MG_HD void rod_AB(const TJ<D, N>& s2, TJ<D, N>& A, TJ<D, N>& B) {
   const real th = sqrt(s2.v);
   if (th < 1e-14) {  // norm3 returns an exact zero: sinc1 terms become constants
     A = tj_const<D, N>(1.0);
@@ -112,6 +111,13 @@ MG_HD void rodrigues(const TJ<D, N> v[3], TJ<D, N> R[9]) {
     const real s0 = sinc1_0(h), s1 = sinc1_1(h), s2d = sinc1_2(h), s3 = sinc1_3(h);
     B = tj_apply(t, 0.5 * s0 * s0, 0.5 * s0 * s1, 0.25 * fma(s1, s1, s0 * s2d), 0.125 * fma(3.0 * s1, s2d, s0 * s3));
   }
+}
+
+template <bool D, int N>
+MG_HD void rodrigues(const TJ<D, N> v[3], TJ<D, N> R[9]) {
+  const TJ<D, N> s2 = tj_dot3(v, v);
+  TJ<D, N> A, B;
+  rod_AB(s2, A, B);
   // S = spin(v): S[2,1]=v3, S[3,1]=-v2, S[1,2]=-v3, S[3,2]=v1, S[1,3]=v2, S[2,3]=-v1
   // S² = v vᵀ - |v|² I  (spin², Rotations.jl:114-122)
   const TJ<D, N> ab = v[0] * v[1], ca = v[2] * v[0], bc = v[1] * v[2];
@@ -122,6 +128,91 @@ MG_HD void rodrigues(const TJ<D, N> v[3], TJ<D, N> R[9]) {
   R[8] = tj_fnma(B, aa + bb, one);
   const TJ<D, N> Bab = B * ab, Bca = B * ca, Bbc = B * bc;
   const TJ<D, N> Av0 = A * v[0], Av1 = A * v[1], Av2 = A * v[2];
+  R[1] = Av2 + Bab;   // [2,1]
+  R[3] = Bab - Av2;   // [1,2]
+  R[2] = Bca - Av1;   // [3,1]
+  R[6] = Av1 + Bca;   // [1,3]
+  R[5] = Av0 + Bbc;   // [3,2]
+  R[7] = Bbc - Av0;   // [2,3]
+}
+
+// Products with the nodal variables vᵢ = xᵢ + εᵢ + x1ᵢ τ + yᵢ τ² (y = ½ x₂) of one
+// node, in closed form: vₐ v_b, and a·vᵢ for a general three-variable a.
+template <bool D>
+MG_HD TJ<D, 3> tj_varprod(int a, int b, const real x[3], const real x1[3], const real y[3]) {
+  TJ<D, 3> r = tj_const<D, 3>(x[a] * x[b]);
+  r.g[a] = x[b];
+  r.g[b] += x[a];
+  r.h[a <= b ? hidx<3>(a, b) : hidx<3>(b, a)] = a == b ? 2.0 : 1.0;
+  if constexpr (D) {
+    r.vt = fma(x[a], x1[b], x1[a] * x[b]);
+    r.vtt = fma(x[a], y[b], fma(x1[a], x1[b], y[a] * x[b]));
+    r.gt[a] = x1[b];
+    r.gt[b] += x1[a];
+    r.gtt[a] = y[b];
+    r.gtt[b] += y[a];
+  }
+  return r;
+}
+template <bool D>
+MG_HD TJ<D, 3> tj_mulvar(const TJ<D, 3>& a, int i, const real x[3], const real x1[3], const real y[3]) {
+  TJ<D, 3> r = tj_scale(a, x[i]);
+  r.g[i] += a.v;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    const int k = m <= i ? hidx<3>(m, i) : hidx<3>(i, m);
+    r.h[k] = m == i ? fma(2.0, a.g[i], r.h[k]) : r.h[k] + a.g[m];
+  }
+  if constexpr (D) {
+    r.vt = fma(a.v, x1[i], r.vt);
+    r.vtt = fma(a.vt, x1[i], fma(a.v, y[i], r.vtt));
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      r.gt[m] = fma(a.g[m], x1[i], r.gt[m]);
+      r.gtt[m] = fma(a.gt[m], x1[i], fma(a.g[m], y[i], r.gtt[m]));
+    }
+    r.gt[i] += a.vt;
+    r.gtt[i] += a.vtt;
+  }
+  return r;
+}
+
+// Rodrigues(v) of a node's rotation dofs v = x + ε (with their time jet), over
+// those three variables
+template <bool D>
+MG_HD void rodrigues_nodal(const double xd[3], const double x1d[3], const double x2d[3], TJ<D, 3> R[9]) {
+  const real x[3] = {xd[0], xd[1], xd[2]};
+  real x1[3] = {0.0, 0.0, 0.0}, y[3] = {0.0, 0.0, 0.0};
+  if constexpr (D)
+    for (int i = 0; i < 3; ++i) {
+      x1[i] = x1d[i];
+      y[i] = 0.5 * x2d[i];
+    }
+  TJ<D, 3> s2 = tj_const<D, 3>(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  for (int i = 0; i < 3; ++i) {
+    s2.g[i] = 2.0 * x[i];
+    s2.h[hidx<3>(i, i)] = 2.0;
+  }
+  if constexpr (D) {
+    s2.vt = 2.0 * (x[0] * x1[0] + x[1] * x1[1] + x[2] * x1[2]);
+    s2.vtt = x1[0] * x1[0] + x1[1] * x1[1] + x1[2] * x1[2] + 2.0 * (x[0] * y[0] + x[1] * y[1] + x[2] * y[2]);
+    for (int i = 0; i < 3; ++i) {
+      s2.gt[i] = 2.0 * x1[i];
+      s2.gtt[i] = 2.0 * y[i];
+    }
+  }
+  TJ<D, 3> A, B;
+  rod_AB(s2, A, B);
+  const TJ<D, 3> ab = tj_varprod<D>(0, 1, x, x1, y), ca = tj_varprod<D>(2, 0, x, x1, y),
+                 bc = tj_varprod<D>(1, 2, x, x1, y);
+  const TJ<D, 3> aa = tj_varprod<D>(0, 0, x, x1, y), bb = tj_varprod<D>(1, 1, x, x1, y),
+                 cc = tj_varprod<D>(2, 2, x, x1, y);
+  const TJ<D, 3> one = tj_const<D, 3>(1.0);
+  R[0] = tj_fnma(B, bb + cc, one);
+  R[4] = tj_fnma(B, aa + cc, one);
+  R[8] = tj_fnma(B, aa + bb, one);
+  const TJ<D, 3> Bab = B * ab, Bca = B * ca, Bbc = B * bc;
+  const TJ<D, 3> Av0 = tj_mulvar(A, 0, x, x1, y), Av1 = tj_mulvar(A, 1, x, x1, y), Av2 = tj_mulvar(A, 2, x, x1, y);
   R[1] = Av2 + Bab;   // [2,1]
   R[3] = Bab - Av2;   // [1,2]
   R[2] = Bca - Av1;   // [3,1]
@@ -207,23 +298,13 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
                         double* H) {
   // ---- rotation core
   // the nodal rotations depend on their own node's three dofs only
-  TJ<D, 3> v1[3], v2[3];
-  for (int i = 0; i < 3; ++i) {
-    if constexpr (D) {
-      v1[i] = tj_var<D, 3>(X0[3 + i], i, X1[3 + i], X2[3 + i]);
-      v2[i] = tj_var<D, 3>(X0[9 + i], i, X1[9 + i], X2[9 + i]);
-    } else {
-      v1[i] = tj_var<D, 3>(X0[3 + i], i);
-      v2[i] = tj_var<D, 3>(X0[9 + i], i);
-    }
-  }
   TJ<D, 3> r1[9];
   TJ<D> rsm[9], dv[3];
   {
     TJ<D, 3> r2[9];
     TJ<D> Q[9];
-    rodrigues(v1, r1);
-    rodrigues(v2, r2);
+    rodrigues_nodal<D>(X0 + 3, X1 + 3, X2 + 3, r1);
+    rodrigues_nodal<D>(X0 + 9, X1 + 9, X2 + 9, r2);
     mul_abt_nodes(r2, r1, Q);
     rodrigues_inv(Q, dv, 0.5);  // Δv = ½ Rodrigues⁻¹(r₂r₁ᵀ)
   }

@@ -46,13 +46,20 @@ MODELS = {"cantilever": lambda: W.cantilever()[0], "lattice": lambda: W.lattice(
           "risers": lambda: W.risers(nriser=2, nel=10)[0]}
 
 
+@pytest.mark.parametrize("rot", ["rotated", "zero rotations"])
 @pytest.mark.parametrize("name", list(MODELS))
-def test_device_element_code_matches_the_oracle(name, host_eval):
+def test_device_element_code_matches_the_oracle(name, rot, host_eval):
+    """Random states, and states whose nodal rotation dofs are zero (the
+    θ = 0 branch of Rodrigues, taken at the start of every sweep)."""
     m = MODELS[name]()
     st = m.initialize()
     rng = np.random.default_rng(11)
     n = m.ndof["X"]
     X = [rng.normal(size=n) * 0.05 for _ in range(3)]
+    if rot == "zero rotations":
+        for f in ("r1", "r2", "r3"):
+            for x in X:
+                x[np.array([str(v) == f for v in st.dis.fieldX])] = 0.0
     U = (np.zeros(m.ndof["U"]),)
     c = REF.newmark_coefficients(2, 0.05, 0.25, 0.5)
     checked = 0
