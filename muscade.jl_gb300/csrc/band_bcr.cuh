@@ -10,9 +10,12 @@
 // until block 0 alone remains.  A solve reduces the right-hand side the same
 // way (z_k = D_k^-1 r_k, r_e -= U_e z_{e+h} + L_e z_{e-h}), solves block 0 and
 // substitutes back level by level (x_k = z_k - W_L(k) x_{k-h} - W_U(k) x_{k+h}).
-// Every level is one launch over all blocks of all components (one warp per
-// block, dense s x s work), so the separators cost log2(N) levels instead of a
-// sequential band factorisation of N s rows.
+// The factorisation runs one launch per level over all blocks of all
+// components (one warp per block, dense s x s work), so the separators cost
+// log2(N) levels instead of a sequential band factorisation of N s rows.  A
+// solve either does the same, level by level, or (components of few
+// interiors) runs inside the fused per-component solve of band_torn.cuh, one
+// block barrier per level.
 //
 // Storage (per separator k, global index; component offset sep0, local index
 // k - sep0; SS = 16 x 16 doubles per block whatever s):

@@ -1094,10 +1094,12 @@ static void torn_fused(mgpu_ctx* c, bool tr, const double* rhs, double* out, int
 }
 
 // Partitioned solve of Lλx (or its transpose) x = rhs.  FP64 directly, or
-// (PATH_TORN32) FP32 factors inside S.nrefine sweeps of FP64 iterative
+// (PATH_TORN32) FP32 factors inside up to S.nrefine sweeps of FP64 iterative
 // refinement, then the FP64 factorisation for the components whose last
-// correction is not below 1e-10 of their solution.  Capturable (no host
-// decision).
+// correction is not below 1e-10 of their solution.  With few interiors per
+// component (fuseW32 > 0) each solve is one launch of the fused
+// per-component kernel; otherwise the solve goes level by level over all
+// components.  Capturable (no host decision).
 static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
