@@ -257,6 +257,12 @@ MG_HD void mul_ab_node1(const TJ<D> A[9], const TJ<D, 3> B[9], TJ<D> C[9]) {
       C[i + 3 * j] = tj_mixA<true>(A[i + 6], B[2 + 3 * j], tj_mixA<true>(A[i + 3], B[1 + 3 * j], z));
     }
 }
+// Σ m[i] v[i] with m over node 1's variables (a column of r₁rₘ) and v over six
+template <bool D>
+MG_HD TJ<D> tj_dot3_node1(const TJ<D, 3> m[3], const TJ<D> v[3]) {
+  const TJ<D> zero = tj_const<D>(0.0);  // not accumulated into (ACC = false)
+  return tj_mixA<true>(v[2], m[2], tj_mixA<true>(v[1], m[1], tj_mixA<false>(v[0], m[0], zero)));
+}
 // C = A M with M a constant matrix
 template <bool D, int N>
 MG_HD void mul_ac(const TJ<D, N> A[9], const double M[9], TJ<D, N> C[9]) {
@@ -308,11 +314,11 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
     mul_abt_nodes(r2, r1, Q);
     rodrigues_inv(Q, dv, 0.5);  // Δv = ½ Rodrigues⁻¹(r₂r₁ᵀ)
   }
+  // rₛₘ = r_Δ (r₁ rₘ): the constant frame goes into the node-1 value first
+  TJ<D, 3> r1m[9];
+  mul_ac(r1, c.rm, r1m);
   {
-    // rₛₘ = r_Δ (r₁ rₘ): the constant frame goes into the node-1 value first
     TJ<D> rD[9];
-    TJ<D, 3> r1m[9];
-    mul_ac(r1, c.rm, r1m);
     rodrigues(dv, rD);
     mul_ab_node1(rD, r1m, rsm);
   }
@@ -332,7 +338,9 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   const real eps = dn * 2.0 / c.L - 1.0;
 
   // ---- strain measures
-  const TJ<D> th_t = tj_dot3(t, dv), th_n = tj_dot3(n, dv), th_b = tj_dot3(b, dv);
+  // (t, n, b)·Δv = rₛₘᵀΔv = (r₁rₘ)ᵀ r_ΔᵀΔv = (r₁rₘ)ᵀΔv, since Rod(Δv) leaves Δv
+  // fixed (S Δv = 0): node-1 × six-variable products
+  const TJ<D> th_t = tj_dot3_node1(r1m, dv), th_n = tj_dot3_node1(r1m + 3, dv), th_b = tj_dot3_node1(r1m + 6, dv);
   const TJ<D> w_n = tj_dot3(n, d);
   const TJ<D> w_b = tj_dot3(b, d);
   // frozen stresses σ = ∂Π/∂q
