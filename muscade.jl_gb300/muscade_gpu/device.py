@@ -125,7 +125,9 @@ class DeviceModel:
                 "ms_linsolve": {L.LINSOLVE_NAME[k]: rep.ms_linsolve[k] for k in range(1, 6) if rep.ms_linsolve[k] >= 0}}
 
     def set_linear_solver(self, kind: str):
-        """'auto' | 'f32ir' (FP32 factors + FP64 refinement) | 'f64' | 'block'."""
+        """'auto' | 'f32ir' (row-band FP32 factors + FP64 refinement) | 'f64' (row-band) |
+        'block' | 'torn' (partitioned, FP64) | 'torn32' (partitioned, FP32 factors +
+        FP64 refinement); see mgpu_set_linear_solver."""
         self._check(self.lib.mgpu_set_linear_solver(self.ctx, L.LINSOLVE[kind]))
 
     def linear_solver_info(self):
@@ -141,12 +143,14 @@ class DeviceModel:
             raise DeviceError(rc, msg)
 
     def close(self):
-        for buf in getattr(self, "_registered", []):
-            self.lib.mgpu_host_unregister(buf.ctypes.data_as(ctypes.c_void_p))
-        self._registered = []
+        # destroy first: it waits for the context's streams, so no copy into a
+        # page-locked buffer (a pipelined assembly's outputs) is still in flight
         if getattr(self, "ctx", None):
             self.lib.mgpu_destroy(self.ctx)
             self.ctx = None
+        for buf in getattr(self, "_registered", []):
+            self.lib.mgpu_host_unregister(buf.ctypes.data_as(ctypes.c_void_p))
+        self._registered = []
 
     def __del__(self):
         try:
