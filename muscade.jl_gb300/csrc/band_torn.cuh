@@ -448,8 +448,12 @@ __device__ __forceinline__ double tb_dot16_sub(const double* a, const double* b,
   return v;
 }
 
+// threads per block of the fused solve at most (13 warps): two blocks per SM fit
+// in the register file at <= 78 registers per thread
+constexpr int kTbFusedMaxThreads = 416;
+
 template <typename T, int WM>
-__global__ void __launch_bounds__(416, 2) tb_fused(TbFusedArgs A, TbFusedFactors<T> F) {
+__global__ void __launch_bounds__(kTbFusedMaxThreads, 2) tb_fused(TbFusedArgs A, TbFusedFactors<T> F) {
   extern __shared__ __align__(16) unsigned char tb_dyn[];
   __shared__ double red[2][32];
   __shared__ int fin[32];

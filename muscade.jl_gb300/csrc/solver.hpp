@@ -15,7 +15,7 @@ constexpr int kNormBlocks = 128;
 constexpr int64_t kTornMinDofs = 512;  // components shorter than this are factorised whole
 constexpr int kInfoSlots = 64;  // a captured step holds up to kInfoSlots-1 iterations
 constexpr int kFusedMaxP = 32;  // the fused per-component partitioned solve takes components of up to 32 interiors
-constexpr int kFusedMaxW = 13;  // and runs at most 13 warps per block (two blocks per SM at <= 78 registers)
+constexpr int kFusedMaxW = kTbFusedMaxThreads / 32;  // and runs at most that many warps per block
 
 enum SolverPath : int {
   PATH_F32IR = 0,  // row-band warp kernels, FP32 factors + FP64 refinement, FP64 fallback per component
