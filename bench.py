@@ -11,7 +11,7 @@ device, then the deterministic scatter into Lλ and Lλx.nzval.
   e2e    the same through the C-ABI call a host caller makes (mgpu_assemble):
          host state in, host Lλ and nzval out, copies inside the timed region
   --impl reference   the CPU arm: the oracle (a C++ dual-number restatement
-         of the reference's assembly) on the host cores, on a bounded sample
+         of the reference's assembly) of the same lattice on the host cores
 
 Launched as `python bench.py --gpus N ...` or under torch.distributed.run for
 N>1; the lattice is a single model, so N>1 runs N independent replicas and the
@@ -133,24 +133,45 @@ def state_for(model, seed=2027):
     return [rng.normal(size=model.ndof["X"]) * 1e-3]
 
 
-def cpu_baseline(model, X, t, sample_beams, threads):
-    """The oracle's assembly of a bounded sample of beams on the host cores."""
-    from oracle import lib as O
+class OracleAssembly:
+    """The CPU leg: the oracle's restatement of the reference's assembly of the
+    same lattice (prepare with asmmat!, then per step every element's R and K
+    by nested duals on all host threads and the serial add_value!/add_∂!
+    scatter into Lλ and Lλx.nzval, src/Assemble.jl:470-608).  It is both the
+    timed CPU baseline and the checker of the device's pattern and values."""
 
-    g = model.groups[0]
-    dis = model.initialize_cached
-    idx = dis.dis[0].index_X[:sample_beams] - 1
-    ele = g.cat("ele")[:sample_beams]
-    Xe = X[0][idx][:, None, :]
-    O.build()
-    O.beam_eval(ele[:64], Xe[:64], mode=1, nthreads=threads)  # warm
-    t0 = time.perf_counter()
-    R, J = O.beam_eval(ele, Xe, mode=1, nthreads=threads)
-    # scatter of the sample into Lλ and the matrix entries (the oracle's add_value!/add_∂! order)
-    Ll = np.zeros(model.ndof["X"])
-    np.add.at(Ll, idx.reshape(-1), R.reshape(-1))
-    dt = time.perf_counter() - t0
-    return sample_beams / dt, dt
+    def __init__(self, model, dis):
+        from oracle import lib as O
+        from oracle import reference as REF
+
+        O.build()
+        self.REF, self.model = REF, model
+        t0 = time.perf_counter()
+        self.prep = REF.Prepared(model, dis)
+        self.prepare_s = time.perf_counter() - t0
+
+    def assemble(self, X, t):
+        """One full assembly; returns (Lλ, nzval, seconds)."""
+        REF = self.REF
+        t0 = time.perf_counter()
+        Ll, nz = REF.assemble(self.prep, tuple(X), (np.zeros(self.model.ndof["U"]),), t, "static",
+                              REF.newmark_coefficients(0, 1.0, 0.25, 0.5))
+        return Ll, nz, time.perf_counter() - t0
+
+    def parity(self, dm, Ll, nz, X, t):
+        """Pattern and asm maps bit-exact, Lλ and nzval relative to their largest entry."""
+        prep = self.prep
+        colptr, rowval = dm.pattern()
+        pat = bool(dm.nnz == prep.nnz and np.array_equal(colptr, prep.colptr) and np.array_equal(rowval, prep.rowval))
+        for ig in range(len(self.model.groups)):
+            a1, a2 = dm.asm(ig)
+            pat &= bool(np.array_equal(a1, prep.asm1[ig]) and np.array_equal(a2, prep.asm2[ig]))
+        Lr, nr, dt = self.assemble(X, t)
+        eL = float(np.max(np.abs(Ll - Lr)) / np.max(np.abs(Lr)))
+        eK = float(np.max(np.abs(nz - nr)) / np.max(np.abs(nr)))
+        return {"pattern_and_asm_bit_exact": pat, "Ll_max_rel_err": eL, "nzval_max_rel_err": eK, "tol": 1e-12,
+                "pass": bool(pat and eL <= 1e-12 and eK <= 1e-12),
+                "checked_against": "oracle assembly of the whole lattice (asmmat! pattern, nested-dual elements)"}, dt
 
 
 def main():
@@ -160,9 +181,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", default="60,60,20")
-    ap.add_argument("--cpu-sample", type=int, default=int(os.environ.get("MGPU_CPU_SAMPLE", "60000")))
-    ap.add_argument("--config", default="lattice", choices=["lattice", "risers", "cantilever", "batched", "adjoint"],
-                    help="lattice: the headline assembly metric; risers/cantilever: whole SweepX solves; "
+    ap.add_argument("--ref-steps", type=int, default=int(os.environ.get("MGPU_REF_STEPS", "20")),
+                    help="reference arm: at most this many timed whole assemblies")
+    ap.add_argument("--config", default="lattice",
+                    choices=["lattice", "lattice-solve", "risers", "cantilever", "batched", "adjoint"],
+                    help="lattice: the headline assembly metric; lattice-solve: the lattice's 5 load steps of "
+                         "SweepX{0} with the multifrontal device solver; risers/cantilever: whole SweepX solves; "
                          "batched: independent cantilevers and portal frames solved together; "
                          "adjoint: cost gradient of the stiffness identification beam")
     ap.add_argument("--adj-nel", type=int, default=5000)
@@ -171,12 +195,14 @@ def main():
     ap.add_argument("--fd-steps", type=int, default=50, help="adjoint: horizon of the finite-difference check")
     ap.add_argument("--models", type=int, default=4096, help="batched: number of models")
     ap.add_argument("--individual", type=int, default=16, help="batched: models also solved one by one")
+    ap.add_argument("--oracle-models", type=int, default=4, help="batched: sampled models also solved by the oracle")
     ap.add_argument("--no-graph", action="store_true", help="risers: launch kernel by kernel instead of replaying "
                                                               "a captured CUDA graph per step")
     ap.add_argument("--autotune", action="store_true",
                     help="risers/batched: pick element block size and linear solver by timing them first")
     ap.add_argument("--risers", type=int, default=200)
-    ap.add_argument("--linsolve", default="auto", choices=["auto", "f32ir", "f64", "block", "torn", "torn32"],
+    ap.add_argument("--linsolve", default="auto",
+                    choices=["auto", "f32ir", "f64", "block", "torn", "torn32", "sparse", "sparse64"],
                     help="device linear solver of the whole-solve modes")
     args = ap.parse_args()
     rank, local_rank, ws, dist = dist_setup()
@@ -184,6 +210,8 @@ def main():
         return bench_batched(args, rank, local_rank, ws, dist)
     if args.config == "adjoint":
         return bench_adjoint(args, rank, local_rank, ws, dist)
+    if args.config == "lattice-solve":
+        return bench_lattice_solve(args, rank, local_rank, ws, dist)
     if args.config != "lattice":
         return bench_solve(args, rank, local_rank, ws, dist)
     nx, ny, nz = (int(v) for v in args.grid.split(","))
@@ -203,20 +231,25 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        sample = min(args.cpu_sample, nbeam)
+        ora = OracleAssembly(model, st.dis)
         per = []
-        for i in range(args.warmup + args.steps):
-            rate, dt = cpu_baseline(model, X, t, sample, threads)
-            if i >= args.warmup:
+        # each step is one whole assembly (about 2 s on 16 cores); the step count
+        # is capped so that the arm ends within a few minutes
+        nsteps = min(args.steps, args.ref_steps)
+        nwarm = min(args.warmup, 1)
+        for i in range(nwarm + nsteps):
+            _, _, dt = ora.assemble(X, t)
+            if i >= nwarm:
                 per.append(dt)
         tstep = sum(per) / len(per)
-        value = sample / tstep
+        value = nbeam / tstep
+        sample = (f"the whole lattice per step ({nbeam} beams: element R and K by nested duals on {threads} "
+                  f"threads, serial add_value!/add_∂! into Lλ and nzval), {nsteps} steps after {nwarm} warm-up")
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": tstep * 1e3, "higher_is_better": True,
+                "steps": nsteps, "warmup": nwarm, "ms_per_step": tstep * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
-                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"{sample} of {nbeam} beams per step (element R and K by nested duals "
-                                           f"+ residual scatter), {threads} threads"},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                                 "prepare_s": ora.prepare_s},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -310,7 +343,11 @@ def main():
     sb = ent * (8 + 4) + dm.nnz * (8 + 4) + vent * (8 + 4) + model.ndof["X"] * (8 + 4)
     roof_scatter = {"bound": "hbm", "unit": "GB/s", "achieved": sb / (ts * 1e-3) / 1e9, "peak": hbm_peak,
                     "frac": sb / (ts * 1e-3) / 1e9 / hbm_peak, "bytes_per_launch": sb, "ms": ts}
-    cpu_rate, cpu_dt = cpu_baseline(model, X, t, min(args.cpu_sample, nbeam), threads)
+    # CPU leg: the oracle's assembly of the same lattice, timed, and the parity
+    # of this run's device assembly (the e2e call's outputs) against it
+    ora = OracleAssembly(model, st.dis)
+    parity, cpu_dt = ora.parity(dm, Ll, nzv, X, t)
+    cpu_rate = nbeam / cpu_dt
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tmax, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -321,7 +358,9 @@ def main():
         "roofline": roof, "roofline_scatter": roof_scatter,
         "kernel_ms": {"beam": tbeam, "other_elements": float(np.sum(tg[1:])), "scatter": ts},
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{min(args.cpu_sample, nbeam)} beams (oracle nested-dual R and K + residual scatter)"},
+                         "sample": f"one whole assembly of the lattice ({nbeam} beams; oracle nested-dual R and K "
+                                   f"on {threads} threads + serial scatter into Lλ and nzval)"},
+        "parity": parity,
         "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
         "create_s": t_create,
     }
@@ -329,6 +368,120 @@ def main():
     dm.close()
     if dist:
         dist.destroy_process_group()
+
+
+def lattice_solve_cpu_leg(grid=(12, 12, 6)):
+    """CPU leg of lattice-solve: the oracle's SweepX{0} (nested-dual assembly,
+    SuperLU factorisation) of a reduced lattice, timed per Newton iteration,
+    and the device's states on the same lattice against it."""
+    from muscade_gpu import workloads
+    from muscade_gpu.device import DeviceModel
+    from oracle import reference as REF
+
+    m, times = workloads.lattice(*grid)
+    st = m.initialize()
+    niter = [0]
+    assemble = REF.assemble
+
+    def counted(*a, **k):
+        niter[0] += 1
+        return assemble(*a, **k)
+
+    REF.assemble = counted
+    try:
+        t0 = time.perf_counter()
+        ref = REF.sweepx(m, st.dis, st, times, OX=0, maxdx=1e-8, maxLl=1e-3)
+        dt = time.perf_counter() - t0
+    finally:
+        REF.assemble = assemble
+    dm = DeviceModel(m, st.dis)
+    rc, states, _ = dm.sweepx(0, times, st.time, list(st.X), maxdx=1e-8, maxLl=1e-3)
+    dm.close()
+    lam = np.array([str(f).startswith("λ") for f in st.dis.fieldX])
+    errs = {}
+    if rc == 0:
+        for name, sel in (("dofs", ~lam), ("multipliers", lam)):
+            dev = max(np.max(np.abs(states[k, 0][sel] - Xr[0][sel])) for k, (_, Xr) in enumerate(ref))
+            errs[name] = float(dev / max(np.max(np.abs(Xr[0][sel])) for _, Xr in ref))
+    return {"ms_per_newton_iteration": dt / niter[0] * 1e3, "newton_iterations": niter[0], "seconds": dt,
+            "dofs": m.ndof["X"], "parity": {"grid": list(grid), "rc": int(rc), "max_rel_state_err": errs,
+                                            "tol": 1e-9, "pass": bool(rc == 0 and all(e <= 1e-9 for e in errs.values())),
+                                            "checked_against": "oracle SweepX{0} (SuperLU) of the same lattice"}}
+
+
+def bench_lattice_solve(args, rank, local_rank, ws, dist):
+    """The lattice's Newton solve on the device: 5 load steps of SweepX{0} on
+    the 60×60×20 frame (453,600 dofs), each Newton iteration an assembly, a
+    multifrontal factorisation (FP32 factors in FP64 refinement) and a
+    decrement.  One bench step is the whole 5-load-step solve.  Replicas only:
+    one model per GPU."""
+    from muscade_gpu import _lib, workloads
+    from muscade_gpu.device import DeviceModel
+
+    _lib.build()
+    nx, ny, nz = (int(v) for v in args.grid.split(","))
+    model, times = workloads.lattice(nx, ny, nz)
+    st = model.initialize()
+    # |Δx| includes the Hold reactions (about 1e4 N at this size); 1e-6 is well
+    # above their rounding floor
+    kw = dict(maxdx=1e-6, maxLl=1e-3)
+    t0 = time.perf_counter()
+    dm = DeviceModel(model, st.dis, device=local_rank, linsolve=args.linsolve)
+    sp0 = dm.sparse_info()  # analysis (first use)
+    t_create = time.perf_counter() - t0
+    X0 = list(st.X)
+    for _ in range(max(args.warmup, 1)):
+        rc, _, _ = dm.sweepx(0, times[:1], st.time, X0, **kw)
+        if rc != 0:
+            raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
+    if dist:
+        dist.barrier()
+    nrep = max(1, min(args.steps, 3))
+    with Clocks(local_rank) as ck:
+        t0 = time.perf_counter()
+        for _ in range(nrep):
+            rc, states, stats = dm.sweepx(0, times, st.time, X0, **kw)
+            if rc != 0:
+                raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
+        dt = (time.perf_counter() - t0) / nrep
+    clocks = ck.summary()
+    dt = reduce_max(dist, dt)
+    sp = dm.sparse_info()
+    info = dm.linear_solver_info()
+    dm.close()
+    if rank != 0:
+        return
+    iters = stats.niter_total
+    ms_iter = dt / iters * 1e3
+    fl = sp["flops"]
+    cpu = lattice_solve_cpu_leg()
+    line = {"metric": "ms per Newton iteration (lattice 60x60x20, SweepX{0}, multifrontal device solve)",
+            "value": ms_iter, "unit": "ms", "higher_is_better": False, "n_gpus": ws, "steps": nrep,
+            "warmup": max(args.warmup, 1), "ms_per_step": dt * 1e3, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (FP32 factors in FP64 refinement)" if not sp["fp64"] else "f64",
+            "data": "synthetic (seeded lattice frame, lognormal sections, Gaussian loads)",
+            "config": {"workload": f"lattice frame {nx}x{ny}x{nz}, SweepX{{0}}, {len(times)} load steps",
+                       "dofs": model.ndof["X"], "newton_iterations": iters, "load_steps": stats.nstep_done,
+                       "ms_per_load_step": dt / stats.nstep_done * 1e3, "linear_solver": info,
+                       "multifrontal": sp0 | {k: sp[k] for k in ("fp64", "last_fallback", "last_sweeps",
+                                                                  "last_perturbed", "last_factor_ms",
+                                                                  "last_refine_ms")},
+                       "l2": "inputs larger than L2 (the factors alone are tens of GB)"},
+            "factorisation": {"ms": sp["last_factor_ms"], "flops": fl,
+                              "achieved_tflops": fl / (sp["last_factor_ms"] * 1e-3) / 1e12
+                              if sp["last_factor_ms"] > 0 else None,
+                              "precision": "FP64" if sp["fp64"] else "FP32"},
+            "e2e": {"value": ms_iter, "unit": "ms", "h2d_bytes_per_step": 8 * (model.ndof["X"] + len(times) * (dm.ntval + 1)),
+                    "d2h_bytes_per_step": 8 * model.ndof["X"] * len(times),
+                    "note": "the whole mgpu_sweepx call with host initial state, load values and states"},
+            "cpu_baseline": {"value": cpu["ms_per_newton_iteration"], "unit": "ms per Newton iteration", "kind": "port",
+                             "cores": os.cpu_count(),
+                             "sample": f"oracle SweepX{{0}} of the 12x12x6 lattice ({cpu['dofs']} dofs, "
+                                       f"{cpu['newton_iterations']} iterations, nested-dual assembly + SuperLU); "
+                                       "the full lattice is out of the CPU's reach"},
+            "parity": cpu["parity"], "create_s": t_create, "clocks": clocks,
+            "gpu_launches": None}
+    print(json.dumps(line), flush=True)
 
 
 def bench_solve(args, rank, local_rank, ws, dist):
@@ -486,6 +639,7 @@ def bench_batched(args, rank, local_rank, ws, dist):
         sel = a >= 0
         same &= rci == 0 and bool(np.array_equal(xi[:, 0, a[sel]], xb[:, 0, b[sel]]))
     per_model = 1.0 / float(np.mean(tind))
+    cpu = batched_cpu_leg(params, pick[: args.oracle_models], times, model, offs, xb, x32 if rc32 == 0 else None)
     value = ws * len(params) / dt
     h2d = 8 * (model.ndof["X"] + len(times) * dm.ntval + len(times))
     d2h = 8 * model.ndof["X"] * len(times)
@@ -505,9 +659,42 @@ def bench_batched(args, rank, local_rank, ws, dist):
                                "states_bitwise_equal_to_batch": same},
             "fp32_refined": {"models_per_s": len(params) / dt32 if rc32 == 0 else None, "rc": rc32,
                              "max_rel_state_dev_vs_fp64": worst, "linear_solver": info32,
-                             "newton_iterations": stats32.niter_total},
+                             "newton_iterations": stats32.niter_total,
+                             "max_rel_state_dev_vs_oracle": cpu["dev_fp32"]},
+            "fp64_max_rel_state_dev_vs_oracle": cpu["dev_fp64"],
+            "cpu_baseline": cpu["baseline"],
             "gpu_launches": args.steps * iters * launches_per_iter, "clocks": clocks, "create_s": t_create}
     print(json.dumps(line), flush=True)
+
+
+def batched_cpu_leg(params, pick, times, model, offs, xb, x32):
+    """CPU leg of the batched mode: the oracle's SweepX{0} (nested-dual
+    assembly, SuperLU) of a few sampled models, timed, and the deviation of
+    the device's FP64 and FP32-refined states from it, per dof class relative
+    to that class's largest value over the trajectory."""
+    from muscade_gpu import workloads
+    from oracle import reference as REF
+
+    dev64 = dev32 = 0.0
+    tcpu = 0.0
+    for i in pick:
+        mi, _, _ = workloads.build_batched([params[i]])
+        si = mi.initialize()
+        t0 = time.perf_counter()
+        ref = REF.sweepx(mi, si.dis, si, times, OX=0, maxdx=1e-9, maxLl=math.inf)
+        tcpu += time.perf_counter() - t0
+        nodes = np.arange(1, mi.nnod + 1)
+        a, b = workloads.node_dofs(mi, nodes), workloads.node_dofs(model, nodes + offs[i])
+        sel = a >= 0
+        R = np.stack([Xr[0] for _, Xr in ref])[:, a[sel]]
+        scale = max(float(np.max(np.abs(R))), 1e-300)
+        dev64 = max(dev64, float(np.max(np.abs(xb[:, 0, b[sel]] - R))) / scale)
+        if x32 is not None:
+            dev32 = max(dev32, float(np.max(np.abs(x32[:, 0, b[sel]] - R))) / scale)
+    return {"dev_fp64": dev64, "dev_fp32": dev32 if x32 is not None else None,
+            "baseline": {"value": len(pick) / tcpu if tcpu > 0 else None, "unit": "models/s", "kind": "port",
+                         "cores": 1, "sample": f"{len(pick)} sampled models solved one by one by the oracle "
+                                               "(nested-dual assembly, SuperLU)"}}
 
 
 def bench_adjoint(args, rank, local_rank, ws, dist):

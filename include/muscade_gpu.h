@@ -6,7 +6,8 @@
  * The Julia side keeps Model / addelement! / initialize! and the element API;
  * it hands the device what its Disassembler already holds (per element type,
  * the model dof indices of each element and the element objects' fields) and
- * calls these entry points from a new solver type.
+ * calls these entry points from a new solver type, SweepXGPU{OX}, that
+ * `solve` dispatches to beside SweepX (src/Solve.jl:16-35).
  *
  * Conventions
  *   - Dof indices are 1-based Int64, exactly `dis.dis[ieletyp].index[iele].X`
@@ -222,25 +223,61 @@ int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *
  *                        FP64 iterative refinement; a component whose last
  *                        correction is not below 1e-10 of its solution is solved
  *                        again with the FP64 partitioned factorisation
+ *   MGPU_LINSOLVE_SPARSE multifrontal LU for matrices whose bands are too wide
+ *                        (3D frames, lattices; AUTO picks it there): groups of
+ *                        dofs with equal couplings (the dofs of a node, a Hold's
+ *                        multiplier with the dof it holds) ordered by nested
+ *                        dissection of the element geometry, fronts of dense
+ *                        blocks factorised without row exchanges (multipliers
+ *                        after the dofs they constrain) on the equilibrated
+ *                        matrix, FP32 factors inside FP64 iterative refinement
+ *                        until the scaled correction is below 1e-14 of the
+ *                        scaled solution or stops shrinking below 1e-10 of it
+ *                        (at most 12 sweeps), else the FP64 factors, which then
+ *                        stay in use for the context
+ *   MGPU_LINSOLVE_SPARSE64 the multifrontal LU in FP64 throughout
  * F64 and BLOCK give bitwise the same Δx.  Returns MGPU_ERR_UNSUPPORTED when
- * the bands are too wide for the requested kind. */
+ * the bands are too wide for the requested kind.  The multifrontal kinds
+ * need fixed_iter steps without graph replay and no per_component test, and
+ * give no transposed solve (mgpu_adjoint_sweepx). */
 #define MGPU_LINSOLVE_AUTO 0
 #define MGPU_LINSOLVE_F32IR 1
 #define MGPU_LINSOLVE_F64 2
 #define MGPU_LINSOLVE_BLOCK 3
 #define MGPU_LINSOLVE_TORN 4
 #define MGPU_LINSOLVE_TORN32 5
+#define MGPU_LINSOLVE_SPARSE 6
+#define MGPU_LINSOLVE_SPARSE64 7
 int mgpu_set_linear_solver(mgpu_ctx *ctx, int32_t kind);
 
 typedef struct {
-  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64, _BLOCK, _TORN or _TORN32 in use */
+  int32_t kind;          /* MGPU_LINSOLVE_F32IR, _F64, _BLOCK, _TORN, _TORN32, _SPARSE or _SPARSE64 in use */
   int32_t ncomp;         /* connected components of Lλx */
-  int32_t max_kl;        /* widest lower / upper band after reordering */
+  int32_t max_kl;        /* widest lower / upper band after reordering (multifrontal: the largest front) */
   int32_t max_ku;
   int32_t last_fallback; /* F32IR, TORN32: components refactorised in FP64 in the last solve */
   int32_t last_sweeps;   /* F32IR, TORN32: refinement sweeps in the last solve */
 } mgpu_linsolve_info;
 int mgpu_linear_solver_info(mgpu_ctx *ctx, mgpu_linsolve_info *info);
+
+/* The multifrontal solver's structure and its last solve (no counterpart in
+ * the reference).  MGPU_ERR_UNSUPPORTED when the model has none. */
+typedef struct {
+  int32_t nfront;         /* fronts (supernodes) */
+  int32_t nheight;        /* levels of the elimination tree, leaves at 0 */
+  int32_t nroot;          /* independent trees (connected components) */
+  int32_t max_front;      /* largest front (dofs) */
+  int32_t max_pivots;     /* most pivots of one front */
+  int32_t fp64;           /* 1 when factorising in FP64 */
+  int64_t front_entries;  /* entries of all fronts (the factor storage) */
+  double flops;           /* flops of one factorisation (2 per multiply-add) */
+  int32_t last_fallback;  /* 1 when the last solve fell back to FP64 factors */
+  int32_t last_sweeps;    /* refinement sweeps of the last solve */
+  int32_t last_perturbed; /* FP32 pivots below 1e-10 set to ±1e-10 in the last factorisation */
+  double last_factor_ms;  /* device time of the last solve's factorisation(s) (CUDA events) */
+  double last_refine_ms;  /* and of its substitutions and refinement sweeps */
+} mgpu_sparse_report;
+int mgpu_sparse_info(mgpu_ctx *ctx, mgpu_sparse_report *rep);
 
 /* Autotuner (no counterpart in the reference): on the resident state (after
  * mgpu_upload_state) times one assembly of `mission` with 64, 128 and 256
@@ -267,16 +304,24 @@ int mgpu_autotune(mgpu_ctx *ctx, int32_t mission, const mgpu_newmark *c, mgpu_tu
  *   asm2[nele][144]    1-based positions in nzval   (asm[2,ieletyp], 0 = skip)
  *   x[nX]              state X
  *   Ll[nX], nzval[nnz] outputs, overwritten (zeroed, then summed)
- * It computes the SweepX{0} residual and tangent of the beams (as
- * mgpu_assemble with MGPU_ASM_STATIC on a model of these beams) and enqueues
+ * It computes the SweepX{0} residual and tangent of the beams and enqueues
  * the work on `stream` (a cudaStream_t, NULL for the legacy stream) without
- * synchronising.  Its scratch is one fixed device array that every GPU loading
- * the library holds until exit, so nele is limited to MGPU_NOALLOC_MAX_BEAMS
- * (returns MGPU_ERR_SIZE above it).  All calls on a device share that array:
- * calls that overlap on the GPU (different streams, or host threads without
- * ordering) race and must be serialised by the caller.  The first call on
- * each device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture. */
+ * synchronising.  For beams without U- or A-dofs and with unit dof scales the
+ * results equal those of mgpu_assemble with MGPU_ASM_STATIC on a model of
+ * these beams; U-dof loads, A-dof EI scales and dis.scaleX are not applied.
+ * No NaN check is made: a NaN in an element shows in Ll / nzval, which the
+ * caller reads.  A CUDA error already pending on the calling thread is
+ * returned as MGPU_ERR_CUDA before anything is enqueued.  Its scratch is one
+ * fixed device array that every GPU loading the library holds until exit, so
+ * nele is limited to MGPU_NOALLOC_MAX_BEAMS (returns MGPU_ERR_SIZE above it).
+ * All calls on a device share that array: calls that overlap on the GPU
+ * (different streams, or host threads without ordering) race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current and
+ * keeps it for the life of the process; make that first call before any
+ * stream capture, and do not call this entry point again after
+ * cudaDeviceReset on that device (the kept address belongs to the old
+ * context). */
 #define MGPU_NOALLOC_MAX_BEAMS 4096
 int mgpu_assemble_beams_noalloc(int64_t nele, int64_t nX, int64_t nnz, const double *fields, const int64_t *indexX,
                                 const int64_t *asm1, const int64_t *asm2, const double *x, double *Ll,

@@ -59,6 +59,11 @@ struct mgpu_ctx {
   double* flush = nullptr;  // L2 flush buffer
   size_t flush_bytes = 0;
   int nXder_resident = 1;
+  // host: coordinates of each X-dof's node from the beam and bar elements'
+  // geometry (NaN where no element gives one) and the constraint multipliers;
+  // the sparse solver's ordering uses them
+  std::vector<double> dof_xyz;   // [nX][3]
+  std::vector<uint8_t> dof_last;  // [nX] 1 for the multiplier of a DofConstraint
   int elem_block = 128;     // threads per block of the beam and bar kernels (mgpu_autotune)
   mgpu::Solver* solver = nullptr;
   // constants of the current step, read by the kernels from device memory so

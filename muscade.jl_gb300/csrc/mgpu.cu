@@ -11,7 +11,10 @@
 //      stores of a warp are coalesced;
 //   2. a gather kernel sums, for every nnz of Lλx and every dof of Lλ, the
 //      element entries that map to it, in the order the reference adds them
-//      (no floating-point atomics: results are deterministic run to run).
+//      (no floating-point atomics: results are deterministic run to run).  A
+//      block takes a run of consecutive nnz, stages all their entries in shared
+//      memory with many independent loads in flight, then each thread adds its
+//      nnz's entries in order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -233,15 +236,68 @@ __global__ void load_kernel(int64_t nele, const int32_t* __restrict__ idx, const
   flag_nan(a.errflag, gid0 + e, isnan(r));
 }
 
-// Deterministic gather-sum: out[k] = Σ buf[src[q]], q = seg[k]..seg[k+1]-1, in order.
-__global__ void scatter_kernel(int64_t n, const uint32_t* __restrict__ seg, const uint32_t* __restrict__ src,
-                               const double* __restrict__ buf, double* __restrict__ out) {
-  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const uint32_t a = __ldg(seg + k), b = __ldg(seg + k + 1);
-  double s = 0.0;
-  for (uint32_t q = a; q < b; ++q) s += __ldg(buf + __ldg(src + q));
-  out[k] = s;
+// Deterministic gather-sum:
+//   out[k] = ((0 + buf[src[q0]]) + buf[src[q0+1]]) + ... ,  q = seg[k] .. seg[k+1]-1.
+// A block takes kGatherOut consecutive outputs.  Their plan positions form one
+// run [seg[k0], seg[k0+kGatherOut]); the block stages the run's entries in
+// shared memory, kGatherStage at a time: each thread first loads kGatherPer
+// plan entries (coalesced), then issues the kGatherPer gathered loads of the
+// values, all independent, so that many loads are in flight per SM.  The
+// gathered values of consecutive nnz come from consecutive elements of one
+// entry plane (neighbouring nodes, neighbouring elements), so sectors are
+// reused through L1 within a block.  Then each thread adds, in order, the
+// staged entries of its outputs.
+constexpr int kGatherThreads = 256;
+constexpr int kGatherOut = 1024;    // outputs per block (4 per thread)
+constexpr int kGatherPer = 8;       // staged entries per thread and pass
+constexpr int kGatherStage = kGatherThreads * kGatherPer;
+__global__ void __launch_bounds__(kGatherThreads) scatter_kernel(int64_t n, const uint32_t* __restrict__ seg,
+                                                                 const uint32_t* __restrict__ src,
+                                                                 const double* __restrict__ buf,
+                                                                 double* __restrict__ out) {
+  __shared__ uint32_t sseg[kGatherOut + 1];
+  __shared__ double sval[kGatherStage];
+  const int tid = threadIdx.x;
+  const int64_t k0 = int64_t(blockIdx.x) * kGatherOut;
+  const int nk = int(n - k0 < kGatherOut ? n - k0 : kGatherOut);
+  for (int t = tid; t <= nk; t += kGatherThreads) sseg[t] = __ldg(seg + k0 + t);
+  __syncthreads();
+  const int64_t qa = sseg[0], qb = sseg[nk];
+  constexpr int R = kGatherOut / kGatherThreads;
+  double acc[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc[r] = 0.0;
+  for (int64_t w0 = qa; w0 < qb; w0 += kGatherStage) {
+    const int wn = int(qb - w0 < kGatherStage ? qb - w0 : kGatherStage);
+    uint32_t s[kGatherPer];
+#pragma unroll
+    for (int u = 0; u < kGatherPer; ++u) {
+      const int t = u * kGatherThreads + tid;
+      s[u] = t < wn ? __ldg(src + w0 + t) : 0u;
+    }
+    double v[kGatherPer];
+#pragma unroll
+    for (int u = 0; u < kGatherPer; ++u) v[u] = (u * kGatherThreads + tid < wn) ? __ldg(buf + s[u]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < kGatherPer; ++u) sval[u * kGatherThreads + tid] = v[u];
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int kk = r * kGatherThreads + tid;
+      if (kk < nk) {
+        const int64_t a = sseg[kk], b = sseg[kk + 1];
+        const int64_t lo = a > w0 ? a : w0;
+        const int64_t hi = b < w0 + wn ? b : w0 + wn;
+        for (int64_t q = lo; q < hi; ++q) acc[r] += sval[q - w0];
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int kk = r * kGatherThreads + tid;
+    if (kk < nk) out[k0 + kk] = acc[r];
+  }
 }
 
 __global__ void newmark_ab_kernel(int64_t n, const double* x1, const double* x2, const double* __restrict__ sc,
@@ -338,8 +394,10 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0)
     if (ev_groups) cudaEventRecord(ev_groups[g], c->stream);
   }
   if (c->pat.nnz > 0)
-    scatter_kernel<<<nblk(c->pat.nnz, 256), 256, 0, c->stream>>>(c->pat.nnz, c->mseg, c->msrc, c->kbuf, c->nzval);
-  if (nX > 0) scatter_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, c->vseg, c->vsrc, c->rbuf, c->Ll);
+    scatter_kernel<<<nblk(c->pat.nnz, kGatherOut), kGatherThreads, 0, c->stream>>>(c->pat.nnz, c->mseg, c->msrc,
+                                                                                  c->kbuf, c->nzval);
+  if (nX > 0)
+    scatter_kernel<<<nblk(nX, kGatherOut), kGatherThreads, 0, c->stream>>>(nX, c->vseg, c->vsrc, c->rbuf, c->Ll);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(c, MGPU_ERR_CUDA, std::string("assembly launch: ") + cudaGetErrorString(e));
   return MGPU_OK;
@@ -513,6 +571,26 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
       tvb += G.nele;
     }
     c->groups.push_back(std::move(D));
+  }
+  // ---- node coordinates of the dofs (element geometry) and the constraint multipliers
+  c->dof_xyz.assign(3 * size_t(c->nX), NAN);
+  c->dof_last.assign(size_t(c->nX), 0);
+  for (int g = 0; g < d->ngroup; ++g) {
+    const mgpu_group& G = d->groups[g];
+    if (G.kind == MGPU_EULERBEAM3D || G.kind == MGPU_BAR3D) {
+      // midpoint cₘ and c₂ − c₁ (tgₘ) in the element record: fields 0-2 and 18-20 (beam), 3-5 (bar)
+      const int nd = G.kind == MGPU_EULERBEAM3D ? 6 : 3, ftg = G.kind == MGPU_EULERBEAM3D ? 18 : 3;
+      for (int64_t e = 0; e < G.nele; ++e) {
+        const double* ed = G.edata + e * G.ndata;
+        for (int i = 0; i < 2 * nd; ++i) {
+          const int64_t dof = G.indexX[e * G.nX + i] - 1;
+          const double sgn = i < nd ? -0.5 : 0.5;
+          for (int k = 0; k < 3; ++k) c->dof_xyz[3 * dof + k] = ed[k] + sgn * ed[ftg + k];
+        }
+      }
+    } else if (G.kind == MGPU_DOFCONSTRAINT_X) {
+      for (int64_t e = 0; e < G.nele; ++e) c->dof_last[G.indexX[e * G.nX + G.nX - 1] - 1] = 1;
+    }
   }
   // ---- buffers and scatter plans
   const Pattern& P = c->pat;

@@ -11,8 +11,10 @@
 // loads this library holds that array until the process exits.
 //
 // The summation follows the reference's assembly order (element by element,
-// entries through the asm maps), so the results equal those of mgpu_assemble
-// for the same beams.
+// entries through the asm maps), so for beams without U- or A-dofs and with
+// unit dof scales the results equal those of mgpu_assemble for the same
+// beams.  U-dof loads, A-dof EI scales and dis.scaleX are not applied, and no
+// NaN check is made: a NaN in an element reaches Lλ / nzval through the sums.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -24,9 +26,10 @@ namespace {
 
 constexpr int64_t kMaxBeams = MGPU_NOALLOC_MAX_BEAMS;
 constexpr int kEntries = 144 + 12;  // element matrix and vector entries
+constexpr int kRows = kEntries + 1;  // and one row of repeated-dof flags
 
 // Shared scratch of every call (and every stream) on a device.
-static __device__ __align__(256) double g_noalloc_scratch[kMaxBeams * kEntries];
+static __device__ __align__(256) double g_noalloc_scratch[kMaxBeams * kRows];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
@@ -34,7 +37,8 @@ double* g_scratch_addr[kMaxDevices] = {nullptr};
 
 // Element kernel: static (SweepX{0}) residual and tangent of each beam, written
 // to scratch entry-major: matrix entry k of element e at k*nele+e, vector entry
-// i at (144+i)*nele+e.
+// i at (144+i)*nele+e, and at (156)*nele+e 1.0 when the element lists one dof
+// twice (its entries may then add into the same place), else 0.0.
 __global__ void noalloc_beam_kernel(int64_t nele, const double* __restrict__ fields,
                                     const int64_t* __restrict__ indexX, const double* __restrict__ x,
                                     double* __restrict__ scratch) {
@@ -42,8 +46,14 @@ __global__ void noalloc_beam_kernel(int64_t nele, const double* __restrict__ fie
   if (e >= nele) return;
   mgpu::BeamConst bc;
   mgpu::beam_const_from_fields(fields + e * 69, bc);
+  int64_t dof[12];
+  for (int i = 0; i < 12; ++i) dof[i] = indexX[e * 12 + i];
+  bool repeated = false;
+  for (int i = 0; i < 12; ++i)
+    for (int j = i + 1; j < 12; ++j) repeated |= dof[i] == dof[j];
+  scratch[int64_t(kEntries) * nele + e] = repeated ? 1.0 : 0.0;
   double X0[12];
-  for (int i = 0; i < 12; ++i) X0[i] = x[indexX[e * 12 + i] - 1];
+  for (int i = 0; i < 12; ++i) X0[i] = x[dof[i] - 1];
   double R[12], K[144];
   mgpu::beam_element<false>(bc, X0, X0, X0, nullptr, mgpu::Perturb{1.0, 0.0, 0.0}, nullptr, nullptr, R, K, nullptr,
                             nullptr);
@@ -52,20 +62,14 @@ __global__ void noalloc_beam_kernel(int64_t nele, const double* __restrict__ fie
 }
 
 // One block adds the elements in order (add_value!/add_∂!, src/Assemble.jl:559-608);
-// the entries of one element go in parallel unless the element repeats a dof.
-__global__ void noalloc_accumulate(int64_t nele, const int64_t* __restrict__ indexX,
-                                   const int64_t* __restrict__ asm1, const int64_t* __restrict__ asm2,
+// the entries of one element go in parallel unless the element repeats a dof
+// (flag row of the element kernel), in which case one thread adds them in the
+// reference's entry order.
+__global__ void noalloc_accumulate(int64_t nele, const int64_t* __restrict__ asm1, const int64_t* __restrict__ asm2,
                                    const double* __restrict__ scratch, double* __restrict__ Ll,
                                    double* __restrict__ nzval) {
-  __shared__ int repeated;
   for (int64_t e = 0; e < nele; ++e) {
-    if (threadIdx.x == 0) {
-      int r = 0;
-      for (int i = 0; i < 12; ++i)
-        for (int j = i + 1; j < 12; ++j) r |= (indexX[e * 12 + i] == indexX[e * 12 + j]);
-      repeated = r;
-    }
-    __syncthreads();
+    const bool repeated = scratch[int64_t(kEntries) * nele + e] != 0.0;  // uniform over the block
     if (!repeated) {
       for (int k = threadIdx.x; k < kEntries; k += blockDim.x) {
         if (k < 144) {
@@ -113,6 +117,9 @@ extern "C" int mgpu_assemble_beams_noalloc(int64_t nele, int64_t nX, int64_t nnz
       (nX > 0 && !Ll) || (nnz > 0 && !nzval))
     return MGPU_ERR_ARG;
   if (nele > kMaxBeams) return MGPU_ERR_SIZE;
+  // an error left by the caller's earlier CUDA work on this thread is reported
+  // as it stands, before anything is enqueued (it is not cleared)
+  if (cudaPeekAtLastError() != cudaSuccess) return MGPU_ERR_CUDA;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return MGPU_ERR_CUDA;
   double* scratch = nullptr;
@@ -124,7 +131,8 @@ extern "C" int mgpu_assemble_beams_noalloc(int64_t nele, int64_t nX, int64_t nnz
   if (nnz > 0 && cudaMemsetAsync(nzval, 0, size_t(nnz) * sizeof(double), st) != cudaSuccess) return MGPU_ERR_CUDA;
   if (nele > 0) {
     noalloc_beam_kernel<<<unsigned((nele + 63) / 64), 64, 0, st>>>(nele, fields, indexX, x, scratch);
-    noalloc_accumulate<<<1, 256, 0, st>>>(nele, indexX, asm1, asm2, scratch, Ll, nzval);
+    if (cudaGetLastError() != cudaSuccess) return MGPU_ERR_CUDA;
+    noalloc_accumulate<<<1, 256, 0, st>>>(nele, asm1, asm2, scratch, Ll, nzval);
   }
   return cudaGetLastError() == cudaSuccess ? MGPU_OK : MGPU_ERR_CUDA;
 }

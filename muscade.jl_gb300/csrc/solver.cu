@@ -748,28 +748,73 @@ __global__ void decrement_kernel(int64_t n, int OX, int first, const double* dx,
 
 }  // namespace mgpu
 
+static bool sparse_usable(const Solver& S) { return S.sparse && S.sparse->why.empty(); }
+static bool is_sparse(int path) { return path == PATH_SPARSE || path == PATH_SPARSE64; }
+
+// the multifrontal solver, analysed on first need
+static int ensure_sparse(mgpu_ctx* c, Solver& S) {
+  if (S.sparse) return MGPU_OK;
+  const int rc = sparse_create(c, S.sparse, c->dof_xyz.empty() ? nullptr : c->dof_xyz.data(),
+                               c->dof_last.empty() ? nullptr : c->dof_last.data());
+  if (rc != MGPU_OK) {
+    sparse_destroy(S.sparse);
+    return rc;
+  }
+  // the Newton loop's buffers (the banded analysis allocates them only when it applies)
+  const int64_t n = std::max<int64_t>(c->nX, 1);
+  if (!S.dx) MG_CUDA(cudaMalloc(&S.dx, n * sizeof(double)));
+  if (!S.red) MG_CUDA(cudaMalloc(&S.red, 4 * sizeof(double)));
+  if (!S.part) MG_CUDA(cudaMalloc(&S.part, 2 * kNormBlocks * sizeof(double)));
+  if (!S.info) {
+    MG_CUDA(cudaMalloc(&S.info, kInfoSlots * sizeof(int)));
+    MG_CUDA(cudaMemset(S.info, 0, kInfoSlots * sizeof(int)));
+  }
+  if (!S.hbuf) MG_CUDA(cudaMallocHost(&S.hbuf, 8 * sizeof(double)));
+  return MGPU_OK;
+}
+
 extern "C" int mgpu_solver_create(mgpu_ctx* c) {
   c->solver = new Solver();
   Solver& S = *c->solver;
   analyse(c, S);
   cudaGetLastError();  // analysis errors are reported at solve time
   // default: the FP64 row-band kernels where they apply, else the FP64 block
-  // kernels (mgpu_set_linear_solver changes it)
+  // kernels; the multifrontal solver where the bands are too wide
+  // (mgpu_set_linear_solver changes it)
   S.path = S.tearable ? PATH_TORN32 : S.wm ? PATH_F64ROWS : PATH_BLOCK;
   S.adaptive = S.tearable;
+  if (!S.ok && c->nX > 0) S.path = PATH_SPARSE;  // analysed on first use (a model may only be assembled)
   if (getenv("MGPU_VERBOSE")) {
     static const char* names[] = {"row-band FP32 + FP64 refinement", "row-band FP64", "block FP64",
                                   "partitioned FP64", "partitioned FP32 + FP64 refinement"};
     fprintf(stderr, "[muscade_gpu] solver: %s, %d components, max kl %d, max ku %d, %s\n",
-            S.ok ? "banded" : S.why.c_str(), S.ncomp, S.maxkl, S.maxku, names[S.path]);
+            S.ok ? "banded" : S.why.c_str(), S.ncomp, S.maxkl, S.maxku,
+            is_sparse(S.path) ? "multifrontal" : names[S.path]);
   }
   return MGPU_OK;
 }
 
 extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
-  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_TORN32)
+  if (!c || !c->solver || kind < MGPU_LINSOLVE_AUTO || kind > MGPU_LINSOLVE_SPARSE64)
     return set_err(c, MGPU_ERR_ARG, "mgpu_set_linear_solver: bad arguments");
   Solver& S = *c->solver;
+  MG_CUDA(cudaSetDevice(c->device));
+  if (kind == MGPU_LINSOLVE_SPARSE || kind == MGPU_LINSOLVE_SPARSE64) {
+    const int rc = ensure_sparse(c, S);
+    if (rc != MGPU_OK) return rc;
+    if (!sparse_usable(S)) return set_err(c, MGPU_ERR_UNSUPPORTED, "multifrontal solver: " + S.sparse->why);
+    S.path = kind == MGPU_LINSOLVE_SPARSE ? PATH_SPARSE : PATH_SPARSE64;
+    S.sparse->fp64_only = kind == MGPU_LINSOLVE_SPARSE64;
+    S.sparse->adaptive = true;
+    return MGPU_OK;
+  }
+  if (kind == MGPU_LINSOLVE_AUTO && !S.ok) {  // the multifrontal solver, analysed on first use
+    S.path = PATH_SPARSE;
+    if (S.sparse) S.sparse->fp64_only = false;
+    return MGPU_OK;
+  }
+  if (!S.ok)
+    return set_err(c, MGPU_ERR_UNSUPPORTED, "banded solver kinds need narrow bands: " + S.why);
   if (kind == MGPU_LINSOLVE_TORN || kind == MGPU_LINSOLVE_TORN32) {
     if (!S.tearable)
       return set_err(c, MGPU_ERR_UNSUPPORTED,
@@ -793,6 +838,19 @@ extern "C" int mgpu_set_linear_solver(mgpu_ctx* c, int32_t kind) {
 extern "C" int mgpu_linear_solver_info(mgpu_ctx* c, mgpu_linsolve_info* info) {
   if (!c || !c->solver || !info) return set_err(c, MGPU_ERR_ARG, "mgpu_linear_solver_info: bad arguments");
   Solver& S = *c->solver;
+  if (is_sparse(S.path)) {
+    MG_CUDA(cudaSetDevice(c->device));
+    const int rc = ensure_sparse(c, S);
+    if (rc != MGPU_OK) return rc;
+    if (!sparse_usable(S)) return set_err(c, MGPU_ERR_UNSUPPORTED, "multifrontal solver: " + S.sparse->why);
+    const SparseDev& sp = *S.sparse;
+    info->kind = S.path == PATH_SPARSE ? MGPU_LINSOLVE_SPARSE : MGPU_LINSOLVE_SPARSE64;
+    info->ncomp = sp.nroot;
+    info->max_kl = info->max_ku = sp.max_m;
+    info->last_fallback = sp.last_fallback;
+    info->last_sweeps = sp.last_sweeps;
+    return MGPU_OK;
+  }
   info->kind = S.path == PATH_F32IR    ? MGPU_LINSOLVE_F32IR
                : S.path == PATH_F64ROWS ? MGPU_LINSOLVE_F64
                : S.path == PATH_TORN    ? MGPU_LINSOLVE_TORN
@@ -897,9 +955,38 @@ extern "C" int mgpu_autotune(mgpu_ctx* c, int32_t mission, const mgpu_newmark* n
   return rc;
 }
 
+extern "C" int mgpu_sparse_info(mgpu_ctx* c, mgpu_sparse_report* rep) {
+  if (!c || !c->solver || !rep) return set_err(c, MGPU_ERR_ARG, "mgpu_sparse_info: bad arguments");
+  Solver& S = *c->solver;
+  MG_CUDA(cudaSetDevice(c->device));
+  if (is_sparse(S.path) || !S.ok) {
+    const int rc = ensure_sparse(c, S);
+    if (rc != MGPU_OK) return rc;
+  }
+  if (!sparse_usable(S))
+    return set_err(c, MGPU_ERR_UNSUPPORTED,
+                   std::string("no multifrontal solver for this model") + (S.sparse ? ": " + S.sparse->why : ""));
+  const SparseDev& sp = *S.sparse;
+  rep->nfront = sp.nfront;
+  rep->nheight = sp.nheight;
+  rep->nroot = sp.nroot;
+  rep->max_front = sp.max_m;
+  rep->max_pivots = sp.max_p;
+  rep->front_entries = sp.fsize;
+  rep->flops = sp.flops;
+  rep->fp64 = sp.fp64_only ? 1 : 0;
+  rep->last_fallback = sp.last_fallback;
+  rep->last_sweeps = sp.last_sweeps;
+  rep->last_perturbed = sp.last_perturbed;
+  rep->last_factor_ms = sp.last_factor_ms;
+  rep->last_refine_ms = sp.last_refine_ms;
+  return MGPU_OK;
+}
+
 extern "C" void mgpu_solver_destroy(mgpu_ctx* c) {
   Solver* S = c->solver;
   if (!S) return;
+  sparse_destroy(S->sparse);
   void* ps[] = {S->cbase, S->cn, S->ckl, S->cku, S->cdof0, S->perm, S->bmap, S->AB, S->ipiv, S->rhs, S->dx,
                 S->red, S->info, S->rbase, S->lbase, S->rbmap, S->rbmapT, S->RB, S->RB32, S->UC32, S->LM32, S->UC64, S->LM64,
                 S->bw, S->xw, S->rw, S->tw32, S->tw64, S->flag, S->nsweep, S->rdiag, S->part, S->cod, S->frozen,
@@ -1151,7 +1238,11 @@ static int torn_solve(mgpu_ctx* c, bool tr, const double* rhs, double* out, int*
 int factor_solve(mgpu_ctx* c, int* info) {
   Solver& S = *c->solver;
   cudaStream_t st = c->stream;
-  if (S.path == PATH_TORN || S.path == PATH_TORN32) {
+  if (is_sparse(S.path)) {
+    const int rc = sparse_factor_solve(c, *S.sparse, c->Ll, S.dx, info);
+    if (rc) return rc;
+    if (S.sparse->fp64_only && S.path == PATH_SPARSE) S.path = PATH_SPARSE64;  // after a fallback
+  } else if (S.path == PATH_TORN || S.path == PATH_TORN32) {
     const int rc = torn_solve(c, false, c->Ll, S.dx, info);
     if (rc) return rc;
   } else if (S.path == PATH_BLOCK) {
@@ -1181,6 +1272,8 @@ int factor_solve(mgpu_ctx* c, int* info) {
 
 int factor_solve_T(mgpu_ctx* c, const double* rhs, double* out, int* info) {
   Solver& S = *c->solver;
+  if (is_sparse(S.path))
+    return set_err(c, MGPU_ERR_UNSUPPORTED, "transposed solve needs a banded solver kind (not the multifrontal one)");
   if (S.path == PATH_TORN || S.path == PATH_TORN32) return torn_solve(c, true, rhs, out, info);
   if (!S.wmT)
     return set_err(c, MGPU_ERR_UNSUPPORTED,
@@ -1434,7 +1527,21 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
     return set_err(c, MGPU_ERR_ARG, "mgpu_sweepx: per_component needs the convergence test (fixed_iter = 0)");
   *stats = mgpu_stats{0, 0, 0, 0, 0.0, 0.0};
   Solver& S = *c->solver;
-  if (!S.ok) return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why);
+  const bool sparse = is_sparse(S.path);
+  MG_CUDA(cudaSetDevice(c->device));
+  if (sparse) {
+    const int rc = ensure_sparse(c, S);
+    if (rc != MGPU_OK) return rc;
+    if (!sparse_usable(S))
+      return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why + "; multifrontal solver: " +
+                                                  S.sparse->why);
+  }
+  if (!S.ok && !sparse)
+    return set_err(c, MGPU_ERR_UNSUPPORTED,
+                   "no device solver for this model: " + S.why +
+                       (S.sparse ? "; multifrontal solver: " + S.sparse->why : std::string()));
+  if (sparse && opts->per_component)
+    return set_err(c, MGPU_ERR_UNSUPPORTED, "per-component convergence needs a banded solver kind");
   MG_CUDA(cudaSetDevice(c->device));
   cudaStream_t st = c->stream;
   const int64_t n = c->nX;
@@ -1443,7 +1550,8 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
   if (nXder0 > 0) MG_CUDA(cudaMemcpyAsync(c->x, x0, nXder0 * n * sizeof(double), cudaMemcpyHostToDevice, st));
   if (c->nU > 0 && u) MG_CUDA(cudaMemcpyAsync(c->u, u, c->nU * sizeof(double), cudaMemcpyHostToDevice, st));
   c->nXder_resident = OX + 1;
-  if (opts->fixed_iter > 0 && opts->fixed_iter < kInfoSlots && !opts->no_graph)
+  // the multifrontal solve decides its FP64 fallback on the host: launched step by step
+  if (opts->fixed_iter > 0 && opts->fixed_iter < kInfoSlots && !opts->no_graph && !sparse)
     return sweep_graph(c, OX, nstep, times, t0, tvals, opts, states, stats);
   const int nder = OX + 1;
   double told = t0;

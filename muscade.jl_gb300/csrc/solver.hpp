@@ -8,6 +8,7 @@
 
 #include "band_torn.cuh"
 #include "ctx.hpp"
+#include "sparse_lu.hpp"
 
 namespace mgpu {
 
@@ -22,11 +23,14 @@ enum SolverPath : int {
   PATH_F64ROWS = 1,  // row-band warp kernels in FP64
   PATH_BLOCK = 2,  // gbtf2-layout block kernels in FP64 (any band width up to 256)
   PATH_TORN = 3,   // long components cut into interiors and separators, FP64
-  PATH_TORN32 = 4  // the same with FP32 factors inside FP64 iterative refinement, FP64 fallback per component
+  PATH_TORN32 = 4,  // the same with FP32 factors inside FP64 iterative refinement, FP64 fallback per component
+  PATH_SPARSE = 5,  // multifrontal LU (sparse_lu.hpp), FP32 factors in FP64 refinement, FP64 fallback
+  PATH_SPARSE64 = 6  // the same in FP64
 };
 
 struct Solver {
   bool ok = false;       // banded scheme applicable
+  SparseDev* sparse = nullptr;  // multifrontal solver (built when the bands are too wide, or on request)
   int path = PATH_BLOCK;
   int wm = 0;            // row-band register window (32 or 64), 0 if the row-band kernels do not apply
   int n32 = 0, n64 = 0;  // components whose band fits a 32- / needs a 64-wide window (substitution)

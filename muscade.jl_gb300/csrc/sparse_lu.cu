@@ -1,0 +1,769 @@
+// Device sparse direct solver: multifrontal LU over nested-dissection fronts
+// (see sparse_lu.hpp and sparse_analysis.hpp).
+#include "sparse_lu.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+
+#include "ctx.hpp"
+#include "sparse_analysis.hpp"
+
+namespace mgpu {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kNB32 = 64;  // pivot block of the FP32 factorisation
+constexpr int kNB64 = 32;  // of the FP64 factorisation (register rows of the L panel)
+constexpr int kTile = 64;  // trailing-update tile
+constexpr int kMaxGridY = 65535;
+constexpr double kRefineTol = 1e-14;   // scaled correction / scaled solution: converged
+constexpr double kRefineStall = 1e-10;  // ... or stalled below this
+
+inline unsigned nblocks(int64_t n, int b) { return unsigned((n + b - 1) / b); }
+
+// ---------------------------------------------------------------- equilibration
+__global__ void sp_scale_diag(int64_t n, const int32_t* __restrict__ diag, const double* __restrict__ nzval,
+                              double* __restrict__ D0) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t q = diag[i];
+  const double a = q >= 0 ? fabs(nzval[q]) : 0.0;
+  D0[i] = a > 0.0 ? 1.0 / sqrt(a) : 0.0;
+}
+
+// a dof without a diagonal value (a constraint multiplier): the scale that makes
+// its largest column entry one, from the scales of the dofs it couples to
+__global__ void sp_scale_zero(int64_t n, const int64_t* __restrict__ colptr, const int32_t* __restrict__ rowval,
+                              const double* __restrict__ nzval, const double* __restrict__ D0,
+                              double* __restrict__ D) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double d = D0[i];
+  if (d == 0.0) {
+    double mx = 0.0;
+    for (int64_t q = colptr[i]; q < colptr[i + 1]; ++q) mx = fmax(mx, fabs(nzval[q]) * D0[rowval[q]]);
+    d = mx > 0.0 ? 1.0 / mx : 1.0;
+  }
+  D[i] = d;
+}
+
+// ---------------------------------------------------------------- assembly of the fronts
+template <class T>
+__global__ void sp_assemble(int64_t cnt, const int32_t* __restrict__ aq, const int64_t* __restrict__ amap,
+                            const int32_t* __restrict__ rowval, const int32_t* __restrict__ acol,
+                            const double* __restrict__ nzval, const double* __restrict__ D, T* __restrict__ F) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= cnt) return;
+  const int32_t q = aq[t];
+  F[amap[q]] = T(nzval[q] * D[rowval[q]] * D[acol[q]]);
+}
+
+// extend-add of one child per parent (the children of rank r): the child's
+// trailing Schur complement into its parent's front; a warp adds two columns
+template <class T>
+__global__ void __launch_bounds__(kThreads) sp_extend_add(const SpFrontDev* __restrict__ fr,
+                                                          const int32_t* __restrict__ list,
+                                                          const int32_t* __restrict__ emap, T* __restrict__ F) {
+  const SpFrontDev C = fr[list[blockIdx.y]];
+  const SpFrontDev P = fr[C.parent];
+  const int uc = C.m - C.p;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int32_t* em = emap + C.eoff;
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    const int k = blockIdx.x * 16 + w * 2 + kk;
+    if (k >= uc) break;
+    const T* src = F + C.off + int64_t(C.p + k) * C.m + C.p;
+    T* dst = F + P.off + int64_t(em[k]) * P.m;
+    for (int l = lane; l < uc; l += 32) dst[em[l]] += src[l];
+  }
+}
+
+// ---------------------------------------------------------------- partial LU of the fronts
+// The kb × kb diagonal block of pivot block k0, loaded from the front and
+// factored in shared memory (no row exchanges; a pivot below tau in magnitude
+// is set to ±tau, counted when `count`; a zero pivot with tau = 0 or a
+// non-finite one sets flags[3]).  Every block that needs it computes it the same
+// way, so the panel kernel reads the block unchanged and the update kernel
+// writes it back.
+template <class T, int NB>
+__device__ void factor_diag(const T* A, int m, int k0, int kb, T (*Dg)[NB + 1], T tau, int* flags, bool count) {
+  const int tid = threadIdx.x;
+  for (int t = tid; t < kb * kb; t += kThreads) {
+    const int i = t % kb, j = t / kb;
+    Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
+  }
+  __syncthreads();
+  for (int k = 0; k < kb; ++k) {
+    if (tid == 0) {
+      const T d = Dg[k][k];
+      if (!isfinite(d) || (d == T(0) && tau == T(0))) {
+        if (count) atomicOr(flags + 3, 1);
+      } else if (fabs(d) < tau) {
+        Dg[k][k] = d < T(0) ? -tau : tau;
+        if (count) atomicAdd(flags + 2, 1);
+      }
+    }
+    __syncthreads();
+    const T piv = Dg[k][k];
+    for (int i = k + 1 + tid; i < kb; i += kThreads) Dg[i][k] /= piv;
+    __syncthreads();
+    const int r = kb - k - 1;
+    for (int t = tid; t < r * r; t += kThreads) {
+      const int i = k + 1 + t % r, j = k + 1 + t / r;
+      Dg[i][j] -= Dg[i][k] * Dg[k][j];
+    }
+    __syncthreads();
+  }
+}
+
+// Pivot block k0 .. k0+kb-1 of every listed front: each block factors the
+// diagonal block (factor_diag), then solves either 256 rows of the L panel
+// (x U₁₁ = a) or 64 columns of the U panel (L₁₁ y = a).  The diagonal block
+// itself is left as it was (other blocks of the launch read it) and written
+// by the update kernel.
+template <class T, int NB>
+__global__ void __launch_bounds__(kThreads) sp_panel(const SpFrontDev* __restrict__ fr,
+                                                     const int32_t* __restrict__ flist, int k0, T* __restrict__ F,
+                                                     T tau, int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p) return;
+  const int kb = min(NB, p - k0);
+  const int r0 = k0 + kb, rest = m - r0;
+  const int nrc = (rest + kThreads - 1) / kThreads, ncc = (rest + 63) / 64;
+  if (int(blockIdx.x) >= nrc + ncc) return;
+  T* A = F + Fr.off;
+  __shared__ T Dg[NB][NB + 1];
+  const int tid = threadIdx.x;
+  factor_diag<T, NB>(A, m, k0, kb, Dg, tau, flags, false);
+  const int b = blockIdx.x;
+  if (b < nrc) {
+    const int i = r0 + b * kThreads + tid;
+    if (i < m) {
+      T x[NB];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) x[c] = c < kb ? A[i + int64_t(k0 + c) * m] : T(0);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < kb) {
+          x[c] /= Dg[c][c];
+#pragma unroll
+          for (int t = c + 1; t < NB; ++t)
+            if (t < kb) x[t] -= x[c] * Dg[c][t];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NB; ++c)
+        if (c < kb) A[i + int64_t(k0 + c) * m] = x[c];
+    }
+  } else if (b < nrc + ncc) {
+    const int w = tid >> 5, lane = tid & 31;
+    for (int jj = 0; jj < 8; ++jj) {
+      const int j = r0 + (b - nrc) * 64 + w * 8 + jj;
+      if (j >= m) break;
+      T* col = A + int64_t(j) * m + k0;
+      T y0 = lane < kb ? col[lane] : T(0);
+      T y1 = (NB > 32 && lane + 32 < kb) ? col[lane + 32] : T(0);
+      for (int c = 0; c < kb; ++c) {
+        const T yc = __shfl_sync(0xffffffffu, c < 32 ? y0 : y1, c & 31);
+        if (lane > c && lane < kb) y0 -= Dg[lane][c] * yc;
+        if (NB > 32 && lane + 32 > c && lane + 32 < kb) y1 -= Dg[(lane + 32) % NB][c] * yc;
+      }
+      if (lane < kb) col[lane] = y0;
+      if (NB > 32 && lane + 32 < kb) col[lane + 32] = y1;
+    }
+  }
+}
+
+// trailing update of every listed front after pivot block k0: A₂₂ -= L₂₁ U₁₂,
+// one 64 × 64 tile per block (4 × 4 per thread; a warp's rows are consecutive);
+// the block after the last tile writes the factored diagonal block
+template <class T, int NB>
+__global__ void __launch_bounds__(kThreads) sp_update(const SpFrontDev* __restrict__ fr,
+                                                      const int32_t* __restrict__ flist, int k0, T* __restrict__ F,
+                                                      T tau, int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p) return;
+  const int kb = min(NB, p - k0), r0 = k0 + kb, rest = m - r0;
+  const int nt = (rest + kTile - 1) / kTile;
+  if (int(blockIdx.x) > nt * nt) return;
+  T* A = F + Fr.off;
+  __shared__ T As[NB][kTile + 1];  // L₂₁ tile, As[c][i]
+  __shared__ T Bs[NB][kTile + 1];  // U₁₂ tile, Bs[c][j]
+  const int tid = threadIdx.x;
+  if (int(blockIdx.x) == nt * nt) {
+    static_assert(NB * (NB + 1) <= NB * (kTile + 1), "the diagonal block fits the tile buffer");
+    T(*Dg)[NB + 1] = reinterpret_cast<T(*)[NB + 1]>(&As[0][0]);
+    factor_diag<T, NB>(A, m, k0, kb, Dg, tau, flags, true);
+    for (int t = tid; t < kb * kb; t += kThreads) {
+      const int i = t % kb, j = t / kb;
+      A[(k0 + i) + int64_t(k0 + j) * m] = Dg[i][j];
+    }
+    return;
+  }
+  const int i0 = r0 + (blockIdx.x % nt) * kTile, j0 = r0 + (blockIdx.x / nt) * kTile;
+  for (int t = tid; t < NB * kTile; t += kThreads) {
+    const int i = t % kTile, c = t / kTile;
+    As[c][i] = (c < kb && i0 + i < m) ? A[(i0 + i) + int64_t(k0 + c) * m] : T(0);
+  }
+  for (int t = tid; t < NB * kTile; t += kThreads) {
+    const int c = t % NB, j = t / NB;
+    Bs[c][j] = (c < kb && j0 + j < m) ? A[(k0 + c) + int64_t(j0 + j) * m] : T(0);
+  }
+  __syncthreads();
+  const int tr = tid & 15, tc = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+#pragma unroll 8
+  for (int c = 0; c < NB; ++c) {
+    T a[4], bb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u] = As[c][tr + 16 * u];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) bb[v] = Bs[c][tc + 16 * v];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] += a[u] * bb[v];
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const int j = j0 + tc + 16 * v;
+    if (j >= m) continue;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + tr + 16 * u;
+      if (i < m) A[i + int64_t(j) * m] -= acc[u][v];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- substitutions (FP64 vectors)
+// forward, leaves first: v = the front's pivot entries plus the children's
+// update vectors (in child order); y = L₁₁⁻¹ v[0:p] by blocks of 32 columns
+// (one warp solves the block, all threads update the rows below); the update
+// part goes to the parent through cvec
+template <class T>
+__global__ void __launch_bounds__(kThreads) sp_forward(const SpFrontDev* __restrict__ fr,
+                                                       const int32_t* __restrict__ flist,
+                                                       const int32_t* __restrict__ clist,
+                                                       const int32_t* __restrict__ emap, const T* __restrict__ F,
+                                                       double* __restrict__ w, double* __restrict__ cvec,
+                                                       const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.x]];
+  extern __shared__ double v[];
+  __shared__ double yb[32];
+  const int m = Fr.m, p = Fr.p, tid = threadIdx.x;
+  for (int t = tid; t < m; t += kThreads) v[t] = t < p ? w[Fr.pos0 + t] : 0.0;
+  __syncthreads();
+  for (int k = 0; k < Fr.nc; ++k) {
+    const SpFrontDev C = fr[clist[Fr.c0 + k]];
+    const int uc = C.m - C.p;
+    for (int t = tid; t < uc; t += kThreads) v[emap[C.eoff + t]] += cvec[C.eoff + t];
+    __syncthreads();
+  }
+  const T* A = F + Fr.off;
+  for (int c0 = 0; c0 < p; c0 += 32) {
+    const int cb = min(32, p - c0);
+    if (tid < 32) {
+      double y = tid < cb ? v[c0 + tid] : 0.0;
+      for (int c = 0; c < cb; ++c) {
+        const double yc = __shfl_sync(0xffffffffu, y, c);
+        if (tid > c && tid < cb) y -= double(A[(c0 + tid) + int64_t(c0 + c) * m]) * yc;
+      }
+      if (tid < cb) {
+        v[c0 + tid] = y;
+        yb[tid] = y;
+      }
+    }
+    __syncthreads();
+    for (int i = c0 + cb + tid; i < m; i += kThreads) {
+      double s = 0.0;
+      for (int c = 0; c < cb; ++c) s += double(A[i + int64_t(c0 + c) * m]) * yb[c];
+      v[i] -= s;
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < p; t += kThreads) w[Fr.pos0 + t] = v[t];
+  if (Fr.parent >= 0)
+    for (int t = p + tid; t < m; t += kThreads) cvec[Fr.eoff + (t - p)] = v[t];
+}
+
+// backward, roots first: x[0:p] = U₁₁⁻¹ (y − U₁₂ x_u), x_u the ancestors' values
+template <class T>
+__global__ void __launch_bounds__(kThreads) sp_backward(const SpFrontDev* __restrict__ fr,
+                                                        const int32_t* __restrict__ flist,
+                                                        const int32_t* __restrict__ fidx, const T* __restrict__ F,
+                                                        double* __restrict__ w, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.x]];
+  extern __shared__ double v[];
+  __shared__ double part[8][33];
+  const int m = Fr.m, p = Fr.p, tid = threadIdx.x;
+  for (int t = tid; t < m; t += kThreads) v[t] = t < p ? w[Fr.pos0 + t] : w[fidx[Fr.idx + t]];
+  __syncthreads();
+  const T* A = F + Fr.off;
+  const int wp = tid >> 5, lane = tid & 31;
+  for (int c1 = p; c1 > 0; c1 -= 32) {
+    const int c0 = max(0, c1 - 32), cb = c1 - c0;
+    double s = 0.0;
+    if (lane < cb)
+      for (int j = c1 + wp; j < m; j += 8) s += double(A[(c0 + lane) + int64_t(j) * m]) * v[j];
+    part[wp][lane] = s;
+    __syncthreads();
+    if (tid < 32) {
+      double b = 0.0;
+      if (lane < cb) {
+        b = v[c0 + lane];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) b -= part[q][lane];
+      }
+      for (int c = cb - 1; c >= 0; --c) {
+        double xc = lane == c ? b / double(A[(c0 + c) + int64_t(c0 + c) * m]) : 0.0;
+        xc = __shfl_sync(0xffffffffu, xc, c);
+        if (lane == c)
+          b = xc;
+        else if (lane < c)
+          b -= double(A[(c0 + lane) + int64_t(c0 + c) * m]) * xc;
+      }
+      if (lane < cb) v[c0 + lane] = b;
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < p; t += kThreads) w[Fr.pos0 + t] = v[t];
+}
+
+// ---------------------------------------------------------------- refinement
+__global__ void sp_gather_scaled(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ D,
+                                 const double* __restrict__ r, double* __restrict__ w, const int* __restrict__ conv) {
+  if (*conv) return;
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int32_t d = perm[k];
+  w[k] = D[d] * r[d];
+}
+
+__device__ __forceinline__ void max_bits(unsigned long long* dst, double v) {
+  // |v| as ordered bits (non-negative doubles order like their bit patterns); NaN wins
+  atomicMax(dst, (unsigned long long)__double_as_longlong(isnan(v) ? INFINITY : fabs(v)));
+}
+
+__global__ void __launch_bounds__(kThreads) sp_accumulate(int64_t n, int first, const int32_t* __restrict__ perm,
+                                                          const double* __restrict__ D, const double* __restrict__ w,
+                                                          double* __restrict__ yacc, double* __restrict__ x,
+                                                          unsigned long long* __restrict__ nrm,
+                                                          const int* __restrict__ conv) {
+  if (*conv) return;
+  __shared__ double smax[2][kThreads / 32];
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  double mw = 0.0, my = 0.0;
+  if (k < n) {
+    const double z = w[k];
+    const double y = first ? z : yacc[k] + z;
+    yacc[k] = y;
+    const int32_t d = perm[k];
+    x[d] = D[d] * y;
+    mw = isnan(z) ? INFINITY : fabs(z);
+    my = isnan(y) ? INFINITY : fabs(y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+    my = fmax(my, __shfl_xor_sync(0xffffffffu, my, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    smax[0][threadIdx.x >> 5] = mw;
+    smax[1][threadIdx.x >> 5] = my;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < kThreads / 32; ++q) {
+      mw = fmax(mw, smax[0][q]);
+      my = fmax(my, smax[1][q]);
+    }
+    max_bits(nrm, mw);
+    max_bits(nrm + 1, my);
+  }
+}
+
+// Converged when the scaled correction is below tol of the scaled solution,
+// or when it has stopped shrinking (no better than half the previous one)
+// while below stall of the solution: the attainable accuracy of the FP64
+// residual is then reached.  prev holds the previous correction's norm.
+__global__ void sp_check(unsigned long long* nrm, double* prev, int* flags, double tol, double stall) {
+  if (flags[0]) return;
+  const double nw = __longlong_as_double((long long)nrm[0]), ny = __longlong_as_double((long long)nrm[1]);
+  flags[1] += 1;
+  if (nw <= tol * ny || (flags[1] > 1 && nw >= 0.5 * *prev && nw <= stall * ny)) flags[0] = 1;
+  *prev = nw;
+  nrm[0] = 0ull;
+  nrm[1] = 0ull;
+}
+
+__global__ void __launch_bounds__(kThreads) sp_residual(int64_t n, const int64_t* __restrict__ rptr,
+                                                        const int32_t* __restrict__ rq,
+                                                        const int32_t* __restrict__ rcol,
+                                                        const double* __restrict__ nzval,
+                                                        const double* __restrict__ x, const double* __restrict__ b,
+                                                        double* __restrict__ r, const int* __restrict__ conv) {
+  if (*conv) return;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = b[i];
+  for (int64_t t = rptr[i]; t < rptr[i + 1]; ++t) s -= nzval[rq[t]] * x[rcol[t]];
+  r[i] = s;
+}
+
+template <class T>
+cudaError_t upload(T** dst, const std::vector<T>& v) {
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(v.size(), 1) * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return v.empty() ? cudaSuccess : cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+template <class T, int NB>
+cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
+  cudaStream_t st = c->stream;
+  for (int h = 0; h < sp.nheight; ++h) {
+    if (sp.h_nlf[h] == 0) continue;
+    cudaError_t e = cudaMemsetAsync(F + sp.h_off0[h], 0, (sp.h_off1[h] - sp.h_off0[h]) * sizeof(T), st);
+    if (e != cudaSuccess) return e;
+    const int64_t na = sp.h_aq0[h + 1] - sp.h_aq0[h];
+    if (na > 0)
+      sp_assemble<T><<<nblocks(na, kThreads), kThreads, 0, st>>>(na, sp.d_aq + sp.h_aq0[h], sp.d_amap, sp.d_rowval,
+                                                                 sp.d_acol, c->nzval, sp.D, F);
+    for (size_t r = 0; r < sp.h_nea[h].size(); ++r) {
+      const int cnt = sp.h_nea[h][r];
+      for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
+        const dim3 g(nblocks(sp.h_eumax[h][r], 16), unsigned(std::min(kMaxGridY, cnt - f0)));
+        sp_extend_add<T><<<g, kThreads, 0, st>>>(sp.d_fr, sp.d_ea + sp.h_ea0[h][r] + f0, sp.d_emap, F);
+      }
+    }
+    const auto& lp = sp.h_lfp[h];  // pivots of the height's fronts, descending
+    for (int k0 = 0; k0 < sp.h_pmax[h]; k0 += NB) {
+      int cnt = 0;
+      while (cnt < int(lp.size()) && lp[cnt] > k0) ++cnt;
+      // rows and columns after the pivot block, bounded over the fronts of this step
+      const int rest = sp.h_mmax[h] - k0;
+      const int nrc = (rest + kThreads - 1) / kThreads, ncc = (rest + 63) / 64;
+      const int nt = (rest + kTile - 1) / kTile;
+      for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
+        const int32_t* fl = sp.d_lf + sp.h_lf0[h] + f0;
+        const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
+        if (nrc + ncc > 0)
+          sp_panel<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+        sp_update<T, NB><<<dim3(unsigned(nt * nt + 1), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+      }
+    }
+  }
+  return cudaGetLastError();
+}
+
+// refinement sweeps with the factors F: x = Lλx⁻¹ b
+template <class T>
+cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int sweeps) {
+  cudaStream_t st = c->stream;
+  const int64_t n = sp.n;
+  const size_t smem = size_t(sp.max_m) * sizeof(double);
+  for (int it = 0; it < sweeps; ++it) {
+    const double* r = b;
+    if (it > 0) {
+      sp_residual<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_rptr, sp.d_rq, sp.d_rcol, c->nzval, sp.xs, b,
+                                                             sp.r, sp.flags);
+      r = sp.r;
+    }
+    sp_gather_scaled<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_perm, sp.D, r, sp.w, sp.flags);
+    for (int h = 0; h < sp.nheight; ++h)
+      if (sp.h_nlf[h])
+        sp_forward<T><<<unsigned(sp.h_nlf[h]), kThreads, smem, st>>>(sp.d_fr, sp.d_lf + sp.h_lf0[h], sp.d_clist,
+                                                                      sp.d_emap, F, sp.w, sp.cvec, sp.flags);
+    for (int h = sp.nheight - 1; h >= 0; --h)
+      if (sp.h_nlf[h])
+        sp_backward<T><<<unsigned(sp.h_nlf[h]), kThreads, smem, st>>>(sp.d_fr, sp.d_lf + sp.h_lf0[h], sp.d_fidx, F,
+                                                                       sp.w, sp.flags);
+    sp_accumulate<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, it == 0, sp.d_perm, sp.D, sp.w, sp.yacc, sp.xs, sp.nrm,
+                                                             sp.flags);
+    sp_check<<<1, 1, 0, st>>>(sp.nrm, sp.prev, sp.flags, kRefineTol, kRefineStall);
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t set_smem(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(sp_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(sp_backward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace
+
+int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uint8_t* last) {
+  spp = new SparseDev();
+  SparseDev& sp = *spp;
+  const Pattern& P = c->pat;
+  const auto t0 = std::chrono::steady_clock::now();
+  SparseInput in;
+  in.n = c->nX;
+  in.colptr = P.colptr.data();
+  in.rowval = P.rowval.data();
+  in.xyz = dof_xyz;
+  in.last = last;
+  in.leaf_groups = 8;
+  SparseAnalysis A;
+  sp.why = sparse_analyse(in, A);
+  if (!sp.why.empty()) return MGPU_OK;
+  // the substitutions keep a front's vector in shared memory
+  if (int64_t(A.max_m) * 8 > 200 * 1024) {
+    sp.why = "front of " + std::to_string(A.max_m) + " dofs exceeds the substitution kernels' shared memory";
+    return MGPU_OK;
+  }
+  sp.n = A.n;
+  sp.nnz = A.nnz;
+  sp.fsize = A.fsize;
+  sp.nfront = int(A.fronts.size());
+  sp.nheight = A.nheight;
+  sp.max_m = A.max_m;
+  sp.max_p = A.max_p;
+  sp.flops = A.flops;
+  const int nf = sp.nfront;
+  // fronts, children in rank order
+  std::vector<SpFrontDev> fr(nf);
+  std::vector<std::vector<int32_t>> kids(nf);
+  for (int f = 0; f < nf; ++f)
+    if (A.fronts[f].parent >= 0) kids[A.fronts[f].parent].push_back(f);
+  std::vector<int32_t> clist;
+  for (int f = 0; f < nf; ++f) {
+    const SparseFront& S = A.fronts[f];
+    std::sort(kids[f].begin(), kids[f].end(), [&](int32_t a, int32_t b) { return A.fronts[a].crank < A.fronts[b].crank; });
+    fr[f] = SpFrontDev{S.off, S.idx, S.eoff, S.m, S.p, S.pos0, S.parent, int32_t(clist.size()), int32_t(kids[f].size())};
+    clist.insert(clist.end(), kids[f].begin(), kids[f].end());
+    if (S.parent < 0) sp.nroot++;
+  }
+  // fronts by height, pivots descending; storage ranges
+  const int H = sp.nheight;
+  std::vector<std::vector<int32_t>> byh(H);
+  for (int f = 0; f < nf; ++f) byh[A.fronts[f].height].push_back(f);
+  std::vector<int32_t> lf;
+  sp.h_lf0.resize(H);
+  sp.h_nlf.resize(H);
+  sp.h_pmax.assign(H, 0);
+  sp.h_mmax.assign(H, 0);
+  sp.h_off0.assign(H, INT64_MAX);
+  sp.h_off1.assign(H, 0);
+  sp.h_lfp.resize(H);
+  for (int h = 0; h < H; ++h) {
+    auto& L = byh[h];
+    std::stable_sort(L.begin(), L.end(), [&](int32_t a, int32_t b) { return A.fronts[a].p > A.fronts[b].p; });
+    sp.h_lf0[h] = int32_t(lf.size());
+    sp.h_nlf[h] = int32_t(L.size());
+    for (int32_t f : L) {
+      const SparseFront& S = A.fronts[f];
+      lf.push_back(f);
+      sp.h_lfp[h].push_back(S.p);
+      sp.h_pmax[h] = std::max(sp.h_pmax[h], S.p);
+      sp.h_mmax[h] = std::max(sp.h_mmax[h], S.m);
+      sp.h_off0[h] = std::min(sp.h_off0[h], S.off);
+      sp.h_off1[h] = std::max(sp.h_off1[h], S.off + int64_t(S.m) * S.m);
+    }
+    if (L.empty()) sp.h_off0[h] = sp.h_off1[h] = 0;
+  }
+  // children to add, by the parent's height and the child's rank
+  std::vector<int32_t> ea;
+  sp.h_ea0.assign(H, {});
+  sp.h_nea.assign(H, {});
+  sp.h_eumax.assign(H, {});
+  for (int h = 0; h < H; ++h) {
+    int maxr = 0;
+    for (int32_t f : byh[h]) maxr = std::max<int>(maxr, int(kids[f].size()));
+    for (int r = 0; r < maxr; ++r) {
+      sp.h_ea0[h].push_back(int32_t(ea.size()));
+      int cnt = 0, um = 0;
+      for (int32_t f : byh[h])
+        if (int(kids[f].size()) > r) {
+          const int32_t ch = kids[f][r];
+          ea.push_back(ch);
+          ++cnt;
+          um = std::max(um, A.fronts[ch].m - A.fronts[ch].p);
+        }
+      sp.h_nea[h].push_back(cnt);
+      sp.h_eumax[h].push_back(um);
+    }
+  }
+  // nnz by the height of their front; column of each nnz; rows for the residual
+  std::vector<int32_t> fh(nf);
+  for (int f = 0; f < nf; ++f) fh[f] = A.fronts[f].height;
+  std::vector<int32_t> fpos(A.n);
+  for (int f = 0; f < nf; ++f)
+    for (int i = 0; i < A.fronts[f].p; ++i) fpos[A.fronts[f].pos0 + i] = f;
+  std::vector<int32_t> acol(A.nnz);
+  std::vector<int64_t> hcnt(H + 1, 0);
+  std::vector<int32_t> qh(A.nnz);
+  for (int64_t j = 0; j < A.n; ++j)
+    for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+      acol[q] = int32_t(j);
+      const int32_t pi = A.ipos[P.rowval[q]], pj = A.ipos[j];
+      qh[q] = fh[fpos[std::min(pi, pj)]];
+      hcnt[qh[q] + 1]++;
+    }
+  for (int h = 0; h < H; ++h) hcnt[h + 1] += hcnt[h];
+  sp.h_aq0.assign(hcnt.begin(), hcnt.end());
+  std::vector<int32_t> aq(A.nnz);
+  {
+    std::vector<int64_t> fill(hcnt.begin(), hcnt.end() - 1);
+    for (int64_t q = 0; q < A.nnz; ++q) aq[fill[qh[q]]++] = int32_t(q);
+  }
+  std::vector<int64_t> rptr(A.n + 1, 0);
+  for (int64_t q = 0; q < A.nnz; ++q) rptr[P.rowval[q] + 1]++;
+  for (int64_t i = 0; i < A.n; ++i) rptr[i + 1] += rptr[i];
+  std::vector<int32_t> rq(A.nnz), rcol(A.nnz);
+  {
+    std::vector<int64_t> fill(rptr.begin(), rptr.end() - 1);
+    for (int64_t j = 0; j < A.n; ++j)
+      for (int64_t q = P.colptr[j]; q < P.colptr[j + 1]; ++q) {
+        const int64_t t = fill[P.rowval[q]]++;
+        rq[t] = int32_t(q);
+        rcol[t] = int32_t(j);
+      }
+  }
+  // upload
+  cudaError_t e = cudaSuccess;
+  auto ok = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+    return e == cudaSuccess;
+  };
+  ok(upload(&sp.d_fr, fr));
+  ok(upload(&sp.d_lf, lf));
+  ok(upload(&sp.d_ea, ea));
+  ok(upload(&sp.d_clist, clist));
+  ok(upload(&sp.d_fidx, A.fidx));
+  ok(upload(&sp.d_emap, A.emap));
+  ok(upload(&sp.d_amap, A.amap));
+  ok(upload(&sp.d_aq, aq));
+  ok(upload(&sp.d_acol, acol));
+  ok(upload(&sp.d_perm, A.perm));
+  ok(upload(&sp.d_diag, A.diag));
+  ok(upload(&sp.d_rptr, rptr));
+  ok(upload(&sp.d_rq, rq));
+  ok(upload(&sp.d_rcol, rcol));
+  ok(upload(&sp.d_colptr, P.colptr));
+  ok(upload(&sp.d_rowval, P.rowval));
+  const int64_t n = A.n;
+  ok(cudaMalloc(&sp.F32, std::max<int64_t>(sp.fsize, 1) * sizeof(float)));
+  ok(cudaMalloc(&sp.D, 2 * n * sizeof(double)));
+  ok(cudaMalloc(&sp.cvec, std::max<size_t>(A.emap.size(), 1) * sizeof(double)));
+  ok(cudaMalloc(&sp.w, n * sizeof(double)));
+  ok(cudaMalloc(&sp.yacc, n * sizeof(double)));
+  ok(cudaMalloc(&sp.r, n * sizeof(double)));
+  ok(cudaMalloc(&sp.xs, n * sizeof(double)));
+  ok(cudaMalloc(&sp.nrm, 2 * sizeof(unsigned long long)));
+  ok(cudaMalloc(&sp.prev, sizeof(double)));
+  ok(cudaMalloc(&sp.flags, 4 * sizeof(int)));
+  ok(cudaMallocHost(&sp.hflags, 4 * sizeof(int)));
+  ok(cudaMemset(sp.nrm, 0, 2 * sizeof(unsigned long long)));
+  for (cudaEvent_t& ev : sp.ev) ok(cudaEventCreate(&ev));
+  const int smem = int(sp.max_m * sizeof(double));
+  if (smem > 48 * 1024) {
+    ok(set_smem<float>(smem));
+    ok(set_smem<double>(smem));
+  }
+  if (e != cudaSuccess) {
+    sp.why = std::string("device upload of the sparse solver: ") + cudaGetErrorString(e);
+    return set_err(c, e == cudaErrorMemoryAllocation ? MGPU_ERR_NOMEM : MGPU_ERR_CUDA, sp.why);
+  }
+  if (getenv("MGPU_VERBOSE")) {
+    const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    fprintf(stderr,
+            "[muscade_gpu] sparse solver: %d groups, %d fronts, %d heights, largest front %d (%d pivots), "
+            "%.3g G front entries, %.3g TFLOP per factorisation, analysis %.2f s\n",
+            A.ngroups, nf, H, A.max_m, A.max_p, double(sp.fsize) / 1e9, sp.flops / 1e12, s);
+  }
+  return MGPU_OK;
+}
+
+void sparse_destroy(SparseDev*& sp) {
+  if (!sp) return;
+  void* ps[] = {sp->d_fr, sp->d_lf, sp->d_ea, sp->d_clist, sp->d_fidx, sp->d_emap, sp->d_amap, sp->d_aq,
+                sp->d_acol, sp->d_perm, sp->d_diag, sp->d_colptr, sp->d_rowval, sp->d_rptr, sp->d_rq, sp->d_rcol,
+                sp->F32, sp->F64, sp->prev,
+                sp->D, sp->cvec, sp->w, sp->yacc, sp->r, sp->xs, sp->nrm, sp->flags};
+  for (void* p : ps) cudaFree(p);
+  if (sp->hflags) cudaFreeHost(sp->hflags);
+  for (cudaEvent_t ev : sp->ev)
+    if (ev) cudaEventDestroy(ev);
+  delete sp;
+  sp = nullptr;
+}
+
+int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* out, int* info) {
+  cudaStream_t st = c->stream;
+  const int64_t n = sp.n;
+  // equilibration from the current values
+  sp_scale_diag<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_diag, c->nzval, sp.D + n);
+  sp_scale_zero<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_colptr, sp.d_rowval, c->nzval, sp.D + n,
+                                                           sp.D);
+  MG_CUDA(cudaMemsetAsync(sp.flags, 0, 4 * sizeof(int), st));
+  bool use64 = sp.fp64_only;
+  sp.last_factor_ms = sp.last_refine_ms = 0.0;
+  auto elapsed = [&](int a, int b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, sp.ev[a], sp.ev[b]);
+    return double(ms);
+  };
+  if (!use64) {
+    MG_CUDA(cudaEventRecord(sp.ev[0], st));
+    MG_CUDA((factorise<float, kNB32>(c, sp, sp.F32, 1e-10f)));
+    MG_CUDA(cudaEventRecord(sp.ev[1], st));
+    MG_CUDA(refine<float>(c, sp, sp.F32, rhs, kSparseSweeps));
+    MG_CUDA(cudaEventRecord(sp.ev[2], st));
+    MG_CUDA(cudaMemcpyAsync(sp.hflags, sp.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaStreamSynchronize(st));
+    sp.last_factor_ms = elapsed(0, 1);
+    sp.last_refine_ms = elapsed(1, 2);
+    sp.last_sweeps = sp.hflags[1];
+    sp.last_perturbed = sp.hflags[2];
+    sp.last_fallback = 0;
+    if (sp.hflags[0] == 0 || sp.hflags[3] != 0) {
+      use64 = true;
+      sp.last_fallback = 1;
+      if (sp.adaptive) sp.fp64_only = true;
+    }
+  }
+  if (use64) {
+    if (!sp.F64) {
+      cudaError_t e = cudaMalloc(&sp.F64, std::max<int64_t>(sp.fsize, 1) * sizeof(double));
+      if (e != cudaSuccess) {
+        sp.F64 = nullptr;
+        return set_err(c, MGPU_ERR_NOMEM, std::string("FP64 factors of the sparse solver: ") + cudaGetErrorString(e));
+      }
+    }
+    MG_CUDA(cudaMemsetAsync(sp.flags, 0, 4 * sizeof(int), st));
+    MG_CUDA(cudaEventRecord(sp.ev[0], st));
+    MG_CUDA((factorise<double, kNB64>(c, sp, sp.F64, 0.0)));
+    MG_CUDA(cudaEventRecord(sp.ev[1], st));
+    MG_CUDA(refine<double>(c, sp, sp.F64, rhs, kSparseSweeps64));
+    MG_CUDA(cudaEventRecord(sp.ev[2], st));
+    MG_CUDA(cudaMemcpyAsync(sp.hflags, sp.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    MG_CUDA(cudaStreamSynchronize(st));
+    sp.last_factor_ms += elapsed(0, 1);
+    sp.last_refine_ms += elapsed(1, 2);
+    sp.last_sweeps = sp.hflags[1];
+    sp.last_perturbed = sp.hflags[2];
+    if (sp.hflags[3] != 0) {  // a zero or non-finite pivot in FP64: the matrix is singular
+      const int one = 1;
+      MG_CUDA(cudaMemcpy(info, &one, sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
+  MG_CUDA(cudaMemcpyAsync(out, sp.xs, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  return MGPU_OK;
+}
+
+}  // namespace mgpu

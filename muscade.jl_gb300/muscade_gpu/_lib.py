@@ -15,9 +15,10 @@ PKG = os.path.dirname(HERE)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
-SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "pattern.cpp"]
+SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "sparse_lu.cu", "pattern.cpp",
+           "sparse_analysis.cpp"]
 HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh",
-           "band_torn.cuh", "band_bcr.cuh", "solver.hpp"]
+           "band_torn.cuh", "band_bcr.cuh", "solver.hpp", "sparse_lu.hpp", "sparse_analysis.hpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes
@@ -96,7 +97,15 @@ class TuneReport(ctypes.Structure):
                 ("ms_linsolve", ctypes.c_double * 6)]
 
 
-LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3, "torn": 4, "torn32": 5}
+class SparseReport(ctypes.Structure):
+    _fields_ = [("nfront", ctypes.c_int32), ("nheight", ctypes.c_int32), ("nroot", ctypes.c_int32),
+                ("max_front", ctypes.c_int32), ("max_pivots", ctypes.c_int32), ("fp64", ctypes.c_int32),
+                ("front_entries", ctypes.c_int64), ("flops", ctypes.c_double), ("last_fallback", ctypes.c_int32),
+                ("last_sweeps", ctypes.c_int32), ("last_perturbed", ctypes.c_int32),
+                ("last_factor_ms", ctypes.c_double), ("last_refine_ms", ctypes.c_double)]
+
+
+LINSOLVE = {"auto": 0, "f32ir": 1, "f64": 2, "block": 3, "torn": 4, "torn32": 5, "sparse": 6, "sparse64": 7}
 LINSOLVE_NAME = {v: k for k, v in LINSOLVE.items()}
 
 # every symbol the header declares (checked by the CPU test suite)
@@ -105,7 +114,7 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
            "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune",
-           "mgpu_assemble_async", "mgpu_assemble_wait"]
+           "mgpu_assemble_async", "mgpu_assemble_wait", "mgpu_sparse_info"]
 
 _lib = None
 
@@ -146,6 +155,7 @@ def load():
     L.mgpu_assemble_beams_noalloc.argtypes = [i64, i64, i64, vp, vp, vp, vp, vp, vp, vp, vp]
     L.mgpu_set_linear_solver.argtypes = [vp, i32]
     L.mgpu_linear_solver_info.argtypes = [vp, P(LinsolveInfo)]
+    L.mgpu_sparse_info.argtypes = [vp, P(SparseReport)]
     L.mgpu_set_A.argtypes = [vp, pd]
     L.mgpu_host_register.argtypes = [vp, i64]
     L.mgpu_autotune.argtypes = [vp, i32, P(Newmark), P(TuneReport)]

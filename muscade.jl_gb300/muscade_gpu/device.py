@@ -127,8 +127,15 @@ class DeviceModel:
     def set_linear_solver(self, kind: str):
         """'auto' | 'f32ir' (row-band FP32 factors + FP64 refinement) | 'f64' (row-band) |
         'block' | 'torn' (partitioned, FP64) | 'torn32' (partitioned, FP32 factors +
-        FP64 refinement); see mgpu_set_linear_solver."""
+        FP64 refinement) | 'sparse' (multifrontal, FP32 factors + FP64 refinement) |
+        'sparse64' (multifrontal, FP64); see mgpu_set_linear_solver."""
         self._check(self.lib.mgpu_set_linear_solver(self.ctx, L.LINSOLVE[kind]))
+
+    def sparse_info(self):
+        """Structure and last solve of the multifrontal solver (mgpu_sparse_info)."""
+        rep = L.SparseReport()
+        self._check(self.lib.mgpu_sparse_info(self.ctx, ctypes.byref(rep)))
+        return {f: getattr(rep, f) for f, _ in L.SparseReport._fields_}
 
     def linear_solver_info(self):
         info = L.LinsolveInfo()

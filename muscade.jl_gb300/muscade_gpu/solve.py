@@ -27,8 +27,9 @@ class SweepXGPU:
 
 def solve(solver, initialstate: State, time, beta=0.25, gamma=0.5, maxiter=50, maxdx=1e-5, maxLl=math.inf,
           pstate=None, device: int = 0, devmodel: DeviceModel | None = None, verbose=False, linsolve="auto"):
-    """`linsolve` picks the device linear solver: 'auto', 'f32ir', 'f64' or 'block'
-    (see DeviceModel.set_linear_solver); it is ignored when `devmodel` is given."""
+    """`linsolve` picks the device linear solver: 'auto', 'f32ir', 'f64', 'block',
+    'torn', 'torn32', 'sparse' or 'sparse64' (see DeviceModel.set_linear_solver);
+    it is ignored when `devmodel` is given."""
     OX = solver.OX
     model, dis = initialstate.model, initialstate.dis
     dm = devmodel or DeviceModel(model, dis, device=device, linsolve=linsolve)

@@ -174,6 +174,32 @@ int oracle_bar_eval(int64_t n, const double* ele, int ND, const double* X, const
   return 0;
 }
 
+// add_value! / add_∂! (src/Assemble.jl:559-608) for one element type, serial
+// like the reference's loop: for each element in order, Lλ[asm1[e,i]] += R[e,i]
+// and nzval[asm2[e,i+nX*j]] += J[e,i,j] (column-major entries, 0 = skip);
+// J[e] is nX × NJ row-major and only its first nX columns are added.
+// minus_col >= 0 also subtracts column minus_col of J from Lλ (the δr part of
+// the Newmark step, add_∂!{1,:minus}).
+void oracle_scatter(int64_t nele, int nX, int NJ, const int64_t* asm1, const int64_t* asm2, const double* R,
+                    const double* J, int minus_col, double* Ll, double* nzval) {
+  for (int64_t e = 0; e < nele; ++e) {
+    const double* Re = R + e * nX;
+    const double* Je = J + e * nX * NJ;
+    const int64_t* a1 = asm1 + e * nX;
+    const int64_t* a2 = asm2 + e * nX * nX;
+    for (int i = 0; i < nX; ++i)
+      if (a1[i]) Ll[a1[i] - 1] += Re[i];
+    if (minus_col >= 0)
+      for (int i = 0; i < nX; ++i)
+        if (a1[i]) Ll[a1[i] - 1] += -Je[i * NJ + minus_col];
+    for (int j = 0; j < nX; ++j)
+      for (int i = 0; i < nX; ++i) {
+        const int64_t q = a2[i + nX * j];
+        if (q) nzval[q - 1] += Je[i * NJ + j];
+      }
+  }
+}
+
 // ---- rotation helpers for the golden tests (test/TestRotations.jl) ----------
 double oracle_sinc1k(int k, double x) {
   switch (k) {

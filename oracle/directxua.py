@@ -1,32 +1,28 @@
-"""Oracle (test infrastructure only): CPU restatement of DirectXUA's
-all-steps-at-once Newton and its cost gradient with respect to the A-dofs,
-for models of residual elements (EulerBeam3D with the EI-scale A-dof, Hold,
-DofLoad) observed by SingleDofCost-type sensor costs, static (OX=0, no U-dofs).
+"""Oracle (test infrastructure only): the static identification problem of
+the device's discrete adjoint, solved all steps at once like DirectXUA: for
+models of residual elements (EulerBeam3D with the EI-scale A-dof, Hold,
+DofLoad) observed by SingleDofCost-type sensor costs, static (OX=0, no
+U-dofs), loads given and A held.
 
-Reference lines followed:
-* Lagrangian per step, scaled by the step length Δt: residual elements add
-  L = Λ·R through add_value!/add_∂! with Δt (src/DirectXUA.jl:85-120), the
-  sensor costs add their value, gradient and Hessian
-  (DirectXUA_lagrangian_addition!, src/DirectXUA.jl:122-171); elements with
-  no second order contribute Lλx = ∂R/∂X and Lxλ = (∂R/∂X)ᵀ only.
-* Time derivatives by finite-difference kernels (src/FiniteDifferences.jl:2-31);
-  with OX = 0 every block uses the order-0 kernel (Δs = 0, w = 1), so the
-  big system couples the steps through nothing but the shared A.
-* Big system per Newton iteration: blocks (λ, x) of every step in step order
-  (assemblebig!, src/DirectXUA.jl:317-356), solved by one sparse LU
-  (src/DirectXUA.jl:486-494), decremented block by block
-  (decrementbig!, :357-383); convergence on the largest squared block
-  correction of each class (:505).
-* Cost gradient with respect to A: the A-block of Lv (block 3·Σnstep+1,
-  :322-326), here evaluated with A held at its given value (the A block is
-  not decremented), i.e. Σₙ Δt Λₙ·∂Rₙ/∂A at the converged (Λ, X).
+It is the stationarity of Σₙ Δt (Λₙ·Rₙ + costₙ) over (Λ, X) with the complete
+Lagrangian: Lλ = R, Lx = (∂R/∂X)ᵀΛ + ∇cost, Lλx = ∂R/∂X, Lxx = ∇²cost (the
+beam's residual has no second-order term in the Newton system), solved by one
+sparse LU per Newton iteration with the block layout of the reference's big
+system (blocks (λ, x) of every step in step order, assemblebig!,
+src/DirectXUA.jl:317-356, decremented block by block like decrementbig!,
+:357-383).  The cost gradient with respect to A is the A-block of Lv at the
+converged (Λ, X): Σₙ Δt Λₙ·∂Rₙ/∂A.  The EI-scale beam residual is affine in
+its A-dof (the bending moments are linear in EI₂, EI₃), so
+∂R_e/∂a_e = R_e(a_e = 1) − R_e(a_e = 0) exactly.
 
-The EI-scale beam residual is affine in its A-dof (the bending moments are
-linear in EI₂, EI₃), so ∂R_e/∂a_e = R_e(a_e = 1) − R_e(a_e = 0) exactly.
-
-Parity: the reference's DirectXUA tests (test/TestDirectXUA001.jl) use 2D
-spring elements that are not on this path, so this restatement is pinned by
-central differences of the oracle's own SweepX{0} cost (tests/test_directxua.py).
+Two differences from the reference's DirectXUA, which oracle/direct.py
+restates and pins to the reference's own tests: there the steps of a static
+problem carry weight 1 (assemble! with idmult, src/DirectXUA.jl:331; the
+factor Δt here is a uniform scaling of the step terms, which leaves Λ and X
+unchanged and scales dC/dA by Δt), and elements without second order, like
+EulerBeam3D, add only Lλ and the Λ-cross blocks (:85-120), not (∂R/∂X)ᵀΛ to
+Lx.  This restatement is pinned by central differences of the oracle's
+SweepX{0} cost (tests/test_directxua.py).
 """
 from __future__ import annotations
 
@@ -76,7 +72,7 @@ def _dR_dA(prep, X, U, t, A):
 
 
 def directxua_static(model, dis, initialstate, times, sensors, w, y, maxiter=50, maxdx=1e-9, maxdl=1e-9):
-    """solve(DirectXUA{0,0,1}) with A held: returns (C, dC/dA, states) where
+    """The all-steps solve with A held: returns (C, dC/dA, states) where
     C = Σₙ Δt Σ_s w (xₙ[d_s] − yₙ,ₛ)² at the converged states, dC/dA the A-block
     of Lv, states the converged X (nstep × nX).  The time grid must be uniform
     (the reference takes a range); Δt = times[1] − times[0]."""

@@ -50,6 +50,9 @@ def lib():
         _lib.oracle_rodrigues.argtypes = [P, P]
         _lib.oracle_rodrigues_roundtrip.argtypes = [P, P, P]
         _lib.oracle_nj.argtypes = [i32, i32, i32, i32]
+        PI = ctypes.POINTER(ctypes.c_int64)
+        _lib.oracle_scatter.argtypes = [i64, i32, i32, PI, PI, P, P, i32, P, P]
+        _lib.oracle_scatter.restype = None
     return _lib
 
 
@@ -137,6 +140,26 @@ def diffed(kind, ele, X, U=None, t=0.0):
     if U is not None:
         out["H"] = J[:, :, ND * nx:ND * nx + 3]
     return out
+
+
+def scatter(asm1, asm2, R, J, Ll, nzval, minus_col=-1):
+    """add_value!/add_∂! of one element type into Ll and nzval (in place),
+    serial in element order like the reference.  asm1 (nele, nX), asm2
+    (nele, nX*nX) 1-based (0 = skip), R (nele, nX), J (nele, nX, NJ)."""
+    nele, nX = R.shape
+    if nele == 0:
+        return
+    NJ = J.shape[2]
+    a1 = np.ascontiguousarray(asm1, dtype=np.int64)
+    a2 = np.ascontiguousarray(asm2, dtype=np.int64)
+    R, J = _c(R), _c(J)
+    assert a1.shape == (nele, nX) and a2.shape == (nele, nX * nX) and J.shape[:2] == (nele, nX)
+    assert Ll.dtype == np.float64 and nzval.dtype == np.float64 and Ll.flags.c_contiguous and nzval.flags.c_contiguous
+    assert a1.size == 0 or (a1.max() <= len(Ll) and a1.min() >= 0)
+    assert a2.size == 0 or (a2.max() <= len(nzval) and a2.min() >= 0)
+    PI = ctypes.POINTER(ctypes.c_int64)
+    lib().oracle_scatter(nele, nX, NJ, a1.ctypes.data_as(PI), a2.ctypes.data_as(PI), _p(R), _p(J), int(minus_col),
+                         _p(Ll), _p(nzval))
 
 
 def sinc1k(k, x):

