@@ -492,7 +492,12 @@ def bench_solve(args, rank, local_rank, ws, dist):
 
     _lib.build()
     if args.config == "risers":
-        model, times = workloads.risers(nriser=args.risers)
+        # one fixed set of risers × ranks, split by muscade_gpu.shard: each rank
+        # solves its own share (no collective on the data path)
+        from muscade_gpu.shard import shard_bounds
+
+        lo, hi = shard_bounds(np.ones(args.risers * ws), ws)[rank]
+        model, times = workloads.risers(nriser=args.risers * ws, subset=(lo, hi))
         st = model.initialize(time=0.0)
         OX, kw = 2, dict(fixed_iter=3, graph=not args.no_graph)
         nstep_w, nstep = args.warmup, args.steps
@@ -566,13 +571,18 @@ def bench_solve(args, rank, local_rank, ws, dist):
 def bench_batched(args, rank, local_rank, ws, dist):
     """Independent models (half cantilevers, half portal frames, 10-400 beams,
     8 load steps of SweepX{0}) solved together with per-model convergence.
-    One bench step is one whole batched solve.  Ranks solve disjoint sets of
-    models (seed per rank) with no collective: weak scaling by models."""
+    One bench step is one whole batched solve.  N ranks split one seeded set of
+    N × --models models by cost, with no collective: weak scaling by models."""
     from muscade_gpu import _lib, workloads
     from muscade_gpu.device import DeviceModel
 
     _lib.build()
-    params = workloads.batched_params(args.models, seed=2030 + rank)
+    # one fixed seeded set of models × ranks, split by cost (element counts)
+    # with muscade_gpu.shard: each rank solves its share, no collective
+    from muscade_gpu.shard import my_share
+
+    allp = workloads.batched_params(args.models * ws, seed=2030)
+    params, _ = my_share(allp, [p["nel"] for p in allp], rank, ws)
     model, offs, times = workloads.build_batched(params)
     st = model.initialize()
     nbeam = model.groups[0].nele
@@ -640,7 +650,7 @@ def bench_batched(args, rank, local_rank, ws, dist):
         same &= rci == 0 and bool(np.array_equal(xi[:, 0, a[sel]], xb[:, 0, b[sel]]))
     per_model = 1.0 / float(np.mean(tind))
     cpu = batched_cpu_leg(params, pick[: args.oracle_models], times, model, offs, xb, x32 if rc32 == 0 else None)
-    value = ws * len(params) / dt
+    value = len(allp) / dt  # all ranks' models over the slowest rank's time
     h2d = 8 * (model.ndof["X"] + len(times) * dm.ntval + len(times))
     d2h = 8 * model.ndof["X"] * len(times)
     launches_per_iter = len(model.groups) + 2 + 9  # element kernels, scatters, solver, decrement, convergence

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 #include "ctx.hpp"
 #include "sparse_analysis.hpp"
@@ -20,6 +21,7 @@ constexpr int kNB32 = 64;  // pivot block of the FP32 factorisation
 constexpr int kNB64 = 32;  // of the FP64 factorisation (register rows of the L panel)
 constexpr int kTile = 64;  // trailing-update tile
 constexpr int kMaxGridY = 65535;
+constexpr size_t kUpd32Smem = size_t(2) * 64 * (128 + 4) * sizeof(float);  // sp_update_f32<64> tiles
 constexpr double kRefineTol = 1e-14;   // scaled correction / scaled solution: converged
 constexpr double kRefineStall = 1e-10;  // ... or stalled below this
 
@@ -247,39 +249,125 @@ __global__ void __launch_bounds__(kThreads) sp_update(const SpFrontDev* __restri
   }
 }
 
+// FP32 trailing update with 128 × 128 tiles (8 × 8 per thread, the L₂₁ and U₁₂
+// panels of the tile in dynamic shared memory); otherwise as sp_update
+constexpr int kTile32 = 128;
+constexpr int kPad32 = 4;
+template <int NB>
+__global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __restrict__ fr,
+                                                          const int32_t* __restrict__ flist, int k0,
+                                                          float* __restrict__ F, float tau, int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p) return;
+  const int kb = min(NB, p - k0), r0 = k0 + kb, rest = m - r0;
+  const int nt = (rest + kTile32 - 1) / kTile32;
+  if (int(blockIdx.x) > nt * nt) return;
+  float* A = F + Fr.off;
+  extern __shared__ float smem32[];
+  float(*As)[kTile32 + kPad32] = reinterpret_cast<float(*)[kTile32 + kPad32]>(smem32);
+  float(*Bs)[kTile32 + kPad32] = reinterpret_cast<float(*)[kTile32 + kPad32]>(smem32 + NB * (kTile32 + kPad32));
+  const int tid = threadIdx.x;
+  if (int(blockIdx.x) == nt * nt) {
+    static_assert(NB * (NB + 1) <= NB * (kTile32 + kPad32), "the diagonal block fits the tile buffer");
+    float(*Dg)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(smem32);
+    factor_diag<float, NB>(A, m, k0, kb, Dg, tau, flags, true);
+    for (int t = tid; t < kb * kb; t += kThreads) {
+      const int i = t % kb, j = t / kb;
+      A[(k0 + i) + int64_t(k0 + j) * m] = Dg[i][j];
+    }
+    return;
+  }
+  const int i0 = r0 + (blockIdx.x % nt) * kTile32, j0 = r0 + (blockIdx.x / nt) * kTile32;
+  for (int t = tid; t < NB * kTile32; t += kThreads) {
+    const int i = t % kTile32, c = t / kTile32;
+    As[c][i] = (c < kb && i0 + i < m) ? A[(i0 + i) + int64_t(k0 + c) * m] : 0.f;
+  }
+  for (int t = tid; t < NB * kTile32; t += kThreads) {
+    const int c = t % NB, j = t / NB;
+    Bs[c][j] = (c < kb && j0 + j < m) ? A[(k0 + c) + int64_t(j0 + j) * m] : 0.f;
+  }
+  __syncthreads();
+  const int tr = tid & 15, tc = tid >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+#pragma unroll 4
+  for (int c = 0; c < NB; ++c) {
+    const float4 a0 = *reinterpret_cast<const float4*>(&As[c][4 * tr]);
+    const float4 a1 = *reinterpret_cast<const float4*>(&As[c][64 + 4 * tr]);
+    const float4 b0 = *reinterpret_cast<const float4*>(&Bs[c][4 * tc]);
+    const float4 b1 = *reinterpret_cast<const float4*>(&Bs[c][64 + 4 * tc]);
+    const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+    const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+    if (j >= m) continue;
+    float* col = A + int64_t(j) * m;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+      if (i < m) col[i] -= acc[u][v];
+    }
+  }
+}
+
 // ---------------------------------------------------------------- substitutions (FP64 vectors)
-// forward, leaves first: v = the front's pivot entries plus the children's
-// update vectors (in child order); y = L₁₁⁻¹ v[0:p] by blocks of 32 columns
-// (one warp solves the block, all threads update the rows below); the update
-// part goes to the parent through cvec
+// Per height, leaves first for the forward substitution (roots first for the
+// backward one), with two kernels each: one block per front solves the
+// triangle of its pivots (blocks of 32 columns: the 32 × 32 diagonal block is
+// staged in shared memory and solved by one warp, then all threads update the
+// pivot rows below), and a grid of blocks, 256 rows each, does the front's
+// rectangular part (L₂₁ y or U₁₂ x_u), one row per thread summing in column
+// order.  Vectors are FP64, factors T.
+constexpr int kTriThreads = 512;
+constexpr int kGemvRows = 256;
+
+// forward, triangle: v = the front's pivot entries plus the children's update
+// vectors (in child order); y = L₁₁⁻¹ v[0:p] -> w; v[p:m] (the children's part of
+// the update rows) -> cvec, to which sp_fwd_gemv adds −L₂₁ y
 template <class T>
-__global__ void __launch_bounds__(kThreads) sp_forward(const SpFrontDev* __restrict__ fr,
-                                                       const int32_t* __restrict__ flist,
-                                                       const int32_t* __restrict__ clist,
-                                                       const int32_t* __restrict__ emap, const T* __restrict__ F,
-                                                       double* __restrict__ w, double* __restrict__ cvec,
-                                                       const int* __restrict__ conv) {
+__global__ void __launch_bounds__(kTriThreads) sp_fwd_tri(const SpFrontDev* __restrict__ fr,
+                                                          const int32_t* __restrict__ flist,
+                                                          const int32_t* __restrict__ clist,
+                                                          const int32_t* __restrict__ emap, const T* __restrict__ F,
+                                                          double* __restrict__ w, double* __restrict__ cvec,
+                                                          const int* __restrict__ conv) {
   if (*conv) return;
   const SpFrontDev Fr = fr[flist[blockIdx.x]];
   extern __shared__ double v[];
+  __shared__ double Dg[32][33];
   __shared__ double yb[32];
   const int m = Fr.m, p = Fr.p, tid = threadIdx.x;
-  for (int t = tid; t < m; t += kThreads) v[t] = t < p ? w[Fr.pos0 + t] : 0.0;
+  for (int t = tid; t < m; t += kTriThreads) v[t] = t < p ? w[Fr.pos0 + t] : 0.0;
   __syncthreads();
   for (int k = 0; k < Fr.nc; ++k) {
     const SpFrontDev C = fr[clist[Fr.c0 + k]];
     const int uc = C.m - C.p;
-    for (int t = tid; t < uc; t += kThreads) v[emap[C.eoff + t]] += cvec[C.eoff + t];
+    for (int t = tid; t < uc; t += kTriThreads) v[emap[C.eoff + t]] += cvec[C.eoff + t];
     __syncthreads();
   }
   const T* A = F + Fr.off;
   for (int c0 = 0; c0 < p; c0 += 32) {
     const int cb = min(32, p - c0);
+    for (int t = tid; t < cb * 32; t += kTriThreads) {
+      const int i = t & 31, j = t >> 5;
+      Dg[i][j] = i < cb ? double(A[(c0 + i) + int64_t(c0 + j) * m]) : 0.0;
+    }
+    __syncthreads();
     if (tid < 32) {
       double y = tid < cb ? v[c0 + tid] : 0.0;
       for (int c = 0; c < cb; ++c) {
         const double yc = __shfl_sync(0xffffffffu, y, c);
-        if (tid > c && tid < cb) y -= double(A[(c0 + tid) + int64_t(c0 + c) * m]) * yc;
+        if (tid > c && tid < cb) y -= Dg[tid][c] * yc;
       }
       if (tid < cb) {
         v[c0 + tid] = y;
@@ -287,30 +375,79 @@ __global__ void __launch_bounds__(kThreads) sp_forward(const SpFrontDev* __restr
       }
     }
     __syncthreads();
-    for (int i = c0 + cb + tid; i < m; i += kThreads) {
+    for (int i = c0 + cb + tid; i < p; i += kTriThreads) {
       double s = 0.0;
       for (int c = 0; c < cb; ++c) s += double(A[i + int64_t(c0 + c) * m]) * yb[c];
       v[i] -= s;
     }
     __syncthreads();
   }
-  for (int t = tid; t < p; t += kThreads) w[Fr.pos0 + t] = v[t];
+  for (int t = tid; t < p; t += kTriThreads) w[Fr.pos0 + t] = v[t];
   if (Fr.parent >= 0)
-    for (int t = p + tid; t < m; t += kThreads) cvec[Fr.eoff + (t - p)] = v[t];
+    for (int t = p + tid; t < m; t += kTriThreads) cvec[Fr.eoff + (t - p)] = v[t];
 }
 
-// backward, roots first: x[0:p] = U₁₁⁻¹ (y − U₁₂ x_u), x_u the ancestors' values
+// forward, rectangle: cvec[f][t] -= Σ_c L₂₁[t, c] y_c for the update rows t of
+// every front of the height (y staged in shared memory)
 template <class T>
-__global__ void __launch_bounds__(kThreads) sp_backward(const SpFrontDev* __restrict__ fr,
-                                                        const int32_t* __restrict__ flist,
-                                                        const int32_t* __restrict__ fidx, const T* __restrict__ F,
-                                                        double* __restrict__ w, const int* __restrict__ conv) {
+__global__ void __launch_bounds__(kGemvRows) sp_fwd_gemv(const SpFrontDev* __restrict__ fr,
+                                                         const int32_t* __restrict__ flist, const T* __restrict__ F,
+                                                         const double* __restrict__ w, double* __restrict__ cvec,
+                                                         const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p, u = m - p;
+  if (Fr.parent < 0 || int(blockIdx.x) * kGemvRows >= u) return;
+  extern __shared__ double y[];
+  for (int c = threadIdx.x; c < p; c += kGemvRows) y[c] = w[Fr.pos0 + c];
+  __syncthreads();
+  const int t = blockIdx.x * kGemvRows + threadIdx.x;
+  if (t >= u) return;
+  const T* L = F + Fr.off + p + t;  // row p+t of the front, column c at L[c*m]
+  double s = 0.0;
+#pragma unroll 8
+  for (int c = 0; c < p; ++c) s += double(L[int64_t(c) * m]) * y[c];
+  cvec[Fr.eoff + t] -= s;
+}
+
+// backward, rectangle: tw[pos0 + r] = Σ_{j ≥ p} U₁₂[r, j] x_j for the pivot rows r
+// (x_u the ancestors' solved values, staged in shared memory)
+template <class T>
+__global__ void __launch_bounds__(kGemvRows) sp_bwd_gemv(const SpFrontDev* __restrict__ fr,
+                                                         const int32_t* __restrict__ flist,
+                                                         const int32_t* __restrict__ fidx, const T* __restrict__ F,
+                                                         const double* __restrict__ w, double* __restrict__ tw,
+                                                         const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p, u = m - p;
+  if (int(blockIdx.x) * kGemvRows >= p) return;
+  extern __shared__ double xu[];
+  for (int j = threadIdx.x; j < u; j += kGemvRows) xu[j] = w[fidx[Fr.idx + p + j]];
+  __syncthreads();
+  const int r = blockIdx.x * kGemvRows + threadIdx.x;
+  if (r >= p) return;
+  const T* U = F + Fr.off + r + int64_t(p) * m;  // row r, column p+j at U[j*m]
+  double s = 0.0;
+#pragma unroll 8
+  for (int j = 0; j < u; ++j) s += double(U[int64_t(j) * m]) * xu[j];
+  tw[Fr.pos0 + r] = s;
+}
+
+// backward, triangle: x[0:p] = U₁₁⁻¹ (y − U₁₂ x_u) -> w
+template <class T>
+__global__ void __launch_bounds__(kTriThreads) sp_bwd_tri(const SpFrontDev* __restrict__ fr,
+                                                          const int32_t* __restrict__ flist, const T* __restrict__ F,
+                                                          double* __restrict__ w, const double* __restrict__ tw,
+                                                          const int* __restrict__ conv) {
   if (*conv) return;
   const SpFrontDev Fr = fr[flist[blockIdx.x]];
   extern __shared__ double v[];
-  __shared__ double part[8][33];
+  constexpr int NW = kTriThreads / 32;
+  __shared__ double part[NW][33];
+  __shared__ double Dg[32][33];
   const int m = Fr.m, p = Fr.p, tid = threadIdx.x;
-  for (int t = tid; t < m; t += kThreads) v[t] = t < p ? w[Fr.pos0 + t] : w[fidx[Fr.idx + t]];
+  for (int t = tid; t < p; t += kTriThreads) v[t] = w[Fr.pos0 + t] - tw[Fr.pos0 + t];
   __syncthreads();
   const T* A = F + Fr.off;
   const int wp = tid >> 5, lane = tid & 31;
@@ -318,29 +455,33 @@ __global__ void __launch_bounds__(kThreads) sp_backward(const SpFrontDev* __rest
     const int c0 = max(0, c1 - 32), cb = c1 - c0;
     double s = 0.0;
     if (lane < cb)
-      for (int j = c1 + wp; j < m; j += 8) s += double(A[(c0 + lane) + int64_t(j) * m]) * v[j];
+      for (int j = c1 + wp; j < p; j += NW) s += double(A[(c0 + lane) + int64_t(j) * m]) * v[j];
     part[wp][lane] = s;
+    for (int t = tid; t < 32 * 32; t += kTriThreads) {
+      const int i = t & 31, j = t >> 5;
+      Dg[i][j] = (i < cb && j < cb) ? double(A[(c0 + i) + int64_t(c0 + j) * m]) : 0.0;
+    }
     __syncthreads();
     if (tid < 32) {
       double b = 0.0;
       if (lane < cb) {
         b = v[c0 + lane];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) b -= part[q][lane];
+        for (int q = 0; q < NW; ++q) b -= part[q][lane];
       }
       for (int c = cb - 1; c >= 0; --c) {
-        double xc = lane == c ? b / double(A[(c0 + c) + int64_t(c0 + c) * m]) : 0.0;
+        double xc = lane == c ? b / Dg[c][c] : 0.0;
         xc = __shfl_sync(0xffffffffu, xc, c);
         if (lane == c)
           b = xc;
         else if (lane < c)
-          b -= double(A[(c0 + lane) + int64_t(c0 + c) * m]) * xc;
+          b -= Dg[lane][c] * xc;
       }
       if (lane < cb) v[c0 + lane] = b;
     }
     __syncthreads();
   }
-  for (int t = tid; t < p; t += kThreads) w[Fr.pos0 + t] = v[t];
+  for (int t = tid; t < p; t += kTriThreads) w[Fr.pos0 + t] = v[t];
 }
 
 // ---------------------------------------------------------------- refinement
@@ -461,7 +602,13 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
         const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
         if (nrc + ncc > 0)
           sp_panel<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
-        sp_update<T, NB><<<dim3(unsigned(nt * nt + 1), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+        if constexpr (std::is_same<T, float>::value) {
+          const int nt32 = (rest + kTile32 - 1) / kTile32;
+          sp_update_f32<NB><<<dim3(unsigned(nt32 * nt32 + 1), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, k0, F,
+                                                                                                tau, sp.flags);
+        } else {
+          sp_update<T, NB><<<dim3(unsigned(nt * nt + 1), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+        }
       }
     }
   }
@@ -482,14 +629,26 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
       r = sp.r;
     }
     sp_gather_scaled<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_perm, sp.D, r, sp.w, sp.flags);
-    for (int h = 0; h < sp.nheight; ++h)
-      if (sp.h_nlf[h])
-        sp_forward<T><<<unsigned(sp.h_nlf[h]), kThreads, smem, st>>>(sp.d_fr, sp.d_lf + sp.h_lf0[h], sp.d_clist,
-                                                                      sp.d_emap, F, sp.w, sp.cvec, sp.flags);
-    for (int h = sp.nheight - 1; h >= 0; --h)
-      if (sp.h_nlf[h])
-        sp_backward<T><<<unsigned(sp.h_nlf[h]), kThreads, smem, st>>>(sp.d_fr, sp.d_lf + sp.h_lf0[h], sp.d_fidx, F,
-                                                                       sp.w, sp.flags);
+    for (int h = 0; h < sp.nheight; ++h) {
+      if (!sp.h_nlf[h]) continue;
+      const int32_t* fl = sp.d_lf + sp.h_lf0[h];
+      sp_fwd_tri<T><<<unsigned(sp.h_nlf[h]), kTriThreads, smem, st>>>(sp.d_fr, fl, sp.d_clist, sp.d_emap, F, sp.w,
+                                                                       sp.cvec, sp.flags);
+      const int ur = (sp.h_umax[h] + kGemvRows - 1) / kGemvRows;
+      for (int f0 = 0; f0 < sp.h_nlf[h] && ur > 0; f0 += kMaxGridY)
+        sp_fwd_gemv<T><<<dim3(unsigned(ur), unsigned(std::min(kMaxGridY, sp.h_nlf[h] - f0))), kGemvRows,
+                         size_t(sp.h_pmax[h]) * sizeof(double), st>>>(sp.d_fr, fl + f0, F, sp.w, sp.cvec, sp.flags);
+    }
+    for (int h = sp.nheight - 1; h >= 0; --h) {
+      if (!sp.h_nlf[h]) continue;
+      const int32_t* fl = sp.d_lf + sp.h_lf0[h];
+      const int pr = (sp.h_pmax[h] + kGemvRows - 1) / kGemvRows;
+      for (int f0 = 0; f0 < sp.h_nlf[h]; f0 += kMaxGridY)
+        sp_bwd_gemv<T><<<dim3(unsigned(pr), unsigned(std::min(kMaxGridY, sp.h_nlf[h] - f0))), kGemvRows,
+                         size_t(std::max(sp.h_umax[h], 1)) * sizeof(double), st>>>(sp.d_fr, fl + f0, sp.d_fidx, F,
+                                                                                   sp.w, sp.tw, sp.flags);
+      sp_bwd_tri<T><<<unsigned(sp.h_nlf[h]), kTriThreads, smem, st>>>(sp.d_fr, fl, F, sp.w, sp.tw, sp.flags);
+    }
     sp_accumulate<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, it == 0, sp.d_perm, sp.D, sp.w, sp.yacc, sp.xs, sp.nrm,
                                                              sp.flags);
     sp_check<<<1, 1, 0, st>>>(sp.nrm, sp.prev, sp.flags, kRefineTol, kRefineStall);
@@ -499,9 +658,12 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
 
 template <class T>
 cudaError_t set_smem(int bytes) {
-  cudaError_t e = cudaFuncSetAttribute(sp_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(sp_backward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  for (const void* k : {reinterpret_cast<const void*>(sp_fwd_tri<T>), reinterpret_cast<const void*>(sp_bwd_tri<T>),
+                        reinterpret_cast<const void*>(sp_fwd_gemv<T>), reinterpret_cast<const void*>(sp_bwd_gemv<T>)}) {
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace
@@ -557,6 +719,7 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   sp.h_nlf.resize(H);
   sp.h_pmax.assign(H, 0);
   sp.h_mmax.assign(H, 0);
+  sp.h_umax.assign(H, 0);
   sp.h_off0.assign(H, INT64_MAX);
   sp.h_off1.assign(H, 0);
   sp.h_lfp.resize(H);
@@ -571,6 +734,7 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
       sp.h_lfp[h].push_back(S.p);
       sp.h_pmax[h] = std::max(sp.h_pmax[h], S.p);
       sp.h_mmax[h] = std::max(sp.h_mmax[h], S.m);
+      sp.h_umax[h] = std::max(sp.h_umax[h], S.m - S.p);
       sp.h_off0[h] = std::min(sp.h_off0[h], S.off);
       sp.h_off1[h] = std::max(sp.h_off1[h], S.off + int64_t(S.m) * S.m);
     }
@@ -661,6 +825,7 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaMalloc(&sp.D, 2 * n * sizeof(double)));
   ok(cudaMalloc(&sp.cvec, std::max<size_t>(A.emap.size(), 1) * sizeof(double)));
   ok(cudaMalloc(&sp.w, n * sizeof(double)));
+  ok(cudaMalloc(&sp.tw, n * sizeof(double)));
   ok(cudaMalloc(&sp.yacc, n * sizeof(double)));
   ok(cudaMalloc(&sp.r, n * sizeof(double)));
   ok(cudaMalloc(&sp.xs, n * sizeof(double)));
@@ -675,6 +840,7 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
     ok(set_smem<float>(smem));
     ok(set_smem<double>(smem));
   }
+  ok(cudaFuncSetAttribute(sp_update_f32<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
   if (e != cudaSuccess) {
     sp.why = std::string("device upload of the sparse solver: ") + cudaGetErrorString(e);
     return set_err(c, e == cudaErrorMemoryAllocation ? MGPU_ERR_NOMEM : MGPU_ERR_CUDA, sp.why);
@@ -694,7 +860,7 @@ void sparse_destroy(SparseDev*& sp) {
   void* ps[] = {sp->d_fr, sp->d_lf, sp->d_ea, sp->d_clist, sp->d_fidx, sp->d_emap, sp->d_amap, sp->d_aq,
                 sp->d_acol, sp->d_perm, sp->d_diag, sp->d_colptr, sp->d_rowval, sp->d_rptr, sp->d_rq, sp->d_rcol,
                 sp->F32, sp->F64, sp->prev,
-                sp->D, sp->cvec, sp->w, sp->yacc, sp->r, sp->xs, sp->nrm, sp->flags};
+                sp->D, sp->cvec, sp->w, sp->tw, sp->yacc, sp->r, sp->xs, sp->nrm, sp->flags};
   for (void* p : ps) cudaFree(p);
   if (sp->hflags) cudaFreeHost(sp->hflags);
   for (cudaEvent_t ev : sp->ev)

@@ -44,7 +44,7 @@ struct SparseDev {
   double flops = 0;
   // per height: fronts (sorted by pivots, descending), storage range, nnz list
   std::vector<int32_t> h_lf0, h_nlf;           // first entry / count in d_lf
-  std::vector<int32_t> h_pmax, h_mmax;
+  std::vector<int32_t> h_pmax, h_mmax, h_umax;  // largest pivots / front / update rows per height
   std::vector<int64_t> h_off0, h_off1;         // front storage range
   std::vector<int64_t> h_aq0;                  // nnz of the height's fronts: d_aq[h_aq0[h] .. h_aq0[h+1])
   std::vector<std::vector<int32_t>> h_lfp;     // per height: p of the fronts in d_lf order (host, for step counts)
@@ -71,6 +71,7 @@ struct SparseDev {
   double* D = nullptr;          // [2n] equilibration, then the diagonal part of it
   double* cvec = nullptr;       // children's update vectors (forward substitution)
   double* w = nullptr;          // [n] elimination order work vector
+  double* tw = nullptr;         // [n] U₁₂ x_u of each pivot (backward substitution)
   double* yacc = nullptr;       // [n] accumulated scaled solution (elimination order)
   double* r = nullptr;          // [n] residual (model order)
   double* xs = nullptr;         // [n] current solution (model order)

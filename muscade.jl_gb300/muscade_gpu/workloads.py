@@ -84,15 +84,21 @@ def lattice(nx=60, ny=60, nz=20, seed=2027, sigma=0.1, load_std=100.0):
     return m, np.round(np.arange(1, 6) * 0.2, 12)
 
 
-def risers(nriser=200, nel=250, length=1000.0, seed=2028, EA=5e9, EI=1e6, GJ=1e6, mu=300.0, iota1=10.0):
+def risers(nriser=200, nel=250, length=1000.0, seed=2028, EA=5e9, EI=1e6, GJ=1e6, mu=300.0, iota1=10.0,
+           subset=None):
+    """`nriser` seeded risers; `subset` = (lo, hi) builds only risers lo..hi-1 of
+    them (the amplitudes and periods are drawn for all, so a subset's risers are
+    those of the whole set)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     A = rng.uniform(1.0, 5.0, nriser)
     T = rng.uniform(8.0, 15.0, nriser)
+    lo, hi = subset if subset is not None else (0, nriser)
+    A, T = A[lo:hi], T[lo:hi]
     m = Model("risers")
     mat = BeamCrossSection(EA=EA, EI2=EI, EI3=EI, GJ=GJ, mu=mu, iota1=iota1)
     zs = np.linspace(0.0, length, nel + 1)
     bottoms, tops = [], []
-    for r in range(nriser):
+    for r in range(lo, hi):
         x0 = 50.0 * (r % 20)
         y0 = 50.0 * (r // 20)
         nodes = m.addnode(np.stack([np.full_like(zs, x0), np.full_like(zs, y0), zs], axis=1))

@@ -28,11 +28,14 @@ Reference lines followed:
   every class's largest squared block decrement is below maxΔ².
 
 Elements with no second order (EulerBeam3D, Bar3D) take another path in the
-reference (:85-120: Lλ and the Λ-cross blocks only) and are not restated here.
+reference (:85-120: Lλ and the Λ-cross blocks only, no (∂R/∂X)ᵀΛ in Lx);
+static_path_without_second_order restates its iterations for beam models
+observed by quadratic sensor costs, where the multipliers never settle.
 
 Pinned by test/TestDirectXUA001.jl:33-51 (golden X and A of the static
-identification with springs, rtol 1e-4) and by the step blocks L1/L2 of
-test/TestDirectXUA.jl:93-108 (tests/test_direct_oracle.py).
+identification with springs, rtol 1e-4), by the step blocks L1/L2 of
+test/TestDirectXUA.jl:93-108 and by the big-system pattern of
+test/TestDirectXUA.jl:109-136 (tests/test_direct_oracle.py).
 """
 from __future__ import annotations
 
@@ -535,3 +538,41 @@ def big_pattern(model, dis, OX, OU, IA, nstep):
         rowval += [r + 1 for r in sorted(c)]
         colptr.append(len(rowval) + 1)
     return np.array(colptr), np.array(rowval), off[:-1] + 1
+
+
+# --------------------------------------------------------------- elements without second order
+def static_path_without_second_order(model, dis, initialstate, times, sensors, y, niter):
+    """The reference's DirectXUA{0,0,0} iterations for residual elements with
+    no_second_order (EulerBeam3D: toolbox/BeamElement.jl:106) observed by
+    quadratic sensor costs Σ (x[d] − y)²: such elements add Lλ = R and the
+    cross blocks Lλx = ∂R/∂X, Lxλ = (∂R/∂X)ᵀ (src/DirectXUA.jl:85-120) but no
+    (∂R/∂X)ᵀΛ to Lx, so Lx is the costs' gradient alone.  Returns the largest
+    |ΔΛ| and |ΔX| over the steps, per Newton iteration."""
+    from . import reference as REF
+
+    prep = REF.Prepared(model, dis)
+    n = prep.n
+    sens = np.asarray(sensors) - 1
+    c0 = REF.newmark_coefficients(0, 1.0, 0.25, 0.5)
+    X = [initialstate.X[0].copy() for _ in times]
+    Lam = [np.zeros(n) for _ in times]
+    out = []
+    for _ in range(niter):
+        blocks, rhs = [], []
+        for k, t in enumerate(times):
+            R, nz = REF.assemble(prep, (X[k],), (np.zeros(model.ndof["U"]),), t, "static", c0, A=initialstate.A)
+            K = prep.matrix(nz)
+            g, h = np.zeros(n), np.zeros(n)
+            np.add.at(g, sens, 2.0 * (X[k][sens] - y[k]))
+            np.add.at(h, sens, 2.0)
+            rhs += [R, g]
+            blocks.append(sp.bmat([[None, K], [K.T, sp.diags(h)]], format="csc"))
+        dv = spla.splu(sp.block_diag(blocks, format="csc")).solve(np.concatenate(rhs))
+        dl = dx = 0.0
+        for k in range(len(times)):
+            d_l, d_x = dv[2 * k * n:(2 * k + 1) * n], dv[(2 * k + 1) * n:(2 * k + 2) * n]
+            Lam[k] -= d_l
+            X[k] -= d_x
+            dl, dx = max(dl, float(np.linalg.norm(d_l))), max(dx, float(np.linalg.norm(d_x)))
+        out.append((dl, dx))
+    return out

@@ -130,3 +130,25 @@ def test_big_system_pattern():
                                  1, 2, 3, 4, 5, 7, 9, 10, 11, 12, 13, 15, 19, 20, 49, 50, 53, 54, 1, 2, 3, 4, 6, 8, 9,
                                  10, 11, 12, 14, 16, 19, 20, 51, 52, 53, 54]
     assert list(lvasm) == [1, 3, 5, 9, 11, 13, 17, 19, 21, 25, 27, 29, 33, 35, 37, 41, 43, 45, 49]
+
+
+def test_reference_path_without_second_order_does_not_settle_the_multipliers():
+    """EulerBeam3D declares no second order; the reference's DirectXUA then
+    leaves (∂R/∂X)ᵀΛ out of Lx (src/DirectXUA.jl:85-120).  On a static beam
+    identification the states converge while every iteration decrements Λ by
+    the same K⁻ᵀ∇cost, so the default convergence test on ΔΛ (1e-5) is never
+    met.  This is why the device differentiates SweepX itself (the discrete
+    adjoint) rather than reproducing DirectXUA for beams."""
+    from muscade_gpu import workloads as W
+    from oracle import reference as REF
+
+    d = W.adjoint_beam(nel=10, nstep=4, seed=2029, load_std=1e5)
+    m = d["model"]
+    st = m.initialize()
+    st.A[:] = 1.0
+    ref = REF.sweepx(m, st.dis, st, d["times"], OX=0, maxdx=1e-5)
+    y = np.stack([X[0][d["sensors"] - 1] for _, X in ref]) + 1e-3
+    it = DX.static_path_without_second_order(m, st.dis, st, d["times"], d["sensors"], y, 8)
+    dls = np.array([dl for dl, _ in it])
+    assert it[-1][1] < 1e-5  # the states have converged
+    assert np.all(dls > 1e-5) and np.max(np.abs(dls[2:] - dls[-1])) <= 1e-9 * dls[-1]  # a constant ΔΛ

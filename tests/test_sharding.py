@@ -66,3 +66,80 @@ def test_two_rank_gloo_run_gives_the_single_process_results(tmp_path):
     single = _solve_models(params)
     for k, i in enumerate(z["idx"]):
         assert np.array_equal(z[f"arr_{k}"], single[i])
+
+
+def test_riser_subset_is_a_slice_of_the_whole_set():
+    """bench.py's riser shards: risers(n, subset=(lo, hi)) builds risers lo..hi-1
+    of the seeded set of n, with their own prescribed motions."""
+    full, _ = W.risers(nriser=6, nel=4)
+    part, _ = W.risers(nriser=6, nel=4, subset=(2, 5))
+    nn = 5  # nodes per riser
+    assert part.nnod == 3 * nn
+    for k in range(3):
+        for j in range(nn):
+            assert np.array_equal(part.coord(1 + k * nn + j), full.coord(1 + (k + 2) * nn + j))
+    from muscade_gpu.elements import group_time_values
+
+    gf = next(g for g in full.groups if g.key[0] == "DofConstraint" and g.key[-1] == "surge")
+    gp = next(g for g in part.groups if g.key[0] == "DofConstraint" and g.key[-1] == "surge")
+    for t in (1.0, 7.5, 12.0):
+        assert np.array_equal(group_time_values(gp, "offset", t), group_time_values(gf, "offset", t)[2:5])
+
+
+def _device_worker(rank, world, port, params, result_path):
+    import torch.distributed as dist
+
+    from muscade_gpu.device import DeviceModel
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    mine, idx = my_share(params, [p["nel"] for p in params], rank, world)
+    res = []
+    if len(mine):
+        m, offs, times = W.build_batched(mine)
+        st = m.initialize()
+        dm = DeviceModel(m, st.dis, device=0)
+        rc, x, _ = dm.sweepx(0, times, st.time, list(st.X), maxdx=1e-9, maxLl=math.inf, per_component=True)
+        dm.close()
+        assert rc == 0
+        bounds = list(offs) + [m.nnod]
+        for k, i in enumerate(idx):
+            d = W.node_dofs(m, np.arange(bounds[k] + 1, bounds[k + 1] + 1))
+            res.append((int(i), x[:, 0, d[d >= 0]]))
+    allres = gather_to_root(res, dist)
+    if rank == 0:
+        flat = [r for part in allres for r in part]
+        np.savez(result_path, idx=np.array([i for i, _ in flat]), *[x for _, x in flat])
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_two_rank_device_run_gives_the_single_process_results(tmp_path):
+    """The same split on the device path: two gloo ranks on one GPU, each
+    solving its share of the models in one context (per-model convergence);
+    every model's states equal, bitwise, those of one process solving all."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    from muscade_gpu import _lib
+    from muscade_gpu.device import DeviceModel
+
+    _lib.build()
+    params = W.batched_params(8, nel_range=(10, 30), seed=5)
+    with socket.socket() as sck:
+        sck.bind(("127.0.0.1", 0))
+        port = sck.getsockname()[1]
+    path = os.path.join(tmp_path, "res.npz")
+    mp.start_processes(_device_worker, args=(2, port, params, path), nprocs=2, join=True, start_method="spawn")
+    z = np.load(path)
+    assert sorted(z["idx"].tolist()) == list(range(len(params)))
+    m, offs, times = W.build_batched(params)
+    st = m.initialize()
+    dm = DeviceModel(m, st.dis, device=0)
+    rc, x, _ = dm.sweepx(0, times, st.time, list(st.X), maxdx=1e-9, maxLl=math.inf, per_component=True)
+    dm.close()
+    assert rc == 0
+    bounds = list(offs) + [m.nnod]
+    for k, i in enumerate(z["idx"]):
+        d = W.node_dofs(m, np.arange(bounds[i] + 1, bounds[i + 1] + 1))
+        assert np.array_equal(z[f"arr_{k}"], x[:, 0, d[d >= 0]]), i
