@@ -1,7 +1,8 @@
 /*
  * muscade_gpu.h -- C ABI of the GB300 assemble-and-solve path for Muscade.jl
  * models built from EulerBeam3D, Bar3D, Hold / DofConstraint{:X} (affine gap,
- * equal mode) and DofLoad elements.
+ * equal mode), DofLoad and the quadratic cost elements SingleDofCost,
+ * SingleUdof and SingleAcost.
  *
  * The Julia side keeps Model / addelement! / initialize! and the element API;
  * it hands the device what its Disassembler already holds (per element type,
@@ -43,6 +44,21 @@ extern "C" {
 #define MGPU_BAR3D 2           /* toolbox/BarElement.jl:89-202; nX=6 (+nU=3); edata: 38 fields */
 #define MGPU_DOFCONSTRAINT_X 3 /* src/BasicElements.jl:406-438,484-488; nX=nx+1; edata: nx gap coefficients */
 #define MGPU_DOFLOAD 4         /* src/BasicElements.jl:275-284; nX=1; no edata */
+/* Cost elements, with the quadratic cost functor cost(v, t) = w (v − y(t))²
+ * whose target y(t) is a time value evaluated by the caller like a load:
+ *   MGPU_DOFCOST     SingleDofCost of class :X (src/BasicElements.jl:32-50,198-208):
+ *                    L = w (x⁽ᵈ⁾ − y(t))² on one X-dof; nX=1; edata: w, d (0, 1 or 2,
+ *                    the time derivative); one time value y(t).  In SweepX
+ *                    R = ∂L/∂Λ = 0.
+ *   MGPU_SINGLEUDOF  SingleUdof (src/BasicElements.jl:239-248): L = w (u − y(t))² − λu
+ *                    with λ the X-dof's multiplier; nX=1, nU=1; edata: w; one time
+ *                    value y(t).  In SweepX R = −u on the X-dof (the U-dof's value
+ *                    is a load).
+ *   MGPU_ACOST       SingleAcost (src/BasicElements.jl:77-86,163-167): the once-off
+ *                    L = w (a − y)² on one A-dof; nX=0, indexA; edata: w, y. */
+#define MGPU_DOFCOST 5
+#define MGPU_SINGLEUDOF 6
+#define MGPU_ACOST 7
 
 /* One element type (one entry of model.eleobj / dis.dis). */
 typedef struct {
@@ -54,9 +70,10 @@ typedef struct {
   const int64_t *indexX; /* [nele][nX] 1-based model X-dof indices */
   const int64_t *indexU; /* [nele][nU] 1-based model U-dof indices (NULL if nU==0) */
   const double *edata;   /* [nele][ndata] element fields in the reference's declaration order */
-  const int64_t *indexA; /* [nele] 1-based A-dof of each element, NULL if none.  EULERBEAM3D only:
+  const int64_t *indexA; /* [nele] 1-based A-dof of each element, NULL if none.  EULERBEAM3D:
                             the EI scale factor of the wrapper element EulerBeam3D{adof}
-                            (bending stiffnesses EI2, EI3 times the A-dof value) */
+                            (bending stiffnesses EI2, EI3 times the A-dof value); ACOST:
+                            the A-dof of the cost (required) */
 } mgpu_group;
 
 typedef struct {
@@ -97,8 +114,9 @@ int mgpu_get_pattern(const mgpu_ctx *ctx, int64_t *colptr, int64_t *rowval);
 int mgpu_get_asm(const mgpu_ctx *ctx, int32_t igroup, int64_t *asm1, int64_t *asm2);
 
 /* Number of time-dependent element values per assembly: one per DofLoad
- * element (F(t)) and one per DofConstraint element (gap offset c(t) in
- * g = Σ aᵢxᵢ − c(t)), concatenated over groups in model order. */
+ * element (F(t)), one per DofConstraint element (gap offset c(t) in
+ * g = Σ aᵢxᵢ − c(t)) and one per DOFCOST or SINGLEUDOF element (the cost
+ * target y(t)), concatenated over groups in model order. */
 int64_t mgpu_ntval(const mgpu_ctx *ctx);
 
 /* One assembly with host buffers (replaces assemble!{:step|:iter} over the
@@ -128,6 +146,23 @@ int mgpu_assemble_wait(mgpu_ctx *ctx, int64_t ticket);
  * i + nX*j) and, when U is given and dRdU != NULL, dRdU[nele][nX][nU]. */
 int mgpu_element_eval(mgpu_ctx *ctx, int32_t igroup, int32_t nXder, const double *X, const double *U, double t,
                       double p0, double p1, double p2, double *R, double *dR, double *dRdU);
+
+/* Element-level Lagrangian like diffed_lagrangian{2} (src/Diagnostic.jl:852-927)
+ * for the elements of group `igroup` of kind DOFLOAD or DOFCONSTRAINT_X
+ * (residual elements, L = Λ·R), DOFCOST, SINGLEUDOF or ACOST: the value and
+ * the first and second derivatives over the element's variables in the order
+ * DirectXUA revariates them (src/DirectXUA.jl:152-171) and adds them into its
+ * per-step gradient and Hessian blocks (:122-151):
+ *   Λ[nX], X⁽⁰⁾[nX], .., X⁽ⁿˣᵈᵉʳ⁻¹⁾[nX], U[nU], A[nA]
+ * so np = nX (1 + nXder) + nU + nA (nA = 1 for ACOST, else 0).  Inputs per
+ * element: lam[nele][nX], X[nele][nXder][nX], U[nele][nU], A[nele][nA] and
+ * tv[nele], the group's time values at the evaluation time (F, c or y; unused
+ * by ACOST, whose target is in edata).  Outputs (each may be NULL): L[nele],
+ * dL[nele][np], d2L[nele][np][np] (symmetric).  A DOFCOST on X⁽ᵈ⁾ needs
+ * nXder > d.  EulerBeam3D and Bar3D (residual elements without second order)
+ * return MGPU_ERR_UNSUPPORTED: use mgpu_element_eval. */
+int mgpu_element_lagrangian(mgpu_ctx *ctx, int32_t igroup, int32_t nXder, const double *lam, const double *X,
+                            const double *U, const double *A, const double *tv, double *L, double *dL, double *d2L);
 
 /* Device-resident assembly for throughput measurement: upload a state once,
  * then assemble repeatedly into device buffers.  mgpu_time_assemble runs
@@ -187,18 +222,25 @@ int mgpu_set_A(mgpu_ctx *ctx, const double *A);
  * per_component = 0; opts as for mgpu_sweepx), keeping the state at the start
  * of every segment of `ckpt` steps (ckpt <= 0: ⌈√nstep⌉), then walks the steps
  * backwards, recomputing each segment from its checkpoint, and solves the
- * transposed tangent of every step.  The cost is
- *   C = Σ_n w_n Σ_s cost_w[s] (x_n[cost_dof[s]] − cost_y[n][s])²
- * with w_n = t_n − t_{n−1} for OX = 2 (t_0 = t0) and 1 for OX = 0;
- * cost_dof[ncost] are distinct 1-based X-dofs (SingleDofCost sensors).
- * Outputs: *cost, dCdA[nA] (EI-scale A-dofs), and, when dCdtv != NULL,
+ * transposed tangent of every step.  The cost is the Lagrangian of the
+ * model's cost elements plus optional sensor arrays:
+ *   C = Σ_n w_n [ Σ_DOFCOST w_e (x_n⁽ᵈᵉ⁾[i_e] − y_e(t_n))² + Σ_SINGLEUDOF w_e (u[j_e] − y_e(t_n))²
+ *               + Σ_s cost_w[s] (x_n[cost_dof[s]] − cost_y[n][s])² ]  +  Σ_ACOST w_e (a[k_e] − y_e)²
+ * with w_n = t_n − t_{n−1} for OX = 2 (t_0 = t0) and 1 for OX = 0 (DirectXUA
+ * weighs its steps alike), the targets y_e(t_n) taken from tvals, the A-costs
+ * counted once, and cost_dof[ncost] distinct 1-based X-dofs (ncost may be 0).
+ * Outputs: *cost, dCdA[nA] (EI-scale and A-cost A-dofs); when dCdtv != NULL,
  * dCdtv[nstep][ntval]: the sensitivities to the load values F(t) of DofLoad
- * elements and the gap offsets c(t) of DofConstraint elements, in the layout of
- * tvals.  Needs the row-band solver for the transposed tangent. */
+ * elements, the gap offsets c(t) of DofConstraint elements and the cost
+ * targets y(t), in the layout of tvals; when dCdU != NULL, dCdU[nU]: the
+ * sensitivities to the U-dofs of SINGLEUDOF elements, held through the sweep
+ * as SweepX holds U (MGPU_ERR_UNSUPPORTED if a beam or bar has U-dofs).
+ * A DOFCOST on X' or X'' needs OX = 2.  Needs the row-band solver for the
+ * transposed tangent. */
 int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, double t0, int32_t nXder0,
                         const double *x0, const double *u, const double *tvals, const mgpu_sweep_opts *opts,
                         int64_t ncost, const int64_t *cost_dof, const double *cost_w, const double *cost_y,
-                        int32_t ckpt, double *cost, double *dCdA, double *dCdtv, mgpu_stats *stats);
+                        int32_t ckpt, double *cost, double *dCdA, double *dCdtv, double *dCdU, mgpu_stats *stats);
 
 /* Linear solver of the Newton loops (no counterpart in the reference, which
  * calls UMFPACK through lu/lu!/\ at src/SweepX.jl:207-210).  Every connected

@@ -5,14 +5,16 @@
 // gradient once the (Λ, X, U) blocks have converged (src/DirectXUA.jl:438-513),
 // over an all-steps system with finite differences in time.  Here the time
 // discretisation is the Newmark-β of SweepX (src/SweepX.jl:3-15, 98-132): the
-// cost
-//     C = Σ_n w_n Σ_s c_s (x_n[d_s] − y_{n,s})²,   w_n = Δt_n (OX = 2) or 1 (OX = 0),
-// is differentiated through the converged steps (the implicit-function adjoint
-// of R(x_n, v_n(x_n, S_{n-1}), a_n(x_n, S_{n-1}); A) = 0):
+// cost, the Lagrangian of the model's cost elements and of optional sensors,
+//     C = Σ_n w_n [Σ_DofCost w_e (x_n⁽ᵈᵉ⁾[i_e] − y_e(t_n))² + Σ_SingleUdof w_e (u[j_e] − y_e(t_n))²
+//                  + Σ_s c_s (x_n[d_s] − y_{n,s})²] + Σ_Acost w_e (a[k_e] − y_e)²,
+// w_n = Δt_n (OX = 2) or 1 (OX = 0), is differentiated through the converged
+// steps (the implicit-function adjoint of R(x_n, v_n(x_n, S_{n-1}),
+// a_n(x_n, S_{n-1}); u, A) = 0):
 //
-//   g_n      = x̄_n + a1 v̄_n + b1 ā_n            (x̄_n includes ∂C/∂x_n)
+//   g_n      = x̄_n + a1 v̄_n + b1 ā_n            (x̄_n, v̄_n, ā_n include ∂C/∂x_n, ∂C/∂v_n, ∂C/∂a_n)
 //   J_nᵀ μ_n = g_n                               J_n = K + a1 C + b1 M at step n
-//   dC/dA   −= μ_nᵀ ∂R_n/∂A,   dC/dF_n = −μ_nᵀ ∂R_n/∂F_n
+//   dC/dA   −= μ_nᵀ ∂R_n/∂A,   dC/dF_n = −μ_nᵀ ∂R_n/∂F_n,   dC/du −= μ_nᵀ ∂R_n/∂u
 //   p = v̄_n − C_nᵀ μ_n,   q = ā_n − M_nᵀ μ_n
 //   x̄_{n-1} = −a1 p − b1 q,  v̄_{n-1} = (1 − a2) p − b2 q,  ā_{n-1} = −a3 p + (1 − b3) q
 //
@@ -61,6 +63,74 @@ __global__ void adj_cost_grad(int64_t ncost, const int32_t* __restrict__ dof, co
                               double* __restrict__ xb) {
   const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (s < ncost) xb[dof[s]] += f * 2.0 * cw[s] * (x[dof[s]] - y[s]);
+}
+
+// Σ_e w_e (v_e − y_e)² over a DofCost group (v = x⁽ᵈᵉ⁾[i_e]) or a SingleUdof
+// group (v = u[j_e]); cdata holds w (and d), tv the targets.  One block, fixed order.
+__global__ void __launch_bounds__(256) adj_group_cost(int64_t nele, int udof, const int32_t* __restrict__ idx,
+                                                      const int32_t* __restrict__ uidx,
+                                                      const double* __restrict__ cdata,
+                                                      const double* __restrict__ tv, const double* __restrict__ x,
+                                                      int64_t nX, const double* __restrict__ u,
+                                                      double* __restrict__ out) {
+  __shared__ double sm[256];
+  double a = 0.0;
+  for (int64_t e = threadIdx.x; e < nele; e += 256) {
+    const double v = udof ? u[uidx[e]] : x[int64_t(cdata[nele + e]) * nX + idx[e]];
+    const double r = v - tv[e];
+    a += cdata[e] * r * r;
+  }
+  sm[threadIdx.x] = a;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) sm[threadIdx.x] += sm[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0];
+}
+
+// Step n's direct partials of a cost group, scaled by the step weight f:
+// DofCost: x̄/v̄/ā[i_e] += f 2 w_e (x⁽ᵈᵉ⁾ − y_e);  SingleUdof: ū[j_e] += f 2 w_e (u − y_e)
+// and ū[j_e] += μ[i_e] s_i (R = −u s on the X-dof);  dC/dy_e = −f 2 w_e (v − y_e)
+// into dtv (may be null).  `serial`: one thread walks the elements in order
+// (groups in which two elements write the same entry), else one per element.
+__global__ void adj_group_grad(int64_t nele, int udof, int serial, const int32_t* __restrict__ idx,
+                               const int32_t* __restrict__ uidx, const double* __restrict__ cdata,
+                               const double* __restrict__ tv, const double* __restrict__ x, int64_t nX,
+                               const double* __restrict__ u, const double* __restrict__ mu,
+                               const double* __restrict__ scale, double f, double* __restrict__ xb,
+                               double* __restrict__ vb, double* __restrict__ ab, double* __restrict__ ub,
+                               double* __restrict__ dtv) {
+  const int64_t e0 = serial ? 0 : int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t e1 = serial ? nele : e0 + 1;
+  for (int64_t e = e0; e < e1 && e < nele; ++e) {
+    const int i = idx[e];
+    if (udof) {
+      const int j = uidx[e];
+      const double r = u[j] - tv[e];
+      ub[j] += f * 2.0 * cdata[e] * r + mu[i] * (scale ? scale[i] : 1.0);
+      if (dtv) dtv[e] = -f * 2.0 * cdata[e] * r;
+    } else {
+      const int d = int(cdata[nele + e]);
+      const double r = x[int64_t(d) * nX + i] - tv[e];
+      double* bar = d == 0 ? xb : d == 1 ? vb : ab;
+      bar[i] += f * 2.0 * cdata[e] * r;
+      if (dtv) dtv[e] = -f * 2.0 * cdata[e] * r;
+    }
+  }
+}
+
+// The once-off A-costs: cost += Σ_e w_e (a[k_e] − y_e)², dC/da[k_e] += 2 w_e (a − y_e), in element order.
+__global__ void adj_acost(int64_t nele, const int32_t* __restrict__ aidx, const double* __restrict__ cdata,
+                          const double* __restrict__ A, double* __restrict__ gradA, double* __restrict__ cost) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double c = 0.0;
+  for (int64_t e = 0; e < nele; ++e) {
+    const double r = A[aidx[e]] - cdata[nele + e];
+    c += cdata[e] * r * r;
+    gradA[aidx[e]] += 2.0 * cdata[e] * r;
+  }
+  *cost = c;
 }
 
 // g = S (x̄ + a1 v̄ + b1 ā)
@@ -153,7 +223,7 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
                                    int32_t nXder0, const double* x0, const double* u, const double* tvals,
                                    const mgpu_sweep_opts* opts, int64_t ncost, const int64_t* cost_dof,
                                    const double* cost_w, const double* cost_y, int32_t ckpt, double* cost,
-                                   double* dCdA, double* dCdtv, mgpu_stats* stats) {
+                                   double* dCdA, double* dCdtv, double* dCdU, mgpu_stats* stats) {
   if (!c || !times || !opts || !stats || !cost || !(OX == 0 || OX == 2) || nstep < 1 || nXder0 < 0 ||
       nXder0 > OX + 1 || (nXder0 > 0 && !x0) || ncost < 0 || (ncost > 0 && (!cost_dof || !cost_w || !cost_y)) ||
       (c->ntval > 0 && !tvals) || (c->nA > 0 && !dCdA))
@@ -162,6 +232,18 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
     return set_err(c, MGPU_ERR_ARG, "mgpu_adjoint_sweepx: the adjoint needs converged steps (fixed_iter = 0, "
                                     "per_component = 0)");
   *stats = mgpu_stats{0, 0, 0, 0, 0.0, 0.0};
+  // cost element groups
+  std::vector<int> cgroups;  // DofCost and SingleUdof groups, model order
+  for (size_t gi = 0; gi < c->groups.size(); ++gi) {
+    const DevGroup& G = c->groups[gi];
+    if ((G.kind == MGPU_DOFCOST || G.kind == MGPU_SINGLEUDOF) && G.nele > 0) cgroups.push_back(int(gi));
+    if (G.kind == MGPU_DOFCOST && G.nele > 0 && G.maxder > OX)
+      return set_err(c, MGPU_ERR_ARG, "mgpu_adjoint_sweepx: a DofCost on a time derivative of X needs OX = 2");
+    if (dCdU && (G.kind == MGPU_EULERBEAM3D || G.kind == MGPU_BAR3D) && G.nU > 0 && G.nele > 0)
+      return set_err(c, MGPU_ERR_UNSUPPORTED, "mgpu_adjoint_sweepx: dCdU covers the U-dofs of SingleUdof elements; "
+                                              "this model has beams or bars with U-dofs");
+  }
+  const int64_t ncs = 1 + int64_t(cgroups.size());  // per step: sensors, then each cost group
   Solver& S = *c->solver;
   if (!S.ok) return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why);
   if (!S.wmT)
@@ -216,12 +298,13 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
     cudaGetLastError();
   };
   const size_t ns = size_t(3) * n;
-  double *ck, *seg, *xb, *vb, *ab, *g, *mu, *tC, *tM, *costs, *cw, *cy, *gradA, *contrib, *dtv = nullptr;
+  double *ck, *seg, *xb, *vb, *ab, *g, *mu, *tC, *tM, *costs, *cw, *cy, *gradA, *contrib, *ub, *acost,
+      *dtv = nullptr;
   int32_t *dcd, *aeled, *rowv;
   int64_t *aptrd, *colp;
   bool ok = alloc(&ck, nseg * ns) && alloc(&seg, size_t(ckpt) * ns) && alloc(&xb, n) && alloc(&vb, n) &&
             alloc(&ab, n) && alloc(&g, n) && alloc(&mu, n) && alloc(&tC, n) && alloc(&tM, n) &&
-            alloc(&costs, nstep) && alloc(&cw, ncost) && alloc(&cy, size_t(nstep) * ncost) &&
+            alloc(&costs, nstep * ncs) && alloc(&ub, c->nU) && alloc(&acost, 1) && alloc(&cw, ncost) && alloc(&cy, size_t(nstep) * ncost) &&
             alloc(&gradA, c->nA) && alloc(&contrib, nbA) && alloc(&dcd, ncost) && alloc(&aeled, aele.size()) &&
             alloc(&aptrd, aptr.size()) && alloc(&colp, n + 1) && alloc(&rowv, c->pat.nnz);
   if (ok && dCdtv && c->ntval > 0) ok = alloc(&dtv, size_t(nstep) * c->ntval);
@@ -233,13 +316,17 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
     std::vector<int32_t> rv(c->pat.rowval.begin(), c->pat.rowval.end());
     ok = cudaMemcpy(colp, c->pat.colptr.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(rowv, rv.data(), rv.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(dcd, cdof.data(), ncost * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(cw, cost_w, ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(cy, cost_y, size_t(nstep) * ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+         (ncost == 0 ||
+          (cudaMemcpy(dcd, cdof.data(), ncost * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+           cudaMemcpy(cw, cost_w, ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+           cudaMemcpy(cy, cost_y, size_t(nstep) * ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess)) &&
          cudaMemcpy(aptrd, aptr.data(), aptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
          (aele.empty() ||
           cudaMemcpy(aeled, aele.data(), aele.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess) &&
          cudaMemsetAsync(gradA, 0, std::max<int64_t>(c->nA, 1) * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(ub, 0, std::max<int64_t>(c->nU, 1) * sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(acost, 0, sizeof(double), st) == cudaSuccess &&
+         cudaMemsetAsync(costs, 0, nstep * ncs * sizeof(double), st) == cudaSuccess &&
          cudaMemsetAsync(xb, 0, n * sizeof(double), st) == cudaSuccess &&
          cudaMemsetAsync(vb, 0, n * sizeof(double), st) == cudaSuccess &&
          cudaMemsetAsync(ab, 0, n * sizeof(double), st) == cudaSuccess &&
@@ -285,13 +372,22 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
     }
     ADJ_TRY(newton_step(c, OX, k, t, dt, tvk(k), opts, stats));
     stats->nstep_done = int(k + 1);
-    if (ncost > 0) adj_cost_value<<<1, 256, 0, st>>>(ncost, dcd, cw, cy + k * ncost, c->x, costs + k);
+    if (ncost > 0) adj_cost_value<<<1, 256, 0, st>>>(ncost, dcd, cw, cy + k * ncost, c->x, costs + k * ncs);
+    for (size_t q = 0; q < cgroups.size(); ++q) {
+      const DevGroup& G = c->groups[cgroups[q]];
+      adj_group_cost<<<1, 256, 0, st>>>(G.nele, G.kind == MGPU_SINGLEUDOF, G.idx, G.uidx, G.cdata,
+                                        c->tv + G.tval_base, c->x, n, c->u, costs + k * ncs + 1 + q);
+    }
   }
   {
-    std::vector<double> hc(nstep, 0.0);
-    if (ncost > 0) ADJ_CUDA(cudaMemcpy(hc.data(), costs, nstep * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<double> hc(nstep * ncs, 0.0);
+    ADJ_CUDA(cudaMemcpy(hc.data(), costs, nstep * ncs * sizeof(double), cudaMemcpyDeviceToHost));
     double C = 0.0;
-    for (int64_t k = 0; k < nstep; ++k) C += (OX == 2 ? times[k] - tprev(k) : 1.0) * hc[k];
+    for (int64_t k = 0; k < nstep; ++k) {
+      double ck_ = 0.0;
+      for (int64_t q = 0; q < ncs; ++q) ck_ += hc[k * ncs + q];
+      C += (OX == 2 ? times[k] - tprev(k) : 1.0) * ck_;
+    }
     *cost = C;
   }
   // ---- reverse pass, segment by segment
@@ -311,6 +407,17 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
         ADJ_CUDA(cudaMemcpyAsync(c->tv, tvk(k), c->ntval * sizeof(double), cudaMemcpyHostToDevice, st));
       if (ncost > 0)
         adj_cost_grad<<<nb(ncost, 256), 256, 0, st>>>(ncost, dcd, cw, cy + k * ncost, c->x, wk, xb);
+      for (int gi : cgroups) {  // DofCost partials (SingleUdof's need μ, below)
+        const DevGroup& G = c->groups[gi];
+        if (G.kind != MGPU_DOFCOST) continue;
+        double* dt = dtv ? dtv + k * c->ntval + G.tval_base : nullptr;
+        if (G.distinct)
+          adj_group_grad<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, 0, 0, G.idx, nullptr, G.cdata, c->tv + G.tval_base,
+                                                          c->x, n, c->u, nullptr, c->scale, wk, xb, vb, ab, ub, dt);
+        else
+          adj_group_grad<<<1, 1, 0, st>>>(G.nele, 0, 1, G.idx, nullptr, G.cdata, c->tv + G.tval_base, c->x, n, c->u,
+                                          nullptr, c->scale, wk, xb, vb, ab, ub, dt);
+      }
       adj_rhs<<<nb(n, 256), 256, 0, st>>>(n, OX, nm.a1, nm.b1, c->scale, xb, vb, ab, g);
       // μ = J⁻ᵀ S g
       ADJ_TRY(upload_stepc(c, t, OX == 2 ? &nm : nullptr));
@@ -326,16 +433,27 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
                                                          contrib + abase[gi]);
         }
       if (c->nA > 0) adj_agrad<<<nb(c->nA, 256), 256, 0, st>>>(c->nA, aptrd, aeled, contrib, gradA);
+      // U-dof sensitivities of SingleUdof: the cost's partial and −μᵀ∂R/∂u
+      for (int gi : cgroups) {
+        const DevGroup& G = c->groups[gi];
+        if (G.kind != MGPU_SINGLEUDOF) continue;
+        double* dt = dtv ? dtv + k * c->ntval + G.tval_base : nullptr;
+        if (G.distinct)
+          adj_group_grad<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, 1, 0, G.idx, G.uidx, G.cdata, c->tv + G.tval_base,
+                                                          c->x, n, c->u, mu, c->scale, wk, xb, vb, ab, ub, dt);
+        else
+          adj_group_grad<<<1, 1, 0, st>>>(G.nele, 1, 1, G.idx, G.uidx, G.cdata, c->tv + G.tval_base, c->x, n, c->u,
+                                          mu, c->scale, wk, xb, vb, ab, ub, dt);
+      }
       // load-value sensitivities
       if (dtv) {
-        int64_t tvb = 0;
         for (auto& G : c->groups) {
           if (G.kind == MGPU_DOFLOAD && G.nele > 0)
-            adj_dtv<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, 1, 1, G.idx, mu, c->scale, dtv + k * c->ntval + tvb);
+            adj_dtv<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, 1, 1, G.idx, mu, c->scale,
+                                                     dtv + k * c->ntval + G.tval_base);
           if (G.kind == MGPU_DOFCONSTRAINT_X && G.nele > 0)
             adj_dtv<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, G.nX, -1, G.idx, mu, c->scale,
-                                                     dtv + k * c->ntval + tvb);
-          if (G.kind == MGPU_DOFLOAD || G.kind == MGPU_DOFCONSTRAINT_X) tvb += G.nele;
+                                                     dtv + k * c->ntval + G.tval_base);
         }
       }
       if (OX == 2) {
@@ -366,7 +484,17 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
       }
     }
   }
+  // the once-off A-costs, in group order
+  for (const DevGroup& G : c->groups)
+    if (G.kind == MGPU_ACOST && G.nele > 0) {
+      adj_acost<<<1, 1, 0, st>>>(G.nele, G.aidx, G.cdata, c->Avec, gradA, acost);
+      double ha = 0.0;
+      ADJ_CUDA(cudaMemcpyAsync(&ha, acost, sizeof(double), cudaMemcpyDeviceToHost, st));
+      ADJ_CUDA(cudaStreamSynchronize(st));
+      *cost += ha;
+    }
   if (c->nA > 0) ADJ_CUDA(cudaMemcpy(dCdA, gradA, c->nA * sizeof(double), cudaMemcpyDeviceToHost));
+  if (dCdU && c->nU > 0) ADJ_CUDA(cudaMemcpy(dCdU, ub, c->nU * sizeof(double), cudaMemcpyDeviceToHost));
   if (dtv) ADJ_CUDA(cudaMemcpy(dCdtv, dtv, size_t(nstep) * c->ntval * sizeof(double), cudaMemcpyDeviceToHost));
   cleanup();
 #undef ADJ_TRY

@@ -25,9 +25,16 @@ struct DevGroup {
   std::vector<int64_t> h_indexA;  // host copy (1-based)
   double* cdata = nullptr;  // [nfield][nele] kernel constants (structure of arrays)
   int32_t nfield = 0;
-  int64_t tval_base = -1;   // offset in the time-value vector (loads, constraints)
+  int64_t tval_base = -1;   // offset in the time-value vector (loads, constraints, cost targets)
+  int32_t maxder = 0;       // DOFCOST: highest time derivative a cost reads
+  bool distinct = true;     // cost groups: no two elements write the same gradient entry
   std::vector<int64_t> h_indexX;  // host copy (1-based) for asm queries
 };
+
+// element kinds with one time value per element (F(t), c(t) or the cost target y(t))
+inline bool has_tval(int kind) {
+  return kind == MGPU_DOFLOAD || kind == MGPU_DOFCONSTRAINT_X || kind == MGPU_DOFCOST || kind == MGPU_SINGLEUDOF;
+}
 
 struct Solver;  // linear solver state (solver.cu)
 

@@ -25,6 +25,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "bar_math.hpp"
@@ -236,6 +237,25 @@ __global__ void load_kernel(int64_t nele, const int32_t* __restrict__ idx, const
   flag_nan(a.errflag, gid0 + e, isnan(r));
 }
 
+// SingleDofCost and SingleUdof in SweepX: the residual of a Lagrangian
+// element is ∂L/∂Λ (src/Assemble.jl:661-677), 0 for a cost and −u for the
+// U-dof load of SingleUdof (L = cost(u,t) − λu); the tangents are zero.
+__global__ void cost_kernel(int64_t nele, int udof, const int32_t* __restrict__ idx,
+                            const int32_t* __restrict__ uidx, AsmArgs a, double* __restrict__ rout,
+                            double* __restrict__ kout, int64_t gid0) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nele) return;
+  double r = 0.0;
+  if (udof) {
+    const int d = __ldg(idx + e);
+    const double s = a.scale ? __ldg(a.scale + d) : 1.0;
+    r = -__ldg(a.u + __ldg(uidx + e)) * s;
+  }
+  rout[e] = r;
+  kout[e] = 0.0;
+  flag_nan(a.errflag, gid0 + e, isnan(r));
+}
+
 // Deterministic gather-sum:
 //   out[k] = ((0 + buf[src[q0]]) + buf[src[q0+1]]) + ... ,  q = seg[k] .. seg[k+1]-1.
 // A block takes kGatherOut consecutive outputs.  Their plan positions form one
@@ -389,6 +409,13 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0)
       case MGPU_DOFLOAD:
         load_kernel<<<nblk(G.nele, 256), 256, 0, c->stream>>>(G.nele, G.idx, ag.tv, ag, rout, kout, gid0);
         break;
+      case MGPU_DOFCOST:
+      case MGPU_SINGLEUDOF:
+        cost_kernel<<<nblk(G.nele, 256), 256, 0, c->stream>>>(G.nele, G.kind == MGPU_SINGLEUDOF, G.idx, G.uidx, ag,
+                                                              rout, kout, gid0);
+        break;
+      case MGPU_ACOST:  // no X-dofs: nothing in SweepX's Lλ and Lλx
+        break;
     }
     gid0 += G.nele;
     if (ev_groups) cudaEventRecord(ev_groups[g], c->stream);
@@ -416,10 +443,11 @@ int nan_error(mgpu_ctx* c, int flag) {
     int64_t gid = flag, base = 0;
     for (size_t g = 0; g < c->groups.size(); ++g) {
       if (gid < base + c->groups[g].nele) {
-        const char* names[] = {"?", "EulerBeam3D", "Bar3D", "DofConstraint", "DofLoad"};
+        const char* names[] = {"?", "EulerBeam3D", "Bar3D", "DofConstraint", "DofLoad", "DofCost", "SingleUdof",
+                               "Acost"};
         int k = c->groups[g].kind;
         return set_err(c, MGPU_ERR_NAN,
-                       std::string("residual(") + names[(k >= 1 && k <= 4) ? k : 0] +
+                       std::string("residual(") + names[(k >= 1 && k <= 7) ? k : 0] +
                            ",...) returned NaN in R, FB or derivatives (ieletyp=" + std::to_string(g + 1) +
                            ", iele=" + std::to_string(gid - base + 1) + ")");
       }
@@ -480,27 +508,40 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
       case MGPU_BAR3D: exp_nX = 6; exp_data = 38; break;
       case MGPU_DOFCONSTRAINT_X: exp_nX = G.nX; exp_data = G.nX - 1; break;
       case MGPU_DOFLOAD: exp_nX = 1; exp_data = 0; break;
+      case MGPU_DOFCOST: exp_nX = 1; exp_data = 2; break;
+      case MGPU_SINGLEUDOF: exp_nX = 1; exp_data = 1; break;
+      case MGPU_ACOST: exp_nX = 0; exp_data = 2; break;
       default:
         return set_err(c, MGPU_ERR_UNSUPPORTED,
                        "element type " + std::to_string(g + 1) + " (kind " + std::to_string(G.kind) +
                            ") is not supported by the GPU path");
     }
-    if (G.nX != exp_nX || G.nX < 1 || (exp_data > 0 && G.ndata != exp_data) || G.nele < 0 || (G.nele > 0 && !G.indexX))
+    if (G.nX != exp_nX || (G.nX < 1 && G.kind != MGPU_ACOST) || (exp_data > 0 && G.ndata != exp_data) ||
+        G.nele < 0 || (G.nele > 0 && G.nX > 0 && !G.indexX) || (G.nele > 0 && exp_data > 0 && !G.edata))
       return set_err(c, MGPU_ERR_ARG, "element type " + std::to_string(g + 1) + ": unexpected layout");
     if ((G.kind == MGPU_EULERBEAM3D || G.kind == MGPU_BAR3D) && !(G.nU == 0 || G.nU == 3))
       return set_err(c, MGPU_ERR_ARG, "beam/bar elements have 0 or 3 U-dofs");
-    if ((G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) && G.nU != 0)
-      return set_err(c, MGPU_ERR_ARG, "constraints and loads have no U-dofs");
+    if ((G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD || G.kind == MGPU_DOFCOST ||
+         G.kind == MGPU_ACOST) && G.nU != 0)
+      return set_err(c, MGPU_ERR_ARG, "constraints, loads and DofCost/Acost elements have no U-dofs");
+    if (G.kind == MGPU_SINGLEUDOF && G.nU != 1) return set_err(c, MGPU_ERR_ARG, "SingleUdof has one U-dof");
     if (G.nU > 0 && G.nele > 0 && !G.indexU) return set_err(c, MGPU_ERR_ARG, "missing indexU");
-    if (G.indexA && G.kind != MGPU_EULERBEAM3D)
-      return set_err(c, MGPU_ERR_UNSUPPORTED, "A-dofs are supported on EulerBeam3D (EI scale) only");
+    if (G.indexA && G.kind != MGPU_EULERBEAM3D && G.kind != MGPU_ACOST)
+      return set_err(c, MGPU_ERR_UNSUPPORTED, "A-dofs are supported on EulerBeam3D (EI scale) and Acost only");
+    if (G.kind == MGPU_ACOST && G.nele > 0 && !G.indexA) return set_err(c, MGPU_ERR_ARG, "Acost needs indexA");
+    if (G.kind == MGPU_DOFCOST)
+      for (int64_t e = 0; e < G.nele; ++e) {
+        const double dd = G.edata[2 * e + 1];
+        if (!(dd == 0.0 || dd == 1.0 || dd == 2.0))
+          return set_err(c, MGPU_ERR_ARG, "DofCost: the derivative must be 0, 1 or 2");
+      }
     if (G.indexA)
       for (int64_t k = 0; k < G.nele; ++k)
         if (G.indexA[k] < 1 || G.indexA[k] > d->nA) return set_err(c, MGPU_ERR_ARG, "A-dof index out of range");
     for (int64_t k = 0; k < G.nele * G.nU; ++k)
       if (G.indexU[k] < 1 || G.indexU[k] > d->nU) return set_err(c, MGPU_ERR_ARG, "U-dof index out of range");
     shapes.push_back(GroupShape{G.nele, G.nX, G.indexX});
-    if (G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) ntv += G.nele;
+    if (has_tval(G.kind)) ntv += G.nele;
   }
   const auto t_pat0 = std::chrono::steady_clock::now();
   std::string perr = build_pattern(d->nX, shapes, c->pat);
@@ -556,8 +597,8 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
         const double* p = reinterpret_cast<const double*>(&bc);
         for (int f = 0; f < D.nfield; ++f) cd[size_t(f) * G.nele + e] = p[f];
       }
-    } else if (G.kind == MGPU_DOFCONSTRAINT_X) {
-      D.nfield = G.nX - 1;
+    } else if (G.ndata > 0) {  // constraint coefficients, cost weights and targets
+      D.nfield = G.ndata;
       cd.resize(size_t(D.nfield) * G.nele);
       for (int64_t e = 0; e < G.nele; ++e)
         for (int f = 0; f < D.nfield; ++f) cd[size_t(f) * G.nele + e] = G.edata[e * D.nfield + f];
@@ -566,9 +607,29 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
       MG_TRY(dalloc(c, &D.cdata, cd.size()));
       MG_CUDA(cudaMemcpy(D.cdata, cd.data(), cd.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    if (G.kind == MGPU_DOFCONSTRAINT_X || G.kind == MGPU_DOFLOAD) {
+    if (has_tval(G.kind)) {
       D.tval_base = tvb;
       tvb += G.nele;
+    }
+    if (G.kind == MGPU_DOFCOST || G.kind == MGPU_SINGLEUDOF || G.kind == MGPU_ACOST) {
+      // gradient entries each element writes: (dof, derivative), (X-dof, U-dof) or the A-dof
+      std::vector<std::pair<int64_t, int64_t>> keys(G.nele), ukeys;
+      for (int64_t e = 0; e < G.nele; ++e) {
+        if (G.kind == MGPU_DOFCOST) {
+          const int d = int(G.edata[2 * e + 1]);
+          D.maxder = std::max(D.maxder, d);
+          keys[e] = {G.indexX[e], d};
+        } else if (G.kind == MGPU_SINGLEUDOF) {
+          keys[e] = {G.indexX[e], 0};
+          ukeys.push_back({G.indexU[e], 0});
+        } else {
+          keys[e] = {G.indexA[e], 0};
+        }
+      }
+      for (auto* v : {&keys, &ukeys}) {
+        std::sort(v->begin(), v->end());
+        D.distinct = D.distinct && std::adjacent_find(v->begin(), v->end()) == v->end();
+      }
     }
     c->groups.push_back(std::move(D));
   }

@@ -16,7 +16,7 @@ std::string build_pattern(int64_t n, const std::vector<GroupShape>& groups, Patt
   int64_t npair = 0, kb = 0, rb = 0;
   for (size_t g = 0; g < ng; ++g) {
     const GroupShape& G = groups[g];
-    if (G.nX <= 0 || G.nele < 0) return "invalid element group shape";
+    if (G.nX < 0 || G.nele < 0) return "invalid element group shape";
     P.pair_base[g] = npair;
     P.kbuf_base[g] = kb;
     P.rbuf_base[g] = rb;

@@ -15,8 +15,8 @@ PKG = os.path.dirname(HERE)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
-SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "sparse_lu.cu", "pattern.cpp",
-           "sparse_analysis.cpp"]
+SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "sparse_lu.cu", "lagrangian.cu",
+           "pattern.cpp", "sparse_analysis.cpp"]
 HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh",
            "band_torn.cuh", "band_bcr.cuh", "solver.hpp", "sparse_lu.hpp", "sparse_analysis.hpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -24,7 +24,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # status codes
 MGPU_OK = 0
 ERRORS = {1: "argument", 2: "cuda", 3: "unsupported", 4: "nan", 5: "singular", 6: "noconvergence", 7: "nomem", 8: "size"}
-EULERBEAM3D, BAR3D, DOFCONSTRAINT_X, DOFLOAD = 1, 2, 3, 4
+EULERBEAM3D, BAR3D, DOFCONSTRAINT_X, DOFLOAD, DOFCOST, SINGLEUDOF, ACOST = 1, 2, 3, 4, 5, 6, 7
 ASM_STATIC, ASM_STEP, ASM_ITER = 0, 1, 2
 
 
@@ -114,7 +114,7 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
            "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune",
-           "mgpu_assemble_async", "mgpu_assemble_wait", "mgpu_sparse_info"]
+           "mgpu_assemble_async", "mgpu_assemble_wait", "mgpu_sparse_info", "mgpu_element_lagrangian"]
 
 _lib = None
 
@@ -161,7 +161,8 @@ def load():
     L.mgpu_autotune.argtypes = [vp, i32, P(Newmark), P(TuneReport)]
     L.mgpu_host_unregister.argtypes = [vp]
     L.mgpu_adjoint_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32, pd,
-                                      pd, pd, P(Stats)]
+                                      pd, pd, pd, P(Stats)]
+    L.mgpu_element_lagrangian.argtypes = [vp, i32, i32, pd, pd, pd, pd, pd, pd, pd, pd]
     for name in SYMBOLS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int and name not in ("mgpu_destroy",):

@@ -12,14 +12,32 @@ import math
 import numpy as np
 
 from . import _lib as L
-from .elements import Bar3D, DofConstraint, DofLoad, EulerBeam3D, Hold, group_time_values
+from .elements import group_cost_targets, group_time_values, quadratic_costs
 from .model import MuscadeError
 
 
 def _kind(g):
     k = g.key[0]
+    if k == "SingleDofCost" and g.key[1] != "X":
+        return None  # a cost on a U-dof: not on the GPU path
     return {"EulerBeam3D": L.EULERBEAM3D, "Bar3D": L.BAR3D, "DofConstraint": L.DOFCONSTRAINT_X,
-            "DofLoad": L.DOFLOAD}.get(k)
+            "DofLoad": L.DOFLOAD, "SingleDofCost": L.DOFCOST, "SingleUdof": L.SINGLEUDOF,
+            "SingleAcost": L.ACOST}.get(k)
+
+
+def _cost_data(g, kind):
+    """Element fields of a cost group: DOFCOST (w, d), SINGLEUDOF (w), ACOST (w, y)."""
+    costs = quadratic_costs(g)
+    w = np.array([c.weight for c in costs], dtype=np.float64)
+    if kind == L.DOFCOST:
+        if g.key[3] not in (0, 1, 2):
+            raise DeviceError(1, f"SingleDofCost: derivative must be 0, 1 or 2, got {g.key[3]}")
+        return np.stack([w, np.full(len(w), float(g.key[3]))], axis=1)
+    if kind == L.SINGLEUDOF:
+        return w[:, None]
+    if any(callable(c.target) for c in costs):
+        raise DeviceError(1, "SingleAcost: the QuadraticCost target must be a constant")
+    return np.stack([w, np.array([c.target_at(None) for c in costs])], axis=1)
 
 
 class DeviceError(MuscadeError):
@@ -50,6 +68,8 @@ class DeviceModel:
                 ed = np.ascontiguousarray(g.cat("ele"), dtype=np.float64)
             elif kind == L.DOFCONSTRAINT_X:
                 ed = np.ascontiguousarray(g.cat("coeffs"), dtype=np.float64)
+            elif kind in (L.DOFCOST, L.SINGLEUDOF, L.ACOST):
+                ed = np.ascontiguousarray(_cost_data(g, kind), dtype=np.float64)
             else:
                 ed = np.zeros((g.nele, 0))
             self._keep += [iX, iU, ed]
@@ -57,12 +77,12 @@ class DeviceModel:
             G.kind, G.nX, G.nU = kind, iX.shape[1], iU.shape[1] if iU.ndim == 2 else 0
             G.ndata = ed.shape[1] if ed.ndim == 2 else 0
             G.nele = g.nele
-            G.indexX = L.ptr(iX, ctypes.c_int64)
+            G.indexX = L.ptr(iX, ctypes.c_int64) if iX.size else None
             G.indexU = L.ptr(iU, ctypes.c_int64) if G.nU else None
             G.edata = L.ptr(ed) if G.ndata else None
             iA = np.ascontiguousarray(dg.index_A, dtype=np.int64)
             if iA.size:
-                if kind != L.EULERBEAM3D or iA.shape[1] != 1:
+                if kind not in (L.EULERBEAM3D, L.ACOST) or iA.shape[1] != 1:
                     raise DeviceError(3, f"A-dofs of element type {g.key[0]} are not supported by the GPU path")
                 iA = np.ascontiguousarray(iA[:, 0])
                 self._keep.append(iA)
@@ -87,31 +107,44 @@ class DeviceModel:
             raise ValueError(f"A must have {self.nA} values")
         self._check(self.lib.mgpu_set_A(self.ctx, L.ptr(a)))
 
-    def adjoint(self, OX, times, t0, X0, cost_dof, cost_w, cost_y, U=None, beta=0.25, gamma=0.5, maxiter=50,
-                maxdx=1e-10, maxLl=math.inf, ckpt=0, load_gradient=False):
+    def adjoint(self, OX, times, t0, X0, cost_dof=(), cost_w=1.0, cost_y=None, U=None, beta=0.25, gamma=0.5,
+                maxiter=50, maxdx=1e-10, maxLl=math.inf, ckpt=0, load_gradient=False, u_gradient=False, tvals=None):
         """Cost and its gradient with respect to the A-dofs (and, with
-        load_gradient, to the load values) by the discrete adjoint of a
-        converged SweepX{OX} sweep; see mgpu_adjoint_sweepx.  cost_dof are
-        1-based X-dofs, cost_y[nstep][ncost].  Returns (cost, dCdA, dCdtv, stats)."""
+        load_gradient, to the time values; with u_gradient, to the U-dofs of
+        SingleUdof elements) by the discrete adjoint of a converged SweepX{OX}
+        sweep; see mgpu_adjoint_sweepx.  The cost is that of the model's cost
+        elements plus optional sensors: cost_dof 1-based X-dofs, cost_y[nstep][ncost].
+        tvals: the time values of every step (time_values(times)), evaluated
+        here when None.  Returns (cost, dCdA, dCdtv, stats), and dCdU after
+        them with u_gradient."""
         times = np.ascontiguousarray(times, dtype=np.float64)
         nstep = len(times)
         X0 = [np.asarray(v, dtype=np.float64) for v in X0][: OX + 1]
         x0 = np.ascontiguousarray(np.concatenate(X0)) if X0 else np.zeros(0)
         u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
-        tv = np.ascontiguousarray(np.stack([self.tvals(t) for t in times]) if self.ntval else np.zeros((nstep, 0)))
-        cd = np.ascontiguousarray(cost_dof, dtype=np.int64)
+        tv = self.time_values(times) if tvals is None else np.ascontiguousarray(tvals, dtype=np.float64)
+        if tv.shape != (nstep, self.ntval):
+            raise ValueError(f"tvals must be [{nstep}][{self.ntval}]")
+        cd = np.ascontiguousarray(cost_dof, dtype=np.int64).reshape(-1)
         cw = np.ascontiguousarray(np.broadcast_to(cost_w, cd.shape), dtype=np.float64)
-        cy = np.ascontiguousarray(cost_y, dtype=np.float64).reshape(nstep, len(cd))
+        cy = np.ascontiguousarray(np.zeros((nstep, 0)) if cost_y is None else cost_y, dtype=np.float64)
+        cy = cy.reshape(nstep, len(cd))
         opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0)
         cost = ctypes.c_double()
         dA = np.zeros(max(self.nA, 1))
         dtv = np.zeros((nstep, self.ntval)) if load_gradient and self.ntval else None
+        dU = np.zeros(max(self.nU, 1)) if u_gradient else None
         stats = L.Stats()
         rc = self.lib.mgpu_adjoint_sweepx(self.ctx, OX, nstep, L.ptr(times), float(t0), len(X0), L.ptr(x0), L.ptr(u),
-                                          L.ptr(tv), ctypes.byref(opts), len(cd), L.ptr(cd, ctypes.c_int64), L.ptr(cw),
-                                          L.ptr(cy), int(ckpt), ctypes.byref(cost), L.ptr(dA),
-                                          L.ptr(dtv) if dtv is not None else None, ctypes.byref(stats))
+                                          L.ptr(tv), ctypes.byref(opts), len(cd),
+                                          L.ptr(cd, ctypes.c_int64) if len(cd) else None,
+                                          L.ptr(cw) if len(cd) else None, L.ptr(cy) if len(cd) else None,
+                                          int(ckpt), ctypes.byref(cost), L.ptr(dA),
+                                          L.ptr(dtv) if dtv is not None else None,
+                                          L.ptr(dU) if dU is not None else None, ctypes.byref(stats))
         self._check(rc)
+        if u_gradient:
+            return cost.value, dA[: self.nA], dtv, stats, dU[: self.nU]
         return cost.value, dA[: self.nA], dtv, stats
 
     def autotune(self, mission=L.ASM_STATIC, c=None):
@@ -179,14 +212,22 @@ class DeviceModel:
         self._check(self.lib.mgpu_get_asm(self.ctx, ig, L.ptr(a1, ctypes.c_int64), L.ptr(a2, ctypes.c_int64)))
         return a1, a2
 
+    def time_values(self, times):
+        """The time values of every step, [nstep][ntval] (see tvals)."""
+        nstep = len(times)
+        return np.ascontiguousarray(np.stack([self.tvals(t) for t in times]) if self.ntval else np.zeros((nstep, 0)))
+
     def tvals(self, t):
-        """Host evaluation of the time functions (DofLoad F(t), constraint offsets c(t))."""
+        """Host evaluation of the time functions (DofLoad F(t), constraint offsets
+        c(t), cost targets y(t)) in the layout of mgpu_ntval."""
         out = []
         for g in self.model.groups:
             if g.key[0] == "DofLoad":
                 out.append(group_time_values(g, "value", t))
             elif g.key[0] == "DofConstraint":
                 out.append(group_time_values(g, "offset", t))
+            elif g.key[0] in ("SingleDofCost", "SingleUdof"):
+                out.append(group_cost_targets(g, t))
         return np.ascontiguousarray(np.concatenate(out) if out else np.zeros(0))
 
     # ---------------------------------------------------------------- assembly
@@ -265,6 +306,39 @@ class DeviceModel:
         if H is not None:
             H = H.reshape(nele, 3, nX).transpose(0, 2, 1)
         return R, dR, H
+
+    def element_lagrangian(self, ig, Lam, X, U=None, A=None, t=0.0):
+        """diffed_lagrangian{2}-like evaluation of the elements of group ig
+        (loads, constraints and cost elements; mgpu_element_lagrangian).
+        Lam (nele,nX), X (nele,nXder,nX), U (nele,nU), A (nele,nA).  Returns L (nele,),
+        dL (nele,np), d2L (nele,np,np) over (Λ, X⁽⁰⁾.., U, A)."""
+        g = self.model.groups[ig]
+        dg = self.dis.dis[ig]
+        nele = g.nele
+        nX = dg.index_X.shape[1]
+        nU = dg.index_U.shape[1] if dg.index_U.ndim == 2 else 0
+        nA = dg.index_A.shape[1] if dg.index_A.ndim == 2 else 0
+        X = np.ascontiguousarray(X, dtype=np.float64).reshape(nele, -1, nX) if nX else np.zeros((nele, 1, 0))
+        nXder = X.shape[1]
+        lam = np.ascontiguousarray(Lam, dtype=np.float64).reshape(nele, nX)
+        Uc = np.ascontiguousarray(U if U is not None else np.zeros((nele, nU)), dtype=np.float64).reshape(nele, nU)
+        Ac = np.ascontiguousarray(A if A is not None else np.zeros((nele, nA)), dtype=np.float64).reshape(nele, nA)
+        tvall = self.tvals(t)
+        tv = None
+        off = 0
+        for h in self.model.groups[:ig]:
+            if h.key[0] in ("DofLoad", "DofConstraint", "SingleDofCost", "SingleUdof"):
+                off += h.nele
+        if g.key[0] in ("DofLoad", "DofConstraint", "SingleDofCost", "SingleUdof"):
+            tv = np.ascontiguousarray(tvall[off:off + nele])
+        npar = nX * (1 + nXder) + nU + nA
+        Lv = np.zeros(nele)
+        dL = np.zeros((nele, npar))
+        d2L = np.zeros((nele, npar, npar))
+        rc = self.lib.mgpu_element_lagrangian(self.ctx, ig, nXder, L.ptr(lam), L.ptr(X), L.ptr(Uc), L.ptr(Ac),
+                                              L.ptr(tv) if tv is not None else None, L.ptr(Lv), L.ptr(dL), L.ptr(d2L))
+        self._check(rc)
+        return Lv, dL, d2L
 
     def upload_state(self, X, U=None, t=0.0):
         x = np.ascontiguousarray(np.concatenate([np.asarray(v, dtype=np.float64) for v in X]))

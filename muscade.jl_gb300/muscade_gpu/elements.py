@@ -11,6 +11,10 @@ with equal keys form one element group (ModelDescription.jl:198-208).
 * Hold                 src/BasicElements.jl:484-488  (DofConstraint{:X} with gap x)
 * DofConstraint        src/BasicElements.jl:406-438  (λclass :X, equal mode, affine gap)
 * DofLoad              src/BasicElements.jl:275-284
+* SingleDofCost        src/BasicElements.jl:198-208 (through DofCost :32-50)
+* SingleUdof           src/BasicElements.jl:239-248
+* SingleAcost          src/BasicElements.jl:163-167 (through Acost :77-86)
+* QuadraticCost        the cost functor form the GPU path evaluates
 """
 from __future__ import annotations
 
@@ -207,6 +211,100 @@ class DofLoad:
     def construct(model, nod, field, value):
         name = getattr(value, "__qualname__", type(value).__name__)
         return {"value": [value], "n": np.full(nod.shape[0], 1)}, ("DofLoad", field, name)
+
+
+class QuadraticCost:
+    """Cost functor cost(v, t) = weight · (v − target(t))², the form of the cost
+    elements' `cost` argument that the GPU path evaluates (the reference takes
+    any functor, src/BasicElements.jl:198-208).  `target` is a constant or a
+    function of t returning a scalar; for SingleAcost it is a constant and the
+    functor is called as cost(a).  Works on floats and on any number type with
+    + − * (dual numbers of the oracle)."""
+
+    def __init__(self, weight=1.0, target=0.0):
+        self.weight = float(weight)
+        self.target = target
+
+    def target_at(self, t):
+        return float(self.target(t)) if callable(self.target) else float(self.target)
+
+    def __call__(self, v, t=None, *costargs):
+        d = v - self.target_at(t)
+        return self.weight * (d * d)
+
+
+def _cost_batch(nod, cost):
+    return {"cost": [cost], "n": np.full(nod.shape[0], 1)}
+
+
+def _cost_name(cost):
+    return getattr(cost, "__qualname__", type(cost).__name__)
+
+
+class SingleDofCost:
+    """SingleDofCost: L = cost(x⁽ᵈ⁾, t) on one dof of class X or U (BasicElements.jl:198-208).
+    The GPU path takes class X with a QuadraticCost."""
+
+    @staticmethod
+    def doflist(key):
+        return (1,), (key[1],), (key[2],)
+
+    @staticmethod
+    def construct(model, nod, cls, field, cost, derivative=0, costargs=()):
+        if cls not in ("X", "U"):
+            raise MuscadeError("'class' must be :X or :U")
+        data = _cost_batch(nod, cost)
+        data["costargs"] = [tuple(costargs)]
+        return data, ("SingleDofCost", cls, field, int(derivative), _cost_name(cost))
+
+
+class SingleUdof:
+    """SingleUdof: a U-dof applied as a load on the X-dof of the same node,
+    L = cost(u, t) − λu (BasicElements.jl:239-248)."""
+
+    @staticmethod
+    def doflist(key):
+        return (1, 1), ("X", "U"), (key[1], key[2])
+
+    @staticmethod
+    def construct(model, nod, Xfield, Ufield, cost, costargs=()):
+        data = _cost_batch(nod, cost)
+        data["costargs"] = [tuple(costargs)]
+        return data, ("SingleUdof", Xfield, Ufield, _cost_name(cost))
+
+
+class SingleAcost:
+    """SingleAcost: a once-off cost(a) on one A-dof (BasicElements.jl:163-167)."""
+
+    @staticmethod
+    def doflist(key):
+        return (1,), ("A",), (key[1],)
+
+    @staticmethod
+    def construct(model, nod, field, cost, costargs=()):
+        data = _cost_batch(nod, cost)
+        data["costargs"] = [tuple(costargs)]
+        return data, ("SingleAcost", field, _cost_name(cost))
+
+
+def quadratic_costs(group):
+    """The QuadraticCost of every element of a cost group (batch costs repeated
+    over their elements); raises if a batch has another cost functor."""
+    out = []
+    for nodes, d in zip(group.nodes, group.data):
+        cost = d["cost"][0]
+        if not isinstance(cost, QuadraticCost) or d.get("costargs", [()])[0]:
+            raise MuscadeError(f"{group.key[0]}: the GPU path evaluates QuadraticCost costs without costargs, "
+                               f"got {type(cost).__name__}")
+        out += [cost] * nodes.shape[0]
+    return out
+
+
+def group_cost_targets(group, t):
+    """The cost target y(t) of every element of a SingleDofCost or SingleUdof group."""
+    counts = [nodes.shape[0] for nodes in group.nodes]
+    vals = np.fromiter((d["cost"][0].target_at(t) for d in group.data), dtype=np.float64, count=len(counts))
+    return np.repeat(vals, counts)
 
 
 def group_time_values(group, name, t):

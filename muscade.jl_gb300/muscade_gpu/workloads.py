@@ -19,7 +19,8 @@ import math
 
 import numpy as np
 
-from .elements import BeamCrossSection, DofConstraint, DofLoad, EulerBeam3D, Hold
+from .elements import (BeamCrossSection, DofConstraint, DofLoad, EulerBeam3D, Hold, QuadraticCost, SingleAcost,
+                       SingleDofCost)
 from .model import Model
 
 EA0, EI0, GJ0, MU0, IOTA0 = 1e8, 1e4, 1e4, 10.0, 1.0
@@ -219,7 +220,8 @@ def node_dofs(model, nodes):
 
 # ---------------------------------------------------------------- identification
 def adjoint_beam(nel=5000, nstep=500, dt=0.01, seed=2029, ele_len=0.1, EA=1e10, EI=1e8, GJ=1e8, mu=1e3, iota1=10.0,
-                 load_std=1e3, corr_x=10.0, corr_t=0.2, nfeat=64, sigma_A=0.2, sensor_frac=0.05):
+                 load_std=1e3, corr_x=10.0, corr_t=0.2, nfeat=64, sigma_A=0.2, sensor_frac=0.05, measurements=None,
+                 a_weight=0.0):
     """Simply supported beam for load and stiffness identification: nel
     EulerBeam3D{adof} of ele_len along x, one EI-scale A-dof per element (on its
     own parameter node), Hold t1, t2, t3 at both ends and r1 at the first node,
@@ -227,7 +229,12 @@ def adjoint_beam(nel=5000, nstep=500, dt=0.01, seed=2029, ele_len=0.1, EA=1e10, 
     in space (correlation length corr_x) and time (corr_t), drawn with nfeat
     random Fourier features.  Returns a dict with the model, the time grid,
     the load table, the true A (lognormal, sigma_A) and the sensor dofs
-    (a random sensor_frac of the free translational dofs, 1-based)."""
+    (a random sensor_frac of the free translational dofs, 1-based).
+
+    With measurements = (y, sd) (y[nstep][nsensor], as synthetic_measurements
+    returns), the model also carries the identification cost as elements: a
+    SingleDofCost per sensor with QuadraticCost(1/sd², yₛ(t)) and, when
+    a_weight > 0, a SingleAcost QuadraticCost(a_weight, 1) on every A-dof."""
     rng = np.random.Generator(np.random.PCG64(seed))
     m = Model("identification")
     xs = np.arange(nel + 1) * ele_len
@@ -262,7 +269,36 @@ def adjoint_beam(nel=5000, nstep=500, dt=0.01, seed=2029, ele_len=0.1, EA=1e10, 
     free = [cand[i, j] for i in range(len(nodes)) for j in range(3) if (int(nodes[i]), j) not in held]
     nsens = max(1, int(round(sensor_frac * len(free))))
     sensors = np.sort(rng.choice(np.asarray(free), nsens, replace=False)) + 1
-    return dict(model=m, times=times, loads=table, A_true=A_true, sensors=sensors, nodes=nodes, seed=seed)
+    if measurements is not None:
+        y, sd = measurements
+        identification_costs(m, sensors, y, sd, times, pnodes if a_weight > 0 else None, a_weight)
+    return dict(model=m, times=times, loads=table, A_true=A_true, sensors=sensors, nodes=nodes, pnodes=pnodes,
+                seed=seed)
+
+
+class _Record:
+    """y(t) of one sensor from its record on the time grid (zero off the grid)."""
+
+    def __init__(self, times, values):
+        self.index = {round(float(t), 12): k for k, t in enumerate(times)}
+        self.values = np.asarray(values, dtype=np.float64)
+
+    def __call__(self, t):
+        k = self.index.get(round(float(t), 12))
+        return 0.0 if k is None else float(self.values[k])
+
+
+def identification_costs(model, sensors, y, sd, times, anodes=None, a_weight=0.0):
+    """Adds a SingleDofCost QuadraticCost(1/sd², yₛ(t)) on each sensor dof
+    (1-based X-dofs, records y[nstep][nsensor]) and, with anodes, a SingleAcost
+    QuadraticCost(a_weight, 1) on the EIscale A-dof of each of those nodes."""
+    for s, dof in enumerate(np.asarray(sensors)):
+        node = int(model.dof_node["X"][dof - 1])
+        field = model.doftyp[model.dof_typ["X"][dof - 1]].field
+        model.addelement(SingleDofCost, [node], cls="X", field=field,
+                         cost=QuadraticCost(1.0 / sd**2, _Record(times, y[:, s])))
+    if anodes is not None:
+        model.addelement(SingleAcost, np.asarray(anodes)[:, None], field="EIscale", cost=QuadraticCost(a_weight, 1.0))
 
 
 def synthetic_measurements(states, sensors, noise=0.01, seed=2031):

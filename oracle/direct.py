@@ -242,6 +242,12 @@ class SingleAcost:
         return p["cost"](A[0])
 
 
+# the cost elements restated here, by element kind: a model built with the
+# package's own SingleDofCost / SingleUdof / SingleAcost (same keys and data)
+# is evaluated by these restatements, not by the package's classes
+COST_ELEMENTS = {"SingleDofCost": SingleDofCost, "SingleUdof": SingleUdof, "SingleAcost": SingleAcost}
+
+
 def _params(g):
     """Per-element parameter dicts of a group (the fields of its batches in order)."""
     out = []
@@ -297,6 +303,8 @@ def element_lagrangian(g, key, p, Lam, Xe, Ue, Ae, t, lay):
         for i in range(nx):
             gap = gap + c[i] * X[0][i]
         R = [-c[i] * X[0][nx] for i in range(nx)] + [-gap]
+    elif kind in COST_ELEMENTS:
+        return COST_ELEMENTS[kind].lagrangian(p, key, L, X, U, A, t)
     elif hasattr(g.etype, "residual"):
         R = g.etype.residual(p, X, U, A, t)
     else:
@@ -372,7 +380,7 @@ def assemble_A(model, dis, A):
         for e, p in enumerate(_params(g)):
             na = ia.shape[1]
             a = [D2.var(A[ia[e, j]], j, na) for j in range(na)]
-            c = g.etype.acost(p, a)
+            c = SingleAcost.acost(p, a)
             np.add.at(g1, ia[e], c.g)
             np.add.at(h1, (ia[e][:, None], ia[e][None, :]), c.h)
     return g1, h1

@@ -119,6 +119,10 @@ def eval_group(model, g, dis_g, X, U, t, mode, c, scaleX=None, A=None):
         Jm[:, nx, :nx] = -coeffs * sX[:, :nx]
     elif kind == "DofLoad":
         R[:, 0] = -group_time_values(g, "value", t)
+    elif kind == "SingleDofCost":
+        pass  # R = ∂L/∂Λ = 0 (getresidual of a Lagrangian element, src/Assemble.jl:661-677)
+    elif kind == "SingleUdof":
+        R[:, 0] = -U[0][dis_g.index_U[:, 0] - 1]  # L = cost(u,t) − λu  ⇒  R = −u
     elif hasattr(g.etype, "oracle_residual"):
         return g.etype.oracle_residual(g, dis_g, X, U, t, mode, c, sX)
     else:
@@ -147,8 +151,8 @@ def assemble(prep, X, U, t, mission, c, A=None):
     nz = np.zeros(prep.nnz)
     mode = {"static": 1, "step": 2, "iter": 3}[mission]
     for g, dg, a1, a2 in zip(model.groups, dis.dis, prep.asm1, prep.asm2):
-        if g.nele == 0:
-            continue
+        if g.nele == 0 or dg.index_X.shape[1] == 0:
+            continue  # no X-dofs (SingleAcost): nothing in SweepX's Lλ, Lλx
         R, J = eval_group(model, g, dg, X, U, t, mode, c, A=A)
         nele, nX = R.shape
         # add_value!(Lλ), add_∂!{1,:minus}(Lλ, ..., (Nx+1,)) for the Newmark step,
@@ -224,3 +228,46 @@ def sweepx(model, dis, initialstate, time, OX=0, beta=0.25, gamma=0.5, maxiter=5
             if it == maxiter:
                 raise NoConvergence(f"no convergence of step {step:3d} after {it:3d} iterations")
     return out
+
+
+def sweep_cost(model, dis, traj, t0, OX, U, A):
+    """The cost of a SweepX trajectory as the device adjoint defines it: the
+    cost elements' Lagrangians summed over the steps, weighted by Δtₙ (OX = 2)
+    or 1 (OX = 0), plus the once-off A-costs.  Each element's cost functor is
+    called as the reference calls it: cost(x⁽ᵈ⁾, t) for SingleDofCost
+    (src/BasicElements.jl:198-208), cost(u, t) for SingleUdof (:239-248; the
+    −λu term is not a cost), cost(a) for SingleAcost (:163-167).
+    traj: list of (t, X tuple) as returned by sweepx."""
+    C = 0.0
+    tprev = t0
+    for t, X in traj:
+        w = (t - tprev) if OX == 2 else 1.0
+        tprev = t
+        c = 0.0
+        for g, dg in zip(model.groups, dis.dis):
+            kind = g.key[0]
+            if kind not in ("SingleDofCost", "SingleUdof"):
+                continue
+            e0 = 0
+            for nodes, d in zip(g.nodes, g.data):
+                cost = d["cost"][0]
+                args = d.get("costargs", [()])[0]
+                for e in range(e0, e0 + nodes.shape[0]):
+                    if kind == "SingleDofCost":
+                        v = X[g.key[3]][dg.index_X[e, 0] - 1]
+                    else:
+                        v = U[0][dg.index_U[e, 0] - 1]
+                    c += cost(v, t, *args)
+                e0 += nodes.shape[0]
+        C += w * c
+    for g, dg in zip(model.groups, dis.dis):
+        if g.key[0] != "SingleAcost":
+            continue
+        e0 = 0
+        for nodes, d in zip(g.nodes, g.data):
+            cost = d["cost"][0]
+            args = d.get("costargs", [()])[0]
+            for e in range(e0, e0 + nodes.shape[0]):
+                C += cost(A[dg.index_A[e, 0] - 1], *args)
+            e0 += nodes.shape[0]
+    return C

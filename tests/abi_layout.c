@@ -42,6 +42,7 @@ int main(void) {
   C(MGPU_OK), C(MGPU_ERR_ARG), C(MGPU_ERR_CUDA), C(MGPU_ERR_UNSUPPORTED), C(MGPU_ERR_NAN), C(MGPU_ERR_SINGULAR);
   C(MGPU_ERR_NOCONV), C(MGPU_ERR_NOMEM), C(MGPU_ERR_SIZE);
   C(MGPU_EULERBEAM3D), C(MGPU_BAR3D), C(MGPU_DOFCONSTRAINT_X), C(MGPU_DOFLOAD);
+  C(MGPU_DOFCOST), C(MGPU_SINGLEUDOF), C(MGPU_ACOST);
   C(MGPU_ASM_STATIC), C(MGPU_ASM_STEP), C(MGPU_ASM_ITER);
   C(MGPU_LINSOLVE_AUTO), C(MGPU_LINSOLVE_F32IR), C(MGPU_LINSOLVE_F64), C(MGPU_LINSOLVE_BLOCK);
   C(MGPU_LINSOLVE_TORN), C(MGPU_LINSOLVE_TORN32), C(MGPU_LINSOLVE_SPARSE), C(MGPU_LINSOLVE_SPARSE64);

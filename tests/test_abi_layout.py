@@ -59,6 +59,7 @@ def test_constants_match(layout):
         assert c["MGPU_ERR_" + name] == code
     assert (c["MGPU_EULERBEAM3D"], c["MGPU_BAR3D"], c["MGPU_DOFCONSTRAINT_X"], c["MGPU_DOFLOAD"]) == \
         (L.EULERBEAM3D, L.BAR3D, L.DOFCONSTRAINT_X, L.DOFLOAD)
+    assert (c["MGPU_DOFCOST"], c["MGPU_SINGLEUDOF"], c["MGPU_ACOST"]) == (L.DOFCOST, L.SINGLEUDOF, L.ACOST)
     assert (c["MGPU_ASM_STATIC"], c["MGPU_ASM_STEP"], c["MGPU_ASM_ITER"]) == (L.ASM_STATIC, L.ASM_STEP, L.ASM_ITER)
     for kind, v in L.LINSOLVE.items():
         assert c["MGPU_LINSOLVE_" + kind.upper()] == v
