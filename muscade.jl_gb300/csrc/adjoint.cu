@@ -268,9 +268,10 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
   std::vector<int32_t> aele;
   std::vector<int64_t> abase;  // per group: offset of its beams in contrib (-1 if none)
   int64_t nbA = 0;
-  for (auto& G : c->groups) {
-    abase.push_back(G.aidx ? nbA : -1);
-    if (G.aidx) nbA += G.nele;
+  for (auto& G : c->groups) {  // the EI-scaled beams (an Acost's A-dof enters through adj_acost)
+    const bool eib = G.kind == MGPU_EULERBEAM3D && G.aidx;
+    abase.push_back(eib ? nbA : -1);
+    if (eib) nbA += G.nele;
   }
   {
     std::vector<std::vector<int32_t>> lists(c->nA);
