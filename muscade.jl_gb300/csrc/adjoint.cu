@@ -382,7 +382,9 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
   }
   {
     std::vector<double> hc(nstep * ncs, 0.0);
-    ADJ_CUDA(cudaMemcpy(hc.data(), costs, nstep * ncs * sizeof(double), cudaMemcpyDeviceToHost));
+    // the context stream does not synchronise with the legacy stream: copy on it and wait
+    ADJ_CUDA(cudaMemcpyAsync(hc.data(), costs, nstep * ncs * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ADJ_CUDA(cudaStreamSynchronize(st));
     double C = 0.0;
     for (int64_t k = 0; k < nstep; ++k) {
       double ck_ = 0.0;
@@ -494,6 +496,7 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
       ADJ_CUDA(cudaStreamSynchronize(st));
       *cost += ha;
     }
+  ADJ_CUDA(cudaStreamSynchronize(st));
   if (c->nA > 0) ADJ_CUDA(cudaMemcpy(dCdA, gradA, c->nA * sizeof(double), cudaMemcpyDeviceToHost));
   if (dCdU && c->nU > 0) ADJ_CUDA(cudaMemcpy(dCdU, ub, c->nU * sizeof(double), cudaMemcpyDeviceToHost));
   if (dtv) ADJ_CUDA(cudaMemcpy(dCdtv, dtv, size_t(nstep) * c->ntval * sizeof(double), cudaMemcpyDeviceToHost));

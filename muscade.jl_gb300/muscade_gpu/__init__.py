@@ -8,6 +8,7 @@ implementation of the device path; calls fail if the library is not built.
 from .model import Model, State, Disassembler, MuscadeError  # noqa: F401
 from .elements import (  # noqa: F401
     EulerBeam3D, Bar3D, Hold, DofConstraint, DofLoad, BeamCrossSection, AxisymmetricBarCrossSection,
+    SingleDofCost, SingleUdof, SingleAcost, QuadraticCost,
 )
 from .solve import solve, SweepXGPU  # noqa: F401
 
