@@ -437,6 +437,7 @@ def bench_lattice_solve(args, rank, local_rank, ws, dist):
     if dist:
         dist.barrier()
     nrep = max(1, min(args.steps, 3))
+    nl0 = dm.launch_count()
     with Clocks(local_rank) as ck:
         t0 = time.perf_counter()
         for _ in range(nrep):
@@ -444,6 +445,7 @@ def bench_lattice_solve(args, rank, local_rank, ws, dist):
             if rc != 0:
                 raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
         dt = (time.perf_counter() - t0) / nrep
+    launches = (dm.launch_count() - nl0) // nrep
     clocks = ck.summary()
     dt = reduce_max(dist, dt)
     sp = dm.sparse_info()
@@ -480,7 +482,7 @@ def bench_lattice_solve(args, rank, local_rank, ws, dist):
                                        f"{cpu['newton_iterations']} iterations, nested-dual assembly + SuperLU); "
                                        "the full lattice is out of the CPU's reach"},
             "parity": cpu["parity"], "create_s": t_create, "clocks": clocks,
-            "gpu_launches": None}
+            "gpu_launches": launches}
     print(json.dumps(line), flush=True)
 
 

@@ -119,6 +119,11 @@ int mgpu_get_asm(const mgpu_ctx *ctx, int32_t igroup, int64_t *asm1, int64_t *as
  * target y(t)), concatenated over groups in model order. */
 int64_t mgpu_ntval(const mgpu_ctx *ctx);
 
+/* Kernel launches enqueued so far by the context's assembly, Newton and
+ * multifrontal paths (the banded solvers' kernels are not counted); the
+ * difference over a region counts the launches inside it. */
+int64_t mgpu_launch_count(const mgpu_ctx *ctx);
+
 /* One assembly with host buffers (replaces assemble!{:step|:iter} over the
  * AssemblySweepX elements, src/Assemble.jl:470-505 with addin!, src/SweepX.jl:39-96).
  *   x[nXder][nX] (X, X', X''), u[nU], tvals[ntval] at time t.
@@ -379,6 +384,13 @@ int mgpu_host_unregister(void *ptr);
  * of `device` in TFLOP/s, from independent DFMA chains timed with CUDA events;
  * the roofline denominator of the FP64-bound element kernels. */
 int mgpu_measure_fp64_peak(int32_t device, double *tflops);
+
+/* Tensor-core check (no counterpart in the reference): C[M×N] −= A[M×K]·B[K×N]
+ * for column-major FP32 host arrays, K ≤ 64, through the tile routine of the
+ * multifrontal solver's FP32 trailing update (tcgen05 kind::tf32 MMAs, each
+ * operand split into a TF32 part and an FP32 remainder, three products per
+ * k-step, FP32 accumulation in tensor memory). */
+int mgpu_tc_gemm_check(int32_t device, int32_t M, int32_t N, int32_t K, const float *A, const float *B, float *C);
 
 #ifdef __cplusplus
 }

@@ -357,7 +357,10 @@ int upload_stepc(mgpu_ctx* c, double t, const mgpu_newmark* nm) {
   return MGPU_OK;
 }
 
-void launch_reset_errflag(mgpu_ctx* c) { set_int_kernel<<<1, 1, 0, c->stream>>>(c->errflag, INT_MAX); }
+void launch_reset_errflag(mgpu_ctx* c) {
+  set_int_kernel<<<1, 1, 0, c->stream>>>(c->errflag, INT_MAX);
+  ++c->launches;
+}
 
 int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0) {
   const int64_t nX = c->nX;
@@ -376,8 +379,10 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0)
   const bool dyn = mission != MGPU_ASM_STATIC;
   a.p0 = p0;
   if (dyn && c->nXder_resident != 3) return set_err(c, MGPU_ERR_ARG, "Newmark assembly needs X, X' and X''");
-  if (mission == MGPU_ASM_STEP && nX > 0)
+  if (mission == MGPU_ASM_STEP && nX > 0) {
     newmark_ab_kernel<<<nblk(nX, 256), 256, 0, c->stream>>>(nX, a.x1, a.x2, c->stepc, c->ab, c->ab + nX);
+    ++c->launches;
+  }
   int64_t gid0 = 0;
   for (size_t g = 0; g < c->groups.size(); ++g) {
     const DevGroup& G = c->groups[g];
@@ -417,14 +422,19 @@ int launch_assembly(mgpu_ctx* c, int mission, cudaEvent_t* ev_groups, double p0)
       case MGPU_ACOST:  // no X-dofs: nothing in SweepX's Lλ and Lλx
         break;
     }
+    if (G.kind != MGPU_ACOST) ++c->launches;
     gid0 += G.nele;
     if (ev_groups) cudaEventRecord(ev_groups[g], c->stream);
   }
-  if (c->pat.nnz > 0)
+  if (c->pat.nnz > 0) {
     scatter_kernel<<<nblk(c->pat.nnz, kGatherOut), kGatherThreads, 0, c->stream>>>(c->pat.nnz, c->mseg, c->msrc,
                                                                                   c->kbuf, c->nzval);
-  if (nX > 0)
+    ++c->launches;
+  }
+  if (nX > 0) {
     scatter_kernel<<<nblk(nX, kGatherOut), kGatherThreads, 0, c->stream>>>(nX, c->vseg, c->vsrc, c->rbuf, c->Ll);
+    ++c->launches;
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(c, MGPU_ERR_CUDA, std::string("assembly launch: ") + cudaGetErrorString(e));
   return MGPU_OK;
@@ -755,6 +765,7 @@ extern "C" int mgpu_set_A(mgpu_ctx* c, const double* A) {
 
 extern "C" int64_t mgpu_nnz(const mgpu_ctx* c) { return c ? c->pat.nnz : -1; }
 extern "C" int64_t mgpu_ntval(const mgpu_ctx* c) { return c ? c->ntval : -1; }
+extern "C" int64_t mgpu_launch_count(const mgpu_ctx* c) { return c ? c->launches : -1; }
 
 extern "C" int mgpu_get_pattern(const mgpu_ctx* cc, int64_t* colptr, int64_t* rowval) {
   if (!cc || !colptr || !rowval) return MGPU_ERR_ARG;

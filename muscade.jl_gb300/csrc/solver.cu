@@ -1266,6 +1266,7 @@ int factor_solve(mgpu_ctx* c, int* info) {
   }
   norms_partial<<<kNormBlocks, 256, 0, st>>>(c->nX, S.dx, c->Ll, S.part);
   norms_final<<<1, 32, 0, st>>>(kNormBlocks, S.part, S.red);
+  c->launches += 2;
   MG_CUDA(cudaGetLastError());
   return MGPU_OK;
 }
@@ -1328,6 +1329,7 @@ int newton_step(mgpu_ctx* c, int OX, int64_t step, double t, double dt, const do
     if (rc) return rc;
     decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, OX, first, S.dx, c->scale, c->stepc, c->x,
                                                   percomp ? S.frozen : nullptr, S.cod);
+    ++c->launches;
     if (percomp) {
       MG_CUDA(cudaMemsetAsync(S.nactive, 0, sizeof(int), st));
       comp_converge<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dx, c->Ll, cdx2, cLl2, S.frozen, S.nactive);

@@ -12,6 +12,7 @@
 
 #include "ctx.hpp"
 #include "sparse_analysis.hpp"
+#include "tc.cuh"
 
 namespace mgpu {
 namespace {
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(kThreads) sp_extend_add(const SpFrontDev* __re
 template <class T, int NB>
 __device__ void factor_diag(const T* A, int m, int k0, int kb, T (*Dg)[NB + 1], T tau, int* flags, bool count) {
   const int tid = threadIdx.x;
-  for (int t = tid; t < kb * kb; t += kThreads) {
+  for (int t = tid; t < kb * kb; t += int(blockDim.x)) {
     const int i = t % kb, j = t / kb;
     Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
   }
@@ -112,10 +113,10 @@ __device__ void factor_diag(const T* A, int m, int k0, int kb, T (*Dg)[NB + 1], 
     }
     __syncthreads();
     const T piv = Dg[k][k];
-    for (int i = k + 1 + tid; i < kb; i += kThreads) Dg[i][k] /= piv;
+    for (int i = k + 1 + tid; i < kb; i += int(blockDim.x)) Dg[i][k] /= piv;
     __syncthreads();
     const int r = kb - k - 1;
-    for (int t = tid; t < r * r; t += kThreads) {
+    for (int t = tid; t < r * r; t += int(blockDim.x)) {
       const int i = k + 1 + t % r, j = k + 1 + t / r;
       Dg[i][j] -= Dg[i][k] * Dg[k][j];
     }
@@ -252,6 +253,7 @@ __global__ void __launch_bounds__(kThreads) sp_update(const SpFrontDev* __restri
 // FP32 trailing update with 128 × 128 tiles (8 × 8 per thread, the L₂₁ and U₁₂
 // panels of the tile in dynamic shared memory); otherwise as sp_update
 constexpr int kTile32 = 128;
+constexpr int kTcMinRest = 512;  // trailing blocks this large take the tensor-core update
 constexpr int kPad32 = 4;
 template <int NB>
 __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __restrict__ fr,
@@ -318,6 +320,54 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
       if (i < m) col[i] -= acc[u][v];
     }
   }
+}
+
+// FP32 trailing update on the tensor cores: one 128 × 128 tile per block
+// (tc::tile_update_tf32x3, three TF32 products per k-step, FP32 accumulators in
+// tensor memory); the block after the last tile writes the factored diagonal
+// block.  flags[3] |= 2 when a tile's MMAs did not complete within the wait.
+template <int NB>
+__global__ void __launch_bounds__(tc::kTcThreads) sp_update_tc(const SpFrontDev* __restrict__ fr,
+                                                                const int32_t* __restrict__ flist, int k0,
+                                                                float* __restrict__ F, float tau,
+                                                                int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p) return;
+  const int kb = min(NB, p - k0), r0 = k0 + kb, rest = m - r0;
+  const int nt = (rest + tc::kTcTile - 1) / tc::kTcTile;
+  if (int(blockIdx.x) > nt * nt) return;
+  float* A = F + Fr.off;
+  extern __shared__ __align__(128) float smem_tc[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  if (int(blockIdx.x) == nt * nt) {
+    float(*Dg)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(smem_tc);
+    factor_diag<float, NB>(A, m, k0, kb, Dg, tau, flags, true);
+    for (int t = threadIdx.x; t < kb * kb; t += blockDim.x) {
+      const int i = t % kb, j = t / kb;
+      A[(k0 + i) + int64_t(k0 + j) * m] = Dg[i][j];
+    }
+    return;
+  }
+  const int i0 = r0 + (blockIdx.x % nt) * tc::kTcTile, j0 = r0 + (blockIdx.x / nt) * tc::kTcTile;
+  const bool ok = tc::tile_update_tf32x3(A + int64_t(k0) * m, m, A + k0, m, A, m, i0, j0, m, m, kb, smem_tc, &bar,
+                                         &tslot);
+  if (!ok && threadIdx.x == 0) atomicOr(flags + 3, 2);
+}
+
+// C −= A B for host arrays through the same tile routine (column-major, K ≤ 64):
+// the tensor-core path's check against a host product
+__global__ void __launch_bounds__(tc::kTcThreads) tc_gemm_check(const float* __restrict__ A, int lda,
+                                                                 const float* __restrict__ B, int ldb,
+                                                                 float* __restrict__ C, int ldc, int M, int N, int K,
+                                                                 int* __restrict__ err) {
+  extern __shared__ __align__(128) float smem_tc[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  const bool ok = tc::tile_update_tf32x3(A, lda, B, ldb, C, ldc, blockIdx.x * tc::kTcTile, blockIdx.y * tc::kTcTile,
+                                         M, N, K, smem_tc, &bar, &tslot);
+  if (!ok && threadIdx.x == 0) atomicOr(err, 1);
 }
 
 // ---------------------------------------------------------------- substitutions (FP64 vectors)
@@ -484,6 +534,261 @@ __global__ void __launch_bounds__(kTriThreads) sp_bwd_tri(const SpFrontDev* __re
   for (int t = tid; t < p; t += kTriThreads) w[Fr.pos0 + t] = v[t];
 }
 
+// ---------------------------------------------------------------- blocked substitutions
+// The kernels above give a front one block for its triangle, which leaves the
+// GPU idle on the few large fronts near the root (the top separator of a
+// 60×60×20 lattice has 7,560 pivots: one block would stream its 114 MB
+// triangle alone).  Fronts with at least kBigPivots pivots take these kernels
+// instead.  The front's vector lives in global memory (V, at the front's
+// index-list offset, m entries).  Its rows are cut into tiles of kSB: pivot
+// tiles from row 0, update tiles from row p.  One launch per column block:
+// every block owning a row tile still to be reduced subtracts that column
+// block's products (columns summed 16 at a time in the factors' precision, the
+// four partial sums added in FP64 in a fixed order), and the block owning the
+// next diagonal tile then solves its triangle from shared memory, so the
+// following launch finds that column block solved.
+constexpr int kSB = 64;
+constexpr int kSBThreads = 256;
+constexpr int kBigPivots = 128;  // default threshold (MGPU_SPARSE_BLOCKED_PIVOTS overrides it)
+
+__device__ __forceinline__ int sb_np(int p) { return (p + kSB - 1) / kSB; }
+__device__ __forceinline__ int sb_nu(int m, int p) { return (m - p + kSB - 1) / kSB; }
+// rows [r0, r1) of row tile t
+__device__ __forceinline__ void sb_rows(int t, int m, int p, int& r0, int& r1) {
+  const int np = sb_np(p);
+  if (t < np) {
+    r0 = t * kSB;
+    r1 = min(r0 + kSB, p);
+  } else {
+    r0 = p + (t - np) * kSB;
+    r1 = min(r0 + kSB, m);
+  }
+}
+
+// v[r0..r1) -= A[r0..r1, c0..c0+cb) · x (x in shared memory); the block's 256
+// threads: row rr = tid % 64, columns 16·(tid / 64) ..; returns the new value of
+// row r0 + tid for tid < 64 (FP64), written back to V as well
+template <class T>
+__device__ __forceinline__ double sb_update(const T* __restrict__ A, int m, int r0, int r1, int c0, int cb,
+                                            const T* xs, double (*part)[kSB], double* __restrict__ Vf) {
+  const int tid = threadIdx.x, rr = tid & (kSB - 1), cq = tid >> 6;
+  const int r = r0 + rr;
+  T sacc = T(0);
+  if (r < r1) {
+    const T* col = A + r + int64_t(c0) * m;
+    const int cbeg = cq * 16;
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      if (cbeg + c < cb) sacc = fma(col[int64_t(cbeg + c) * m], xs[cbeg + c], sacc);
+  }
+  part[cq][rr] = double(sacc);
+  __syncthreads();
+  double v = 0.0;
+  if (tid < kSB && r0 + tid < r1) {
+    v = Vf[r0 + tid] - (((part[0][tid] + part[1][tid]) + part[2][tid]) + part[3][tid]);
+    Vf[r0 + tid] = v;
+  }
+  return v;
+}
+
+// unit lower triangle of the diagonal tile rows [r0, r0+nr): v = L⁻¹ v, in place
+// (vals: the tile's current values, threads 0..63); the block's threads stage
+// the tile, warp 0 solves (lane l holds rows l and l + 32)
+template <class T>
+__device__ void sb_tri_lower(const T* __restrict__ A, int m, int r0, int nr, T (*Dg)[kSB + 1], T* vs,
+                             double* __restrict__ Vf) {
+  const int tid = threadIdx.x;
+  for (int q = tid; q < kSB * kSB; q += kSBThreads) {
+    const int i = q & (kSB - 1), c = q >> 6;
+    Dg[i][c] = (i < nr && c < nr && c < i) ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
+  }
+  __syncthreads();
+  if (tid < 32) {
+    T a0 = vs[tid], a1 = vs[tid + 32];
+    for (int c = 0; c < nr; ++c) {
+      const T yc = __shfl_sync(0xffffffffu, c < 32 ? a0 : a1, c & 31);
+      a0 = fma(-Dg[tid][c], yc, a0);
+      a1 = fma(-Dg[tid + 32][c], yc, a1);
+    }
+    if (tid < nr) Vf[r0 + tid] = double(a0);
+    if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+  }
+}
+
+// upper triangle of the diagonal tile: x = U⁻¹ v, in place
+template <class T>
+__device__ void sb_tri_upper(const T* __restrict__ A, int m, int r0, int nr, T (*Dg)[kSB + 1], T* vs,
+                             double* __restrict__ Vf) {
+  const int tid = threadIdx.x;
+  for (int q = tid; q < kSB * kSB; q += kSBThreads) {
+    const int i = q & (kSB - 1), c = q >> 6;
+    Dg[i][c] = (i < nr && c < nr && c >= i) ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
+  }
+  __syncthreads();
+  if (tid < 32) {
+    T a0 = vs[tid], a1 = vs[tid + 32];
+    for (int c = nr - 1; c >= 0; --c) {
+      const bool lo = c < 32;
+      T xc = (lo ? a0 : a1) / Dg[c][c];
+      xc = __shfl_sync(0xffffffffu, xc, c & 31);
+      if (tid == c) a0 = xc;
+      else if (tid < c) a0 = fma(-Dg[tid][c], xc, a0);
+      if (tid + 32 == c) a1 = xc;
+      else if (tid + 32 < c) a1 = fma(-Dg[tid + 32][c], xc, a1);
+    }
+    if (tid < nr) Vf[r0 + tid] = double(a0);
+    if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+  }
+}
+
+// forward: V = the front's pivot entries, zero update rows
+__global__ void sp_fwdb_init(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
+                             const double* __restrict__ w, double* __restrict__ V, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t < Fr.m) V[Fr.idx + t] = t < Fr.p ? w[Fr.pos0 + t] : 0.0;
+}
+
+// forward: add child number r's update vector (the children in rank order)
+__global__ void sp_fwdb_ext(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
+                            const int32_t* __restrict__ clist, const int32_t* __restrict__ emap, int r,
+                            const double* __restrict__ cvec, double* __restrict__ V, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  if (r >= Fr.nc) return;
+  const SpFrontDev C = fr[clist[Fr.c0 + r]];
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t < C.m - C.p) V[Fr.idx + emap[C.eoff + t]] += cvec[C.eoff + t];
+}
+
+// forward: the triangle of pivot tile 0
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_fwdb_first(const SpFrontDev* __restrict__ fr,
+                                                            const int32_t* __restrict__ flist,
+                                                            const T* __restrict__ F, double* __restrict__ V,
+                                                            const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.x]];
+  __shared__ T Dg[kSB][kSB + 1];
+  __shared__ T vs[kSB];
+  double* Vf = V + Fr.idx;
+  const int nr = min(kSB, Fr.p);
+  if (threadIdx.x < kSB) vs[threadIdx.x] = threadIdx.x < nr ? T(Vf[threadIdx.x]) : T(0);
+  sb_tri_lower<T>(F + Fr.off, Fr.m, 0, nr, Dg, vs, Vf);
+}
+
+// forward, column block j (solved): the row tiles after it take its products;
+// the block of tile j + 1 (a pivot tile) then solves that tile
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_fwdb_step(const SpFrontDev* __restrict__ fr,
+                                                           const int32_t* __restrict__ flist, int j,
+                                                           const T* __restrict__ F, double* __restrict__ V,
+                                                           const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p, np = sb_np(p), nt = np + sb_nu(m, p);
+  const int t = j + 1 + int(blockIdx.x);
+  if (j >= np || t >= nt) return;
+  __shared__ T xs[kSB];
+  __shared__ double part[4][kSB];
+  __shared__ T Dg[kSB][kSB + 1];
+  __shared__ T vs[kSB];
+  const int c0 = j * kSB, cb = min(kSB, p - c0);
+  double* Vf = V + Fr.idx;
+  const T* A = F + Fr.off;
+  if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(Vf[c0 + threadIdx.x]) : T(0);
+  __syncthreads();
+  int r0, r1;
+  sb_rows(t, m, p, r0, r1);
+  const double v = sb_update<T>(A, m, r0, r1, c0, cb, xs, part, Vf);
+  if (t != j + 1 || t >= np) return;
+  if (threadIdx.x < kSB) vs[threadIdx.x] = T(v);
+  sb_tri_lower<T>(A, m, r0, r1 - r0, Dg, vs, Vf);
+}
+
+// forward: y to w, the update rows to the parent's extend-add vector
+__global__ void sp_fwdb_fin(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
+                            const double* __restrict__ V, double* __restrict__ w, double* __restrict__ cvec,
+                            const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= Fr.m) return;
+  if (t < Fr.p)
+    w[Fr.pos0 + t] = V[Fr.idx + t];
+  else if (Fr.parent >= 0)
+    cvec[Fr.eoff + (t - Fr.p)] = V[Fr.idx + t];
+}
+
+// backward: V = y of the pivots; a front without update rows solves its last
+// pivot tile here (the others when their last update block is done)
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_bwdb_init(const SpFrontDev* __restrict__ fr,
+                                                           const int32_t* __restrict__ flist,
+                                                           const T* __restrict__ F, const double* __restrict__ w,
+                                                           double* __restrict__ V, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.x]];
+  double* Vf = V + Fr.idx;
+  for (int t = threadIdx.x; t < Fr.p; t += kSBThreads) Vf[t] = w[Fr.pos0 + t];
+  if (Fr.m > Fr.p) return;
+  __shared__ T Dg[kSB][kSB + 1];
+  __shared__ T vs[kSB];
+  const int r0 = (sb_np(Fr.p) - 1) * kSB, nr = Fr.p - r0;
+  if (threadIdx.x < kSB) vs[threadIdx.x] = threadIdx.x < nr ? T(w[Fr.pos0 + r0 + threadIdx.x]) : T(0);
+  __syncthreads();
+  sb_tri_upper<T>(F + Fr.off, Fr.m, r0, nr, Dg, vs, Vf);
+}
+
+// backward, step s: column block b = (blocks of the front) − 1 − s, descending
+// over the update blocks (x from the ancestors' solution in w) and then the
+// pivot blocks (x solved in V); the pivot tiles above it take its products and
+// the block of tile b − 1 then solves that tile
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_bwdb_step(const SpFrontDev* __restrict__ fr,
+                                                           const int32_t* __restrict__ flist, int s,
+                                                           const int32_t* __restrict__ fidx,
+                                                           const T* __restrict__ F, const double* __restrict__ w,
+                                                           double* __restrict__ V, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p, np = sb_np(p), nb = np + sb_nu(m, p);
+  const int b = nb - 1 - s, t = int(blockIdx.x);
+  if (b < 1 || t >= min(b, np)) return;
+  __shared__ T xs[kSB];
+  __shared__ double part[4][kSB];
+  __shared__ T Dg[kSB][kSB + 1];
+  __shared__ T vs[kSB];
+  double* Vf = V + Fr.idx;
+  const T* A = F + Fr.off;
+  int c0, cb;
+  if (b >= np) {
+    c0 = p + (b - np) * kSB;
+    cb = min(kSB, m - c0);
+    if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(w[fidx[Fr.idx + c0 + threadIdx.x]]) : T(0);
+  } else {
+    c0 = b * kSB;
+    cb = min(kSB, p - c0);
+    if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(Vf[c0 + threadIdx.x]) : T(0);
+  }
+  __syncthreads();
+  const int r0 = t * kSB, r1 = min(r0 + kSB, p);
+  const double v = sb_update<T>(A, m, r0, r1, c0, cb, xs, part, Vf);
+  if (t != b - 1) return;
+  if (threadIdx.x < kSB) vs[threadIdx.x] = T(v);
+  sb_tri_upper<T>(A, m, r0, r1 - r0, Dg, vs, Vf);
+}
+
+// backward: x to w
+__global__ void sp_bwdb_fin(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
+                            const double* __restrict__ V, double* __restrict__ w, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t < Fr.p) w[Fr.pos0 + t] = V[Fr.idx + t];
+}
+
 // ---------------------------------------------------------------- refinement
 __global__ void sp_gather_scaled(int64_t n, const int32_t* __restrict__ perm, const double* __restrict__ D,
                                  const double* __restrict__ r, double* __restrict__ w, const int* __restrict__ conv) {
@@ -579,14 +884,17 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
     cudaError_t e = cudaMemsetAsync(F + sp.h_off0[h], 0, (sp.h_off1[h] - sp.h_off0[h]) * sizeof(T), st);
     if (e != cudaSuccess) return e;
     const int64_t na = sp.h_aq0[h + 1] - sp.h_aq0[h];
-    if (na > 0)
+    if (na > 0) {
       sp_assemble<T><<<nblocks(na, kThreads), kThreads, 0, st>>>(na, sp.d_aq + sp.h_aq0[h], sp.d_amap, sp.d_rowval,
                                                                  sp.d_acol, c->nzval, sp.D, F);
+      ++c->launches;
+    }
     for (size_t r = 0; r < sp.h_nea[h].size(); ++r) {
       const int cnt = sp.h_nea[h][r];
       for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
         const dim3 g(nblocks(sp.h_eumax[h][r], 16), unsigned(std::min(kMaxGridY, cnt - f0)));
         sp_extend_add<T><<<g, kThreads, 0, st>>>(sp.d_fr, sp.d_ea + sp.h_ea0[h][r] + f0, sp.d_emap, F);
+        ++c->launches;
       }
     }
     const auto& lp = sp.h_lfp[h];  // pivots of the height's fronts, descending
@@ -600,14 +908,24 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
       for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
         const int32_t* fl = sp.d_lf + sp.h_lf0[h] + f0;
         const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
-        if (nrc + ncc > 0)
+        if (nrc + ncc > 0) {
           sp_panel<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+          ++c->launches;
+        }
         if constexpr (std::is_same<T, float>::value) {
           const int nt32 = (rest + kTile32 - 1) / kTile32;
-          sp_update_f32<NB><<<dim3(unsigned(nt32 * nt32 + 1), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, k0, F,
-                                                                                                tau, sp.flags);
+          if (sp.tensor_cores && rest >= kTcMinRest) {
+            sp_update_tc<NB><<<dim3(unsigned(nt32 * nt32 + 1), gy), tc::kTcThreads, tc::kTcSmem, st>>>(
+                sp.d_fr, fl, k0, F, tau, sp.flags);
+            ++c->launches;
+          } else {
+            sp_update_f32<NB><<<dim3(unsigned(nt32 * nt32 + 1), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, k0, F,
+                                                                                                  tau, sp.flags);
+            ++c->launches;
+          }
         } else {
           sp_update<T, NB><<<dim3(unsigned(nt * nt + 1), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+          ++c->launches;
         }
       }
     }
@@ -615,43 +933,97 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
   return cudaGetLastError();
 }
 
-// refinement sweeps with the factors F: x = Lλx⁻¹ b
+// refinement sweeps with the factors F: x = Lλx⁻¹ b.  Per height, the fronts
+// with fewer than sp.big_pivots pivots (the tail of the height's list) take
+// the one-block-per-front kernels, the others the blocked ones.
 template <class T>
 cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int sweeps) {
   cudaStream_t st = c->stream;
   const int64_t n = sp.n;
-  const size_t smem = size_t(sp.max_m) * sizeof(double);
+  const size_t smem = size_t(std::max(sp.max_m_small, 1)) * sizeof(double);
   for (int it = 0; it < sweeps; ++it) {
     const double* r = b;
     if (it > 0) {
       sp_residual<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_rptr, sp.d_rq, sp.d_rcol, c->nzval, sp.xs, b,
                                                              sp.r, sp.flags);
+      ++c->launches;
       r = sp.r;
     }
     sp_gather_scaled<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_perm, sp.D, r, sp.w, sp.flags);
+    ++c->launches;
     for (int h = 0; h < sp.nheight; ++h) {
       if (!sp.h_nlf[h]) continue;
       const int32_t* fl = sp.d_lf + sp.h_lf0[h];
-      sp_fwd_tri<T><<<unsigned(sp.h_nlf[h]), kTriThreads, smem, st>>>(sp.d_fr, fl, sp.d_clist, sp.d_emap, F, sp.w,
-                                                                       sp.cvec, sp.flags);
-      const int ur = (sp.h_umax[h] + kGemvRows - 1) / kGemvRows;
-      for (int f0 = 0; f0 < sp.h_nlf[h] && ur > 0; f0 += kMaxGridY)
-        sp_fwd_gemv<T><<<dim3(unsigned(ur), unsigned(std::min(kMaxGridY, sp.h_nlf[h] - f0))), kGemvRows,
-                         size_t(sp.h_pmax[h]) * sizeof(double), st>>>(sp.d_fr, fl + f0, F, sp.w, sp.cvec, sp.flags);
+      const int nbig = sp.h_nbig[h], nsmall = sp.h_nlf[h] - nbig;
+      if (nsmall > 0) {
+        const int32_t* fs = fl + nbig;
+        sp_fwd_tri<T><<<unsigned(nsmall), kTriThreads, smem, st>>>(sp.d_fr, fs, sp.d_clist, sp.d_emap, F, sp.w,
+                                                                    sp.cvec, sp.flags);
+        ++c->launches;
+        const int ur = (sp.h_sumax[h] + kGemvRows - 1) / kGemvRows;
+        for (int f0 = 0; f0 < nsmall && ur > 0; f0 += kMaxGridY) {
+          sp_fwd_gemv<T><<<dim3(unsigned(ur), unsigned(std::min(kMaxGridY, nsmall - f0))), kGemvRows,
+                           size_t(sp.h_spmax[h]) * sizeof(double), st>>>(sp.d_fr, fs + f0, F, sp.w, sp.cvec, sp.flags);
+          ++c->launches;
+        }
+      }
+      if (nbig > 0) {
+        const unsigned gm = nblocks(sp.h_mmax[h], kThreads);
+        sp_fwdb_init<<<dim3(gm, unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.w, sp.V, sp.flags);
+        ++c->launches;
+        for (size_t rk = 0; rk < sp.h_nea[h].size(); ++rk) {
+          sp_fwdb_ext<<<dim3(nblocks(std::max(sp.h_eumax[h][rk], 1), kThreads), unsigned(nbig)), kThreads, 0, st>>>(
+              sp.d_fr, fl, sp.d_clist, sp.d_emap, int(rk), sp.cvec, sp.V, sp.flags);
+          ++c->launches;
+        }
+        sp_fwdb_first<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.V, sp.flags);
+        ++c->launches;
+        for (int j = 0; j < sp.h_bnp[h]; ++j) {
+          const int g = sp.h_bnt[h] - j - 1;
+          if (g > 0) {
+            sp_fwdb_step<T><<<dim3(unsigned(g), unsigned(nbig)), kSBThreads, 0, st>>>(sp.d_fr, fl, j, F, sp.V,
+                                                                                     sp.flags);
+            ++c->launches;
+          }
+        }
+        sp_fwdb_fin<<<dim3(gm, unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.V, sp.w, sp.cvec, sp.flags);
+        ++c->launches;
+      }
     }
     for (int h = sp.nheight - 1; h >= 0; --h) {
       if (!sp.h_nlf[h]) continue;
       const int32_t* fl = sp.d_lf + sp.h_lf0[h];
-      const int pr = (sp.h_pmax[h] + kGemvRows - 1) / kGemvRows;
-      for (int f0 = 0; f0 < sp.h_nlf[h]; f0 += kMaxGridY)
-        sp_bwd_gemv<T><<<dim3(unsigned(pr), unsigned(std::min(kMaxGridY, sp.h_nlf[h] - f0))), kGemvRows,
-                         size_t(std::max(sp.h_umax[h], 1)) * sizeof(double), st>>>(sp.d_fr, fl + f0, sp.d_fidx, F,
-                                                                                   sp.w, sp.tw, sp.flags);
-      sp_bwd_tri<T><<<unsigned(sp.h_nlf[h]), kTriThreads, smem, st>>>(sp.d_fr, fl, F, sp.w, sp.tw, sp.flags);
+      const int nbig = sp.h_nbig[h], nsmall = sp.h_nlf[h] - nbig;
+      if (nsmall > 0) {
+        const int32_t* fs = fl + nbig;
+        const int pr = (sp.h_spmax[h] + kGemvRows - 1) / kGemvRows;
+        for (int f0 = 0; f0 < nsmall; f0 += kMaxGridY) {
+          sp_bwd_gemv<T><<<dim3(unsigned(pr), unsigned(std::min(kMaxGridY, nsmall - f0))), kGemvRows,
+                           size_t(std::max(sp.h_sumax[h], 1)) * sizeof(double), st>>>(sp.d_fr, fs + f0, sp.d_fidx, F,
+                                                                                      sp.w, sp.tw, sp.flags);
+          ++c->launches;
+        }
+        sp_bwd_tri<T><<<unsigned(nsmall), kTriThreads, smem, st>>>(sp.d_fr, fs, F, sp.w, sp.tw, sp.flags);
+        ++c->launches;
+      }
+      if (nbig > 0) {
+        sp_bwdb_init<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.w, sp.V, sp.flags);
+        ++c->launches;
+        for (int s2 = 0; s2 + 1 < sp.h_bnt[h]; ++s2) {
+          sp_bwdb_step<T><<<dim3(unsigned(sp.h_bnp[h]), unsigned(nbig)), kSBThreads, 0, st>>>(
+              sp.d_fr, fl, s2, sp.d_fidx, F, sp.w, sp.V, sp.flags);
+          ++c->launches;
+        }
+        sp_bwdb_fin<<<dim3(nblocks(sp.h_pmax[h], kThreads), unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.V,
+                                                                                               sp.w, sp.flags);
+        ++c->launches;
+      }
     }
     sp_accumulate<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, it == 0, sp.d_perm, sp.D, sp.w, sp.yacc, sp.xs, sp.nrm,
                                                              sp.flags);
+    ++c->launches;
     sp_check<<<1, 1, 0, st>>>(sp.nrm, sp.prev, sp.flags, kRefineTol, kRefineStall);
+    ++c->launches;
   }
   return cudaGetLastError();
 }
@@ -683,9 +1055,14 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   SparseAnalysis A;
   sp.why = sparse_analyse(in, A);
   if (!sp.why.empty()) return MGPU_OK;
-  // the substitutions keep a front's vector in shared memory
-  if (int64_t(A.max_m) * 8 > 200 * 1024) {
-    sp.why = "front of " + std::to_string(A.max_m) + " dofs exceeds the substitution kernels' shared memory";
+  // the one-block substitutions keep a front's vector in shared memory (fronts
+  // with many pivots keep it in global memory)
+  sp.big_pivots = kBigPivots;
+  if (const char* ev = getenv("MGPU_SPARSE_BLOCKED_PIVOTS")) sp.big_pivots = std::max(1, atoi(ev));
+  for (const SparseFront& S : A.fronts)
+    if (S.p < sp.big_pivots) sp.max_m_small = std::max(sp.max_m_small, int(S.m));
+  if (int64_t(sp.max_m_small) * 8 > 200 * 1024) {
+    sp.why = "front of " + std::to_string(sp.max_m_small) + " dofs exceeds the substitution kernels' shared memory";
     return MGPU_OK;
   }
   sp.n = A.n;
@@ -723,6 +1100,11 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   sp.h_off0.assign(H, INT64_MAX);
   sp.h_off1.assign(H, 0);
   sp.h_lfp.resize(H);
+  sp.h_nbig.assign(H, 0);
+  sp.h_bnp.assign(H, 0);
+  sp.h_bnt.assign(H, 0);
+  sp.h_spmax.assign(H, 0);
+  sp.h_sumax.assign(H, 0);
   for (int h = 0; h < H; ++h) {
     auto& L = byh[h];
     std::stable_sort(L.begin(), L.end(), [&](int32_t a, int32_t b) { return A.fronts[a].p > A.fronts[b].p; });
@@ -737,6 +1119,15 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
       sp.h_umax[h] = std::max(sp.h_umax[h], S.m - S.p);
       sp.h_off0[h] = std::min(sp.h_off0[h], S.off);
       sp.h_off1[h] = std::max(sp.h_off1[h], S.off + int64_t(S.m) * S.m);
+      if (S.p >= sp.big_pivots) {  // the prefix of the list (pivots descending)
+        const int np = (S.p + kSB - 1) / kSB, nu = (S.m - S.p + kSB - 1) / kSB;
+        sp.h_nbig[h]++;
+        sp.h_bnp[h] = std::max(sp.h_bnp[h], np);
+        sp.h_bnt[h] = std::max(sp.h_bnt[h], np + nu);
+      } else {
+        sp.h_spmax[h] = std::max(sp.h_spmax[h], S.p);
+        sp.h_sumax[h] = std::max(sp.h_sumax[h], S.m - S.p);
+      }
     }
     if (L.empty()) sp.h_off0[h] = sp.h_off1[h] = 0;
   }
@@ -825,6 +1216,7 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaMalloc(&sp.D, 2 * n * sizeof(double)));
   ok(cudaMalloc(&sp.cvec, std::max<size_t>(A.emap.size(), 1) * sizeof(double)));
   ok(cudaMalloc(&sp.w, n * sizeof(double)));
+  ok(cudaMalloc(&sp.V, std::max<size_t>(A.fidx.size(), 1) * sizeof(double)));
   ok(cudaMalloc(&sp.tw, n * sizeof(double)));
   ok(cudaMalloc(&sp.yacc, n * sizeof(double)));
   ok(cudaMalloc(&sp.r, n * sizeof(double)));
@@ -835,12 +1227,14 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaMallocHost(&sp.hflags, 4 * sizeof(int)));
   ok(cudaMemset(sp.nrm, 0, 2 * sizeof(unsigned long long)));
   for (cudaEvent_t& ev : sp.ev) ok(cudaEventCreate(&ev));
-  const int smem = int(sp.max_m * sizeof(double));
+  const int smem = int(sp.max_m_small * sizeof(double));
   if (smem > 48 * 1024) {
     ok(set_smem<float>(smem));
     ok(set_smem<double>(smem));
   }
   ok(cudaFuncSetAttribute(sp_update_f32<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
+  ok(cudaFuncSetAttribute(sp_update_tc<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
+  if (const char* ev = getenv("MGPU_SPARSE_TC")) sp.tensor_cores = atoi(ev) != 0;
   if (e != cudaSuccess) {
     sp.why = std::string("device upload of the sparse solver: ") + cudaGetErrorString(e);
     return set_err(c, e == cudaErrorMemoryAllocation ? MGPU_ERR_NOMEM : MGPU_ERR_CUDA, sp.why);
@@ -860,7 +1254,7 @@ void sparse_destroy(SparseDev*& sp) {
   void* ps[] = {sp->d_fr, sp->d_lf, sp->d_ea, sp->d_clist, sp->d_fidx, sp->d_emap, sp->d_amap, sp->d_aq,
                 sp->d_acol, sp->d_perm, sp->d_diag, sp->d_colptr, sp->d_rowval, sp->d_rptr, sp->d_rq, sp->d_rcol,
                 sp->F32, sp->F64, sp->prev,
-                sp->D, sp->cvec, sp->w, sp->tw, sp->yacc, sp->r, sp->xs, sp->nrm, sp->flags};
+                sp->D, sp->cvec, sp->w, sp->V, sp->tw, sp->yacc, sp->r, sp->xs, sp->nrm, sp->flags};
   for (void* p : ps) cudaFree(p);
   if (sp->hflags) cudaFreeHost(sp->hflags);
   for (cudaEvent_t ev : sp->ev)
@@ -874,8 +1268,10 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
   const int64_t n = sp.n;
   // equilibration from the current values
   sp_scale_diag<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_diag, c->nzval, sp.D + n);
+  ++c->launches;
   sp_scale_zero<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_colptr, sp.d_rowval, c->nzval, sp.D + n,
                                                            sp.D);
+  ++c->launches;
   MG_CUDA(cudaMemsetAsync(sp.flags, 0, 4 * sizeof(int), st));
   bool use64 = sp.fp64_only;
   sp.last_factor_ms = sp.last_refine_ms = 0.0;
@@ -933,3 +1329,40 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
 }
 
 }  // namespace mgpu
+
+// C[M×N] −= A[M×K] B[K×N] (column-major host arrays, K ≤ 64) on the tensor cores
+extern "C" int mgpu_tc_gemm_check(int32_t device, int32_t M, int32_t N, int32_t K, const float* A, const float* B,
+                                  float* C) {
+  using namespace mgpu;
+  if (M <= 0 || N <= 0 || K <= 0 || K > 64 || !A || !B || !C) return MGPU_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MGPU_ERR_CUDA;
+  float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int* derr = nullptr;
+  int herr = 0, rc = MGPU_OK;
+  const size_t na = size_t(M) * K, nb = size_t(K) * N, nc = size_t(M) * N;
+  if (cudaMalloc(&dA, na * 4) != cudaSuccess || cudaMalloc(&dB, nb * 4) != cudaSuccess ||
+      cudaMalloc(&dC, nc * 4) != cudaSuccess || cudaMalloc(&derr, sizeof(int)) != cudaSuccess) {
+    rc = MGPU_ERR_NOMEM;
+  } else if (cudaMemcpy(dA, A, na * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(dB, B, nb * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemcpy(dC, C, nc * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+             cudaMemset(derr, 0, sizeof(int)) != cudaSuccess ||
+             cudaFuncSetAttribute(tc_gemm_check, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)) !=
+                 cudaSuccess) {
+    rc = MGPU_ERR_CUDA;
+  } else {
+    const dim3 g((M + tc::kTcTile - 1) / tc::kTcTile, (N + tc::kTcTile - 1) / tc::kTcTile);
+    tc_gemm_check<<<g, tc::kTcThreads, tc::kTcSmem>>>(dA, M, dB, K, dC, M, M, N, K, derr);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(C, dC, nc * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = MGPU_ERR_CUDA;
+    else if (herr)
+      rc = MGPU_ERR_CUDA;
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  cudaFree(derr);
+  return rc;
+}

@@ -48,6 +48,13 @@ struct SparseDev {
   std::vector<int64_t> h_off0, h_off1;         // front storage range
   std::vector<int64_t> h_aq0;                  // nnz of the height's fronts: d_aq[h_aq0[h] .. h_aq0[h+1])
   std::vector<std::vector<int32_t>> h_lfp;     // per height: p of the fronts in d_lf order (host, for step counts)
+  // per height: fronts taking the blocked substitutions (a prefix of the list),
+  // their most pivot tiles and most row tiles (pivot + update)
+  std::vector<int32_t> h_nbig, h_bnp, h_bnt;
+  std::vector<int32_t> h_spmax, h_sumax;       // most pivots / update rows of the other fronts
+  int max_m_small = 0;                         // largest front of the one-block substitutions
+  int big_pivots = 0;                          // fronts with this many pivots or more: blocked substitutions
+  bool tensor_cores = false;                   // FP32 trailing update on the tensor cores (TF32 ×3; MGPU_SPARSE_TC=1)
   // per height and child rank: children to add
   std::vector<std::vector<int32_t>> h_ea0, h_nea, h_eumax;
   SpFrontDev* d_fr = nullptr;
@@ -71,6 +78,7 @@ struct SparseDev {
   double* D = nullptr;          // [2n] equilibration, then the diagonal part of it
   double* cvec = nullptr;       // children's update vectors (forward substitution)
   double* w = nullptr;          // [n] elimination order work vector
+  double* V = nullptr;          // [Σ m] the blocked substitutions' front vectors (at each front's idx)
   double* tw = nullptr;         // [n] U₁₂ x_u of each pivot (backward substitution)
   double* yacc = nullptr;       // [n] accumulated scaled solution (elimination order)
   double* r = nullptr;          // [n] residual (model order)

@@ -114,7 +114,8 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_download", "mgpu_time_assemble", "mgpu_sweepx", "mgpu_measure_fp64_peak",
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
            "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune",
-           "mgpu_assemble_async", "mgpu_assemble_wait", "mgpu_sparse_info", "mgpu_element_lagrangian"]
+           "mgpu_assemble_async", "mgpu_assemble_wait", "mgpu_sparse_info", "mgpu_element_lagrangian",
+           "mgpu_tc_gemm_check", "mgpu_launch_count"]
 
 _lib = None
 
@@ -140,6 +141,8 @@ def load():
     L.mgpu_nnz.restype = i64
     L.mgpu_ntval.argtypes = [vp]
     L.mgpu_ntval.restype = i64
+    L.mgpu_launch_count.argtypes = [vp]
+    L.mgpu_launch_count.restype = i64
     L.mgpu_get_pattern.argtypes = [vp, pi64, pi64]
     L.mgpu_get_asm.argtypes = [vp, i32, pi64, pi64]
     L.mgpu_assemble.argtypes = [vp, i32, i32, pd, pd, d, pd, P(Newmark), pd, pd]
@@ -163,6 +166,8 @@ def load():
     L.mgpu_adjoint_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32, pd,
                                       pd, pd, pd, P(Stats)]
     L.mgpu_element_lagrangian.argtypes = [vp, i32, i32, pd, pd, pd, pd, pd, pd, pd, pd]
+    pf = P(ctypes.c_float)
+    L.mgpu_tc_gemm_check.argtypes = [i32, i32, i32, i32, pf, pf, pf]
     for name in SYMBOLS:
         f = getattr(L, name)
         if f.restype is ctypes.c_int and name not in ("mgpu_destroy",):

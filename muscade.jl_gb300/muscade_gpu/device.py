@@ -164,6 +164,10 @@ class DeviceModel:
         'sparse64' (multifrontal, FP64); see mgpu_set_linear_solver."""
         self._check(self.lib.mgpu_set_linear_solver(self.ctx, L.LINSOLVE[kind]))
 
+    def launch_count(self):
+        """Kernel launches of the assembly, Newton and multifrontal paths so far (mgpu_launch_count)."""
+        return int(self.lib.mgpu_launch_count(self.ctx))
+
     def sparse_info(self):
         """Structure and last solve of the multifrontal solver (mgpu_sparse_info)."""
         rep = L.SparseReport()

@@ -80,6 +80,33 @@ def test_multifrontal_and_banded_solvers_agree():
     assert all(e <= TOL_STATE for e in errs.values()), errs
 
 
+@pytest.mark.parametrize("threshold", ["64", "1"])
+def test_blocked_substitutions_match_oracle(lattice, monkeypatch, threshold):
+    """Fronts with many pivots take the blocked substitutions (one launch per
+    column block over a grid of row tiles); lowering the threshold sends most
+    (64) or all (1) fronts of the 12×12×6 lattice through them."""
+    m, st, times, ref = lattice
+    monkeypatch.setenv("MGPU_SPARSE_BLOCKED_PIVOTS", threshold)
+    out = {}
+    for kind in ("sparse", "sparse64"):
+        dm = DeviceModel(m, st.dis, linsolve=kind)
+        rc, states, stats = dm.sweepx(0, times, st.time, list(st.X), maxdx=1e-8, maxLl=1e-3)
+        sp = dm.sparse_info()
+        dm.close()
+        assert rc == 0 and stats.nstep_done == len(times)
+        errs = state_errors(states, ref, st.dis.fieldX)
+        print(f"blocked from {threshold} pivots ({kind}): {errs}, sweeps {sp['last_sweeps']}")
+        assert all(e <= TOL_STATE for e in errs.values()), errs
+        out[kind] = states
+    monkeypatch.delenv("MGPU_SPARSE_BLOCKED_PIVOTS")
+    dm = DeviceModel(m, st.dis, linsolve="sparse64")
+    rc, states, _ = dm.sweepx(0, times, st.time, list(st.X), maxdx=1e-8, maxLl=1e-3)
+    dm.close()
+    ref64 = [(0.0, (states[k, 0],)) for k in range(len(states))]
+    errs = state_errors(out["sparse64"], ref64, st.dis.fieldX)
+    assert all(e <= 1e-12 for e in errs.values()), errs  # FP64 blocked vs one-block: rounding only
+
+
 def test_fixed_iterations_without_graph_replay(lattice):
     m, st, times, _ = lattice
     dm = DeviceModel(m, st.dis)
