@@ -247,6 +247,22 @@ int mgpu_adjoint_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *
                         int64_t ncost, const int64_t *cost_dof, const double *cost_w, const double *cost_y,
                         int32_t ckpt, double *cost, double *dCdA, double *dCdtv, double *dCdU, mgpu_stats *stats);
 
+/* Forward sensitivities of a SweepX{OX} run with respect to a few A-dofs (the
+ * forward-mode counterpart of mgpu_adjoint_sweepx; SweepXA assembles the same
+ * sensitivity system, src/SweepXA.jl:49-221).  Runs the converged forward
+ * sweep and, after every step, solves the step's tangent once per selected
+ * A-dof θ:  Jₙ sₓ = −∂R/∂θ − Cₙ gᵥ − Mₙ gₐ  (gᵥ, gₐ the parts of X′, X″ carried
+ * from the previous step's sensitivities), sᵥ = a1 sₓ + gᵥ, sₐ = b1 sₓ + gₐ.
+ * sel[nsel] are distinct 1-based A-dofs; the cost is that of
+ * mgpu_adjoint_sweepx (cost elements plus optional sensor arrays).  Outputs
+ * (each may be NULL): dXdA[nstep][nsel][OX+1][nX], the sensitivities of X (and
+ * X′, X″); dCdA[nsel], the cost gradient at the selected A-dofs. */
+int mgpu_sensitivity_sweepx(mgpu_ctx *ctx, int32_t OX, int64_t nstep, const double *times, double t0,
+                            int32_t nXder0, const double *x0, const double *u, const double *tvals,
+                            const mgpu_sweep_opts *opts, int64_t ncost, const int64_t *cost_dof, const double *cost_w,
+                            const double *cost_y, int32_t nsel, const int64_t *sel, double *dXdA, double *dCdA,
+                            mgpu_stats *stats);
+
 /* Linear solver of the Newton loops (no counterpart in the reference, which
  * calls UMFPACK through lu/lu!/\ at src/SweepX.jl:207-210).  Every connected
  * component of Lλx is reordered (reverse Cuthill-McKee) and factorised as a

@@ -505,3 +505,354 @@ extern "C" int mgpu_adjoint_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const
 #undef ADJ_CUDA
   return MGPU_OK;
 }
+
+// ====================================================================== forward sensitivities
+// The forward-mode counterpart of the adjoint above: for a few A-dofs θ, the
+// derivatives of the converged states, step by step.  Differentiating
+// R(xₙ, vₙ, aₙ; θ) = 0 with vₙ = a1 xₙ + gᵥ(Sₙ₋₁), aₙ = b1 xₙ + gₐ(Sₙ₋₁):
+//   Jₙ sₓ = −∂R/∂θ − Cₙ gᵥ′ − Mₙ gₐ′,   sᵥ = a1 sₓ + gᵥ′,   sₐ = b1 sₓ + gₐ′
+//   gᵥ′ = −a1 sₓ⁻ + (1 − a2) sᵥ⁻ − a3 sₐ⁻,   gₐ′ = −b1 sₓ⁻ − b2 sᵥ⁻ + (1 − b3) sₐ⁻
+// (⁻ the previous step's sensitivities, zero before the first), and
+// dC/dθ = Σₙ wₙ (∂cₙ/∂x·sₓ + ∂cₙ/∂v·sᵥ + ∂cₙ/∂a·sₐ) + ∂C_A/∂θ.  This is what
+// SweepXA assembles for its sensitivity solve (src/SweepXA.jl:49-221), here
+// on the Newmark discretisation of SweepX.
+
+namespace mgpu {
+
+// Σ_i a[i] b[i] over one block in a fixed order, added to *out
+__global__ void __launch_bounds__(256) sens_dot_add(int64_t n, const double* __restrict__ a,
+                                                    const double* __restrict__ b, double* __restrict__ out) {
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += 256) s += a[i] * b[i];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) sm[threadIdx.x] += sm[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out += sm[0];
+}
+
+// gᵥ′, gₐ′ from the previous sensitivities; gv/ga scaled by 1/S for the products with S X S
+__global__ void sens_carry(int64_t n, double a1, double a2, double a3, double b1, double b2, double b3,
+                           const double* __restrict__ sx, const double* __restrict__ sv, const double* __restrict__ sa,
+                           const double* __restrict__ scale, double* __restrict__ gv, double* __restrict__ ga,
+                           double* __restrict__ gvs, double* __restrict__ gas) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = -a1 * sx[i] + (1.0 - a2) * sv[i] - a3 * sa[i];
+  const double a = -b1 * sx[i] - b2 * sv[i] + (1.0 - b3) * sa[i];
+  gv[i] = v;
+  ga[i] = a;
+  const double s = scale ? scale[i] : 1.0;
+  gvs[i] = v / s;
+  gas[i] = a / s;
+}
+
+// rhs_i −= Σ_t nz[rq[t]] x[rcol[t]] over row i (CSR of the pattern, fixed order)
+__global__ void sens_csr_sub(int64_t n, const int64_t* __restrict__ rptr, const int32_t* __restrict__ rq,
+                             const int32_t* __restrict__ rcol, const double* __restrict__ nz,
+                             const double* __restrict__ x, double* __restrict__ rhs) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int64_t t = rptr[i]; t < rptr[i + 1]; ++t) s += nz[rq[t]] * x[rcol[t]];
+  rhs[i] -= s;
+}
+
+// ∂R_e/∂θ of the listed EI-scaled beams (the bending-only residual, R being
+// linear in the bending stiffnesses), one thread per beam, into Re[list][12]
+__global__ void __launch_bounds__(128) sens_beam_dRdA(int64_t nlist, const int32_t* __restrict__ list,
+                                                      int64_t nele, const int32_t* __restrict__ idx,
+                                                      const double* __restrict__ cdata,
+                                                      const double* __restrict__ x0, double* __restrict__ Re) {
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= nlist) return;
+  const int64_t e = list[q];
+  BeamConst bc;
+  double* d = reinterpret_cast<double*>(&bc);
+  for (int f = 0; f < int(sizeof(BeamConst) / sizeof(double)); ++f) d[f] = __ldg(cdata + f * nele + e);
+  bc.ke = 0.0;
+  bc.kt = 0.0;
+  bc.mu = 0.0;
+  bc.iota1 = 0.0;
+  bc.w = 0.0;
+  for (int k = 0; k < 3; ++k) bc.Ca[k] = bc.Cl[k] = bc.Cq[k] = 0.0;
+  double X0[12], R[12], K[144];
+  for (int i = 0; i < 12; ++i) X0[i] = __ldg(x0 + __ldg(idx + i * nele + e));
+  beam_element<false>(bc, X0, X0, X0, nullptr, Perturb{1.0, 0.0, 0.0}, nullptr, nullptr, R, K, nullptr, nullptr);
+  for (int i = 0; i < 12; ++i) Re[q * 12 + i] = R[i];
+}
+
+// rhs[d] −= S_d Re[q][i] over the beams q of one θ, in list order (one thread)
+__global__ void sens_beam_rhs(int64_t q0, int64_t q1, const int32_t* __restrict__ list, int64_t nele,
+                              const int32_t* __restrict__ idx, const double* __restrict__ Re,
+                              const double* __restrict__ scale, double* __restrict__ rhs) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int64_t q = q0; q < q1; ++q) {
+    const int64_t e = list[q];
+    for (int i = 0; i < 12; ++i) {
+      const int dd = idx[i * nele + e];
+      rhs[dd] -= Re[q * 12 + i] * (scale ? scale[dd] : 1.0);
+    }
+  }
+}
+
+// sₓ = S z;  sᵥ = a1 sₓ + gᵥ′, sₐ = b1 sₓ + gₐ′
+__global__ void sens_update(int64_t n, int OX, double a1, double b1, const double* __restrict__ z,
+                            const double* __restrict__ scale, const double* __restrict__ gv,
+                            const double* __restrict__ ga, double* __restrict__ sx, double* __restrict__ sv,
+                            double* __restrict__ sa) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = z[i] * (scale ? scale[i] : 1.0);
+  sx[i] = s;
+  if (OX == 2) {
+    sv[i] = a1 * s + gv[i];
+    sa[i] = b1 * s + ga[i];
+  }
+}
+
+// dC/dθ += 2 w (a − y) for the A-costs on θ (element order, one thread)
+__global__ void sens_acost(int64_t nele, const int32_t* __restrict__ aidx, const double* __restrict__ cdata,
+                           const double* __restrict__ A, int32_t theta, double* __restrict__ out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int64_t e = 0; e < nele; ++e)
+    if (aidx[e] == theta) *out += 2.0 * cdata[e] * (A[theta] - cdata[nele + e]);
+}
+
+}  // namespace mgpu
+
+extern "C" int mgpu_sensitivity_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double* times, double t0,
+                                       int32_t nXder0, const double* x0, const double* u, const double* tvals,
+                                       const mgpu_sweep_opts* opts, int64_t ncost, const int64_t* cost_dof,
+                                       const double* cost_w, const double* cost_y, int32_t nsel, const int64_t* sel,
+                                       double* dXdA, double* dCdA, mgpu_stats* stats) {
+  if (!c || !times || !opts || !stats || !(OX == 0 || OX == 2) || nstep < 1 || nXder0 < 0 || nXder0 > OX + 1 ||
+      (nXder0 > 0 && !x0) || ncost < 0 || (ncost > 0 && (!cost_dof || !cost_w || !cost_y)) ||
+      (c->ntval > 0 && !tvals) || nsel < 1 || !sel)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_sensitivity_sweepx: bad arguments");
+  if (opts->fixed_iter > 0 || opts->per_component)
+    return set_err(c, MGPU_ERR_ARG, "mgpu_sensitivity_sweepx: the sensitivities need converged steps (fixed_iter = 0, "
+                                    "per_component = 0)");
+  *stats = mgpu_stats{0, 0, 0, 0, 0.0, 0.0};
+  const int64_t n = c->nX;
+  for (int32_t q = 0; q < nsel; ++q)
+    if (sel[q] < 1 || sel[q] > c->nA) return set_err(c, MGPU_ERR_ARG, "selected A-dof out of range");
+  std::vector<int32_t> cdof(ncost);
+  for (int64_t s = 0; s < ncost; ++s) {
+    if (cost_dof[s] < 1 || cost_dof[s] > n) return set_err(c, MGPU_ERR_ARG, "cost dof out of range");
+    cdof[s] = int32_t(cost_dof[s] - 1);
+  }
+  for (const DevGroup& G : c->groups)
+    if (G.kind == MGPU_DOFCOST && G.nele > 0 && G.maxder > OX)
+      return set_err(c, MGPU_ERR_ARG, "mgpu_sensitivity_sweepx: a DofCost on a time derivative of X needs OX = 2");
+  Solver& S = *c->solver;
+  if (!S.ok && S.path != PATH_SPARSE && S.path != PATH_SPARSE64)
+    return set_err(c, MGPU_ERR_UNSUPPORTED, "no device solver for this model: " + S.why);
+  MG_CUDA(cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  // the beams of each selected θ (group, element) and the CSR of the pattern
+  std::vector<int64_t> lptr(nsel + 1, 0);
+  std::vector<int32_t> lele;
+  std::vector<int32_t> lgrp;
+  for (int32_t q = 0; q < nsel; ++q) {
+    for (size_t g = 0; g < c->groups.size(); ++g) {
+      const DevGroup& G = c->groups[g];
+      if (G.kind != MGPU_EULERBEAM3D || !G.aidx) continue;
+      for (int64_t e = 0; e < G.nele; ++e)
+        if (G.h_indexA[e] == sel[q]) {
+          lele.push_back(int32_t(e));
+          lgrp.push_back(int32_t(g));
+        }
+    }
+    lptr[q + 1] = int64_t(lele.size());
+  }
+  std::vector<int64_t> rptr(n + 1, 0);
+  for (int64_t q = 0; q < c->pat.nnz; ++q) rptr[c->pat.rowval[q] + 1]++;
+  for (int64_t i = 0; i < n; ++i) rptr[i + 1] += rptr[i];
+  std::vector<int32_t> rq(c->pat.nnz), rcol(c->pat.nnz);
+  {
+    std::vector<int64_t> fill(rptr.begin(), rptr.end() - 1);
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t q = c->pat.colptr[j]; q < c->pat.colptr[j + 1]; ++q) {
+        const int64_t t = fill[c->pat.rowval[q]]++;
+        rq[t] = int32_t(q);
+        rcol[t] = int32_t(j);
+      }
+  }
+  std::vector<void*> owned;
+  auto alloc = [&](auto** p, size_t count) -> bool {
+    using T = typename std::remove_pointer<typename std::remove_reference<decltype(*p)>::type>::type;
+    if (cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return false;
+    owned.push_back(*p);
+    return true;
+  };
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(st);
+    for (void* p : owned) cudaFree(p);
+    cudaGetLastError();
+  };
+  const size_t ns = size_t(nsel) * n;
+  double *sx, *sv, *sa, *gv, *ga, *gvs, *gas, *rhs, *nzC, *nzM, *gx, *gvc, *gac, *dC, *Re, *cw, *cy, *ub;
+  int32_t *dcd, *dl, *drq, *drcol;
+  int64_t* drptr;
+  bool ok = alloc(&sx, ns) && alloc(&sv, ns) && alloc(&sa, ns) && alloc(&gv, n) && alloc(&ga, n) && alloc(&gvs, n) &&
+            alloc(&gas, n) && alloc(&rhs, n) && alloc(&gx, n) && alloc(&gvc, n) && alloc(&gac, n) &&
+            alloc(&dC, nsel) && alloc(&Re, lele.size() * 12) && alloc(&cw, ncost) && alloc(&cy, size_t(nstep) * ncost) &&
+            alloc(&ub, c->nU) && alloc(&dcd, ncost) && alloc(&dl, lele.size()) && alloc(&drq, rq.size()) &&
+            alloc(&drcol, rcol.size()) && alloc(&drptr, rptr.size());
+  if (ok && OX == 2) ok = alloc(&nzC, c->pat.nnz) && alloc(&nzM, c->pat.nnz);
+  if (!ok) {
+    cleanup();
+    return set_err(c, MGPU_ERR_NOMEM, "device allocation failed for the sensitivities");
+  }
+  ok = cudaMemcpy(drptr, rptr.data(), rptr.size() * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+       (rq.empty() || cudaMemcpy(drq, rq.data(), rq.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess) &&
+       (rcol.empty() ||
+        cudaMemcpy(drcol, rcol.data(), rcol.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess) &&
+       (lele.empty() ||
+        cudaMemcpy(dl, lele.data(), lele.size() * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess) &&
+       (ncost == 0 ||
+        (cudaMemcpy(dcd, cdof.data(), ncost * sizeof(int32_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(cw, cost_w, ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(cy, cost_y, size_t(nstep) * ncost * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess)) &&
+       cudaMemsetAsync(sx, 0, ns * sizeof(double), st) == cudaSuccess &&
+       cudaMemsetAsync(sv, 0, ns * sizeof(double), st) == cudaSuccess &&
+       cudaMemsetAsync(sa, 0, ns * sizeof(double), st) == cudaSuccess &&
+       cudaMemsetAsync(dC, 0, nsel * sizeof(double), st) == cudaSuccess;
+  if (!ok) {
+    cleanup();
+    return set_err(c, MGPU_ERR_CUDA, "sensitivities: upload failed");
+  }
+  int rc = MGPU_OK;
+#define SENS_TRY(x) \
+  do {              \
+    rc = (x);       \
+    if (rc) {       \
+      cleanup();    \
+      return rc;    \
+    }               \
+  } while (0)
+#define SENS_CUDA(call)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      rc = set_err(c, MGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+      cleanup();                                                                          \
+      return rc;                                                                          \
+    }                                                                                     \
+  } while (0)
+  const size_t nsx = size_t(3) * n;
+  SENS_CUDA(cudaMemsetAsync(c->x, 0, nsx * sizeof(double), st));
+  if (nXder0 > 0) SENS_CUDA(cudaMemcpyAsync(c->x, x0, nXder0 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (c->nU > 0 && u) SENS_CUDA(cudaMemcpyAsync(c->u, u, c->nU * sizeof(double), cudaMemcpyHostToDevice, st));
+  c->nXder_resident = OX + 1;
+  double told = t0;
+  for (int64_t k = 0; k < nstep; ++k) {
+    const double t = times[k], dt = t - told;
+    told = t;
+    if (OX > 0 && !(dt > 0)) {
+      cleanup();
+      return set_err(c, MGPU_ERR_ARG, "Time step length not strictly positive at step=" + std::to_string(k + 1));
+    }
+    const double* tvk = c->ntval > 0 ? tvals + k * c->ntval : nullptr;
+    SENS_TRY(newton_step(c, OX, k, t, dt, tvk, opts, stats));
+    stats->nstep_done = int(k + 1);
+    const double wk = OX == 2 ? dt : 1.0;
+    const mgpu_newmark nm = OX == 2 ? newmark_coefficients(opts->beta, opts->gamma, dt) : mgpu_newmark{0, 0, 0, 0, 0, 0};
+    // the cost's partials at step k
+    SENS_CUDA(cudaMemsetAsync(gx, 0, n * sizeof(double), st));
+    SENS_CUDA(cudaMemsetAsync(gvc, 0, n * sizeof(double), st));
+    SENS_CUDA(cudaMemsetAsync(gac, 0, n * sizeof(double), st));
+    if (ncost > 0) adj_cost_grad<<<nb(ncost, 256), 256, 0, st>>>(ncost, dcd, cw, cy + k * ncost, c->x, wk, gx);
+    for (const DevGroup& G : c->groups)
+      if (G.kind == MGPU_DOFCOST && G.nele > 0) {
+        if (G.distinct)
+          adj_group_grad<<<nb(G.nele, 256), 256, 0, st>>>(G.nele, 0, 0, G.idx, nullptr, G.cdata, c->tv + G.tval_base,
+                                                          c->x, n, c->u, nullptr, c->scale, wk, gx, gvc, gac, ub,
+                                                          nullptr);
+        else
+          adj_group_grad<<<1, 1, 0, st>>>(G.nele, 0, 1, G.idx, nullptr, G.cdata, c->tv + G.tval_base, c->x, n, c->u,
+                                          nullptr, c->scale, wk, gx, gvc, gac, ub, nullptr);
+      }
+    // damping and mass matrices of the step (S C S, S M S)
+    if (OX == 2) {
+      const mgpu_newmark onlyC{1.0, 0, 0, 0.0, 0, 0}, onlyM{0.0, 0, 0, 1.0, 0, 0};
+      SENS_TRY(upload_stepc(c, t, &onlyC));
+      SENS_TRY(launch_assembly(c, MGPU_ASM_ITER, nullptr, 0.0));
+      SENS_CUDA(cudaMemcpyAsync(nzC, c->nzval, c->pat.nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      SENS_TRY(upload_stepc(c, t, &onlyM));
+      SENS_TRY(launch_assembly(c, MGPU_ASM_ITER, nullptr, 0.0));
+      SENS_CUDA(cudaMemcpyAsync(nzM, c->nzval, c->pat.nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+    // the tangent at the converged state, factorised with each θ's right-hand side in Lλ
+    SENS_TRY(upload_stepc(c, t, OX == 2 ? &nm : nullptr));
+    launch_reset_errflag(c);
+    SENS_TRY(launch_assembly(c, OX == 2 ? MGPU_ASM_ITER : MGPU_ASM_STATIC, nullptr, 1.0));
+    for (int32_t q = 0; q < nsel; ++q) {
+      double* sxq = sx + size_t(q) * n;
+      double* svq = sv + size_t(q) * n;
+      double* saq = sa + size_t(q) * n;
+      SENS_CUDA(cudaMemsetAsync(rhs, 0, n * sizeof(double), st));
+      if (OX == 2) {
+        sens_carry<<<nb(n, 256), 256, 0, st>>>(n, nm.a1, nm.a2, nm.a3, nm.b1, nm.b2, nm.b3, sxq, svq, saq, c->scale, gv,
+                                               ga, gvs, gas);
+        sens_csr_sub<<<nb(n, 256), 256, 0, st>>>(n, drptr, drq, drcol, nzC, gvs, rhs);
+        sens_csr_sub<<<nb(n, 256), 256, 0, st>>>(n, drptr, drq, drcol, nzM, gas, rhs);
+      }
+      const int64_t q0 = lptr[q], q1 = lptr[q + 1];
+      for (int64_t r0 = q0; r0 < q1;) {  // beams of θ by group
+        int64_t r1 = r0;
+        while (r1 < q1 && lgrp[r1] == lgrp[r0]) ++r1;
+        const DevGroup& G = c->groups[lgrp[r0]];
+        sens_beam_dRdA<<<nb(r1 - r0, 128), 128, 0, st>>>(r1 - r0, dl + r0, G.nele, G.idx, G.cdata, c->x, Re + r0 * 12);
+        sens_beam_rhs<<<1, 1, 0, st>>>(0, r1 - r0, dl + r0, G.nele, G.idx, Re + r0 * 12, c->scale, rhs);
+        r0 = r1;
+      }
+      // S J S z = rhs
+      SENS_CUDA(cudaMemcpyAsync(c->Ll, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      SENS_CUDA(cudaMemsetAsync(S.info, 0, sizeof(int), st));
+      SENS_TRY(factor_solve(c, S.info));
+      sens_update<<<nb(n, 256), 256, 0, st>>>(n, OX, nm.a1, nm.b1, S.dx, c->scale, gv, ga, sxq, svq, saq);
+      sens_dot_add<<<1, 256, 0, st>>>(n, gx, sxq, dC + q);
+      if (OX == 2) {
+        sens_dot_add<<<1, 256, 0, st>>>(n, gvc, svq, dC + q);
+        sens_dot_add<<<1, 256, 0, st>>>(n, gac, saq, dC + q);
+      }
+      if (dXdA) {
+        double* out = dXdA + (size_t(k) * nsel + q) * size_t(OX + 1) * n;
+        SENS_CUDA(cudaMemcpyAsync(out, sxq, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (OX == 2) {
+          SENS_CUDA(cudaMemcpyAsync(out + n, svq, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+          SENS_CUDA(cudaMemcpyAsync(out + 2 * n, saq, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
+      }
+      int hinfo = 0, hflag = INT_MAX;
+      SENS_CUDA(cudaMemcpyAsync(&hinfo, S.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+      SENS_CUDA(cudaMemcpyAsync(&hflag, c->errflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      SENS_CUDA(cudaStreamSynchronize(st));
+      if (hflag != INT_MAX) {
+        rc = nan_error(c, hflag);
+        cleanup();
+        return rc;
+      }
+      if (hinfo != 0) {
+        cleanup();
+        return set_err(c, MGPU_ERR_SINGULAR,
+                       "sensitivities: factorization failed at step=" + std::to_string(k + 1));
+      }
+    }
+  }
+  for (int32_t q = 0; q < nsel; ++q)
+    for (const DevGroup& G : c->groups)
+      if (G.kind == MGPU_ACOST && G.nele > 0)
+        sens_acost<<<1, 1, 0, st>>>(G.nele, G.aidx, G.cdata, c->Avec, int32_t(sel[q] - 1), dC + q);
+  SENS_CUDA(cudaStreamSynchronize(st));
+  if (dCdA) SENS_CUDA(cudaMemcpy(dCdA, dC, nsel * sizeof(double), cudaMemcpyDeviceToHost));
+  cleanup();
+#undef SENS_TRY
+#undef SENS_CUDA
+  return MGPU_OK;
+}

@@ -281,13 +281,26 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
     return;
   }
   const int i0 = r0 + (blockIdx.x % nt) * kTile32, j0 = r0 + (blockIdx.x / nt) * kTile32;
-  for (int t = tid; t < NB * kTile32; t += kThreads) {
-    const int i = t % kTile32, c = t / kTile32;
-    As[c][i] = (c < kb && i0 + i < m) ? A[(i0 + i) + int64_t(k0 + c) * m] : 0.f;
-  }
-  for (int t = tid; t < NB * kTile32; t += kThreads) {
-    const int c = t % NB, j = t / NB;
-    Bs[c][j] = (c < kb && j0 + j < m) ? A[(k0 + c) + int64_t(j0 + j) * m] : 0.f;
+  // the tile's operand loads in batches of 16 per thread, all in flight together
+  constexpr int kPer = NB * kTile32 / kThreads;
+  static_assert(kPer % 16 == 0, "whole batches");
+#pragma unroll
+  for (int b0 = 0; b0 < kPer; b0 += 16) {
+    float va[16], vb[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int t = (b0 + u) * kThreads + tid;
+      const int i = t % kTile32, c = t / kTile32;
+      va[u] = (c < kb && i0 + i < m) ? A[(i0 + i) + int64_t(k0 + c) * m] : 0.f;
+      const int cb = t % NB, j = t / NB;
+      vb[u] = (cb < kb && j0 + j < m) ? A[(k0 + cb) + int64_t(j0 + j) * m] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int t = (b0 + u) * kThreads + tid;
+      As[t / kTile32][t % kTile32] = va[u];
+      Bs[t % NB][t / NB] = vb[u];
+    }
   }
   __syncthreads();
   const int tr = tid & 15, tc = tid >> 4;
@@ -309,15 +322,29 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
 #pragma unroll
       for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
   }
+  // read-modify-write of the tile: two columns' 16 loads in flight at a time
 #pragma unroll
-  for (int v = 0; v < 8; ++v) {
-    const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
-    if (j >= m) continue;
-    float* col = A + int64_t(j) * m;
+  for (int v0 = 0; v0 < 8; v0 += 2) {
+    float cv[2][8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
-      if (i < m) col[i] -= acc[u][v];
+    for (int dv = 0; dv < 2; ++dv) {
+      const int v = v0 + dv;
+      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+        cv[dv][u] = (i < m && j < m) ? A[i + int64_t(j) * m] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int dv = 0; dv < 2; ++dv) {
+      const int v = v0 + dv;
+      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+        if (i < m && j < m) A[i + int64_t(j) * m] = cv[dv][u] - acc[u][v];
+      }
     }
   }
 }

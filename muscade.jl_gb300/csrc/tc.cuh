@@ -139,6 +139,65 @@ constexpr int kTcTile = 128;
 constexpr int kTcThreads = 128;
 constexpr size_t kTcSmem = size_t(4) * kTcTile * 32 * sizeof(float);
 
+// operand values of one K half (32) in registers: A row `tid` (32 values) and,
+// for B, lane l's four K values of eight columns (see tile_update_tf32x3)
+struct TcHalf {
+  float a[32];
+  float b[32];
+};
+
+__device__ __forceinline__ void tc_load_half(TcHalf& v, const float* __restrict__ A, int64_t lda,
+                                             const float* __restrict__ B, int64_t ldb, int i0, int j0, int mrows,
+                                             int ncols, int kb, int kbeg) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int i = i0 + tid;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    const int kk = kbeg + k;
+    v.a[k] = (kk < kb && i < mrows) ? A[i + int64_t(kk) * lda] : 0.f;
+  }
+#pragma unroll
+  for (int tt = 0; tt < 8; ++tt) {
+    const int task = warp + 4 * tt;
+    const int n = 8 * (task >> 1) + (lane & 7), kq = (lane >> 3) + 4 * (task & 1);
+    const int j = j0 + n;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int kk = kbeg + 4 * kq + q;
+      v.b[4 * tt + q] = (kk < kb && j < ncols) ? B[kk + int64_t(j) * ldb] : 0.f;
+    }
+  }
+}
+
+// split and store one half's operands in the canonical K-major layout, 16-byte stores
+__device__ __forceinline__ void tc_store_half(const TcHalf& v, float* Ah, float* Al, float* Bh, float* Bl) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+  for (int kq = 0; kq < 8; ++kq) {
+    float4 h4, l4;
+    split_tf32(v.a[4 * kq + 0], h4.x, l4.x);
+    split_tf32(v.a[4 * kq + 1], h4.y, l4.y);
+    split_tf32(v.a[4 * kq + 2], h4.z, l4.z);
+    split_tf32(v.a[4 * kq + 3], h4.w, l4.w);
+    const uint32_t o = kmajor_offset(tid, 4 * kq, 32) >> 2;
+    *reinterpret_cast<float4*>(Ah + o) = h4;
+    *reinterpret_cast<float4*>(Al + o) = l4;
+  }
+#pragma unroll
+  for (int tt = 0; tt < 8; ++tt) {
+    const int task = warp + 4 * tt;
+    const int n = 8 * (task >> 1) + (lane & 7), kq = (lane >> 3) + 4 * (task & 1);
+    float4 h4, l4;
+    split_tf32(v.b[4 * tt + 0], h4.x, l4.x);
+    split_tf32(v.b[4 * tt + 1], h4.y, l4.y);
+    split_tf32(v.b[4 * tt + 2], h4.z, l4.z);
+    split_tf32(v.b[4 * tt + 3], h4.w, l4.w);
+    const uint32_t o = kmajor_offset(n, 4 * kq, 32) >> 2;
+    *reinterpret_cast<float4*>(Bh + o) = h4;
+    *reinterpret_cast<float4*>(Bl + o) = l4;
+  }
+}
+
 __device__ __forceinline__ bool tile_update_tf32x3(const float* __restrict__ A, int64_t lda,
                                                    const float* __restrict__ B, int64_t ldb, float* __restrict__ C,
                                                    int64_t ldc, int i0, int j0, int mrows, int ncols, int kb,
@@ -148,6 +207,9 @@ __device__ __forceinline__ bool tile_update_tf32x3(const float* __restrict__ A, 
   float* Bh = smem + 2 * kTcTile * 32;
   float* Bl = smem + 3 * kTcTile * 32;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // every operand load of the first half is in flight before any is used
+  TcHalf v;
+  tc_load_half(v, A, lda, B, ldb, i0, j0, mrows, ncols, kb, 0);
   if (warp == 0) tmem_alloc(tslot, kTcTile);
   if (tid == 0) mbar_init(bar, 1);
   fence_before_sync();
@@ -155,44 +217,10 @@ __device__ __forceinline__ bool tile_update_tf32x3(const float* __restrict__ A, 
   fence_after_sync();
   const uint32_t tmem = *tslot;
   constexpr uint32_t idesc = idesc_tf32(kTcTile, kTcTile);
+  const int nhalf = kb > 32 ? 2 : 1;
   bool ok = true;
-  for (int h = 0; h < 2 && 32 * h < kb; ++h) {
-    const int kbeg = 32 * h;
-    {  // A: thread t stages row t of the tile, four K values per 16-byte store (coalesced along the rows)
-      const int i = i0 + tid;
-      for (int kq = 0; kq < 8; ++kq) {
-        float4 h4, l4;
-        float* hp = &h4.x;
-        float* lp = &l4.x;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int kk = kbeg + 4 * kq + q;
-          const float x = (kk < kb && i < mrows) ? A[i + int64_t(kk) * lda] : 0.f;
-          split_tf32(x, hp[q], lp[q]);
-        }
-        const uint32_t o = kmajor_offset(tid, 4 * kq, 32) >> 2;
-        *reinterpret_cast<float4*>(Ah + o) = h4;
-        *reinterpret_cast<float4*>(Al + o) = l4;
-      }
-    }
-    {  // B: lane l takes column n = 8 r + (l % 8) and K values 4 (l / 8) + 16 s .. +3 of it
-      for (int task = warp; task < (kTcTile / 8) * 2; task += kTcThreads / 32) {
-        const int n = 8 * (task >> 1) + (lane & 7), kq = (lane >> 3) + 4 * (task & 1);
-        const int j = j0 + n;
-        float4 h4, l4;
-        float* hp = &h4.x;
-        float* lp = &l4.x;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int kk = kbeg + 4 * kq + q;
-          const float x = (kk < kb && j < ncols) ? B[kk + int64_t(j) * ldb] : 0.f;
-          split_tf32(x, hp[q], lp[q]);
-        }
-        const uint32_t o = kmajor_offset(n, 4 * kq, 32) >> 2;
-        *reinterpret_cast<float4*>(Bh + o) = h4;
-        *reinterpret_cast<float4*>(Bl + o) = l4;
-      }
-    }
+  for (int h = 0; h < nhalf; ++h) {
+    tc_store_half(v, Ah, Al, Bh, Bl);
     fence_async_smem();
     __syncthreads();
     if (tid == 0) {
@@ -207,20 +235,29 @@ __device__ __forceinline__ bool tile_update_tf32x3(const float* __restrict__ A, 
       }
       mma_commit(bar);
     }
+    if (h + 1 < nhalf) tc_load_half(v, A, lda, B, ldb, i0, j0, mrows, ncols, kb, 32);  // overlaps the MMAs
     ok = mbar_wait(bar, uint32_t(h & 1)) && ok;
     fence_after_sync();
     __syncthreads();  // the next half overwrites the operands the MMAs read
   }
+  // epilogue: 32 accumulator columns at a time, their C loads all in flight together
   const int i = i0 + 32 * warp + lane;
-  for (int c = 0; c < kTcTile; c += 16) {
-    float v[16];
-    tmem_ld16(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c), v);
-    if (ok && i < mrows)
+  const bool row_ok = ok && i < mrows;
+  for (int c = 0; c < kTcTile; c += 32) {
+    float v0[16], v1[16];
+    tmem_ld16(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c), v0);
+    tmem_ld16(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c + 16), v1);
+    float cv[32];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int j = j0 + c + q;
-        if (j < ncols) C[i + int64_t(j) * ldc] -= v[q];
-      }
+    for (int q = 0; q < 32; ++q) {
+      const int j = j0 + c + q;
+      cv[q] = (row_ok && j < ncols) ? C[i + int64_t(j) * ldc] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int j = j0 + c + q;
+      if (row_ok && j < ncols) C[i + int64_t(j) * ldc] = cv[q] - (q < 16 ? v0[q] : v1[q - 16]);
+    }
   }
   fence_before_sync();
   __syncthreads();

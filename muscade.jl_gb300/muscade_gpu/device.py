@@ -147,6 +147,35 @@ class DeviceModel:
             return cost.value, dA[: self.nA], dtv, stats, dU[: self.nU]
         return cost.value, dA[: self.nA], dtv, stats
 
+    def sensitivity(self, OX, times, t0, X0, sel, cost_dof=(), cost_w=1.0, cost_y=None, U=None, beta=0.25,
+                    gamma=0.5, maxiter=50, maxdx=1e-10, maxLl=math.inf, states=False, tvals=None):
+        """Forward sensitivities with respect to the A-dofs `sel` (1-based) of a
+        converged SweepX{OX} sweep (mgpu_sensitivity_sweepx).  Returns (dCdA[nsel],
+        dXdA[nstep][nsel][OX+1][nX] or None, stats); the cost as in adjoint()."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        nstep = len(times)
+        X0 = [np.asarray(v, dtype=np.float64) for v in X0][: OX + 1]
+        x0 = np.ascontiguousarray(np.concatenate(X0)) if X0 else np.zeros(0)
+        u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
+        tv = self.time_values(times) if tvals is None else np.ascontiguousarray(tvals, dtype=np.float64)
+        cd = np.ascontiguousarray(cost_dof, dtype=np.int64).reshape(-1)
+        cw = np.ascontiguousarray(np.broadcast_to(cost_w, cd.shape), dtype=np.float64)
+        cy = np.ascontiguousarray(np.zeros((nstep, 0)) if cost_y is None else cost_y, dtype=np.float64)
+        cy = cy.reshape(nstep, len(cd))
+        sl = np.ascontiguousarray(sel, dtype=np.int64).reshape(-1)
+        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0)
+        dC = np.zeros(len(sl))
+        dX = np.zeros((nstep, len(sl), OX + 1, self.nX)) if states else None
+        stats = L.Stats()
+        rc = self.lib.mgpu_sensitivity_sweepx(self.ctx, OX, nstep, L.ptr(times), float(t0), len(X0), L.ptr(x0),
+                                              L.ptr(u), L.ptr(tv), ctypes.byref(opts), len(cd),
+                                              L.ptr(cd, ctypes.c_int64) if len(cd) else None,
+                                              L.ptr(cw) if len(cd) else None, L.ptr(cy) if len(cd) else None,
+                                              len(sl), L.ptr(sl, ctypes.c_int64), L.ptr(dX) if dX is not None else None,
+                                              L.ptr(dC), ctypes.byref(stats))
+        self._check(rc)
+        return dC, dX, stats
+
     def autotune(self, mission=L.ASM_STATIC, c=None):
         """Time the element kernels' block sizes and the applicable linear solvers on
         the resident state (see upload_state) and keep the fastest (mgpu_autotune)."""
