@@ -614,6 +614,14 @@ def bench_batched(args, rank, local_rank, ws, dist):
     dt = reduce_max(dist, dt)
     iters = stats.niter_total
     info64 = dm.linear_solver_info()
+    # the same sweep as one graph launch with the load steps and Newton
+    # iterations looped on the device (no per-iteration host read-back)
+    dm.sweepx(0, times, st.time, X0, device_loop=True, **kw)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc_dl, x_dl, stats_dl = dm.sweepx(0, times, st.time, X0, device_loop=True, **kw)
+    dt_dl = reduce_max(dist, (time.perf_counter() - t0) / args.steps)
+    same_dl = rc_dl == 0 and bool(np.array_equal(x_dl, xb)) and stats_dl.niter_total == iters
     # the same batch with FP32 factors and FP64 refinement
     dm.set_linear_solver("f32ir")
     dm.sweepx(0, times, st.time, X0, **kw)
@@ -669,6 +677,9 @@ def bench_batched(args, rank, local_rank, ws, dist):
                     "note": "the whole mgpu_sweepx call with host initial state, load values and states"},
             "per_model_path": {"models_per_s": per_model, "sample": int(len(pick)), "speedup_of_batch": value / per_model,
                                "states_bitwise_equal_to_batch": same},
+            "device_loop": {"models_per_s": len(allp) / dt_dl if rc_dl == 0 else None, "rc": rc_dl,
+                            "states_bitwise_equal_to_host_loop": same_dl, "graph_launches_per_sweep": 1,
+                            "note": "load steps and Newton iterations looped on the device by conditional graph nodes"},
             "fp32_refined": {"models_per_s": len(params) / dt32 if rc32 == 0 else None, "rc": rc32,
                              "max_rel_state_dev_vs_fp64": worst, "linear_solver": info32,
                              "newton_iterations": stats32.niter_total,

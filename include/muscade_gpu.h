@@ -196,6 +196,10 @@ typedef struct {
                             that passes stops iterating while the others go on, so each follows
                             the iterations it would take alone.  Needs fixed_iter = 0. */
   int32_t no_graph;      /* != 0: fixed-iteration steps are launched kernel by kernel */
+  int32_t device_loop;   /* != 0 (SweepX{0}, banded FP64 or F32IR solver, convergence test): the whole
+                            sweep is one CUDA graph launch whose conditional WHILE nodes loop over the
+                            load steps and the Newton iterations on the device (per-component test with
+                            per_component), bounded by maxiter; the host reads nothing until it ends */
 } mgpu_sweep_opts;
 
 typedef struct {

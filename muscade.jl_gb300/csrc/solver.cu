@@ -1519,6 +1519,240 @@ static int sweep_graph(mgpu_ctx* c, int OX, int64_t nstep, const double* times, 
 }
 }  // namespace mgpu
 
+// ---------------------------------------------------------------- the Newton loop on the device
+// SweepX{0} as one graph launch: a conditional WHILE node over the load steps
+// whose body copies the step's constants and load values into place, runs a
+// nested WHILE node over the Newton iterations and stores the converged state.
+// The iteration body is the captured iteration (assembly, factorisation and
+// solve, decrement, convergence test) followed by a controller kernel that
+// counts the iteration and ends the loop when every model has converged (or
+// the whole system, without per_component), when maxiter is reached, or on a
+// NaN or singular factorisation.  The host reads nothing until the sweep ends.
+namespace {
+struct DevLoop {
+  int* step = nullptr;     // current step
+  int* iter = nullptr;     // iterations of the current step
+  int* status = nullptr;   // [nstep] 0 converged, 1 no convergence, 2 singular, 3 NaN, -1 not run
+  int* iters = nullptr;    // [nstep] iterations taken
+  double* stepc = nullptr;  // [nstep][8] t and the Newmark coefficients (zero for SweepX{0})
+  double* tv = nullptr;    // [nstep][ntval]
+  double* states = nullptr;  // [nstep][n]
+};
+
+__global__ void dl_step_begin(const int* __restrict__ step, const double* __restrict__ stepc_all,
+                              const double* __restrict__ tv_all, int64_t ntval, double* __restrict__ stepc,
+                              double* __restrict__ tv, int* __restrict__ iter, int* __restrict__ frozen, int ncomp,
+                              cudaGraphConditionalHandle hi) {
+  const int64_t k = *step;
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < 8) stepc[i] = stepc_all[k * 8 + i];
+  if (i < ntval) tv[i] = tv_all[k * ntval + i];
+  if (frozen && i < ncomp) frozen[i] = 0;
+  if (i == 0) {
+    *iter = 0;
+    cudaGraphSetConditional(hi, 1u);
+  }
+}
+
+__global__ void dl_iter_ctl(const int* __restrict__ step, int* __restrict__ iter, int maxiter, int percomp,
+                            const int* __restrict__ nactive, const double* __restrict__ red, double cdx2, double cLl2,
+                            const int* __restrict__ info, const int* __restrict__ errflag, int* __restrict__ status,
+                            int* __restrict__ iters, cudaGraphConditionalHandle hi) {
+  const int it = ++*iter;
+  const bool conv = percomp ? *nactive == 0 : (red[0] <= cdx2 && red[1] <= cLl2);
+  const bool nan = *errflag != INT_MAX, sing = *info != 0;
+  const int k = *step;
+  iters[k] = it;
+  if (nan || sing || conv || it >= maxiter) {
+    status[k] = nan ? 3 : sing ? 2 : conv ? 0 : 1;
+    cudaGraphSetConditional(hi, 0u);
+  } else {
+    cudaGraphSetConditional(hi, 1u);
+  }
+}
+
+__global__ void dl_store(const int* __restrict__ step, const double* __restrict__ x, int64_t n,
+                         double* __restrict__ states) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) states[int64_t(*step) * n + i] = x[i];
+}
+
+__global__ void dl_step_next(int* __restrict__ step, int nstep, const int* __restrict__ status,
+                             cudaGraphConditionalHandle hs) {
+  const int k = *step;
+  *step = k + 1;
+  cudaGraphSetConditional(hs, (status[k] == 0 && k + 1 < nstep) ? 1u : 0u);
+}
+
+cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, const cudaGraphNode_t* deps, size_t ndeps,
+                       const void* func, unsigned grid, unsigned block, void** args) {
+  cudaKernelNodeParams kp = {};
+  kp.func = const_cast<void*>(func);
+  kp.gridDim = dim3(grid);
+  kp.blockDim = dim3(block);
+  kp.sharedMemBytes = 0;
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  return cudaGraphAddKernelNode(node, g, deps, ndeps, &kp);
+}
+}  // namespace
+
+static int sweep_device_loop(mgpu_ctx* c, int64_t nstep, const double* times, const double* tvals,
+                             const mgpu_sweep_opts* opts, double* states, mgpu_stats* stats) {
+  Solver& S = *c->solver;
+  cudaStream_t st = c->stream;
+  const int64_t n = c->nX;
+  const bool percomp = opts->per_component != 0;
+  DevLoop d;
+  cudaGraph_t g = nullptr, bs = nullptr, bi = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<void*> owned;
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(st);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    for (void* p : owned) cudaFree(p);
+    cudaGetLastError();
+  };
+  auto fail = [&](cudaError_t e, const char* what) {
+    const int rc = set_err(c, MGPU_ERR_CUDA, std::string("device Newton loop: ") + what + ": " + cudaGetErrorString(e));
+    cleanup();
+    return rc;
+  };
+  auto alloc = [&](auto** p, size_t count) -> cudaError_t {
+    using T = typename std::remove_pointer<typename std::remove_reference<decltype(*p)>::type>::type;
+    const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) owned.push_back(*p);
+    return e;
+  };
+  cudaError_t e = cudaSuccess;
+  for (auto r : {alloc(&d.step, 1), alloc(&d.iter, 1), alloc(&d.status, nstep), alloc(&d.iters, nstep),
+                 alloc(&d.stepc, size_t(nstep) * 8), alloc(&d.tv, size_t(nstep) * c->ntval),
+                 alloc(&d.states, size_t(nstep) * n)})
+    if (e == cudaSuccess) e = r;
+  if (e != cudaSuccess) {
+    cleanup();
+    return set_err(c, MGPU_ERR_NOMEM, "device Newton loop: device allocation failed");
+  }
+  {
+    std::vector<double> sc(size_t(nstep) * 8, 0.0);
+    for (int64_t k = 0; k < nstep; ++k) sc[k * 8] = times[k];
+    std::vector<int> minus(nstep, -1);
+    if ((e = cudaMemcpy(d.stepc, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (c->ntval > 0 && (e = cudaMemcpy(d.tv, tvals, size_t(nstep) * c->ntval * sizeof(double),
+                                         cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (e = cudaMemcpy(d.status, minus.data(), nstep * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemset(d.step, 0, sizeof(int))) != cudaSuccess || (e = cudaMemset(d.iters, 0, nstep * sizeof(int))) != cudaSuccess)
+      return fail(e, "upload");
+  }
+  // graph: WHILE(steps) { begin ; WHILE(iterations) { iteration ; controller } ; store ; next }
+  cudaGraphConditionalHandle hs, hi;
+  if ((e = cudaGraphCreate(&g, 0)) != cudaSuccess) return fail(e, "graph");
+  if ((e = cudaGraphConditionalHandleCreate(&hs, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+    return fail(e, "conditional handle");
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hs;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t nsteps;
+  if ((e = cudaGraphAddNode(&nsteps, g, nullptr, nullptr, 0, &cp)) != cudaSuccess) return fail(e, "step loop node");
+  bs = cp.conditional.phGraph_out[0];
+  if ((e = cudaGraphConditionalHandleCreate(&hi, bs, 1, cudaGraphCondAssignDefault)) != cudaSuccess)
+    return fail(e, "conditional handle");
+  const int64_t ntv = c->ntval;
+  int* frozen = percomp ? S.frozen : nullptr;
+  int ncomp = S.ncomp;
+  cudaGraphNode_t kbegin, niter, kstore, knext;
+  {
+    void* args[] = {&d.step, &d.stepc, &d.tv, const_cast<int64_t*>(&ntv), &c->stepc, &c->tv, &d.iter, &frozen, &ncomp,
+                    &hi};
+    const int64_t cnt = std::max<int64_t>(std::max<int64_t>(ntv, 8), percomp ? ncomp : 0);
+    if ((e = add_kernel(bs, &kbegin, nullptr, 0, reinterpret_cast<const void*>(dl_step_begin), nb(cnt, 256), 256,
+                        args)) != cudaSuccess)
+      return fail(e, "step begin node");
+  }
+  cudaGraphNodeParams ip = {};
+  ip.type = cudaGraphNodeTypeConditional;
+  ip.conditional.handle = hi;
+  ip.conditional.type = cudaGraphCondTypeWhile;
+  ip.conditional.size = 1;
+  if ((e = cudaGraphAddNode(&niter, bs, &kbegin, nullptr, 1, &ip)) != cudaSuccess) return fail(e, "iteration loop node");
+  bi = ip.conditional.phGraph_out[0];
+  {
+    double* xs = c->x;
+    int64_t nn = n;
+    void* args[] = {&d.step, &xs, &nn, &d.states};
+    if ((e = add_kernel(bs, &kstore, &niter, 1, reinterpret_cast<const void*>(dl_store), nb(n, 256), 256, args)) !=
+        cudaSuccess)
+      return fail(e, "store node");
+    int ns = int(nstep);
+    void* args2[] = {&d.step, &ns, &d.status, &hs};
+    if ((e = add_kernel(bs, &knext, &kstore, 1, reinterpret_cast<const void*>(dl_step_next), 1, 1, args2)) !=
+        cudaSuccess)
+      return fail(e, "next-step node");
+  }
+  // the iteration body, captured
+  const double cdx2 = opts->maxdx * opts->maxdx, cLl2 = opts->maxLl * opts->maxLl;
+  if ((e = cudaStreamBeginCaptureToGraph(st, bi, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return fail(e, "capture");
+  {
+    launch_reset_errflag(c);
+    cudaMemsetAsync(S.info, 0, sizeof(int), st);
+    int rc = launch_assembly(c, MGPU_ASM_STATIC, nullptr);
+    if (rc == MGPU_OK) rc = factor_solve(c, S.info);
+    if (rc == MGPU_OK) {
+      decrement_kernel<<<nb(n, 256), 256, 0, st>>>(n, 0, 1, S.dx, c->scale, c->stepc, c->x, frozen, S.cod);
+      if (percomp) {
+        cudaMemsetAsync(S.nactive, 0, sizeof(int), st);
+        comp_converge<<<S.ncomp, 32, 0, st>>>(S.cn, S.cdof0, S.perm, S.dx, c->Ll, cdx2, cLl2, S.frozen, S.nactive);
+      }
+      dl_iter_ctl<<<1, 1, 0, st>>>(d.step, d.iter, opts->maxiter, int(percomp), S.nactive, S.red, cdx2, cLl2, S.info,
+                                   c->errflag, d.status, d.iters, hi);
+    }
+    cudaGraph_t out = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &out);
+    if (rc != MGPU_OK) {
+      cleanup();
+      return rc;
+    }
+    if (ec != cudaSuccess) return fail(ec, "capture of the iteration");
+  }
+  if ((e = cudaGraphInstantiate(&exec, g, 0)) != cudaSuccess) return fail(e, "instantiate");
+  if ((e = cudaGraphLaunch(exec, st)) != cudaSuccess) return fail(e, "launch");
+  std::vector<int> status(nstep), iters(nstep);
+  if ((e = cudaMemcpyAsync(status.data(), d.status, nstep * sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(iters.data(), d.iters, nstep * sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return fail(e, "sweep");
+  int64_t done = 0;
+  while (done < nstep && status[done] == 0) ++done;
+  for (int64_t k = 0; k < nstep && k <= done && k < int64_t(iters.size()); ++k) stats->niter_total += iters[k];
+  if (done > 0 && (e = cudaMemcpy(states, d.states, size_t(done) * n * sizeof(double), cudaMemcpyDeviceToHost)) !=
+                      cudaSuccess)
+    return fail(e, "states");
+  stats->nstep_done = int(done);
+  int rc = MGPU_OK;
+  if (done < nstep) {
+    const int k = int(done);
+    stats->fail_step = k + 1;
+    stats->fail_iter = iters[k];
+    if (status[k] == 3) {
+      int flag = INT_MAX;
+      cudaMemcpy(&flag, c->errflag, sizeof(int), cudaMemcpyDeviceToHost);
+      rc = nan_error(c, flag);
+    } else if (status[k] == 2) {
+      rc = singular_error(c, stats, k, iters[k]);
+    } else {
+      char msg[160];
+      snprintf(msg, sizeof msg, "no convergence of step %3d after %3d iterations", k + 1, iters[k]);
+      rc = set_err(c, MGPU_ERR_NOCONV, msg);
+    }
+  }
+  cleanup();
+  return rc;
+}
+
 extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double* times, double t0, int32_t nXder0,
                            const double* x0, const double* u, const double* tvals, const mgpu_sweep_opts* opts,
                            double* states, mgpu_stats* stats) {
@@ -1555,6 +1789,13 @@ extern "C" int mgpu_sweepx(mgpu_ctx* c, int32_t OX, int64_t nstep, const double*
   // the multifrontal solve decides its FP64 fallback on the host: launched step by step
   if (opts->fixed_iter > 0 && opts->fixed_iter < kInfoSlots && !opts->no_graph && !sparse)
     return sweep_graph(c, OX, nstep, times, t0, tvals, opts, states, stats);
+  if (opts->device_loop) {
+    if (OX != 0 || sparse || opts->fixed_iter > 0 || S.path == PATH_TORN32)
+      return set_err(c, MGPU_ERR_UNSUPPORTED, "the device Newton loop runs SweepX{0} with a banded FP64 or F32IR "
+                                              "solver and the convergence test");
+    if (nstep == 0) return MGPU_OK;
+    return sweep_device_loop(c, nstep, times, tvals, opts, states, stats);
+  }
   const int nder = OX + 1;
   double told = t0;
   for (int64_t step = 0; step < nstep; ++step) {

@@ -748,57 +748,103 @@ __global__ void sp_fwdb_fin(const SpFrontDev* __restrict__ fr, const int32_t* __
     cvec[Fr.eoff + (t - Fr.p)] = V[Fr.idx + t];
 }
 
-// backward: V = y of the pivots; a front without update rows solves its last
-// pivot tile here (the others when their last update block is done)
+// backward: V = y of the pivots
+__global__ void sp_bwdb_init(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
+                             const double* __restrict__ w, double* __restrict__ V, const int* __restrict__ conv) {
+  if (*conv) return;
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t < Fr.p) V[Fr.idx + t] = w[Fr.pos0 + t];
+}
+
+// backward, the update columns all at once: block (t, b) forms the products of
+// pivot tile t with update column block b (x from the ancestors' solution) into
+// P[poff(front) + b·p + row]; sp_bwdb_red subtracts them in block order
 template <class T>
-__global__ void __launch_bounds__(kSBThreads) sp_bwdb_init(const SpFrontDev* __restrict__ fr,
+__global__ void __launch_bounds__(kSBThreads) sp_bwdb_u12(const SpFrontDev* __restrict__ fr,
+                                                          const int32_t* __restrict__ flist,
+                                                          const int64_t* __restrict__ poff,
+                                                          const int32_t* __restrict__ fidx,
+                                                          const T* __restrict__ F, const double* __restrict__ w,
+                                                          double* __restrict__ P, const int* __restrict__ conv) {
+  if (*conv) return;
+  const int32_t f = flist[blockIdx.z];
+  const SpFrontDev Fr = fr[f];
+  const int m = Fr.m, p = Fr.p, t = int(blockIdx.x), b = int(blockIdx.y);
+  if (t >= sb_np(p) || b >= sb_nu(m, p)) return;
+  __shared__ T xs[kSB];
+  __shared__ double part[4][kSB];
+  const int c0 = p + b * kSB, cb = min(kSB, m - c0);
+  if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(w[fidx[Fr.idx + c0 + threadIdx.x]]) : T(0);
+  __syncthreads();
+  const int r0 = t * kSB, r1 = min(r0 + kSB, p);
+  const int tid = threadIdx.x, rr = tid & (kSB - 1), cq = tid >> 6;
+  const int r = r0 + rr;
+  T sacc = T(0);
+  if (r < r1) {
+    const T* col = F + Fr.off + r + int64_t(c0) * m;
+    const int cbeg = cq * 16;
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      if (cbeg + c < cb) sacc = fma(col[int64_t(cbeg + c) * m], xs[cbeg + c], sacc);
+  }
+  part[cq][rr] = double(sacc);
+  __syncthreads();
+  if (tid < kSB && r0 + tid < r1)
+    P[poff[f] + int64_t(b) * p + r0 + tid] = ((part[0][tid] + part[1][tid]) + part[2][tid]) + part[3][tid];
+}
+
+__global__ void sp_bwdb_red(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
+                            const int64_t* __restrict__ poff, const double* __restrict__ P, double* __restrict__ V,
+                            const int* __restrict__ conv) {
+  if (*conv) return;
+  const int32_t f = flist[blockIdx.y];
+  const SpFrontDev Fr = fr[f];
+  const int r = blockIdx.x * kThreads + threadIdx.x;
+  if (r >= Fr.p) return;
+  const int nu = sb_nu(Fr.m, Fr.p);
+  double s = 0.0;
+  for (int b = 0; b < nu; ++b) s += P[poff[f] + int64_t(b) * Fr.p + r];
+  V[Fr.idx + r] -= s;
+}
+
+// backward: the triangle of the last pivot tile, once the update columns are in
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_bwdb_last(const SpFrontDev* __restrict__ fr,
                                                            const int32_t* __restrict__ flist,
-                                                           const T* __restrict__ F, const double* __restrict__ w,
-                                                           double* __restrict__ V, const int* __restrict__ conv) {
+                                                           const T* __restrict__ F, double* __restrict__ V,
+                                                           const int* __restrict__ conv) {
   if (*conv) return;
   const SpFrontDev Fr = fr[flist[blockIdx.x]];
-  double* Vf = V + Fr.idx;
-  for (int t = threadIdx.x; t < Fr.p; t += kSBThreads) Vf[t] = w[Fr.pos0 + t];
-  if (Fr.m > Fr.p) return;
   __shared__ T Dg[kSB][kSB + 1];
   __shared__ T vs[kSB];
+  double* Vf = V + Fr.idx;
   const int r0 = (sb_np(Fr.p) - 1) * kSB, nr = Fr.p - r0;
-  if (threadIdx.x < kSB) vs[threadIdx.x] = threadIdx.x < nr ? T(w[Fr.pos0 + r0 + threadIdx.x]) : T(0);
-  __syncthreads();
+  if (threadIdx.x < kSB) vs[threadIdx.x] = threadIdx.x < nr ? T(Vf[r0 + threadIdx.x]) : T(0);
   sb_tri_upper<T>(F + Fr.off, Fr.m, r0, nr, Dg, vs, Vf);
 }
 
-// backward, step s: column block b = (blocks of the front) − 1 − s, descending
-// over the update blocks (x from the ancestors' solution in w) and then the
-// pivot blocks (x solved in V); the pivot tiles above it take its products and
-// the block of tile b − 1 then solves that tile
+// backward, step s over the pivot blocks: column block b = np − 1 − s (solved);
+// the pivot tiles above it take its products and the block of tile b − 1 then
+// solves that tile
 template <class T>
 __global__ void __launch_bounds__(kSBThreads) sp_bwdb_step(const SpFrontDev* __restrict__ fr,
                                                            const int32_t* __restrict__ flist, int s,
-                                                           const int32_t* __restrict__ fidx,
-                                                           const T* __restrict__ F, const double* __restrict__ w,
-                                                           double* __restrict__ V, const int* __restrict__ conv) {
+                                                           const T* __restrict__ F, double* __restrict__ V,
+                                                           const int* __restrict__ conv) {
   if (*conv) return;
   const SpFrontDev Fr = fr[flist[blockIdx.y]];
-  const int m = Fr.m, p = Fr.p, np = sb_np(p), nb = np + sb_nu(m, p);
-  const int b = nb - 1 - s, t = int(blockIdx.x);
-  if (b < 1 || t >= min(b, np)) return;
+  const int m = Fr.m, p = Fr.p, np = sb_np(p);
+  const int b = np - 1 - s, t = int(blockIdx.x);
+  if (b < 1 || t >= b) return;
   __shared__ T xs[kSB];
   __shared__ double part[4][kSB];
   __shared__ T Dg[kSB][kSB + 1];
   __shared__ T vs[kSB];
   double* Vf = V + Fr.idx;
   const T* A = F + Fr.off;
-  int c0, cb;
-  if (b >= np) {
-    c0 = p + (b - np) * kSB;
-    cb = min(kSB, m - c0);
-    if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(w[fidx[Fr.idx + c0 + threadIdx.x]]) : T(0);
-  } else {
-    c0 = b * kSB;
-    cb = min(kSB, p - c0);
-    if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(Vf[c0 + threadIdx.x]) : T(0);
-  }
+  const int c0 = b * kSB, cb = min(kSB, p - c0);
+  if (threadIdx.x < kSB) xs[threadIdx.x] = threadIdx.x < cb ? T(Vf[c0 + threadIdx.x]) : T(0);
   __syncthreads();
   const int r0 = t * kSB, r1 = min(r0 + kSB, p);
   const double v = sb_update<T>(A, m, r0, r1, c0, cb, xs, part, Vf);
@@ -964,11 +1010,11 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
 // with fewer than sp.big_pivots pivots (the tail of the height's list) take
 // the one-block-per-front kernels, the others the blocked ones.
 template <class T>
-cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int sweeps) {
+cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int it0, int it1) {
   cudaStream_t st = c->stream;
   const int64_t n = sp.n;
   const size_t smem = size_t(std::max(sp.max_m_small, 1)) * sizeof(double);
-  for (int it = 0; it < sweeps; ++it) {
+  for (int it = it0; it < it1; ++it) {
     const double* r = b;
     if (it > 0) {
       sp_residual<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_rptr, sp.d_rq, sp.d_rcol, c->nzval, sp.xs, b,
@@ -1034,11 +1080,20 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
         ++c->launches;
       }
       if (nbig > 0) {
-        sp_bwdb_init<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.w, sp.V, sp.flags);
+        const unsigned gp = nblocks(sp.h_pmax[h], kThreads);
+        sp_bwdb_init<<<dim3(gp, unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.w, sp.V, sp.flags);
         ++c->launches;
-        for (int s2 = 0; s2 + 1 < sp.h_bnt[h]; ++s2) {
-          sp_bwdb_step<T><<<dim3(unsigned(sp.h_bnp[h]), unsigned(nbig)), kSBThreads, 0, st>>>(
-              sp.d_fr, fl, s2, sp.d_fidx, F, sp.w, sp.V, sp.flags);
+        if (sp.h_bnu[h] > 0) {
+          sp_bwdb_u12<T><<<dim3(unsigned(sp.h_bnp[h]), unsigned(sp.h_bnu[h]), unsigned(nbig)), kSBThreads, 0, st>>>(
+              sp.d_fr, fl, sp.d_poff, sp.d_fidx, F, sp.w, sp.P, sp.flags);
+          sp_bwdb_red<<<dim3(gp, unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.d_poff, sp.P, sp.V, sp.flags);
+          c->launches += 2;
+        }
+        sp_bwdb_last<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.V, sp.flags);
+        ++c->launches;
+        for (int s2 = 0; s2 + 1 < sp.h_bnp[h]; ++s2) {
+          sp_bwdb_step<T><<<dim3(unsigned(sp.h_bnp[h]), unsigned(nbig)), kSBThreads, 0, st>>>(sp.d_fr, fl, s2, F, sp.V,
+                                                                                              sp.flags);
           ++c->launches;
         }
         sp_bwdb_fin<<<dim3(nblocks(sp.h_pmax[h], kThreads), unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.V,
@@ -1053,6 +1108,26 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
     ++c->launches;
   }
   return cudaGetLastError();
+}
+
+// the refinement sweeps in batches: after each batch the host reads the
+// convergence flag, so that few sweeps are enqueued after convergence
+// (every kernel of a converged sweep returns at once, but is still launched)
+template <class T>
+cudaError_t refine_batches(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int sweeps, int first) {
+  int done = 0;
+  while (done < sweeps) {
+    const int nb_ = done == 0 ? std::min(first, sweeps) : std::min(2, sweeps - done);
+    cudaError_t e = refine<T>(c, sp, F, b, done, done + nb_);
+    if (e != cudaSuccess) return e;
+    done += nb_;
+    if (done >= sweeps) break;
+    e = cudaMemcpyAsync(sp.hflags, sp.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return e;
+    if (sp.hflags[0] != 0 || sp.hflags[3] != 0) break;
+  }
+  return cudaSuccess;
 }
 
 template <class T>
@@ -1132,6 +1207,9 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   sp.h_bnt.assign(H, 0);
   sp.h_spmax.assign(H, 0);
   sp.h_sumax.assign(H, 0);
+  sp.h_bnu.assign(H, 0);
+  std::vector<int64_t> poff(nf, 0);
+  int64_t psize = 0;
   for (int h = 0; h < H; ++h) {
     auto& L = byh[h];
     std::stable_sort(L.begin(), L.end(), [&](int32_t a, int32_t b) { return A.fronts[a].p > A.fronts[b].p; });
@@ -1151,6 +1229,9 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
         sp.h_nbig[h]++;
         sp.h_bnp[h] = std::max(sp.h_bnp[h], np);
         sp.h_bnt[h] = std::max(sp.h_bnt[h], np + nu);
+        sp.h_bnu[h] = std::max(sp.h_bnu[h], nu);
+        poff[f] = psize;
+        psize += int64_t(nu) * S.p;
       } else {
         sp.h_spmax[h] = std::max(sp.h_spmax[h], S.p);
         sp.h_sumax[h] = std::max(sp.h_sumax[h], S.m - S.p);
@@ -1244,6 +1325,8 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaMalloc(&sp.cvec, std::max<size_t>(A.emap.size(), 1) * sizeof(double)));
   ok(cudaMalloc(&sp.w, n * sizeof(double)));
   ok(cudaMalloc(&sp.V, std::max<size_t>(A.fidx.size(), 1) * sizeof(double)));
+  ok(cudaMalloc(&sp.P, std::max<int64_t>(psize, 1) * sizeof(double)));
+  ok(upload(&sp.d_poff, poff));
   ok(cudaMalloc(&sp.tw, n * sizeof(double)));
   ok(cudaMalloc(&sp.yacc, n * sizeof(double)));
   ok(cudaMalloc(&sp.r, n * sizeof(double)));
@@ -1281,7 +1364,8 @@ void sparse_destroy(SparseDev*& sp) {
   void* ps[] = {sp->d_fr, sp->d_lf, sp->d_ea, sp->d_clist, sp->d_fidx, sp->d_emap, sp->d_amap, sp->d_aq,
                 sp->d_acol, sp->d_perm, sp->d_diag, sp->d_colptr, sp->d_rowval, sp->d_rptr, sp->d_rq, sp->d_rcol,
                 sp->F32, sp->F64, sp->prev,
-                sp->D, sp->cvec, sp->w, sp->V, sp->tw, sp->yacc, sp->r, sp->xs, sp->nrm, sp->flags};
+                sp->D, sp->cvec, sp->w, sp->V, sp->P, sp->d_poff, sp->tw, sp->yacc, sp->r, sp->xs, sp->nrm,
+                sp->flags};
   for (void* p : ps) cudaFree(p);
   if (sp->hflags) cudaFreeHost(sp->hflags);
   for (cudaEvent_t ev : sp->ev)
@@ -1311,7 +1395,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
     MG_CUDA(cudaEventRecord(sp.ev[0], st));
     MG_CUDA((factorise<float, kNB32>(c, sp, sp.F32, 1e-10f)));
     MG_CUDA(cudaEventRecord(sp.ev[1], st));
-    MG_CUDA(refine<float>(c, sp, sp.F32, rhs, kSparseSweeps));
+    MG_CUDA(refine_batches<float>(c, sp, sp.F32, rhs, kSparseSweeps, 8));
     MG_CUDA(cudaEventRecord(sp.ev[2], st));
     MG_CUDA(cudaMemcpyAsync(sp.hflags, sp.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaStreamSynchronize(st));
@@ -1338,7 +1422,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
     MG_CUDA(cudaEventRecord(sp.ev[0], st));
     MG_CUDA((factorise<double, kNB64>(c, sp, sp.F64, 0.0)));
     MG_CUDA(cudaEventRecord(sp.ev[1], st));
-    MG_CUDA(refine<double>(c, sp, sp.F64, rhs, kSparseSweeps64));
+    MG_CUDA(refine_batches<double>(c, sp, sp.F64, rhs, kSparseSweeps64, 4));
     MG_CUDA(cudaEventRecord(sp.ev[2], st));
     MG_CUDA(cudaMemcpyAsync(sp.hflags, sp.flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
     MG_CUDA(cudaStreamSynchronize(st));

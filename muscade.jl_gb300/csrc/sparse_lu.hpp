@@ -52,6 +52,7 @@ struct SparseDev {
   // their most pivot tiles and most row tiles (pivot + update)
   std::vector<int32_t> h_nbig, h_bnp, h_bnt;
   std::vector<int32_t> h_spmax, h_sumax;       // most pivots / update rows of the other fronts
+  std::vector<int32_t> h_bnu;                  // most update column blocks of the blocked fronts
   int max_m_small = 0;                         // largest front of the one-block substitutions
   int big_pivots = 0;                          // fronts with this many pivots or more: blocked substitutions
   bool tensor_cores = false;                   // FP32 trailing update on the tensor cores (TF32 ×3; MGPU_SPARSE_TC=1)
@@ -79,6 +80,8 @@ struct SparseDev {
   double* cvec = nullptr;       // children's update vectors (forward substitution)
   double* w = nullptr;          // [n] elimination order work vector
   double* V = nullptr;          // [Σ m] the blocked substitutions' front vectors (at each front's idx)
+  double* P = nullptr;          // partial products of the blocked fronts' update columns [Σ p·nu]
+  int64_t* d_poff = nullptr;    // [nfront] offset of each blocked front's partials in P
   double* tw = nullptr;         // [n] U₁₂ x_u of each pivot (backward substitution)
   double* yacc = nullptr;       // [n] accumulated scaled solution (elimination order)
   double* r = nullptr;          // [n] residual (model order)

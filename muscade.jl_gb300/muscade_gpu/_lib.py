@@ -79,7 +79,7 @@ class Newmark(ctypes.Structure):
 class SweepOpts(ctypes.Structure):
     _fields_ = [("beta", ctypes.c_double), ("gamma", ctypes.c_double), ("maxiter", ctypes.c_int32),
                 ("maxdx", ctypes.c_double), ("maxLl", ctypes.c_double), ("fixed_iter", ctypes.c_int32),
-                ("per_component", ctypes.c_int32), ("no_graph", ctypes.c_int32)]
+                ("per_component", ctypes.c_int32), ("no_graph", ctypes.c_int32), ("device_loop", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):

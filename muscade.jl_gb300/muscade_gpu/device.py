@@ -129,7 +129,7 @@ class DeviceModel:
         cw = np.ascontiguousarray(np.broadcast_to(cost_w, cd.shape), dtype=np.float64)
         cy = np.ascontiguousarray(np.zeros((nstep, 0)) if cost_y is None else cost_y, dtype=np.float64)
         cy = cy.reshape(nstep, len(cd))
-        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0)
+        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0, 0)
         cost = ctypes.c_double()
         dA = np.zeros(max(self.nA, 1))
         dtv = np.zeros((nstep, self.ntval)) if load_gradient and self.ntval else None
@@ -163,7 +163,7 @@ class DeviceModel:
         cy = np.ascontiguousarray(np.zeros((nstep, 0)) if cost_y is None else cost_y, dtype=np.float64)
         cy = cy.reshape(nstep, len(cd))
         sl = np.ascontiguousarray(sel, dtype=np.int64).reshape(-1)
-        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0)
+        opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, 0, 0, 0, 0)
         dC = np.zeros(len(sl))
         dX = np.zeros((nstep, len(sl), OX + 1, self.nX)) if states else None
         stats = L.Stats()
@@ -390,11 +390,13 @@ class DeviceModel:
 
     # ---------------------------------------------------------------- solver
     def sweepx(self, OX, times, t0, X0, U=None, beta=0.25, gamma=0.5, maxiter=50, maxdx=1e-5, maxLl=math.inf,
-               fixed_iter=0, per_component=False, graph=True):
+               fixed_iter=0, per_component=False, graph=True, device_loop=False):
         """Whole SweepX{OX} on the device.  fixed_iter > 0 runs exactly that many
         Newton iterations per step (replayed from a captured CUDA graph unless
         graph=False); per_component applies the convergence test to each
-        connected component (independent models) on its own."""
+        connected component (independent models) on its own; device_loop runs
+        the load steps and Newton iterations of a SweepX{0} as one graph launch
+        with device-side loops (see mgpu_sweep_opts.device_loop)."""
         times = np.ascontiguousarray(times, dtype=np.float64)
         nstep = len(times)
         X0 = [np.asarray(v, dtype=np.float64) for v in X0][: OX + 1]
@@ -402,7 +404,7 @@ class DeviceModel:
         u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)
         tv = np.ascontiguousarray(np.stack([self.tvals(t) for t in times]) if self.ntval else np.zeros((nstep, 0)))
         opts = L.SweepOpts(beta, gamma, maxiter, maxdx, maxLl, fixed_iter, int(bool(per_component)),
-                           int(not graph))
+                           int(not graph), int(bool(device_loop)))
         states = np.zeros((nstep, OX + 1, self.nX))
         stats = L.Stats()
         rc = self.lib.mgpu_sweepx(self.ctx, OX, nstep, L.ptr(times), float(t0), len(X0), L.ptr(x0), L.ptr(u),

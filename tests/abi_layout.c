@@ -23,7 +23,7 @@ int main(void) {
   S(mgpu_sweep_opts);
   F(mgpu_sweep_opts, beta), F(mgpu_sweep_opts, gamma), F(mgpu_sweep_opts, maxiter), F(mgpu_sweep_opts, maxdx);
   F(mgpu_sweep_opts, maxLl), F(mgpu_sweep_opts, fixed_iter), F(mgpu_sweep_opts, per_component);
-  F(mgpu_sweep_opts, no_graph);
+  F(mgpu_sweep_opts, no_graph), F(mgpu_sweep_opts, device_loop);
   S(mgpu_stats);
   F(mgpu_stats, nstep_done), F(mgpu_stats, niter_total), F(mgpu_stats, fail_step), F(mgpu_stats, fail_iter);
   F(mgpu_stats, last_dx), F(mgpu_stats, last_Ll);
