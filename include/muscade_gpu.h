@@ -169,6 +169,14 @@ int mgpu_element_eval(mgpu_ctx *ctx, int32_t igroup, int32_t nXder, const double
 int mgpu_element_lagrangian(mgpu_ctx *ctx, int32_t igroup, int32_t nXder, const double *lam, const double *X,
                             const double *U, const double *A, const double *tv, double *L, double *dL, double *d2L);
 
+/* Element results of the EulerBeam3D group `igroup`, like getresult
+ * (src/Output.jl:131-181) of the values its residual makes requestable
+ * (toolbox/BeamElement.jl:151-189): for each of nstate states X[nstate][nX]
+ * and each element, 50 values: ε, rₛₘ (9, column-major), then per Gauss point
+ * (4) x (3), κ (3), fᵢ = EA ε and mᵢ = (GJ κ₁, EI₃ κ₂, EI₂ κ₃) (the EI scale
+ * of an A-dof applied).  out[nstate][nele][50]. */
+int mgpu_beam_results(mgpu_ctx *ctx, int32_t igroup, int64_t nstate, const double *X, double *out);
+
 /* Device-resident assembly for throughput measurement: upload a state once,
  * then assemble repeatedly into device buffers.  mgpu_time_assemble runs
  * `reps` assemblies timed with CUDA events on the context stream (optionally

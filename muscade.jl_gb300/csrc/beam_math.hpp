@@ -713,4 +713,78 @@ MG_HD void beam_element(const BeamConst& c, const double* X0, const double* X1, 
   }
 }
 
+// ---- element results of one beam at a state (getresult of the residual's
+// requestable values, toolbox/BeamElement.jl:151-189): the element record's
+// 69 fields f, the dofs X0[12], the EI scale a (1 without an A-dof); out[50]:
+// ε, rₛₘ (9, column-major), then per Gauss point x (3), κ (3), fᵢ = EA ε and
+// mᵢ = (GJ κ₁, a EI₃ κ₂, a EI₂ κ₃).  The rotation core is the element's own
+// (static jets; only the values are used), the rest follows kinematics
+// (:177-189): uₗ₂ = rₛₘᵀ d − L/2 e₁ and vₗ₂ = rₛₘᵀΔv.
+MG_HD void beam_results(const double* f, const double* X0, double a, double* out) {
+  const double* rm = f + 3;
+  const double* cm = f;
+  const double* zgp = f + 12;
+  const double* tgm = f + 18;
+  const double* tge = f + 21;
+  const double* ya = f + 24;
+  const double* yu = f + 28;
+  const double* yv = f + 32;
+  const double* ka = f + 36;
+  const double* ku = f + 40;
+  const double* kv = f + 44;
+  const double L = f[48];
+  const double EA = f[53], EI2 = a * f[54], EI3 = a * f[55], GJ = f[56];
+  TJ<false, 3> r1[9];
+  TJ<false> dv[3], rsm[9];
+  {
+    TJ<false, 3> r2[9];
+    TJ<false> Q[9];
+    const double zero[3] = {0.0, 0.0, 0.0};
+    rodrigues_nodal<false>(X0 + 3, zero, zero, r1);
+    rodrigues_nodal<false>(X0 + 9, zero, zero, r2);
+    mul_abt_nodes(r2, r1, Q);
+    rodrigues_inv(Q, dv, 0.5);
+  }
+  {
+    double rmc[9];
+    for (int k = 0; k < 9; ++k) rmc[k] = rm[k];
+    TJ<false, 3> r1m[9];
+    mul_ac(r1, rmc, r1m);
+    TJ<false> rD[9];
+    rodrigues(dv, rD);
+    mul_ab_node1(rD, r1m, rsm);
+  }
+  double r[9], d[3], cs[3], ul2[3], vl2[3];
+  for (int k = 0; k < 9; ++k) r[k] = rsm[k].v;
+  for (int i = 0; i < 3; ++i) {
+    d[i] = 0.5 * (X0[6 + i] - X0[i]) + 0.5 * tgm[i];
+    cs[i] = 0.5 * (X0[i] + X0[6 + i]) + cm[i];
+  }
+  for (int k = 0; k < 3; ++k) {
+    ul2[k] = r[3 * k] * d[0] + r[3 * k + 1] * d[1] + r[3 * k + 2] * d[2];
+    vl2[k] = r[3 * k] * dv[0].v + r[3 * k + 1] * dv[1].v + r[3 * k + 2] * dv[2].v;
+  }
+  ul2[0] -= 0.5 * L;
+  const double eps = sqrt((ul2[0] + 0.5 * L) * (ul2[0] + 0.5 * L) + ul2[1] * ul2[1] + ul2[2] * ul2[2]) * 2.0 / L - 1.0;
+  out[0] = eps;
+  for (int k = 0; k < 9; ++k) out[1 + k] = r[k];
+  for (int g = 0; g < 4; ++g) {
+    double* o = out + 10 + 10 * g;
+    const double k0 = ka[g] * vl2[0];
+    const double k1 = ku[g] * ul2[1] + kv[g] * vl2[2];
+    const double k2 = ku[g] * ul2[2] - kv[g] * vl2[1];
+    const double y[3] = {ya[g] * ul2[0], yu[g] * ul2[1] + yv[g] * vl2[2], yu[g] * ul2[2] - yv[g] * vl2[1]};
+    double pp[3];
+    for (int i = 0; i < 3; ++i) pp[i] = tge[i] * zgp[g] + y[i];
+    for (int i = 0; i < 3; ++i) o[i] = r[i] * pp[0] + r[i + 3] * pp[1] + r[i + 6] * pp[2] + cs[i];
+    o[3] = k0;
+    o[4] = k1;
+    o[5] = k2;
+    o[6] = EA * eps;
+    o[7] = GJ * k0;
+    o[8] = EI3 * k1;
+    o[9] = EI2 * k2;
+  }
+}
+
 }  // namespace mgpu

@@ -29,6 +29,7 @@ struct DevGroup {
   int32_t maxder = 0;       // DOFCOST: highest time derivative a cost reads
   bool distinct = true;     // cost groups: no two elements write the same gradient entry
   std::vector<int64_t> h_indexX;  // host copy (1-based) for asm queries
+  std::vector<double> h_edata;    // EULERBEAM3D: the element records as given (for mgpu_beam_results)
 };
 
 // element kinds with one time value per element (F(t), c(t) or the cost target y(t))

@@ -589,6 +589,7 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
       MG_CUDA(cudaMemcpy(D.aidx, aidx.data(), aidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     }
     std::vector<double> cd;
+    if (G.kind == MGPU_EULERBEAM3D) D.h_edata.assign(G.edata, G.edata + G.nele * BEAM_NFIELD);
     if (G.kind == MGPU_EULERBEAM3D) {
       D.nfield = BEAM_NCONST;
       cd.resize(size_t(D.nfield) * G.nele);
@@ -1021,5 +1022,57 @@ extern "C" int mgpu_element_eval(mgpu_ctx* c, int32_t g, int32_t nXder, const do
   cudaFree(dRv);
   cudaFree(dK);
   cudaFree(dH);
+  return MGPU_OK;
+}
+
+// ------------------------------------------------------------------ element results
+__global__ void beam_results_kernel(int64_t nele, int64_t nstate, int64_t nX, const int32_t* __restrict__ idx,
+                                    const double* __restrict__ fields, const int32_t* __restrict__ aidx,
+                                    const double* __restrict__ Avec, const double* __restrict__ X,
+                                    double* __restrict__ out) {
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= nele * nstate) return;
+  const int64_t e = q % nele, k = q / nele;
+  double X0[12];
+  for (int i = 0; i < 12; ++i) X0[i] = X[k * nX + __ldg(idx + i * nele + e)];
+  const double a = aidx ? Avec[aidx[e]] : 1.0;
+  beam_results(fields + e * BEAM_NFIELD, X0, a, out + q * 50);
+}
+
+extern "C" int mgpu_beam_results(mgpu_ctx* c, int32_t g, int64_t nstate, const double* X, double* out) {
+  if (!c || g < 0 || g >= int32_t(c->groups.size()) || nstate < 0 || (nstate > 0 && (!X || !out)))
+    return set_err(c, MGPU_ERR_ARG, "mgpu_beam_results: bad arguments");
+  const DevGroup& G = c->groups[g];
+  if (G.kind != MGPU_EULERBEAM3D) return set_err(c, MGPU_ERR_ARG, "mgpu_beam_results: not an EulerBeam3D group");
+  const int64_t n = G.nele * nstate;
+  if (n == 0) return MGPU_OK;
+  MG_CUDA(cudaSetDevice(c->device));
+  double *df = nullptr, *dX = nullptr, *dout = nullptr;
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(df);
+    cudaFree(dX);
+    cudaFree(dout);
+  };
+  cudaError_t e = cudaMalloc(&df, G.h_edata.size() * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dX, size_t(nstate) * c->nX * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&dout, size_t(n) * 50 * sizeof(double));
+  if (e != cudaSuccess) {
+    cleanup();
+    return set_err(c, MGPU_ERR_NOMEM, std::string("mgpu_beam_results: ") + cudaGetErrorString(e));
+  }
+  e = cudaMemcpyAsync(df, G.h_edata.data(), G.h_edata.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dX, X, size_t(nstate) * c->nX * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    beam_results_kernel<<<nblk(n, 128), 128, 0, c->stream>>>(G.nele, nstate, c->nX, G.idx, df, G.aidx, c->Avec, dX,
+                                                             dout);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, dout, size_t(n) * 50 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cleanup();
+  if (e != cudaSuccess) return set_err(c, MGPU_ERR_CUDA, std::string("mgpu_beam_results: ") + cudaGetErrorString(e));
   return MGPU_OK;
 }

@@ -115,7 +115,7 @@ SYMBOLS = ["mgpu_create", "mgpu_destroy", "mgpu_last_error", "mgpu_nnz", "mgpu_g
            "mgpu_assemble_beams_noalloc", "mgpu_set_linear_solver", "mgpu_linear_solver_info", "mgpu_set_A",
            "mgpu_adjoint_sweepx", "mgpu_host_register", "mgpu_host_unregister", "mgpu_autotune",
            "mgpu_assemble_async", "mgpu_assemble_wait", "mgpu_sparse_info", "mgpu_element_lagrangian",
-           "mgpu_tc_gemm_check", "mgpu_launch_count", "mgpu_sensitivity_sweepx"]
+           "mgpu_tc_gemm_check", "mgpu_launch_count", "mgpu_sensitivity_sweepx", "mgpu_beam_results"]
 
 _lib = None
 
@@ -166,6 +166,7 @@ def load():
     L.mgpu_adjoint_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32, pd,
                                       pd, pd, pd, P(Stats)]
     L.mgpu_element_lagrangian.argtypes = [vp, i32, i32, pd, pd, pd, pd, pd, pd, pd, pd]
+    L.mgpu_beam_results.argtypes = [vp, i32, i64, pd, pd]
     L.mgpu_sensitivity_sweepx.argtypes = [vp, i32, i64, pd, d, i32, pd, pd, pd, P(SweepOpts), i64, pi64, pd, pd, i32,
                                           pi64, pd, pd, P(Stats)]
     pf = P(ctypes.c_float)

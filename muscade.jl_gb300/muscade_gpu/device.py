@@ -373,6 +373,21 @@ class DeviceModel:
         self._check(rc)
         return Lv, dL, d2L
 
+    BEAM_RESULTS = ("eps", "rsm", "x", "kappa", "fi", "mi")
+
+    def beam_results(self, ig, X):
+        """getresult of an EulerBeam3D group at states X[nstate][nX] (mgpu_beam_results):
+        a dict of arrays eps (nstate, nele), rsm (nstate, nele, 3, 3), and per Gauss
+        point x, kappa, mi (nstate, nele, 4, 3) and fi (nstate, nele, 4)."""
+        X = np.ascontiguousarray(np.atleast_2d(X), dtype=np.float64)
+        nstate = X.shape[0]
+        nele = self.model.groups[ig].nele
+        out = np.zeros((nstate, nele, 50))
+        self._check(self.lib.mgpu_beam_results(self.ctx, ig, nstate, L.ptr(X), L.ptr(out)))
+        gp = out[:, :, 10:].reshape(nstate, nele, 4, 10)
+        return {"eps": out[:, :, 0], "rsm": out[:, :, 1:10].reshape(nstate, nele, 3, 3).transpose(0, 1, 3, 2),
+                "x": gp[..., 0:3], "kappa": gp[..., 3:6], "fi": gp[..., 6], "mi": gp[..., 7:10]}
+
     def upload_state(self, X, U=None, t=0.0):
         x = np.ascontiguousarray(np.concatenate([np.asarray(v, dtype=np.float64) for v in X]))
         u = np.ascontiguousarray(U if U is not None else np.zeros(self.nU), dtype=np.float64)

@@ -104,6 +104,33 @@ int oracle_bar_construct(int64_t n, const double* c1, const double* c2, const do
   return 0;
 }
 
+// Element results of EulerBeam3D at states X[n][12] (getresult of the
+// residual's requestable values, toolbox/BeamElement.jl:151-189 with
+// kinematics :177-189 and resultants :28-62): out[n][50] = ε, rₛₘ (9,
+// column-major), then per Gauss point x (3), κ (3), fᵢ, mᵢ (3).
+int oracle_beam_results(int64_t n, const double* ele, const double* X, double* out) {
+  for (int64_t e = 0; e < n; ++e) {
+    BeamEle o;
+    std::memcpy(&o, ele + 69 * e, sizeof(BeamEle));
+    BeamKin<double> k;
+    kinematics(o, X + 12 * e, k);
+    double* r = out + 50 * e;
+    r[0] = k.eps;
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) r[1 + i + 3 * j] = k.rsm.m[i + 3 * j];
+    for (int g = 0; g < 4; ++g) {
+      double* q = r + 10 + 10 * g;
+      for (int i = 0; i < 3; ++i) q[i] = k.x[g].v[i];
+      for (int i = 0; i < 3; ++i) q[3 + i] = k.kappa[g].v[i];
+      q[6] = o.mat.EA * k.eps;
+      q[7] = o.mat.GJ * k.kappa[g].v[0];
+      q[8] = o.mat.EI3 * k.kappa[g].v[1];
+      q[9] = o.mat.EI2 * k.kappa[g].v[2];
+    }
+  }
+  return 0;
+}
+
 // Number of partials returned in J for a given mode.
 int oracle_nj(int nx, int ND, int nU, int mode) {
   if (mode == 0) return nx * ND + nU;

@@ -50,6 +50,7 @@ def lib():
         _lib.oracle_rodrigues.argtypes = [P, P]
         _lib.oracle_rodrigues_roundtrip.argtypes = [P, P, P]
         _lib.oracle_nj.argtypes = [i32, i32, i32, i32]
+        _lib.oracle_beam_results.argtypes = [i64, P, P, P]
         PI = ctypes.POINTER(ctypes.c_int64)
         _lib.oracle_scatter.argtypes = [i64, i32, i32, PI, PI, P, P, i32, P, P]
         _lib.oracle_scatter.restype = None
@@ -122,6 +123,16 @@ def _eval(kind, ele, X, U=None, t=0.0, mode=0, a1=0.0, b1=0.0, scaleX=None, a=No
 def beam_eval(ele, X, U=None, **kw):
     """Residual and partials of EulerBeam3D elements (see oracle_api.cpp for modes)."""
     return _eval("beam", ele, X, U, **kw)
+
+
+def beam_results(ele, X):
+    """EulerBeam3D element results (oracle_beam_results): ele (n, 69), X (n, 12) -> (n, 50)."""
+    ele = _c(ele)
+    X = _c(X)
+    n = ele.shape[0]
+    out = np.zeros((n, 50))
+    lib().oracle_beam_results(n, _p(ele), _p(X), _p(out))
+    return out
 
 
 def bar_eval(ele, X, U=None, t=0.0, **kw):
