@@ -526,9 +526,16 @@ def bench_solve(args, rank, local_rank, ws, dist):
         dm.sweepx(OX, T[:nstep_w], st.time, X0, **kw)
     if dist:
         dist.barrier()
-    t0 = time.perf_counter()
-    rc, states, stats = dm.sweepx(OX, T if args.config == "cantilever" else T[:nstep], st.time, X0, **kw)
-    dt = time.perf_counter() - t0
+    nl0 = dm.launch_count()
+    with Clocks(local_rank) as ck:
+        t0 = time.perf_counter()
+        rc, states, stats = dm.sweepx(OX, T if args.config == "cantilever" else T[:nstep], st.time, X0, **kw)
+        dt = time.perf_counter() - t0
+    clocks = ck.summary()
+    # a replayed step graph is captured (and counted) once: its kernels run every step
+    launches = dm.launch_count() - nl0
+    if kw.get("graph") and kw.get("fixed_iter"):
+        launches *= max(stats.nstep_done, 1)
     if rc != 0:
         raise SystemExit(dm.lib.mgpu_last_error(dm.ctx).decode())
     dt = reduce_max(dist, dt)
@@ -564,7 +571,8 @@ def bench_solve(args, rank, local_rank, ws, dist):
                        "linear_solver": dm.linear_solver_info()},
             "beam_assemblies_per_s": value, "e2e": {"value": ms_step, "unit": "ms", "note": "whole solve incl. copies"},
             "cpu_baseline": {"value": cpu_rate, "unit": "beam assemblies/s", "kind": "port", "sample": sample,
-                             "cores": os.cpu_count()}}
+                             "cores": os.cpu_count()},
+            "gpu_launches": launches, "clocks": clocks}
     print(json.dumps(line), flush=True)
     dm.close()
 

@@ -74,6 +74,7 @@ struct mgpu_ctx {
   std::vector<uint8_t> dof_last;  // [nX] 1 for the multiplier of a DofConstraint
   int elem_block = 128;     // threads per block of the beam and bar kernels (mgpu_autotune)
   int64_t launches = 0;     // kernel launches of the assembly, Newton and multifrontal paths (mgpu_launch_count)
+  bool device_pattern = false;  // the pattern and plans were built on the device
   mgpu::Solver* solver = nullptr;
   // constants of the current step, read by the kernels from device memory so
   // that a captured step replays with new values: t, a1, a2, a3, b1, b2, b3

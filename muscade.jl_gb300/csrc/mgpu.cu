@@ -477,6 +477,8 @@ static int reset_errflag(mgpu_ctx* c) {
 }  // namespace mgpu
 
 // ------------------------------------------------------------------ C ABI
+constexpr int64_t kDevicePatternPairs = int64_t(1) << 22;  // element entries from which the device builds the pattern
+
 template <class T>
 static int dalloc(mgpu_ctx* c, T** p, size_t n) {
   if (n == 0) n = 1;
@@ -553,10 +555,6 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
     shapes.push_back(GroupShape{G.nele, G.nX, G.indexX});
     if (has_tval(G.kind)) ntv += G.nele;
   }
-  const auto t_pat0 = std::chrono::steady_clock::now();
-  std::string perr = build_pattern(d->nX, shapes, c->pat);
-  if (!perr.empty()) return set_err(c, MGPU_ERR_ARG, perr);
-  const auto t_pat1 = std::chrono::steady_clock::now();
   c->ntval = ntv;
   // ---- per-group device data
   int64_t tvb = 0;
@@ -644,6 +642,24 @@ extern "C" int mgpu_create(mgpu_ctx** out, const mgpu_model_desc* d) {
     }
     c->groups.push_back(std::move(D));
   }
+  // ---- pattern and gather plans: on the host, or on the device (a radix sort of the
+  // element entries) when MGPU_DEVICE_PATTERN is set or the model has 4 M entries or more
+  const auto t_pat0 = std::chrono::steady_clock::now();
+  int64_t npairs = 0;
+  for (const GroupShape& G : shapes) npairs += G.nele * G.nX * G.nX;
+  bool dev_pattern = npairs >= kDevicePatternPairs;
+  if (const char* ev = getenv("MGPU_DEVICE_PATTERN")) dev_pattern = atoi(ev) != 0;
+  std::string perr;
+  if (dev_pattern) {
+    std::vector<const int32_t*> didx;
+    for (const DevGroup& D : c->groups) didx.push_back(D.idx);
+    perr = build_pattern_device(d->nX, shapes, didx, c->stream, c->pat);
+  } else {
+    perr = build_pattern(d->nX, shapes, c->pat);
+  }
+  if (!perr.empty()) return set_err(c, MGPU_ERR_ARG, perr);
+  c->device_pattern = dev_pattern;
+  const auto t_pat1 = std::chrono::steady_clock::now();
   // ---- node coordinates of the dofs (element geometry) and the constraint multipliers
   c->dof_xyz.assign(3 * size_t(c->nX), NAN);
   c->dof_last.assign(size_t(c->nX), 0);

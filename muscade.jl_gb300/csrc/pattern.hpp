@@ -48,3 +48,13 @@ struct Pattern {
 std::string build_pattern(int64_t n, const std::vector<GroupShape>& groups, Pattern& P);
 
 }  // namespace mgpu
+
+#include <cuda_runtime.h>
+
+namespace mgpu {
+// The same pattern and plans built on the device (pattern_dev.cu): d_idx[g] the
+// group's dof map on the device ([nX][nele], 0-based), on stream st.
+std::string build_pattern_device(int64_t n, const std::vector<GroupShape>& groups,
+                                 const std::vector<const int32_t*>& d_idx, cudaStream_t st, Pattern& P);
+
+}  // namespace mgpu

@@ -16,9 +16,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libmuscade_gpu.so")
 SOURCES = ["mgpu.cu", "solver.cu", "adjoint.cu", "peak.cu", "noalloc.cu", "sparse_lu.cu", "lagrangian.cu",
-           "pattern.cpp", "sparse_analysis.cpp"]
+           "pattern_dev.cu", "pattern.cpp", "sparse_analysis.cpp"]
 HEADERS = ["tj.hpp", "beam_math.hpp", "beam_const.hpp", "bar_math.hpp", "ctx.hpp", "pattern.hpp", "band_rows.cuh",
-           "band_torn.cuh", "band_bcr.cuh", "solver.hpp", "sparse_lu.hpp", "sparse_analysis.hpp"]
+           "band_torn.cuh", "band_bcr.cuh", "solver.hpp", "sparse_lu.hpp", "sparse_analysis.hpp", "tc.cuh"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # status codes

@@ -2,8 +2,11 @@
 the values EulerBeam3D's residual makes requestable (toolbox/BeamElement.jl:
 151-189) -- ε, rₛₘ, and per Gauss point x, κ, fᵢ = EA ε, mᵢ = (GJ κ₁, EI₃ κ₂,
 EI₂ κ₃) -- for every element and state, against the oracle's kinematics and
-resultants: 1e-12 relative to each quantity's largest value.  The EI scale of
-an A-dof multiplies the bending moments.
+resultants: 1e-12 relative to each quantity's largest value, or to its natural
+scale where that is larger (ε is the difference of a length ratio from 1, so
+its rounding is absolute: scale 1 for ε and EA for fᵢ; the curvatures and
+moments inherit the rounding of the local displacements, scale |κᵤ|·L and
+EI·|κᵤ|·L).  The EI scale of an A-dof multiplies the bending moments.
 """
 import numpy as np
 import pytest
@@ -25,17 +28,21 @@ def built():
     O.build()
 
 
-def _compare(dev, ref):
+def _compare(dev, ref, ele):
     n = ref.shape[0]
     names = {"eps": ref[:, 0], "rsm": ref[:, 1:10]}
     gp = ref[:, 10:].reshape(n, 4, 10)
     names.update(x=gp[..., 0:3], kappa=gp[..., 3:6], fi=gp[..., 6], mi=gp[..., 7:10])
+    kuL = float(np.max(np.abs(ele[:, 40:44]) * ele[:, 48:49]))
+    EI = float(np.max(ele[:, 54:57]))
+    natural = {"eps": 1.0, "fi": float(np.max(ele[:, 53])), "kappa": kuL, "mi": EI * kuL}
     out = {}
     for k, r in names.items():
         d = dev[k]
         if k == "rsm":
             d = d.transpose(0, 2, 1).reshape(n, 9)
-        out[k] = float(np.max(np.abs(d.reshape(r.shape) - r)) / max(np.max(np.abs(r)), 1e-300))
+        scale = max(np.max(np.abs(r)), natural.get(k, 0.0), 1e-300)
+        out[k] = float(np.max(np.abs(d.reshape(r.shape) - r)) / scale)
     return out
 
 
@@ -55,7 +62,7 @@ def test_beam_results_match_oracle():
     ele = m.groups[0].cat("ele")
     for k in range(nstate):
         ref = O.beam_results(ele, states[k][dg.index_X - 1])
-        errs = _compare({q: v[k] for q, v in res.items()}, ref)
+        errs = _compare({q: v[k] for q, v in res.items()}, ref, ele)
         print(f"state {k}: {errs}")
         assert all(e <= TOL for e in errs.values()), errs
 
@@ -77,5 +84,5 @@ def test_beam_results_with_ei_scale():
     ele[:, 55] *= a
     for k in range(states.shape[0]):
         ref = O.beam_results(ele, states[k, 0][dg.index_X - 1])
-        errs = _compare({q: v[k] for q, v in res.items()}, ref)
+        errs = _compare({q: v[k] for q, v in res.items()}, ref, ele)
         assert all(e <= TOL for e in errs.values()), errs
