@@ -281,6 +281,19 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
     return;
   }
   const int i0 = r0 + (blockIdx.x % nt) * kTile32, j0 = r0 + (blockIdx.x / nt) * kTile32;
+  const int tr = tid & 15, tc = tid >> 4;
+  // the accumulator starts from the tile of C: its loads are in flight while the
+  // operands are staged, and the tile is written once at the end
+  float acc[8][8];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+      acc[u][v] = (i < m && j < m) ? A[i + int64_t(j) * m] : 0.f;
+    }
+  }
   // the tile's operand loads in batches of 16 per thread, all in flight together
   constexpr int kPer = NB * kTile32 / kThreads;
   static_assert(kPer % 16 == 0, "whole batches");
@@ -303,12 +316,6 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
     }
   }
   __syncthreads();
-  const int tr = tid & 15, tc = tid >> 4;
-  float acc[8][8];
-#pragma unroll
-  for (int u = 0; u < 8; ++u)
-#pragma unroll
-    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
 #pragma unroll 4
   for (int c = 0; c < NB; ++c) {
     const float4 a0 = *reinterpret_cast<const float4*>(&As[c][4 * tr]);
@@ -320,31 +327,15 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(-a[u], bb[v], acc[u][v]);
   }
-  // read-modify-write of the tile: two columns' 16 loads in flight at a time
 #pragma unroll
-  for (int v0 = 0; v0 < 8; v0 += 2) {
-    float cv[2][8];
+  for (int v = 0; v < 8; ++v) {
+    const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
 #pragma unroll
-    for (int dv = 0; dv < 2; ++dv) {
-      const int v = v0 + dv;
-      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
-        cv[dv][u] = (i < m && j < m) ? A[i + int64_t(j) * m] : 0.f;
-      }
-    }
-#pragma unroll
-    for (int dv = 0; dv < 2; ++dv) {
-      const int v = v0 + dv;
-      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
-        if (i < m && j < m) A[i + int64_t(j) * m] = cv[dv][u] - acc[u][v];
-      }
+    for (int u = 0; u < 8; ++u) {
+      const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+      if (i < m && j < m) A[i + int64_t(j) * m] = acc[u][v];
     }
   }
 }
