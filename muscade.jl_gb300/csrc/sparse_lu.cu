@@ -281,19 +281,6 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
     return;
   }
   const int i0 = r0 + (blockIdx.x % nt) * kTile32, j0 = r0 + (blockIdx.x / nt) * kTile32;
-  const int tr = tid & 15, tc = tid >> 4;
-  // the accumulator starts from the tile of C: its loads are in flight while the
-  // operands are staged, and the tile is written once at the end
-  float acc[8][8];
-#pragma unroll
-  for (int v = 0; v < 8; ++v) {
-    const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
-      acc[u][v] = (i < m && j < m) ? A[i + int64_t(j) * m] : 0.f;
-    }
-  }
   // the tile's operand loads in batches of 16 per thread, all in flight together
   constexpr int kPer = NB * kTile32 / kThreads;
   static_assert(kPer % 16 == 0, "whole batches");
@@ -316,6 +303,12 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
     }
   }
   __syncthreads();
+  const int tr = tid & 15, tc = tid >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
 #pragma unroll 4
   for (int c = 0; c < NB; ++c) {
     const float4 a0 = *reinterpret_cast<const float4*>(&As[c][4 * tr]);
@@ -327,16 +320,173 @@ __global__ void __launch_bounds__(kThreads) sp_update_f32(const SpFrontDev* __re
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(-a[u], bb[v], acc[u][v]);
+      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
   }
+  // read-modify-write of the tile: two columns' 16 loads in flight at a time
 #pragma unroll
-  for (int v = 0; v < 8; ++v) {
-    const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+  for (int v0 = 0; v0 < 8; v0 += 2) {
+    float cv[2][8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
-      if (i < m && j < m) A[i + int64_t(j) * m] = acc[u][v];
+    for (int dv = 0; dv < 2; ++dv) {
+      const int v = v0 + dv;
+      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+        cv[dv][u] = (i < m && j < m) ? A[i + int64_t(j) * m] : 0.f;
+      }
     }
+#pragma unroll
+    for (int dv = 0; dv < 2; ++dv) {
+      const int v = v0 + dv;
+      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+        if (i < m && j < m) A[i + int64_t(j) * m] = cv[dv][u] - acc[u][v];
+      }
+    }
+  }
+}
+
+// ---- FP32 factorisation by super-panels of kSuper pivots: inside a
+// super-panel each 64-column block first takes the products of the
+// super-panel's earlier blocks (its column block and its row block, the
+// left-looking part), then its panel is factored; the trailing block takes
+// the whole super-panel's products at once (K = kSuper), so that it is read
+// and written once per kSuper pivots instead of once per 64.
+constexpr int kSuper = 256;
+
+// C −= L U over 128 × 128 tiles of a rectangle of every listed front, K in
+// chunks of 64.  mode 0: rows [k0, m) × columns [k0, min(k0+64, p)), K [s0, k0)
+// (the column block); mode 1: rows [k0, min(k0+64, p)) × columns [min(k0+64, p), m),
+// K [s0, k0) (the row block); mode 2: rows and columns [e0, m) with
+// e0 = min(s0 + kSuper, p), K [s0, e0) (the trailing block).  The products
+// are summed apart from C and subtracted once: accumulating them into C would
+// round every product at the scale of C, which leaves the FP32 factors of the
+// large lattice fronts too coarse for the refinement.
+__global__ void __launch_bounds__(kThreads, 2) sp_rect_f32(const SpFrontDev* __restrict__ fr,
+                                                        const int32_t* __restrict__ flist, int mode, int s0, int k0,
+                                                        int ntc, float* __restrict__ F) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  int ra, rb, ca, cb, ka, kz;
+  if (mode == 2) {
+    const int e0 = min(s0 + kSuper, p);
+    ra = ca = e0;
+    rb = cb = m;
+    ka = s0;
+    kz = e0;
+  } else {
+    if (k0 >= p) return;
+    ka = s0;
+    kz = k0;
+    if (mode == 0) {
+      ra = k0;
+      rb = m;
+      ca = k0;
+      cb = min(k0 + 64, p);
+    } else {
+      ra = k0;
+      rb = min(k0 + 64, p);
+      ca = rb;
+      cb = m;
+    }
+  }
+  if (kz <= ka) return;
+  const int i0 = ra + int(blockIdx.x / ntc) * kTile32;
+  const int j0 = ca + int(blockIdx.x % ntc) * kTile32;
+  if (i0 >= rb || j0 >= cb) return;
+  float* A = F + Fr.off;
+  extern __shared__ float smem32[];
+  float(*As)[kTile32 + kPad32] = reinterpret_cast<float(*)[kTile32 + kPad32]>(smem32);
+  float(*Bs)[kTile32 + kPad32] = reinterpret_cast<float(*)[kTile32 + kPad32]>(smem32 + 64 * (kTile32 + kPad32));
+  const int tid = threadIdx.x, tr = tid & 15, tc = tid >> 4;
+  float acc[8][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+  for (int kc = ka; kc < kz; kc += 64) {
+    const int kn = min(64, kz - kc);
+    constexpr int kPer = 64 * kTile32 / kThreads;
+#pragma unroll
+    for (int b0 = 0; b0 < kPer; b0 += 8) {
+      float va[8], vb[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int t = (b0 + u) * kThreads + tid;
+        const int i = t % kTile32, c = t / kTile32;
+        va[u] = (c < kn && i0 + i < rb) ? A[(i0 + i) + int64_t(kc + c) * m] : 0.f;
+        const int cc = t % 64, j = t / 64;
+        vb[u] = (cc < kn && j0 + j < cb) ? A[(kc + cc) + int64_t(j0 + j) * m] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int t = (b0 + u) * kThreads + tid;
+        As[t / kTile32][t % kTile32] = va[u];
+        Bs[t % 64][t / 64] = vb[u];
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int c = 0; c < 64; ++c) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[c][4 * tr]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[c][64 + 4 * tr]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[c][4 * tc]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[c][64 + 4 * tc]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  // read-modify-write of the tile, two columns' 16 loads in flight at a time
+#pragma unroll
+  for (int v0 = 0; v0 < 8; v0 += 2) {
+    float cv[2][8];
+#pragma unroll
+    for (int dv = 0; dv < 2; ++dv) {
+      const int v = v0 + dv;
+      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+        cv[dv][u] = (i < rb && j < cb) ? A[i + int64_t(j) * m] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int dv = 0; dv < 2; ++dv) {
+      const int v = v0 + dv;
+      const int j = j0 + (v < 4 ? 4 * tc + v : 64 + 4 * tc + v - 4);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + (u < 4 ? 4 * tr + u : 64 + 4 * tr + u - 4);
+        if (i < rb && j < cb) A[i + int64_t(j) * m] = cv[dv][u] - acc[u][v];
+      }
+    }
+  }
+}
+
+// the factored diagonal block of pivot block k0 written back into every listed
+// front (after the panel kernel, which reads it unfactored)
+template <class T, int NB>
+__global__ void __launch_bounds__(kThreads) sp_diag_store(const SpFrontDev* __restrict__ fr,
+                                                          const int32_t* __restrict__ flist, int k0,
+                                                          T* __restrict__ F, T tau, int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.x]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p) return;
+  const int kb = min(NB, p - k0);
+  T* A = F + Fr.off;
+  __shared__ T Dg[NB][NB + 1];
+  factor_diag<T, NB>(A, m, k0, kb, Dg, tau, flags, true);
+  for (int t = threadIdx.x; t < kb * kb; t += kThreads) {
+    const int i = t % kb, j = t / kb;
+    A[(k0 + i) + int64_t(k0 + j) * m] = Dg[i][j];
   }
 }
 
@@ -962,6 +1112,46 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
       }
     }
     const auto& lp = sp.h_lfp[h];  // pivots of the height's fronts, descending
+    if constexpr (std::is_same<T, float>::value) {
+      if (sp.super_panels) {
+        const int mmax = sp.h_mmax[h];
+        for (int s0 = 0; s0 < sp.h_pmax[h]; s0 += kSuper) {
+          for (int k0 = s0; k0 < std::min(s0 + kSuper, sp.h_pmax[h]); k0 += NB) {
+            int cnt = 0;
+            while (cnt < int(lp.size()) && lp[cnt] > k0) ++cnt;
+            const int rest = mmax - k0;
+            const int nrc = (rest + kThreads - 1) / kThreads, ncc = (rest + 63) / 64;
+            for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
+              const int32_t* fl = sp.d_lf + sp.h_lf0[h] + f0;
+              const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
+              if (k0 > s0) {
+                const int ntr = (rest + kTile32 - 1) / kTile32;
+                sp_rect_f32<<<dim3(unsigned(ntr), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 0, s0, k0, 1, F);
+                ++c->launches;
+                const int ntc = (rest + kTile32 - 1) / kTile32;  // columns from min(k0 + 64, p)
+                if (ntc > 0) {
+                  sp_rect_f32<<<dim3(unsigned(ntc), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 1, s0, k0, ntc, F);
+                  ++c->launches;
+                }
+              }
+              sp_panel<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+              sp_diag_store<T, NB><<<gy, kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+              c->launches += 2;
+            }
+          }
+          int cnt = 0;
+          while (cnt < int(lp.size()) && lp[cnt] > s0) ++cnt;
+          const int nt = (mmax - s0 + kTile32 - 1) / kTile32;
+          for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
+            const int32_t* fl = sp.d_lf + sp.h_lf0[h] + f0;
+            const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
+            sp_rect_f32<<<dim3(unsigned(nt * nt), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 2, s0, 0, nt, F);
+            ++c->launches;
+          }
+        }
+        continue;
+      }
+    }
     for (int k0 = 0; k0 < sp.h_pmax[h]; k0 += NB) {
       int cnt = 0;
       while (cnt < int(lp.size()) && lp[cnt] > k0) ++cnt;
@@ -1335,6 +1525,8 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   }
   ok(cudaFuncSetAttribute(sp_update_f32<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
   ok(cudaFuncSetAttribute(sp_update_tc<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
+  ok(cudaFuncSetAttribute(sp_rect_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
+  if (const char* ev = getenv("MGPU_SPARSE_SUPER")) sp.super_panels = atoi(ev) != 0;
   if (const char* ev = getenv("MGPU_SPARSE_TC")) sp.tensor_cores = atoi(ev) != 0;
   if (e != cudaSuccess) {
     sp.why = std::string("device upload of the sparse solver: ") + cudaGetErrorString(e);

@@ -56,6 +56,7 @@ struct SparseDev {
   int max_m_small = 0;                         // largest front of the one-block substitutions
   int big_pivots = 0;                          // fronts with this many pivots or more: blocked substitutions
   bool tensor_cores = false;                   // FP32 trailing update on the tensor cores (TF32 ×3; MGPU_SPARSE_TC=1)
+  bool super_panels = true;                    // FP32 factorisation by super-panels (MGPU_SPARSE_SUPER=0: per 64-column block)
   // per height and child rank: children to add
   std::vector<std::vector<int32_t>> h_ea0, h_nea, h_eumax;
   SpFrontDev* d_fr = nullptr;

@@ -125,3 +125,31 @@ def test_per_component_convergence_is_rejected(lattice):
         dm._check(dm.sweepx(0, times[:1], st.time, list(st.X), per_component=True)[0])
     dm.close()
     assert e.value.kind == "unsupported"
+
+
+@pytest.mark.parametrize("grid", [(12, 12, 6), (20, 20, 8)])
+def test_super_panel_factorisation(monkeypatch, grid):
+    """The FP32 factors by super-panels of 256 pivots (left-looking inside,
+    one trailing update per super-panel) against those by 64-column blocks:
+    both refine to the FP64 solution without falling back to FP64 factors,
+    and their iterates agree to the state tolerance."""
+    m, times = W.lattice(*grid)
+    st = m.initialize()
+    out, info = {}, {}
+    for sup in ("1", "0"):
+        monkeypatch.setenv("MGPU_SPARSE_SUPER", sup)
+        dm = DeviceModel(m, st.dis, linsolve="sparse")
+        rc, states, _ = dm.sweepx(0, times[:2], st.time, list(st.X), fixed_iter=3)
+        info[sup] = dm.sparse_info()
+        dm.close()
+        assert rc == 0
+        out[sup] = states
+    monkeypatch.delenv("MGPU_SPARSE_SUPER")
+    print(f"super-panels {grid}: pivots {info['1']['max_pivots']}, sweeps {info['1']['last_sweeps']} "
+          f"(per block {info['0']['last_sweeps']})")
+    assert info["1"]["max_pivots"] > 256  # more than one super-panel in the largest front
+    assert info["1"]["last_fallback"] == 0 and info["0"]["last_fallback"] == 0
+    assert info["1"]["last_sweeps"] <= info["0"]["last_sweeps"] + 2
+    ref = [(0.0, (out["0"][k, 0],)) for k in range(len(out["0"]))]
+    errs = state_errors(out["1"], ref, st.dis.fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs
