@@ -61,7 +61,8 @@ __global__ void __launch_bounds__(kRsThreads) pd_hist(int64_t m, const uint64_t*
   counts[int64_t(threadIdx.x) * ntile + blockIdx.x] = h[threadIdx.x];  // digit-major
 }
 
-// exclusive scan of cnt elements in place, one block walking the array in chunks
+// exclusive scan of cnt elements in place, one block walking the array in
+// chunks (used for the per-chunk totals of the multi-block scan below)
 __global__ void __launch_bounds__(1024) pd_scan(int64_t cnt, uint32_t* __restrict__ a) {
   __shared__ uint32_t s[1024];
   __shared__ uint32_t carry;
@@ -83,6 +84,59 @@ __global__ void __launch_bounds__(1024) pd_scan(int64_t cnt, uint32_t* __restric
     if (threadIdx.x == 0) carry += s[1023];
     __syncthreads();
   }
+}
+
+// multi-block exclusive scan: each block scans a chunk of kScanChunk elements
+// (kScanPer consecutive ones per thread) and leaves the chunk's total in
+// sums; pd_scan turns the totals into offsets and pd_scan_add adds them
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 8;
+constexpr int64_t kScanChunk = int64_t(kScanThreads) * kScanPer;
+
+__global__ void __launch_bounds__(kScanThreads) pd_scan_chunk(int64_t cnt, uint32_t* __restrict__ a,
+                                                              uint32_t* __restrict__ sums) {
+  __shared__ uint32_t s[kScanThreads];
+  const int64_t base = int64_t(blockIdx.x) * kScanChunk + int64_t(threadIdx.x) * kScanPer;
+  uint32_t v[kScanPer], run = 0;
+#pragma unroll
+  for (int u = 0; u < kScanPer; ++u) {
+    v[u] = base + u < cnt ? a[base + u] : 0u;
+    run += v[u];
+  }
+  s[threadIdx.x] = run;
+  __syncthreads();
+  for (int d = 1; d < kScanThreads; d <<= 1) {
+    const uint32_t t = threadIdx.x >= d ? s[threadIdx.x - d] : 0u;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  uint32_t off = s[threadIdx.x] - run;
+#pragma unroll
+  for (int u = 0; u < kScanPer; ++u) {
+    if (base + u < cnt) a[base + u] = off;
+    off += v[u];
+  }
+  if (threadIdx.x == kScanThreads - 1) sums[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kScanThreads) pd_scan_add(int64_t cnt, uint32_t* __restrict__ a,
+                                                            const uint32_t* __restrict__ sums) {
+  const uint32_t add = sums[blockIdx.x];
+  const int64_t base = int64_t(blockIdx.x) * kScanChunk;
+  for (int u = 0; u < kScanPer; ++u) {
+    const int64_t q = base + int64_t(u) * kScanThreads + threadIdx.x;
+    if (q < cnt) a[q] += add;
+  }
+}
+
+// exclusive scan of cnt elements of a (sums: one entry per chunk)
+void scan(int64_t cnt, uint32_t* a, uint32_t* sums, cudaStream_t st) {
+  const int64_t nb = (cnt + kScanChunk - 1) / kScanChunk;
+  if (nb <= 0) return;
+  pd_scan_chunk<<<unsigned(nb), kScanThreads, 0, st>>>(cnt, a, sums);
+  pd_scan<<<1, 1024, 0, st>>>(nb, sums);
+  pd_scan_add<<<unsigned(nb), kScanThreads, 0, st>>>(cnt, a, sums);
 }
 
 // stable scatter of one tile: a key's destination is its digit's offset for
@@ -219,12 +273,13 @@ std::string build_pattern_device(int64_t n, const std::vector<GroupShape>& group
   };
   const int64_t ntile = (m + kRsTile - 1) / kRsTile;
   uint64_t *k1, *k2;
-  uint32_t *i1, *i2, *counts, *head, *hs, *colcnt, *mseg, *msrc;
+  uint32_t *i1, *i2, *counts, *head, *hs, *colcnt, *mseg, *msrc, *sums;
   int32_t *rowval, *pnnz;
   GroupDev* dgroups;
   if (!dal(&k1, m) || !dal(&k2, m) || !dal(&i1, m) || !dal(&i2, m) || !dal(&counts, size_t(kRsDigits) * ntile) ||
       !dal(&head, m) || !dal(&hs, m) || !dal(&colcnt, n + 1) || !dal(&mseg, m) || !dal(&msrc, m) ||
-      !dal(&rowval, m) || !dal(&pnnz, m) || !dal(&dgroups, ng)) {
+      !dal(&rowval, m) || !dal(&pnnz, m) || !dal(&dgroups, ng) ||
+      !dal(&sums, size_t(std::max<int64_t>(int64_t(kRsDigits) * ntile, m) / kScanChunk + 1))) {
     cleanup();
     return "device pattern: allocation failed";
   }
@@ -240,7 +295,7 @@ std::string build_pattern_device(int64_t n, const std::vector<GroupShape>& group
   while (bits < 64 && (uint64_t(1) << bits) < uint64_t(n) * uint64_t(n)) ++bits;
   for (int shift = 0; shift < bits && e == cudaSuccess; shift += 8) {
     pd_hist<<<unsigned(ntile), kRsThreads, 0, st>>>(m, k1, shift, counts, ntile);
-    pd_scan<<<1, 1024, 0, st>>>(int64_t(kRsDigits) * ntile, counts);
+    scan(int64_t(kRsDigits) * ntile, counts, sums, st);
     pd_scatter<<<unsigned(ntile), kRsThreads, 0, st>>>(m, k1, i1, shift, counts, ntile, k2, i2);
     std::swap(k1, k2);
     std::swap(i1, i2);
@@ -252,7 +307,7 @@ std::string build_pattern_device(int64_t n, const std::vector<GroupShape>& group
   }
   if (e == cudaSuccess) {
     // an exclusive scan of the heads (in chunks of the counts scan) and the emission
-    pd_scan<<<1, 1024, 0, st>>>(m, hs);
+    scan(m, hs, sums, st);
     e = cudaMemsetAsync(colcnt, 0, (n + 1) * sizeof(uint32_t), st);
   }
   if (e == cudaSuccess) {

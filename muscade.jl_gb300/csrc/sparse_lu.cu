@@ -183,6 +183,81 @@ __global__ void __launch_bounds__(kThreads) sp_panel(const SpFrontDev* __restric
   }
 }
 
+// The same panels once the diagonal block has been factored in place
+// (sp_diag_store), so that no block repeats its factorisation: blocks
+// [0, nrc) solve 256 rows of the L panel (one row per thread), blocks
+// [nrc, nrc + ncc) 64 columns of the U panel, a warp taking eight columns at
+// once (lanes over rows) so that eight substitution chains interleave.
+template <class T, int NB>
+__global__ void __launch_bounds__(kThreads) sp_panel_f(const SpFrontDev* __restrict__ fr,
+                                                       const int32_t* __restrict__ flist, int k0,
+                                                       T* __restrict__ F) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p) return;
+  const int kb = min(NB, p - k0);
+  const int r0 = k0 + kb, rest = m - r0;
+  const int nrc = (rest + kThreads - 1) / kThreads, ncc = (rest + 63) / 64;
+  if (int(blockIdx.x) >= nrc + ncc) return;
+  T* A = F + Fr.off;
+  __shared__ T Dg[NB][NB + 1];
+  const int tid = threadIdx.x;
+  for (int t = tid; t < kb * kb; t += kThreads) {
+    const int i = t % kb, j = t / kb;
+    Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
+  }
+  __syncthreads();
+  const int b = blockIdx.x;
+  if (b < nrc) {
+    const int i = r0 + b * kThreads + tid;
+    if (i < m) {
+      T x[NB];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) x[c] = c < kb ? A[i + int64_t(k0 + c) * m] : T(0);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < kb) {
+          x[c] /= Dg[c][c];
+#pragma unroll
+          for (int t = c + 1; t < NB; ++t)
+            if (t < kb) x[t] -= x[c] * Dg[c][t];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NB; ++c)
+        if (c < kb) A[i + int64_t(k0 + c) * m] = x[c];
+    }
+    return;
+  }
+  const int w = tid >> 5, lane = tid & 31;
+  const int jb = r0 + (b - nrc) * 64 + w * 8;
+  T y0[8], y1[8];
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    const bool ok = jb + jj < m;
+    const T* col = A + int64_t(jb + jj) * m + k0;
+    y0[jj] = ok && lane < kb ? col[lane] : T(0);
+    y1[jj] = ok && NB > 32 && lane + 32 < kb ? col[lane + 32] : T(0);
+  }
+  for (int c = 0; c < kb; ++c) {
+    const T l0 = lane > c && lane < kb ? Dg[lane][c] : T(0);
+    const T l1 = NB > 32 && lane + 32 > c && lane + 32 < kb ? Dg[(lane + 32) % NB][c] : T(0);
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      const T yc = __shfl_sync(0xffffffffu, c < 32 ? y0[jj] : y1[jj], c & 31);
+      if (lane > c && lane < kb) y0[jj] -= l0 * yc;
+      if (NB > 32 && lane + 32 > c && lane + 32 < kb) y1[jj] -= l1 * yc;
+    }
+  }
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    if (jb + jj >= m) break;
+    T* col = A + int64_t(jb + jj) * m + k0;
+    if (lane < kb) col[lane] = y0[jj];
+    if (NB > 32 && lane + 32 < kb) col[lane + 32] = y1[jj];
+  }
+}
+
 // trailing update of every listed front after pivot block k0: A₂₂ -= L₂₁ U₁₂,
 // one 64 × 64 tile per block (4 × 4 per thread; a warp's rows are consecutive);
 // the block after the last tile writes the factored diagonal block
@@ -471,8 +546,8 @@ __global__ void __launch_bounds__(kThreads, 2) sp_rect_f32(const SpFrontDev* __r
   }
 }
 
-// the factored diagonal block of pivot block k0 written back into every listed
-// front (after the panel kernel, which reads it unfactored)
+// the diagonal block of pivot block k0 factored in place in every listed front
+// (before sp_panel_f, which reads it factored)
 template <class T, int NB>
 __global__ void __launch_bounds__(kThreads) sp_diag_store(const SpFrontDev* __restrict__ fr,
                                                           const int32_t* __restrict__ flist, int k0,
@@ -994,6 +1069,237 @@ __global__ void __launch_bounds__(kSBThreads) sp_bwdb_step(const SpFrontDev* __r
   sb_tri_upper<T>(A, m, r0, r1 - r0, Dg, vs, Vf);
 }
 
+// ---- chained substitutions: one launch per height and direction.  The
+// blocks take work items (row tile t of front f) from a counter in the order
+// t·nf + f (forward; backward by distance from the last pivot tile), so that
+// every tile an item waits for was taken earlier by a block that is running:
+// the waits always end.  A pivot tile, once solved, publishes its values and
+// then its flag (the launch's epoch); a tile that needs column block j waits
+// for the flag of tile j, its factor entries already loaded.  The arithmetic
+// is that of the launch-per-column-block kernels above, in the same order, so
+// both give bitwise the same vectors.  Every wait is bounded: when one runs
+// out, the block sets the abort word and flags[3], and the other blocks stop
+// at their next wait or item.
+constexpr int64_t kTileWaitPolls = int64_t(1) << 22;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_relaxed_i32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// flags of front fid's tiles: (idx / 64) + 2·fid leaves every front room for its tiles
+__device__ __forceinline__ int64_t sb_flag_base(const SpFrontDev& Fr, int32_t fid) {
+  return (Fr.idx >> 6) + 2 * int64_t(fid);
+}
+
+// thread 0 waits for *flag == epoch, then the block synchronises; false (for
+// the whole block) when the wait ran out or another block gave up
+__device__ bool sb_wait(const unsigned* flag, unsigned epoch, int* abort_word, int* flags, int* ok_s) {
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    for (int64_t i = 0;; ++i) {
+      if (ld_acquire_u32(flag) == epoch) break;
+      if ((i & 63) == 63 && ld_relaxed_i32(abort_word)) {
+        ok = 0;
+        break;
+      }
+      if (i >= kTileWaitPolls) {
+        atomicExch(abort_word, 1);
+        atomicOr(flags + 3, 2);
+        ok = 0;
+        break;
+      }
+      if (i > 32) __nanosleep(128);
+    }
+    *ok_s = ok;
+  }
+  __syncthreads();
+  const bool ok = *ok_s != 0;
+  __syncthreads();
+  return ok;
+}
+
+// next work item of the block (total when there is none left or the launch aborted)
+__device__ int sb_claim(int* ctr, int total, const int* abort_word, int* item_s) {
+  if (threadIdx.x == 0) *item_s = ld_relaxed_i32(abort_word) ? total : atomicAdd(ctr, 1);
+  __syncthreads();
+  const int item = *item_s;
+  __syncthreads();
+  return item;
+}
+
+// v -= A[r0..r1, c0..c0+cb) · x for the block's rows, x the solved tile of
+// column block j (a[]: this thread's 16 factor entries, loaded before the wait)
+template <class T>
+__device__ __forceinline__ void sb_chain_load(const T* __restrict__ A, int m, int r0, int r1, int c0, int cb,
+                                              T (&a)[16]) {
+  const int tid = threadIdx.x, rr = tid & (kSB - 1), cq = tid >> 6;
+  const int r = r0 + rr, cbeg = cq * 16;
+#pragma unroll
+  for (int c = 0; c < 16; ++c)
+    a[c] = (r < r1 && cbeg + c < cb) ? A[r + int64_t(c0 + cbeg + c) * m] : T(0);
+}
+template <class T>
+__device__ __forceinline__ void sb_chain_apply(const T (&a)[16], int cb, const double* Vx, T* xs,
+                                               double (*part)[kSB], double& v) {
+  const int tid = threadIdx.x, rr = tid & (kSB - 1), cq = tid >> 6;
+  if (tid < kSB) xs[tid] = tid < cb ? T(__ldcg(Vx + tid)) : T(0);
+  __syncthreads();
+  const int cbeg = cq * 16;
+  T sacc = T(0);
+#pragma unroll
+  for (int c = 0; c < 16; ++c)
+    if (cbeg + c < cb) sacc = fma(a[c], xs[cbeg + c], sacc);
+  part[cq][rr] = double(sacc);
+  __syncthreads();
+  if (tid < kSB) v = v - (((part[0][tid] + part[1][tid]) + part[2][tid]) + part[3][tid]);
+  __syncthreads();
+}
+
+// stage the strict lower (lower = true) or the upper triangle of the diagonal tile
+template <class T>
+__device__ __forceinline__ void sb_stage_diag(const T* __restrict__ A, int m, int r0, int nr, bool lower,
+                                              T (*Dg)[kSB + 1]) {
+  for (int q = threadIdx.x; q < kSB * kSB; q += kSBThreads) {
+    const int i = q & (kSB - 1), c = q >> 6;
+    const bool in = i < nr && c < nr && (lower ? c < i : c >= i);
+    Dg[i][c] = in ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_fwdb_chain(const SpFrontDev* __restrict__ fr,
+                                                            const int32_t* __restrict__ flist, int nf, int ntmax,
+                                                            const T* __restrict__ F, double* __restrict__ V,
+                                                            unsigned* __restrict__ tflag, unsigned epoch,
+                                                            int* __restrict__ ctr, int* __restrict__ abort_word,
+                                                            int* __restrict__ flags) {
+  if (flags[0]) return;
+  __shared__ T xs[kSB];
+  __shared__ double part[4][kSB];
+  __shared__ T Dg[kSB][kSB + 1];
+  __shared__ T vs[kSB];
+  __shared__ int sync_s[2];
+  const int tid = threadIdx.x;
+  const int total = ntmax * nf;
+  for (;;) {
+    const int item = sb_claim(ctr, total, abort_word, &sync_s[0]);
+    if (item >= total) return;
+    const int t = item / nf;
+    const int32_t fid = flist[item % nf];
+    const SpFrontDev Fr = fr[fid];
+    const int m = Fr.m, p = Fr.p, np = sb_np(p), nt = np + sb_nu(m, p);
+    if (t >= nt) continue;
+    int r0, r1;
+    sb_rows(t, m, p, r0, r1);
+    const T* A = F + Fr.off;
+    double* Vf = V + Fr.idx;
+    unsigned* tf = tflag + sb_flag_base(Fr, fid);
+    const bool piv = t < np;
+    if (piv) sb_stage_diag<T>(A, m, r0, r1 - r0, true, Dg);
+    double v = (tid < kSB && r0 + tid < r1) ? Vf[r0 + tid] : 0.0;
+    const int jmax = min(t, np);
+    bool ok = true;
+    for (int j = 0; j < jmax && ok; ++j) {
+      const int c0 = j * kSB, cb = min(kSB, p - c0);
+      T a[16];
+      sb_chain_load<T>(A, m, r0, r1, c0, cb, a);
+      ok = sb_wait(tf + j, epoch, abort_word, flags, &sync_s[1]);
+      if (ok) sb_chain_apply<T>(a, cb, Vf + c0, xs, part, v);
+    }
+    if (!ok) return;
+    if (!piv) {
+      if (tid < kSB && r0 + tid < r1) Vf[r0 + tid] = v;
+      continue;
+    }
+    const int nr = r1 - r0;
+    if (tid < kSB) vs[tid] = T(v);
+    __syncthreads();
+    if (tid < 32) {
+      T a0 = vs[tid], a1 = vs[tid + 32];
+      for (int c = 0; c < nr; ++c) {
+        const T yc = __shfl_sync(0xffffffffu, c < 32 ? a0 : a1, c & 31);
+        a0 = fma(-Dg[tid][c], yc, a0);
+        a1 = fma(-Dg[tid + 32][c], yc, a1);
+      }
+      if (tid < nr) Vf[r0 + tid] = double(a0);
+      if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) st_release_u32(tf + t, epoch);
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kSBThreads) sp_bwdb_chain(const SpFrontDev* __restrict__ fr,
+                                                            const int32_t* __restrict__ flist, int nf, int npmax,
+                                                            const T* __restrict__ F, double* __restrict__ V,
+                                                            unsigned* __restrict__ tflag, unsigned epoch,
+                                                            int* __restrict__ ctr, int* __restrict__ abort_word,
+                                                            int* __restrict__ flags) {
+  if (flags[0]) return;
+  __shared__ T xs[kSB];
+  __shared__ double part[4][kSB];
+  __shared__ T Dg[kSB][kSB + 1];
+  __shared__ T vs[kSB];
+  __shared__ int sync_s[2];
+  const int tid = threadIdx.x;
+  const int total = npmax * nf;
+  for (;;) {
+    const int item = sb_claim(ctr, total, abort_word, &sync_s[0]);
+    if (item >= total) return;
+    const int32_t fid = flist[item % nf];
+    const SpFrontDev Fr = fr[fid];
+    const int m = Fr.m, p = Fr.p, np = sb_np(p);
+    const int t = np - 1 - item / nf;
+    if (t < 0) continue;
+    const int r0 = t * kSB, r1 = min(r0 + kSB, p), nr = r1 - r0;
+    const T* A = F + Fr.off;
+    double* Vf = V + Fr.idx;
+    unsigned* tf = tflag + sb_flag_base(Fr, fid);
+    sb_stage_diag<T>(A, m, r0, nr, false, Dg);
+    double v = (tid < kSB && r0 + tid < r1) ? Vf[r0 + tid] : 0.0;
+    bool ok = true;
+    for (int b = np - 1; b > t && ok; --b) {
+      const int c0 = b * kSB, cb = min(kSB, p - c0);
+      T a[16];
+      sb_chain_load<T>(A, m, r0, r1, c0, cb, a);
+      ok = sb_wait(tf + b, epoch, abort_word, flags, &sync_s[1]);
+      if (ok) sb_chain_apply<T>(a, cb, Vf + c0, xs, part, v);
+    }
+    if (!ok) return;
+    if (tid < kSB) vs[tid] = T(v);
+    __syncthreads();
+    if (tid < 32) {
+      T a0 = vs[tid], a1 = vs[tid + 32];
+      for (int c = nr - 1; c >= 0; --c) {
+        const bool lo = c < 32;
+        T xc = (lo ? a0 : a1) / Dg[c][c];
+        xc = __shfl_sync(0xffffffffu, xc, c & 31);
+        if (tid == c) a0 = xc;
+        else if (tid < c) a0 = fma(-Dg[tid][c], xc, a0);
+        if (tid + 32 == c) a1 = xc;
+        else if (tid + 32 < c) a1 = fma(-Dg[tid + 32][c], xc, a1);
+      }
+      if (tid < nr) Vf[r0 + tid] = double(a0);
+      if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) st_release_u32(tf + t, epoch);
+  }
+}
+
 // backward: x to w
 __global__ void sp_bwdb_fin(const SpFrontDev* __restrict__ fr, const int32_t* __restrict__ flist,
                             const double* __restrict__ V, double* __restrict__ w, const int* __restrict__ conv) {
@@ -1134,8 +1440,8 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
                   ++c->launches;
                 }
               }
-              sp_panel<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
               sp_diag_store<T, NB><<<gy, kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+              sp_panel_f<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F);
               c->launches += 2;
             }
           }
@@ -1187,6 +1493,16 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
   return cudaGetLastError();
 }
 
+// epoch of the next chained launch (never 0, the flags' initial value; on
+// wrap-around the flags are cleared)
+unsigned next_epoch(SparseDev& sp, cudaStream_t st) {
+  if (++sp.epoch == 0) {
+    cudaMemsetAsync(sp.tflag, 0, sp.ntflag * sizeof(unsigned), st);
+    sp.epoch = 1;
+  }
+  return sp.epoch;
+}
+
 // refinement sweeps with the factors F: x = Lλx⁻¹ b.  Per height, the fronts
 // with fewer than sp.big_pivots pivots (the tail of the height's list) take
 // the one-block-per-front kernels, the others the blocked ones.
@@ -1195,7 +1511,12 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
   cudaStream_t st = c->stream;
   const int64_t n = sp.n;
   const size_t smem = size_t(std::max(sp.max_m_small, 1)) * sizeof(double);
+  const int grid = std::is_same<T, float>::value ? sp.chain_grid32 : sp.chain_grid64;
   for (int it = it0; it < it1; ++it) {
+    if (sp.chained) {
+      const cudaError_t e = cudaMemsetAsync(sp.chain, 0, (2 * size_t(sp.nheight) + 1) * sizeof(int), st);
+      if (e != cudaSuccess) return e;
+    }
     const double* r = b;
     if (it > 0) {
       sp_residual<<<nblocks(n, kThreads), kThreads, 0, st>>>(n, sp.d_rptr, sp.d_rq, sp.d_rcol, c->nzval, sp.xs, b,
@@ -1230,14 +1551,22 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
               sp.d_fr, fl, sp.d_clist, sp.d_emap, int(rk), sp.cvec, sp.V, sp.flags);
           ++c->launches;
         }
-        sp_fwdb_first<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.V, sp.flags);
-        ++c->launches;
-        for (int j = 0; j < sp.h_bnp[h]; ++j) {
-          const int g = sp.h_bnt[h] - j - 1;
-          if (g > 0) {
-            sp_fwdb_step<T><<<dim3(unsigned(g), unsigned(nbig)), kSBThreads, 0, st>>>(sp.d_fr, fl, j, F, sp.V,
-                                                                                     sp.flags);
-            ++c->launches;
+        if (sp.chained) {
+          const int items = sp.h_bnt[h] * nbig;
+          sp_fwdb_chain<T><<<unsigned(std::min(items, grid)), kSBThreads, 0, st>>>(
+              sp.d_fr, fl, nbig, sp.h_bnt[h], F, sp.V, sp.tflag, next_epoch(sp, st), sp.chain + h,
+              sp.chain + 2 * sp.nheight, sp.flags);
+          ++c->launches;
+        } else {
+          sp_fwdb_first<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.V, sp.flags);
+          ++c->launches;
+          for (int j = 0; j < sp.h_bnp[h]; ++j) {
+            const int g = sp.h_bnt[h] - j - 1;
+            if (g > 0) {
+              sp_fwdb_step<T><<<dim3(unsigned(g), unsigned(nbig)), kSBThreads, 0, st>>>(sp.d_fr, fl, j, F, sp.V,
+                                                                                       sp.flags);
+              ++c->launches;
+            }
           }
         }
         sp_fwdb_fin<<<dim3(gm, unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.V, sp.w, sp.cvec, sp.flags);
@@ -1270,12 +1599,20 @@ cudaError_t refine(mgpu_ctx* c, SparseDev& sp, const T* F, const double* b, int 
           sp_bwdb_red<<<dim3(gp, unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.d_poff, sp.P, sp.V, sp.flags);
           c->launches += 2;
         }
-        sp_bwdb_last<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.V, sp.flags);
-        ++c->launches;
-        for (int s2 = 0; s2 + 1 < sp.h_bnp[h]; ++s2) {
-          sp_bwdb_step<T><<<dim3(unsigned(sp.h_bnp[h]), unsigned(nbig)), kSBThreads, 0, st>>>(sp.d_fr, fl, s2, F, sp.V,
-                                                                                              sp.flags);
+        if (sp.chained) {
+          const int items = sp.h_bnp[h] * nbig;
+          sp_bwdb_chain<T><<<unsigned(std::min(items, grid)), kSBThreads, 0, st>>>(
+              sp.d_fr, fl, nbig, sp.h_bnp[h], F, sp.V, sp.tflag, next_epoch(sp, st), sp.chain + sp.nheight + h,
+              sp.chain + 2 * sp.nheight, sp.flags);
           ++c->launches;
+        } else {
+          sp_bwdb_last<T><<<unsigned(nbig), kSBThreads, 0, st>>>(sp.d_fr, fl, F, sp.V, sp.flags);
+          ++c->launches;
+          for (int s2 = 0; s2 + 1 < sp.h_bnp[h]; ++s2) {
+            sp_bwdb_step<T><<<dim3(unsigned(sp.h_bnp[h]), unsigned(nbig)), kSBThreads, 0, st>>>(sp.d_fr, fl, s2, F,
+                                                                                                sp.V, sp.flags);
+            ++c->launches;
+          }
         }
         sp_bwdb_fin<<<dim3(nblocks(sp.h_pmax[h], kThreads), unsigned(nbig)), kThreads, 0, st>>>(sp.d_fr, fl, sp.V,
                                                                                                sp.w, sp.flags);
@@ -1516,6 +1853,22 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaMalloc(&sp.prev, sizeof(double)));
   ok(cudaMalloc(&sp.flags, 4 * sizeof(int)));
   ok(cudaMallocHost(&sp.hflags, 4 * sizeof(int)));
+  sp.ntflag = int64_t(A.fidx.size()) / 64 + 2 * int64_t(sp.nfront) + 64;
+  ok(cudaMalloc(&sp.tflag, sp.ntflag * sizeof(unsigned)));
+  ok(cudaMemset(sp.tflag, 0, sp.ntflag * sizeof(unsigned)));
+  ok(cudaMalloc(&sp.chain, (2 * size_t(sp.nheight) + 1) * sizeof(int)));
+  {
+    int dev = 0, nsm = 0, b32 = 0, b64 = 0, f32 = 0, f64 = 0;
+    ok(cudaGetDevice(&dev));
+    ok(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f32, sp_fwdb_chain<float>, kSBThreads, 0));
+    ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b32, sp_bwdb_chain<float>, kSBThreads, 0));
+    ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f64, sp_fwdb_chain<double>, kSBThreads, 0));
+    ok(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b64, sp_bwdb_chain<double>, kSBThreads, 0));
+    sp.chain_grid32 = std::max(1, nsm * std::max(1, std::min(f32, b32)));
+    sp.chain_grid64 = std::max(1, nsm * std::max(1, std::min(f64, b64)));
+  }
+  if (const char* ev = getenv("MGPU_SPARSE_CHAINED")) sp.chained = atoi(ev) != 0;
   ok(cudaMemset(sp.nrm, 0, 2 * sizeof(unsigned long long)));
   for (cudaEvent_t& ev : sp.ev) ok(cudaEventCreate(&ev));
   const int smem = int(sp.max_m_small * sizeof(double));
@@ -1548,7 +1901,7 @@ void sparse_destroy(SparseDev*& sp) {
                 sp->d_acol, sp->d_perm, sp->d_diag, sp->d_colptr, sp->d_rowval, sp->d_rptr, sp->d_rq, sp->d_rcol,
                 sp->F32, sp->F64, sp->prev,
                 sp->D, sp->cvec, sp->w, sp->V, sp->P, sp->d_poff, sp->tw, sp->yacc, sp->r, sp->xs, sp->nrm,
-                sp->flags};
+                sp->flags, sp->tflag, sp->chain};
   for (void* p : ps) cudaFree(p);
   if (sp->hflags) cudaFreeHost(sp->hflags);
   for (cudaEvent_t ev : sp->ev)
@@ -1586,6 +1939,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
     sp.last_refine_ms = elapsed(1, 2);
     sp.last_sweeps = sp.hflags[1];
     sp.last_perturbed = sp.hflags[2];
+    if (sp.hflags[3] & 2) return set_err(c, MGPU_ERR_CUDA, "sparse solve: a chained substitution's wait ran out");
     sp.last_fallback = 0;
     if (sp.hflags[0] == 0 || sp.hflags[3] != 0) {
       use64 = true;
@@ -1613,6 +1967,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
     sp.last_refine_ms += elapsed(1, 2);
     sp.last_sweeps = sp.hflags[1];
     sp.last_perturbed = sp.hflags[2];
+    if (sp.hflags[3] & 2) return set_err(c, MGPU_ERR_CUDA, "sparse solve: a chained substitution's wait ran out");
     if (sp.hflags[3] != 0) {  // a zero or non-finite pivot in FP64: the matrix is singular
       const int one = 1;
       MG_CUDA(cudaMemcpy(info, &one, sizeof(int), cudaMemcpyHostToDevice));

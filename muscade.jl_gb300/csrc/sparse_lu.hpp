@@ -90,6 +90,13 @@ struct SparseDev {
   unsigned long long* nrm = nullptr;  // [2] max |correction|, max |solution| (as ordered bits)
   double* prev = nullptr;       // the previous sweep's max |correction|
   int* flags = nullptr;         // [0] converged, [1] sweeps done, [2] perturbed pivots, [3] non-finite pivot
+                                // (bit 1: a chained substitution's wait ran out)
+  unsigned* tflag = nullptr;    // [ntflag] per blocked front and pivot tile: epoch of the launch that solved it
+  int64_t ntflag = 0;
+  int* chain = nullptr;         // [2·nheight + 1] work counters of the chained substitutions, abort word
+  unsigned epoch = 0;           // of the last chained launch
+  int chain_grid32 = 1, chain_grid64 = 1;  // resident blocks of the chained substitutions
+  bool chained = true;          // chained substitutions (MGPU_SPARSE_CHAINED=0: one launch per column block)
   int* hflags = nullptr;        // pinned copy
   int last_sweeps = 0, last_fallback = 0, last_perturbed = 0;
   double last_factor_ms = 0, last_refine_ms = 0;  // CUDA-event times of the last solve's factorisation(s), sweeps

@@ -153,3 +153,24 @@ def test_super_panel_factorisation(monkeypatch, grid):
     ref = [(0.0, (out["0"][k, 0],)) for k in range(len(out["0"]))]
     errs = state_errors(out["1"], ref, st.dis.fieldX)
     assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+@pytest.mark.parametrize("kind", ["sparse", "sparse64"])
+def test_chained_substitutions_match_launch_per_block(lattice, monkeypatch, kind):
+    """The chained substitutions (one launch per height and direction, tiles
+    published through flags) repeat the arithmetic of the launch-per-column-
+    block kernels in the same order: the trajectories are bitwise equal, with
+    every front of 1 pivot or more on the blocked path."""
+    m, st, times, ref = lattice
+    monkeypatch.setenv("MGPU_SPARSE_BLOCKED_PIVOTS", "1")
+    out = {}
+    for chained in ("1", "0"):
+        monkeypatch.setenv("MGPU_SPARSE_CHAINED", chained)
+        dm = DeviceModel(m, st.dis, linsolve=kind)
+        rc, states, _ = dm.sweepx(0, times[:2], st.time, list(st.X), maxdx=1e-8, maxLl=1e-3)
+        dm.close()
+        assert rc == 0
+        out[chained] = states
+    assert np.array_equal(out["1"], out["0"])
+    errs = state_errors(out["1"], ref[:2], st.dis.fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs

@@ -221,3 +221,40 @@ def test_unconnected_models_and_chains():
     roots = np.nonzero(A["fronts"][:, 6] < 0)[0]
     assert len(roots) >= 3  # one tree per model at least
     check_solve(A, prep, nz, Ll, last)
+
+
+def test_chained_substitution_schedule():
+    """The chained substitutions (sparse_lu.cu, sp_fwdb_chain/sp_bwdb_chain)
+    give front f's pivot tile t the flag (idx_f >> 6) + 2 f + t: the ranges of
+    distinct fronts do not overlap and fit the flag array.  Work items are
+    taken in the order t·nf + f (forward) and (np_f − 1 − t)·nf + f
+    (backward); every tile an item waits for belongs to an earlier item, so a
+    block that takes an item only ever waits for blocks that are running."""
+    m, _ = W.lattice(9, 8, 5)
+    st, prep, Ll, nz = _system(m)
+    xyz, last = dof_coords_and_multipliers(m, st.dis)
+    A = analyse(prep.colptr, prep.rowval, xyz, last, leaf=8)
+    fr = A["fronts"]
+    nf = len(fr)
+    ntflag = len(A["fidx"]) // 64 + 2 * nf + 64
+    spans = []
+    for f in range(nf):
+        idx, mf, pf = int(fr[f, 1]), int(fr[f, 3]), int(fr[f, 4])
+        npt = (pf + 63) // 64
+        base = (idx >> 6) + 2 * f
+        spans.append((base, base + npt))
+        assert base + npt <= ntflag
+    spans.sort()
+    assert all(a[1] <= b[0] for a, b in zip(spans, spans[1:]))
+    # dependency order within one height's list of fronts (here: all fronts)
+    fl = list(range(nf))
+    npf = [(int(fr[f, 4]) + 63) // 64 for f in fl]
+    ntf = [npf[k] + (int(fr[f, 3]) - int(fr[f, 4]) + 63) // 64 for k, f in enumerate(fl)]
+    for k in range(nf):
+        for t in range(ntf[k]):
+            item = t * nf + k
+            assert all(j * nf + k < item for j in range(min(t, npf[k])))
+        for tb in range(npf[k]):
+            t = npf[k] - 1 - tb
+            item = tb * nf + k
+            assert all((npf[k] - 1 - b) * nf + k < item for b in range(t + 1, npf[k]))
