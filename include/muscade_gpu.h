@@ -414,7 +414,7 @@ int mgpu_host_unregister(void *ptr);
 int mgpu_measure_fp64_peak(int32_t device, double *tflops);
 
 /* Tensor-core check (no counterpart in the reference): C[M×N] −= A[M×K]·B[K×N]
- * for column-major FP32 host arrays, K ≤ 64, through the tile routine of the
+ * for column-major FP32 host arrays, K ≤ 4096, through the tile routine of the
  * multifrontal solver's FP32 trailing update (tcgen05 kind::tf32 MMAs, each
  * operand split into a TF32 part and an FP32 remainder, three products per
  * k-step, FP32 accumulation in tensor memory). */

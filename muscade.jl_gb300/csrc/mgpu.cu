@@ -260,44 +260,98 @@ __global__ void cost_kernel(int64_t nele, int udof, const int32_t* __restrict__ 
 //   out[k] = ((0 + buf[src[q0]]) + buf[src[q0+1]]) + ... ,  q = seg[k] .. seg[k+1]-1.
 // A block takes kGatherOut consecutive outputs.  Their plan positions form one
 // run [seg[k0], seg[k0+kGatherOut]); the block stages the run's entries in
-// shared memory, kGatherStage at a time: each thread first loads kGatherPer
-// plan entries (coalesced), then issues the kGatherPer gathered loads of the
-// values, all independent, so that many loads are in flight per SM.  The
-// gathered values of consecutive nnz come from consecutive elements of one
-// entry plane (neighbouring nodes, neighbouring elements), so sectors are
-// reused through L1 within a block.  Then each thread adds, in order, the
-// staged entries of its outputs.
+// shared memory: each thread first loads kGatherPer plan entries (coalesced),
+// then issues the kGatherPer gathered loads of the values, all independent, so
+// that many loads are in flight per SM.  The gathered values of consecutive
+// nnz come from consecutive elements of one entry plane (neighbouring nodes,
+// neighbouring elements), so sectors are reused through L1 within a block.
+// The sums are FP64 additions, and GB300 issues few of them: the first term
+// needs none (0 + v is v, with −0 turned into +0 as the addition would), and
+// the outputs of more than one term are listed and shared out one per thread,
+// so that a warp's lanes add about as many terms each instead of waiting on
+// the longest sum of 32 neighbouring outputs.  A run longer than one staging
+// pass takes the general loop (one output per thread, pass by pass).
 constexpr int kGatherThreads = 256;
 constexpr int kGatherOut = 1024;    // outputs per block (4 per thread)
 constexpr int kGatherPer = 8;       // staged entries per thread and pass
 constexpr int kGatherStage = kGatherThreads * kGatherPer;
+
+// 0 + v: v itself, except that −0 becomes +0
+__device__ __forceinline__ double plus_zero(double v) {
+  return __double_as_longlong(v) == (long long)0x8000000000000000ULL ? 0.0 : v;
+}
+
 __global__ void __launch_bounds__(kGatherThreads) scatter_kernel(int64_t n, const uint32_t* __restrict__ seg,
                                                                  const uint32_t* __restrict__ src,
                                                                  const double* __restrict__ buf,
                                                                  double* __restrict__ out) {
   __shared__ uint32_t sseg[kGatherOut + 1];
   __shared__ double sval[kGatherStage];
-  const int tid = threadIdx.x;
+  __shared__ int16_t slist[kGatherOut];
+  __shared__ int nlist;
+  const int tid = threadIdx.x, lane = tid & 31;
   const int64_t k0 = int64_t(blockIdx.x) * kGatherOut;
   const int nk = int(n - k0 < kGatherOut ? n - k0 : kGatherOut);
   for (int t = tid; t <= nk; t += kGatherThreads) sseg[t] = __ldg(seg + k0 + t);
+  if (tid == 0) nlist = 0;
   __syncthreads();
   const int64_t qa = sseg[0], qb = sseg[nk];
   constexpr int R = kGatherOut / kGatherThreads;
+  if (qb - qa <= kGatherStage) {
+    const int wn = int(qb - qa);
+    uint32_t sidx[kGatherPer];
+#pragma unroll
+    for (int u = 0; u < kGatherPer; ++u) {
+      const int t = u * kGatherThreads + tid;
+      sidx[u] = t < wn ? __ldg(src + qa + t) : 0u;
+    }
+    double v[kGatherPer];
+#pragma unroll
+    for (int u = 0; u < kGatherPer; ++u) v[u] = (u * kGatherThreads + tid < wn) ? __ldg(buf + sidx[u]) : 0.0;
+#pragma unroll
+    for (int u = 0; u < kGatherPer; ++u) sval[u * kGatherThreads + tid] = v[u];
+    __syncthreads();
+    // outputs of zero or one term now; the others to the list
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int kk = r * kGatherThreads + tid;
+      int len = 0, a = 0;
+      if (kk < nk) {
+        a = int(sseg[kk] - qa);
+        len = int(sseg[kk + 1] - sseg[kk]);
+        if (len <= 1) out[k0 + kk] = len ? plus_zero(sval[a]) : 0.0;
+      }
+      const bool longer = len > 1;
+      const unsigned mask = __ballot_sync(0xffffffffu, longer);
+      int base = 0;
+      if (lane == 0 && mask) base = atomicAdd(&nlist, __popc(mask));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (longer) slist[base + __popc(mask & ((1u << lane) - 1u))] = int16_t(kk);
+    }
+    __syncthreads();
+    for (int i = tid; i < nlist; i += kGatherThreads) {
+      const int kk = slist[i];
+      const int a = int(sseg[kk] - qa), b = int(sseg[kk + 1] - qa);
+      double acc = plus_zero(sval[a]);
+      for (int q = a + 1; q < b; ++q) acc += sval[q];
+      out[k0 + kk] = acc;
+    }
+    return;
+  }
   double acc[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r] = 0.0;
   for (int64_t w0 = qa; w0 < qb; w0 += kGatherStage) {
     const int wn = int(qb - w0 < kGatherStage ? qb - w0 : kGatherStage);
-    uint32_t s[kGatherPer];
+    uint32_t sidx[kGatherPer];
 #pragma unroll
     for (int u = 0; u < kGatherPer; ++u) {
       const int t = u * kGatherThreads + tid;
-      s[u] = t < wn ? __ldg(src + w0 + t) : 0u;
+      sidx[u] = t < wn ? __ldg(src + w0 + t) : 0u;
     }
     double v[kGatherPer];
 #pragma unroll
-    for (int u = 0; u < kGatherPer; ++u) v[u] = (u * kGatherThreads + tid < wn) ? __ldg(buf + s[u]) : 0.0;
+    for (int u = 0; u < kGatherPer; ++u) v[u] = (u * kGatherThreads + tid < wn) ? __ldg(buf + sidx[u]) : 0.0;
 #pragma unroll
     for (int u = 0; u < kGatherPer; ++u) sval[u * kGatherThreads + tid] = v[u];
     __syncthreads();

@@ -22,6 +22,22 @@ constexpr int kNB32 = 64;  // pivot block of the FP32 factorisation
 constexpr int kNB64 = 32;  // of the FP64 factorisation (register rows of the L panel)
 constexpr int kTile = 64;  // trailing-update tile
 constexpr int kMaxGridY = 65535;
+
+// device-scope loads and stores of flags written by other blocks
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_relaxed_i32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 constexpr size_t kUpd32Smem = size_t(2) * 64 * (128 + 4) * sizeof(float);  // sp_update_f32<64> tiles
 constexpr double kRefineTol = 1e-14;   // scaled correction / scaled solution: converged
 constexpr double kRefineStall = 1e-10;  // ... or stalled below this
@@ -209,23 +225,53 @@ __global__ void __launch_bounds__(kThreads) sp_panel_f(const SpFrontDev* __restr
   __syncthreads();
   const int b = blockIdx.x;
   if (b < nrc) {
+    // one row per thread, x U₁₁ = a; for NB = 64 in two halves of 32 columns
+    // (the second half first takes the first half's products, in the same
+    // order as a single pass), so that 32 values, not 64, are live
     const int i = r0 + b * kThreads + tid;
     if (i < m) {
-      T x[NB];
+      T* row = A + i;
+      constexpr int H = NB > 32 ? NB / 2 : NB;
+      {
+        T x[H];
 #pragma unroll
-      for (int c = 0; c < NB; ++c) x[c] = c < kb ? A[i + int64_t(k0 + c) * m] : T(0);
+        for (int c = 0; c < H; ++c) x[c] = c < kb ? row[int64_t(k0 + c) * m] : T(0);
 #pragma unroll
-      for (int c = 0; c < NB; ++c) {
-        if (c < kb) {
-          x[c] /= Dg[c][c];
+        for (int c = 0; c < H; ++c) {
+          if (c < kb) {
+            x[c] /= Dg[c][c];
 #pragma unroll
-          for (int t = c + 1; t < NB; ++t)
-            if (t < kb) x[t] -= x[c] * Dg[c][t];
+            for (int t = c + 1; t < H; ++t)
+              if (t < kb) x[t] -= x[c] * Dg[c][t];
+          }
         }
-      }
 #pragma unroll
-      for (int c = 0; c < NB; ++c)
-        if (c < kb) A[i + int64_t(k0 + c) * m] = x[c];
+        for (int c = 0; c < H; ++c)
+          if (c < kb) row[int64_t(k0 + c) * m] = x[c];
+      }
+      if constexpr (NB > H) {
+        T y[NB - H];
+#pragma unroll
+        for (int t = 0; t < NB - H; ++t) y[t] = H + t < kb ? row[int64_t(k0 + H + t) * m] : T(0);
+        for (int c = 0; c < H && c < kb; ++c) {
+          const T xc = row[int64_t(k0 + c) * m];
+#pragma unroll
+          for (int t = 0; t < NB - H; ++t)
+            if (H + t < kb) y[t] -= xc * Dg[c][H + t];
+        }
+#pragma unroll
+        for (int c = 0; c < NB - H; ++c) {
+          if (H + c < kb) {
+            y[c] /= Dg[H + c][H + c];
+#pragma unroll
+            for (int t = c + 1; t < NB - H; ++t)
+              if (H + t < kb) y[t] -= y[c] * Dg[H + c][H + t];
+          }
+        }
+#pragma unroll
+        for (int t = 0; t < NB - H; ++t)
+          if (H + t < kb) row[int64_t(k0 + H + t) * m] = y[t];
+      }
     }
     return;
   }
@@ -546,23 +592,68 @@ __global__ void __launch_bounds__(kThreads, 2) sp_rect_f32(const SpFrontDev* __r
   }
 }
 
+// the trailing block of a super-panel on the tensor cores (what sp_rect_f32
+// does in mode 2: rows and columns [e0, m) −= the super-panel's L and U parts,
+// K [s0, e0)), one 128 × 128 tile per block
+__global__ void __launch_bounds__(tc::kTcThreads) sp_trail_tc(const SpFrontDev* __restrict__ fr,
+                                                               const int32_t* __restrict__ flist, int s0, int nt,
+                                                               float* __restrict__ F, int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  const int e0 = min(s0 + kSuper, p);
+  if (e0 <= s0) return;
+  const int i0 = e0 + int(blockIdx.x / nt) * tc::kTcTile, j0 = e0 + int(blockIdx.x % nt) * tc::kTcTile;
+  if (i0 >= m || j0 >= m) return;
+  if (ld_relaxed_i32(flags + 3) & 4) return;  // a tile's wait ran out: the factors are discarded
+  float* A = F + Fr.off;
+  extern __shared__ __align__(128) float smem_tc[];
+  __shared__ uint64_t bar[2];
+  __shared__ uint32_t tslot;
+  const bool ok = tc::tile_update_tf32x3(A, m, A, m, A, m, i0, j0, m, m, s0, e0, smem_tc, bar, &tslot);
+  if (!ok && threadIdx.x == 0) atomicOr(flags + 3, 4);
+}
+
 // the diagonal block of pivot block k0 factored in place in every listed front
-// (before sp_panel_f, which reads it factored)
+// (before sp_panel_f, which reads it factored), with the arithmetic of
+// factor_diag: NB threads, thread i owning row i of the staged block; one
+// block barrier per step (after it, row k is final).  Every thread applies the
+// pivot rule to its read of the pivot itself (the rule is idempotent, so the
+// owner's write-back of a raised pivot cannot change what another reads).
 template <class T, int NB>
-__global__ void __launch_bounds__(kThreads) sp_diag_store(const SpFrontDev* __restrict__ fr,
-                                                          const int32_t* __restrict__ flist, int k0,
-                                                          T* __restrict__ F, T tau, int* __restrict__ flags) {
+__global__ void __launch_bounds__(NB) sp_diag_store(const SpFrontDev* __restrict__ fr,
+                                                    const int32_t* __restrict__ flist, int k0, T* __restrict__ F,
+                                                    T tau, int* __restrict__ flags) {
   const SpFrontDev Fr = fr[flist[blockIdx.x]];
   const int m = Fr.m, p = Fr.p;
   if (k0 >= p) return;
   const int kb = min(NB, p - k0);
   T* A = F + Fr.off;
   __shared__ T Dg[NB][NB + 1];
-  factor_diag<T, NB>(A, m, k0, kb, Dg, tau, flags, true);
-  for (int t = threadIdx.x; t < kb * kb; t += kThreads) {
-    const int i = t % kb, j = t / kb;
-    A[(k0 + i) + int64_t(k0 + j) * m] = Dg[i][j];
+  const int i = threadIdx.x;
+  for (int j = 0; j < kb; ++j)
+    if (i < kb) Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
+  for (int k = 0; k < kb; ++k) {
+    __syncthreads();
+    const T d = Dg[k][k];
+    const bool bad = !isfinite(d) || (d == T(0) && tau == T(0));
+    const bool raise = !bad && fabs(d) < tau;
+    const T piv = raise ? (d < T(0) ? -tau : tau) : d;
+    if (i == k) {
+      if (bad) atomicOr(flags + 3, 1);
+      if (raise) {
+        Dg[k][k] = piv;
+        atomicAdd(flags + 2, 1);
+      }
+    } else if (i > k && i < kb) {
+      const T l = Dg[i][k] / piv;
+      Dg[i][k] = l;
+#pragma unroll 8
+      for (int j = k + 1; j < kb; ++j) Dg[i][j] -= l * Dg[k][j];
+    }
   }
+  __syncthreads();
+  for (int j = 0; j < kb; ++j)
+    if (i < kb) A[(k0 + i) + int64_t(k0 + j) * m] = Dg[i][j];
 }
 
 // FP32 trailing update on the tensor cores: one 128 × 128 tile per block
@@ -582,7 +673,7 @@ __global__ void __launch_bounds__(tc::kTcThreads) sp_update_tc(const SpFrontDev*
   if (int(blockIdx.x) > nt * nt) return;
   float* A = F + Fr.off;
   extern __shared__ __align__(128) float smem_tc[];
-  __shared__ uint64_t bar;
+  __shared__ uint64_t bar[2];
   __shared__ uint32_t tslot;
   if (int(blockIdx.x) == nt * nt) {
     float(*Dg)[NB + 1] = reinterpret_cast<float(*)[NB + 1]>(smem_tc);
@@ -594,9 +685,8 @@ __global__ void __launch_bounds__(tc::kTcThreads) sp_update_tc(const SpFrontDev*
     return;
   }
   const int i0 = r0 + (blockIdx.x % nt) * tc::kTcTile, j0 = r0 + (blockIdx.x / nt) * tc::kTcTile;
-  const bool ok = tc::tile_update_tf32x3(A + int64_t(k0) * m, m, A + k0, m, A, m, i0, j0, m, m, kb, smem_tc, &bar,
-                                         &tslot);
-  if (!ok && threadIdx.x == 0) atomicOr(flags + 3, 2);
+  const bool ok = tc::tile_update_tf32x3(A, m, A, m, A, m, i0, j0, m, m, k0, k0 + kb, smem_tc, bar, &tslot);
+  if (!ok && threadIdx.x == 0) atomicOr(flags + 3, 4);
 }
 
 // C −= A B for host arrays through the same tile routine (column-major, K ≤ 64):
@@ -606,10 +696,10 @@ __global__ void __launch_bounds__(tc::kTcThreads) tc_gemm_check(const float* __r
                                                                  float* __restrict__ C, int ldc, int M, int N, int K,
                                                                  int* __restrict__ err) {
   extern __shared__ __align__(128) float smem_tc[];
-  __shared__ uint64_t bar;
+  __shared__ uint64_t bar[2];
   __shared__ uint32_t tslot;
   const bool ok = tc::tile_update_tf32x3(A, lda, B, ldb, C, ldc, blockIdx.x * tc::kTcTile, blockIdx.y * tc::kTcTile,
-                                         M, N, K, smem_tc, &bar, &tslot);
+                                         M, N, 0, K, smem_tc, bar, &tslot);
   if (!ok && threadIdx.x == 0) atomicOr(err, 1);
 }
 
@@ -858,30 +948,39 @@ __device__ void sb_tri_lower(const T* __restrict__ A, int m, int r0, int nr, T (
   }
 }
 
+// x = U⁻¹ v for the staged upper triangle of a diagonal tile (warp 0; lane l
+// holds rows l and l + 32), with the reciprocals rd[] of its diagonal, formed
+// while staging so that no division sits on the substitution's critical path
+template <class T>
+__device__ __forceinline__ void sb_solve_upper(const T (*Dg)[kSB + 1], const T* rd, const T* vs, int nr, int r0,
+                                               double* __restrict__ Vf) {
+  const int tid = threadIdx.x;
+  T a0 = vs[tid], a1 = vs[tid + 32];
+  for (int c = nr - 1; c >= 0; --c) {
+    T xc = (c < 32 ? a0 : a1) * rd[c];
+    xc = __shfl_sync(0xffffffffu, xc, c & 31);
+    if (tid == c) a0 = xc;
+    else if (tid < c) a0 = fma(-Dg[tid][c], xc, a0);
+    if (tid + 32 == c) a1 = xc;
+    else if (tid + 32 < c) a1 = fma(-Dg[tid + 32][c], xc, a1);
+  }
+  if (tid < nr) Vf[r0 + tid] = double(a0);
+  if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+}
+
 // upper triangle of the diagonal tile: x = U⁻¹ v, in place
 template <class T>
 __device__ void sb_tri_upper(const T* __restrict__ A, int m, int r0, int nr, T (*Dg)[kSB + 1], T* vs,
                              double* __restrict__ Vf) {
   const int tid = threadIdx.x;
+  __shared__ T rd[kSB];
   for (int q = tid; q < kSB * kSB; q += kSBThreads) {
     const int i = q & (kSB - 1), c = q >> 6;
     Dg[i][c] = (i < nr && c < nr && c >= i) ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
   }
+  if (tid < nr) rd[tid] = T(1) / A[(r0 + tid) + int64_t(r0 + tid) * m];
   __syncthreads();
-  if (tid < 32) {
-    T a0 = vs[tid], a1 = vs[tid + 32];
-    for (int c = nr - 1; c >= 0; --c) {
-      const bool lo = c < 32;
-      T xc = (lo ? a0 : a1) / Dg[c][c];
-      xc = __shfl_sync(0xffffffffu, xc, c & 31);
-      if (tid == c) a0 = xc;
-      else if (tid < c) a0 = fma(-Dg[tid][c], xc, a0);
-      if (tid + 32 == c) a1 = xc;
-      else if (tid + 32 < c) a1 = fma(-Dg[tid + 32][c], xc, a1);
-    }
-    if (tid < nr) Vf[r0 + tid] = double(a0);
-    if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
-  }
+  if (tid < 32) sb_solve_upper<T>(Dg, rd, vs, nr, r0, Vf);
 }
 
 // forward: V = the front's pivot entries, zero update rows
@@ -1082,20 +1181,6 @@ __global__ void __launch_bounds__(kSBThreads) sp_bwdb_step(const SpFrontDev* __r
 // at their next wait or item.
 constexpr int64_t kTileWaitPolls = int64_t(1) << 22;
 
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ int ld_relaxed_i32(const int* p) {
-  int v;
-  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
 // flags of front fid's tiles: (idx / 64) + 2·fid leaves every front room for its tiles
 __device__ __forceinline__ int64_t sb_flag_base(const SpFrontDev& Fr, int32_t fid) {
   return (Fr.idx >> 6) + 2 * int64_t(fid);
@@ -1252,6 +1337,7 @@ __global__ void __launch_bounds__(kSBThreads) sp_bwdb_chain(const SpFrontDev* __
   __shared__ double part[4][kSB];
   __shared__ T Dg[kSB][kSB + 1];
   __shared__ T vs[kSB];
+  __shared__ T rd[kSB];
   __shared__ int sync_s[2];
   const int tid = threadIdx.x;
   const int total = npmax * nf;
@@ -1268,6 +1354,7 @@ __global__ void __launch_bounds__(kSBThreads) sp_bwdb_chain(const SpFrontDev* __
     double* Vf = V + Fr.idx;
     unsigned* tf = tflag + sb_flag_base(Fr, fid);
     sb_stage_diag<T>(A, m, r0, nr, false, Dg);
+    if (tid < nr) rd[tid] = T(1) / A[(r0 + tid) + int64_t(r0 + tid) * m];
     double v = (tid < kSB && r0 + tid < r1) ? Vf[r0 + tid] : 0.0;
     bool ok = true;
     for (int b = np - 1; b > t && ok; --b) {
@@ -1281,18 +1368,7 @@ __global__ void __launch_bounds__(kSBThreads) sp_bwdb_chain(const SpFrontDev* __
     if (tid < kSB) vs[tid] = T(v);
     __syncthreads();
     if (tid < 32) {
-      T a0 = vs[tid], a1 = vs[tid + 32];
-      for (int c = nr - 1; c >= 0; --c) {
-        const bool lo = c < 32;
-        T xc = (lo ? a0 : a1) / Dg[c][c];
-        xc = __shfl_sync(0xffffffffu, xc, c & 31);
-        if (tid == c) a0 = xc;
-        else if (tid < c) a0 = fma(-Dg[tid][c], xc, a0);
-        if (tid + 32 == c) a1 = xc;
-        else if (tid + 32 < c) a1 = fma(-Dg[tid + 32][c], xc, a1);
-      }
-      if (tid < nr) Vf[r0 + tid] = double(a0);
-      if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+      sb_solve_upper<T>(Dg, rd, vs, nr, r0, Vf);
       __threadfence();
     }
     __syncthreads();
@@ -1440,7 +1516,7 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
                   ++c->launches;
                 }
               }
-              sp_diag_store<T, NB><<<gy, kThreads, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
+              sp_diag_store<T, NB><<<gy, NB, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
               sp_panel_f<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F);
               c->launches += 2;
             }
@@ -1451,7 +1527,11 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
           for (int f0 = 0; f0 < cnt; f0 += kMaxGridY) {
             const int32_t* fl = sp.d_lf + sp.h_lf0[h] + f0;
             const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
-            sp_rect_f32<<<dim3(unsigned(nt * nt), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 2, s0, 0, nt, F);
+            if (sp.tensor_cores && mmax - s0 >= kTcMinRest)
+              sp_trail_tc<<<dim3(unsigned(nt * nt), gy), tc::kTcThreads, tc::kTcSmem, st>>>(sp.d_fr, fl, s0, nt, F,
+                                                                                          sp.flags);
+            else
+              sp_rect_f32<<<dim3(unsigned(nt * nt), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 2, s0, 0, nt, F);
             ++c->launches;
           }
         }
@@ -1879,6 +1959,7 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaFuncSetAttribute(sp_update_f32<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
   ok(cudaFuncSetAttribute(sp_update_tc<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
   ok(cudaFuncSetAttribute(sp_rect_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
+  ok(cudaFuncSetAttribute(sp_trail_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
   if (const char* ev = getenv("MGPU_SPARSE_SUPER")) sp.super_panels = atoi(ev) != 0;
   if (const char* ev = getenv("MGPU_SPARSE_TC")) sp.tensor_cores = atoi(ev) != 0;
   if (e != cudaSuccess) {
@@ -1939,7 +2020,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
     sp.last_refine_ms = elapsed(1, 2);
     sp.last_sweeps = sp.hflags[1];
     sp.last_perturbed = sp.hflags[2];
-    if (sp.hflags[3] & 2) return set_err(c, MGPU_ERR_CUDA, "sparse solve: a chained substitution's wait ran out");
+    if (sp.hflags[3] & 6) return set_err(c, MGPU_ERR_CUDA, "sparse solve: a bounded wait on the device ran out");
     sp.last_fallback = 0;
     if (sp.hflags[0] == 0 || sp.hflags[3] != 0) {
       use64 = true;
@@ -1967,7 +2048,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
     sp.last_refine_ms += elapsed(1, 2);
     sp.last_sweeps = sp.hflags[1];
     sp.last_perturbed = sp.hflags[2];
-    if (sp.hflags[3] & 2) return set_err(c, MGPU_ERR_CUDA, "sparse solve: a chained substitution's wait ran out");
+    if (sp.hflags[3] & 6) return set_err(c, MGPU_ERR_CUDA, "sparse solve: a bounded wait on the device ran out");
     if (sp.hflags[3] != 0) {  // a zero or non-finite pivot in FP64: the matrix is singular
       const int one = 1;
       MG_CUDA(cudaMemcpy(info, &one, sizeof(int), cudaMemcpyHostToDevice));
@@ -1983,7 +2064,7 @@ int sparse_factor_solve(mgpu_ctx* c, SparseDev& sp, const double* rhs, double* o
 extern "C" int mgpu_tc_gemm_check(int32_t device, int32_t M, int32_t N, int32_t K, const float* A, const float* B,
                                   float* C) {
   using namespace mgpu;
-  if (M <= 0 || N <= 0 || K <= 0 || K > 64 || !A || !B || !C) return MGPU_ERR_ARG;
+  if (M <= 0 || N <= 0 || K <= 0 || K > 4096 || !A || !B || !C) return MGPU_ERR_ARG;
   if (cudaSetDevice(device) != cudaSuccess) return MGPU_ERR_CUDA;
   float *dA = nullptr, *dB = nullptr, *dC = nullptr;
   int* derr = nullptr;

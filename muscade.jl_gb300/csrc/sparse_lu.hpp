@@ -55,7 +55,7 @@ struct SparseDev {
   std::vector<int32_t> h_bnu;                  // most update column blocks of the blocked fronts
   int max_m_small = 0;                         // largest front of the one-block substitutions
   int big_pivots = 0;                          // fronts with this many pivots or more: blocked substitutions
-  bool tensor_cores = false;                   // FP32 trailing update on the tensor cores (TF32 ×3; MGPU_SPARSE_TC=1)
+  bool tensor_cores = true;                    // FP32 trailing updates on the tensor cores (TF32 ×3; MGPU_SPARSE_TC=0: SIMT)
   bool super_panels = true;                    // FP32 factorisation by super-panels (MGPU_SPARSE_SUPER=0: per 64-column block)
   // per height and child rank: children to add
   std::vector<std::vector<int32_t>> h_ea0, h_nea, h_eumax;
@@ -90,7 +90,7 @@ struct SparseDev {
   unsigned long long* nrm = nullptr;  // [2] max |correction|, max |solution| (as ordered bits)
   double* prev = nullptr;       // the previous sweep's max |correction|
   int* flags = nullptr;         // [0] converged, [1] sweeps done, [2] perturbed pivots, [3] non-finite pivot
-                                // (bit 1: a chained substitution's wait ran out)
+                                // (bit 1: a chained substitution's wait ran out, bit 2: a tensor-core tile's)
   unsigned* tflag = nullptr;    // [ntflag] per blocked front and pivot tile: epoch of the launch that solved it
   int64_t ntflag = 0;
   int* chain = nullptr;         // [2·nheight + 1] work counters of the chained substitutions, abort word

@@ -126,123 +126,158 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 // ---- C tile −= A · B on the tensor cores, FP32 accuracy from three TF32 products
-// C[i0 .. i0+128) × [j0 .. j0+128) −= A[·, 0..kb) · B[0..kb, ·] for kb ≤ 64, with
+// C[i0 .. i0+128) × [j0 .. j0+128) −= A[·, kbeg..kend) · B[kbeg..kend, ·], with
 // A(i, k) = A[i + k·lda], B(k, j) = B[k + j·ldb], C(i, j) = C[i + j·ldc], rows
 // below mrows and columns below ncols.  Each operand is split as x = hi + lo
 // (hi its TF32 rounding) and the accumulator takes Aₕ·Bₕ + Aₕ·Bₗ + Aₗ·Bₕ.
-// 128 threads; smem: 64 KB (the four split operand tiles of one K half of 32),
-// 128-byte aligned; bar, tslot: shared.  Warp 0 holds 128 tensor-memory
+// K runs in chunks of kTcKc through two shared-memory stages: the threads load
+// chunk c + 1 into registers while the MMAs of chunk c run, and overwrite a
+// stage only after the MMAs of its previous chunk have completed (one
+// mbarrier per stage, bounded waits).  128 threads; smem: kTcSmem bytes,
+// 128-byte aligned; bar[2], tslot: shared.  Warp 0 holds 128 tensor-memory
 // columns for the 128 × 128 FP32 accumulator (row i in lane i) and frees them
 // before returning.  Returns false when the MMAs did not complete within the
-// bounded wait (then C is left unchanged).
+// bounded waits (then C is left unchanged).
 constexpr int kTcTile = 128;
 constexpr int kTcThreads = 128;
-constexpr size_t kTcSmem = size_t(4) * kTcTile * 32 * sizeof(float);
+constexpr int kTcKc = 16;                                 // K per stage
+constexpr int kTcOperand = kTcTile * kTcKc;               // floats of one split operand of a stage
+constexpr int kTcStage = 4 * kTcOperand;                  // Aₕ, Aₗ, Bₕ, Bₗ
+constexpr size_t kTcSmem = size_t(2) * kTcStage * sizeof(float);
+constexpr int64_t kTcPolls = int64_t(1) << 20;  // bound of one wait (a chunk's MMAs take well under a microsecond)
 
-// operand values of one K half (32) in registers: A row `tid` (32 values) and,
-// for B, lane l's four K values of eight columns (see tile_update_tf32x3)
-struct TcHalf {
-  float a[32];
-  float b[32];
+// one chunk's operands in registers: A row `tid` (kTcKc values) and, for B,
+// lane l's k-quad (l >> 3) of column 8·task + (l & 7) for the warp's four tasks
+struct TcChunk {
+  float a[kTcKc];
+  float b[kTcKc];
 };
 
-__device__ __forceinline__ void tc_load_half(TcHalf& v, const float* __restrict__ A, int64_t lda,
-                                             const float* __restrict__ B, int64_t ldb, int i0, int j0, int mrows,
-                                             int ncols, int kb, int kbeg) {
+__device__ __forceinline__ void tc_load_chunk(TcChunk& v, const float* __restrict__ A, int64_t lda,
+                                              const float* __restrict__ B, int64_t ldb, int i0, int j0, int mrows,
+                                              int ncols, int kc, int kend) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int i = i0 + tid;
 #pragma unroll
-  for (int k = 0; k < 32; ++k) {
-    const int kk = kbeg + k;
-    v.a[k] = (kk < kb && i < mrows) ? A[i + int64_t(kk) * lda] : 0.f;
+  for (int k = 0; k < kTcKc; ++k) {
+    const int kk = kc + k;
+    v.a[k] = (kk < kend && i < mrows) ? A[i + int64_t(kk) * lda] : 0.f;
   }
 #pragma unroll
-  for (int tt = 0; tt < 8; ++tt) {
+  for (int tt = 0; tt < 4; ++tt) {
     const int task = warp + 4 * tt;
-    const int n = 8 * (task >> 1) + (lane & 7), kq = (lane >> 3) + 4 * (task & 1);
-    const int j = j0 + n;
+    const int j = j0 + 8 * task + (lane & 7), kq = lane >> 3;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const int kk = kbeg + 4 * kq + q;
-      v.b[4 * tt + q] = (kk < kb && j < ncols) ? B[kk + int64_t(j) * ldb] : 0.f;
+      const int kk = kc + 4 * kq + q;
+      v.b[4 * tt + q] = (kk < kend && j < ncols) ? B[kk + int64_t(j) * ldb] : 0.f;
     }
   }
 }
 
-// split and store one half's operands in the canonical K-major layout, 16-byte stores
-__device__ __forceinline__ void tc_store_half(const TcHalf& v, float* Ah, float* Al, float* Bh, float* Bl) {
+// split and store one chunk in the canonical K-major layout (16-byte stores,
+// a warp's 32 stores covering 512 contiguous bytes)
+__device__ __forceinline__ void tc_store_chunk(const TcChunk& v, float* Ah, float* Al, float* Bh, float* Bl) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 #pragma unroll
-  for (int kq = 0; kq < 8; ++kq) {
+  for (int kq = 0; kq < kTcKc / 4; ++kq) {
     float4 h4, l4;
     split_tf32(v.a[4 * kq + 0], h4.x, l4.x);
     split_tf32(v.a[4 * kq + 1], h4.y, l4.y);
     split_tf32(v.a[4 * kq + 2], h4.z, l4.z);
     split_tf32(v.a[4 * kq + 3], h4.w, l4.w);
-    const uint32_t o = kmajor_offset(tid, 4 * kq, 32) >> 2;
+    const uint32_t o = kmajor_offset(tid, 4 * kq, kTcKc) >> 2;
     *reinterpret_cast<float4*>(Ah + o) = h4;
     *reinterpret_cast<float4*>(Al + o) = l4;
   }
 #pragma unroll
-  for (int tt = 0; tt < 8; ++tt) {
+  for (int tt = 0; tt < 4; ++tt) {
     const int task = warp + 4 * tt;
-    const int n = 8 * (task >> 1) + (lane & 7), kq = (lane >> 3) + 4 * (task & 1);
+    const int n = 8 * task + (lane & 7), kq = lane >> 3;
     float4 h4, l4;
     split_tf32(v.b[4 * tt + 0], h4.x, l4.x);
     split_tf32(v.b[4 * tt + 1], h4.y, l4.y);
     split_tf32(v.b[4 * tt + 2], h4.z, l4.z);
     split_tf32(v.b[4 * tt + 3], h4.w, l4.w);
-    const uint32_t o = kmajor_offset(n, 4 * kq, 32) >> 2;
+    const uint32_t o = kmajor_offset(n, 4 * kq, kTcKc) >> 2;
     *reinterpret_cast<float4*>(Bh + o) = h4;
     *reinterpret_cast<float4*>(Bl + o) = l4;
   }
 }
 
+// one chunk through its stage: wait until the stage's previous chunk has been
+// consumed (block-uniform outcome), split and store, one thread issues the
+// six MMAs and commits them to the stage's mbarrier
+__device__ __forceinline__ bool tc_chunk_mma(const TcChunk& v, int c, float* smem, uint64_t* bar, uint32_t tmem) {
+  const int tid = threadIdx.x;
+  const int s = c & 1;
+  float* Ah = smem + s * kTcStage;
+  float* Al = Ah + kTcOperand;
+  float* Bh = Al + kTcOperand;
+  float* Bl = Bh + kTcOperand;
+  if (c >= 2 && !__syncthreads_and(mbar_wait(bar + s, uint32_t(((c - 2) >> 1) & 1), kTcPolls) ? 1 : 0)) return false;
+  tc_store_chunk(v, Ah, Al, Bh, Bl);
+  fence_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+    fence_after_sync();
+    constexpr uint32_t idesc = idesc_tf32(kTcTile, kTcTile);
+    constexpr uint32_t kLbo = 128, kSbo = (kTcKc / 4) * 128;  // core matrices along K, along M/N
+#pragma unroll
+    for (int ks = 0; ks < kTcKc / 8; ++ks) {  // K = 8 per MMA: two core matrices along K
+      const uint32_t off = uint32_t(ks) * 256;
+      const uint64_t ah = smem_desc(smem_addr(Ah) + off, kLbo, kSbo), al = smem_desc(smem_addr(Al) + off, kLbo, kSbo);
+      const uint64_t bh = smem_desc(smem_addr(Bh) + off, kLbo, kSbo), bl = smem_desc(smem_addr(Bl) + off, kLbo, kSbo);
+      mma_tf32(tmem, ah, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+      mma_tf32(tmem, ah, bl, idesc, 1u);
+      mma_tf32(tmem, al, bh, idesc, 1u);
+    }
+    mma_commit(bar + s);
+  }
+  return true;
+}
+
 __device__ __forceinline__ bool tile_update_tf32x3(const float* __restrict__ A, int64_t lda,
                                                    const float* __restrict__ B, int64_t ldb, float* __restrict__ C,
-                                                   int64_t ldc, int i0, int j0, int mrows, int ncols, int kb,
-                                                   float* smem, uint64_t* bar, uint32_t* tslot) {
-  float* Ah = smem;
-  float* Al = smem + kTcTile * 32;
-  float* Bh = smem + 2 * kTcTile * 32;
-  float* Bl = smem + 3 * kTcTile * 32;
+                                                   int64_t ldc, int i0, int j0, int mrows, int ncols, int kbeg,
+                                                   int kend, float* smem, uint64_t* bar, uint32_t* tslot) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // every operand load of the first half is in flight before any is used
-  TcHalf v;
-  tc_load_half(v, A, lda, B, ldb, i0, j0, mrows, ncols, kb, 0);
-  if (warp == 0) tmem_alloc(tslot, kTcTile);
-  if (tid == 0) mbar_init(bar, 1);
+  const int nch = (kend - kbeg + kTcKc - 1) / kTcKc;
+  // the loads of two chunks in flight: chunk c + 2 is loaded once chunk c is stored
+  TcChunk v0, v1;
+  tc_load_chunk(v0, A, lda, B, ldb, i0, j0, mrows, ncols, kbeg, kend);
+  if (nch > 1) tc_load_chunk(v1, A, lda, B, ldb, i0, j0, mrows, ncols, kbeg + kTcKc, kend);
+  if (warp == 0) {
+    tmem_alloc(tslot, kTcTile);
+    tmem_relinquish();  // lets the SM's other blocks allocate while this one runs
+  }
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+  }
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = *tslot;
-  constexpr uint32_t idesc = idesc_tf32(kTcTile, kTcTile);
-  const int nhalf = kb > 32 ? 2 : 1;
   bool ok = true;
-  for (int h = 0; h < nhalf; ++h) {
-    tc_store_half(v, Ah, Al, Bh, Bl);
-    fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      fence_after_sync();
-      for (int s = 0; s < 4; ++s) {  // K = 8 per MMA: two core matrices along K
-        const uint32_t ks = uint32_t(s) * 256;
-        const uint64_t ah = smem_desc(smem_addr(Ah) + ks, 128, 1024), al = smem_desc(smem_addr(Al) + ks, 128, 1024);
-        const uint64_t bh = smem_desc(smem_addr(Bh) + ks, 128, 1024), bl = smem_desc(smem_addr(Bl) + ks, 128, 1024);
-        mma_tf32(tmem, ah, bh, idesc, (h > 0 || s > 0) ? 1u : 0u);
-        mma_tf32(tmem, ah, bl, idesc, 1u);
-        mma_tf32(tmem, al, bh, idesc, 1u);
-      }
-      mma_commit(bar);
+#pragma unroll 1
+  for (int c = 0; c < nch && ok; c += 2) {
+    ok = tc_chunk_mma(v0, c, smem, bar, tmem);
+    if (!ok) break;
+    if (c + 2 < nch) tc_load_chunk(v0, A, lda, B, ldb, i0, j0, mrows, ncols, kbeg + (c + 2) * kTcKc, kend);
+    if (c + 1 < nch) {
+      ok = tc_chunk_mma(v1, c + 1, smem, bar, tmem);
+      if (!ok) break;
+      if (c + 3 < nch) tc_load_chunk(v1, A, lda, B, ldb, i0, j0, mrows, ncols, kbeg + (c + 3) * kTcKc, kend);
     }
-    if (h + 1 < nhalf) tc_load_half(v, A, lda, B, ldb, i0, j0, mrows, ncols, kb, 32);  // overlaps the MMAs
-    ok = mbar_wait(bar, uint32_t(h & 1)) && ok;
-    fence_after_sync();
-    __syncthreads();  // the next half overwrites the operands the MMAs read
   }
+  // the last chunk's commit arrives once every MMA of the tile has completed
+  if (ok && nch > 0)
+    ok = __syncthreads_and(mbar_wait(bar + ((nch - 1) & 1), uint32_t(((nch - 1) >> 1) & 1), kTcPolls) ? 1 : 0) != 0;
+  fence_after_sync();
   // epilogue: 32 accumulator columns at a time, their C loads all in flight together
   const int i = i0 + 32 * warp + lane;
-  const bool row_ok = ok && i < mrows;
+  const bool row_ok = ok && nch > 0 && i < mrows;
   for (int c = 0; c < kTcTile; c += 32) {
     float v0[16], v1[16];
     tmem_ld16(tmem + (uint32_t(32 * warp) << 16) + uint32_t(c), v0);

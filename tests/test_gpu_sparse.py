@@ -174,3 +174,27 @@ def test_chained_substitutions_match_launch_per_block(lattice, monkeypatch, kind
     assert np.array_equal(out["1"], out["0"])
     errs = state_errors(out["1"], ref[:2], st.dis.fieldX)
     assert all(e <= TOL_STATE for e in errs.values()), errs
+
+
+def test_tensor_core_trailing_update(monkeypatch):
+    """The super-panels' trailing blocks on the tensor cores (tcgen05 TF32 ×3,
+    MGPU_SPARSE_TC=1) against the FP32 SIMT kernel: no fallback to FP64
+    factors, iterates within the state tolerance of each other."""
+    m, times = W.lattice(20, 20, 8)
+    st = m.initialize()
+    out, info = {}, {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("MGPU_SPARSE_TC", tc)
+        dm = DeviceModel(m, st.dis, linsolve="sparse")
+        rc, states, _ = dm.sweepx(0, times[:2], st.time, list(st.X), fixed_iter=3)
+        info[tc] = dm.sparse_info()
+        dm.close()
+        assert rc == 0
+        out[tc] = states
+    monkeypatch.delenv("MGPU_SPARSE_TC")
+    print(f"tensor-core trailing update: sweeps {info['1']['last_sweeps']} (SIMT {info['0']['last_sweeps']}), "
+          f"factor {info['1']['last_factor_ms']:.2f} ms (SIMT {info['0']['last_factor_ms']:.2f} ms)")
+    assert info["1"]["last_fallback"] == 0
+    ref = [(0.0, (out["0"][k, 0],)) for k in range(len(out["0"]))]
+    errs = state_errors(out["1"], ref, st.dis.fieldX)
+    assert all(e <= TOL_STATE for e in errs.values()), errs

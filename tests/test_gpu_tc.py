@@ -1,8 +1,9 @@
 """The tensor-core tile routine of the multifrontal solver's FP32 trailing
 update (GPU): C −= A·B with tcgen05 kind::tf32 MMAs on split operands
 (x = TF32 part + FP32 remainder, three products), FP32 accumulators in tensor
-memory.  Against the FP64 product on the host: error within 2e-6 of
-max(|A|·|B|) (FP32-level accuracy; a single TF32 product would be near 1e-3).
+memory, K in chunks of 16 through two shared-memory stages.  Against the FP64
+product on the host: error within 2e-6 of max(|A|·|B|) (FP32-level accuracy; a
+single TF32 product would be near 1e-3).
 """
 import ctypes
 
@@ -21,7 +22,8 @@ def lib():
 
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (128, 128, 8), (200, 300, 37), (1, 1, 1), (130, 129, 64),
-                                   (256, 128, 32), (100, 260, 33)])
+                                   (256, 128, 32), (100, 260, 33), (256, 256, 256), (128, 128, 100),
+                                   (300, 200, 17), (129, 127, 255)])
 def test_tf32x3_tile_update_matches_fp64_product(lib, M, N, K):
     rng = np.random.default_rng(M * 1000 + N * 10 + K)
     A = np.asfortranarray(rng.normal(size=(M, K)).astype(np.float32))
