@@ -102,6 +102,27 @@ __global__ void __launch_bounds__(kThreads) sp_extend_add(const SpFrontDev* __re
   }
 }
 
+// Stage the kb × kb block at (k0, k0) of a column-major front (leading
+// dimension m) into Dg, 8 loads per thread in flight before their stores (a
+// load-then-store loop would wait for each load in turn).
+template <class T, int NB>
+__device__ __forceinline__ void stage_diag_block(const T* __restrict__ A, int m, int k0, int kb, T (*Dg)[NB + 1]) {
+  const int n = kb * kb, nt = int(blockDim.x);
+  for (int t0 = int(threadIdx.x); t0 < n; t0 += 8 * nt) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + u * nt;
+      v[u] = t < n ? A[(k0 + t % kb) + int64_t(k0 + t / kb) * m] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int t = t0 + u * nt;
+      if (t < n) Dg[t % kb][t / kb] = v[u];
+    }
+  }
+}
+
 // ---------------------------------------------------------------- partial LU of the fronts
 // The kb × kb diagonal block of pivot block k0, loaded from the front and
 // factored in shared memory (no row exchanges; a pivot below tau in magnitude
@@ -112,10 +133,7 @@ __global__ void __launch_bounds__(kThreads) sp_extend_add(const SpFrontDev* __re
 template <class T, int NB>
 __device__ void factor_diag(const T* A, int m, int k0, int kb, T (*Dg)[NB + 1], T tau, int* flags, bool count) {
   const int tid = threadIdx.x;
-  for (int t = tid; t < kb * kb; t += int(blockDim.x)) {
-    const int i = t % kb, j = t / kb;
-    Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
-  }
+  stage_diag_block<T, NB>(A, m, k0, kb, Dg);
   __syncthreads();
   for (int k = 0; k < kb; ++k) {
     if (tid == 0) {
@@ -217,11 +235,10 @@ __global__ void __launch_bounds__(kThreads) sp_panel_f(const SpFrontDev* __restr
   if (int(blockIdx.x) >= nrc + ncc) return;
   T* A = F + Fr.off;
   __shared__ T Dg[NB][NB + 1];
+  __shared__ T rdg[NB];  // reciprocal pivots: no division on the rows' substitution chains
   const int tid = threadIdx.x;
-  for (int t = tid; t < kb * kb; t += kThreads) {
-    const int i = t % kb, j = t / kb;
-    Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
-  }
+  stage_diag_block<T, NB>(A, m, k0, kb, Dg);
+  if (tid < kb) rdg[tid] = T(1) / A[(k0 + tid) + int64_t(k0 + tid) * m];
   __syncthreads();
   const int b = blockIdx.x;
   if (b < nrc) {
@@ -239,7 +256,7 @@ __global__ void __launch_bounds__(kThreads) sp_panel_f(const SpFrontDev* __restr
 #pragma unroll
         for (int c = 0; c < H; ++c) {
           if (c < kb) {
-            x[c] /= Dg[c][c];
+            x[c] *= rdg[c];
 #pragma unroll
             for (int t = c + 1; t < H; ++t)
               if (t < kb) x[t] -= x[c] * Dg[c][t];
@@ -262,7 +279,7 @@ __global__ void __launch_bounds__(kThreads) sp_panel_f(const SpFrontDev* __restr
 #pragma unroll
         for (int c = 0; c < NB - H; ++c) {
           if (H + c < kb) {
-            y[c] /= Dg[H + c][H + c];
+            y[c] *= rdg[H + c];
 #pragma unroll
             for (int t = c + 1; t < NB - H; ++t)
               if (H + t < kb) y[t] -= y[c] * Dg[H + c][H + t];
@@ -630,8 +647,7 @@ __global__ void __launch_bounds__(NB) sp_diag_store(const SpFrontDev* __restrict
   T* A = F + Fr.off;
   __shared__ T Dg[NB][NB + 1];
   const int i = threadIdx.x;
-  for (int j = 0; j < kb; ++j)
-    if (i < kb) Dg[i][j] = A[(k0 + i) + int64_t(k0 + j) * m];
+  stage_diag_block<T, NB>(A, m, k0, kb, Dg);
   for (int k = 0; k < kb; ++k) {
     __syncthreads();
     const T d = Dg[k][k];
@@ -647,8 +663,20 @@ __global__ void __launch_bounds__(NB) sp_diag_store(const SpFrontDev* __restrict
     } else if (i > k && i < kb) {
       const T l = Dg[i][k] / piv;
       Dg[i][k] = l;
-#pragma unroll 8
-      for (int j = k + 1; j < kb; ++j) Dg[i][j] -= l * Dg[k][j];
+      // eight entries of row k and of row i loaded before any is stored (the
+      // compiler cannot tell the rows apart, so a plain loop would wait for
+      // each load behind the previous store)
+      for (int j0 = k + 1; j0 < kb; j0 += 8) {
+        T u[8], r[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          u[q] = j0 + q < kb ? Dg[k][j0 + q] : T(0);
+          r[q] = j0 + q < kb ? Dg[i][j0 + q] : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (j0 + q < kb) Dg[i][j0 + q] = r[q] - l * u[q];
+      }
     }
   }
   __syncthreads();
@@ -924,6 +952,30 @@ __device__ __forceinline__ double sb_update(const T* __restrict__ A, int m, int 
   return v;
 }
 
+// stage the strict lower (lower = true) or the upper triangle of the diagonal
+// tile, zeros elsewhere; 8 loads per thread in flight before their stores
+template <class T>
+__device__ __forceinline__ void sb_stage_diag(const T* __restrict__ A, int m, int r0, int nr, bool lower,
+                                              T (*Dg)[kSB + 1]) {
+  static_assert(kSB * kSB == 16 * kSBThreads, "two batches of 8 per thread");
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = (8 * h + u) * kSBThreads + threadIdx.x;
+      const int i = q & (kSB - 1), c = q >> 6;
+      const bool in = i < nr && c < nr && (lower ? c < i : c >= i);
+      v[u] = in ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = (8 * h + u) * kSBThreads + threadIdx.x;
+      Dg[q & (kSB - 1)][q >> 6] = v[u];
+    }
+  }
+}
+
 // unit lower triangle of the diagonal tile rows [r0, r0+nr): v = L⁻¹ v, in place
 // (vals: the tile's current values, threads 0..63); the block's threads stage
 // the tile, warp 0 solves (lane l holds rows l and l + 32)
@@ -931,10 +983,7 @@ template <class T>
 __device__ void sb_tri_lower(const T* __restrict__ A, int m, int r0, int nr, T (*Dg)[kSB + 1], T* vs,
                              double* __restrict__ Vf) {
   const int tid = threadIdx.x;
-  for (int q = tid; q < kSB * kSB; q += kSBThreads) {
-    const int i = q & (kSB - 1), c = q >> 6;
-    Dg[i][c] = (i < nr && c < nr && c < i) ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
-  }
+  sb_stage_diag<T>(A, m, r0, nr, true, Dg);
   __syncthreads();
   if (tid < 32) {
     T a0 = vs[tid], a1 = vs[tid + 32];
@@ -974,10 +1023,7 @@ __device__ void sb_tri_upper(const T* __restrict__ A, int m, int r0, int nr, T (
                              double* __restrict__ Vf) {
   const int tid = threadIdx.x;
   __shared__ T rd[kSB];
-  for (int q = tid; q < kSB * kSB; q += kSBThreads) {
-    const int i = q & (kSB - 1), c = q >> 6;
-    Dg[i][c] = (i < nr && c < nr && c >= i) ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
-  }
+  sb_stage_diag<T>(A, m, r0, nr, false, Dg);
   if (tid < nr) rd[tid] = T(1) / A[(r0 + tid) + int64_t(r0 + tid) * m];
   __syncthreads();
   if (tid < 32) sb_solve_upper<T>(Dg, rd, vs, nr, r0, Vf);
@@ -1250,16 +1296,6 @@ __device__ __forceinline__ void sb_chain_apply(const T (&a)[16], int cb, const d
   __syncthreads();
 }
 
-// stage the strict lower (lower = true) or the upper triangle of the diagonal tile
-template <class T>
-__device__ __forceinline__ void sb_stage_diag(const T* __restrict__ A, int m, int r0, int nr, bool lower,
-                                              T (*Dg)[kSB + 1]) {
-  for (int q = threadIdx.x; q < kSB * kSB; q += kSBThreads) {
-    const int i = q & (kSB - 1), c = q >> 6;
-    const bool in = i < nr && c < nr && (lower ? c < i : c >= i);
-    Dg[i][c] = in ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
-  }
-}
 
 template <class T>
 __global__ void __launch_bounds__(kSBThreads) sp_fwdb_chain(const SpFrontDev* __restrict__ fr,

@@ -23,7 +23,7 @@ def lib():
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 64), (128, 128, 8), (200, 300, 37), (1, 1, 1), (130, 129, 64),
                                    (256, 128, 32), (100, 260, 33), (256, 256, 256), (128, 128, 100),
-                                   (300, 200, 17), (129, 127, 255)])
+                                   (300, 200, 17), (129, 127, 255), (4096, 4096, 256)])
 def test_tf32x3_tile_update_matches_fp64_product(lib, M, N, K):
     rng = np.random.default_rng(M * 1000 + N * 10 + K)
     A = np.asfortranarray(rng.normal(size=(M, K)).astype(np.float32))
