@@ -306,10 +306,10 @@ __global__ void __launch_bounds__(kThreads) sp_panel_f(const SpFrontDev* __restr
     const T l0 = lane > c && lane < kb ? Dg[lane][c] : T(0);
     const T l1 = NB > 32 && lane + 32 > c && lane + 32 < kb ? Dg[(lane + 32) % NB][c] : T(0);
 #pragma unroll
-    for (int jj = 0; jj < 8; ++jj) {
+    for (int jj = 0; jj < 8; ++jj) {  // l0, l1 are zero outside the triangle
       const T yc = __shfl_sync(0xffffffffu, c < 32 ? y0[jj] : y1[jj], c & 31);
-      if (lane > c && lane < kb) y0[jj] -= l0 * yc;
-      if (NB > 32 && lane + 32 > c && lane + 32 < kb) y1[jj] -= l1 * yc;
+      y0[jj] -= l0 * yc;
+      if (NB > 32) y1[jj] -= l1 * yc;
     }
   }
 #pragma unroll
@@ -771,14 +771,15 @@ __global__ void __launch_bounds__(kTriThreads) sp_fwd_tri(const SpFrontDev* __re
     const int cb = min(32, p - c0);
     for (int t = tid; t < cb * 32; t += kTriThreads) {
       const int i = t & 31, j = t >> 5;
-      Dg[i][j] = i < cb ? double(A[(c0 + i) + int64_t(c0 + j) * m]) : 0.0;
+      Dg[i][j] = (i < cb && j < i) ? double(A[(c0 + i) + int64_t(c0 + j) * m]) : 0.0;  // strict lower
     }
     __syncthreads();
     if (tid < 32) {
       double y = tid < cb ? v[c0 + tid] : 0.0;
-      for (int c = 0; c < cb; ++c) {
+#pragma unroll 4
+      for (int c = 0; c < cb; ++c) {  // branch-free: zeros at and above the diagonal
         const double yc = __shfl_sync(0xffffffffu, y, c);
-        if (tid > c && tid < cb) y -= Dg[tid][c] * yc;
+        y -= Dg[tid][c] * yc;
       }
       if (tid < cb) {
         v[c0 + tid] = y;
@@ -857,6 +858,7 @@ __global__ void __launch_bounds__(kTriThreads) sp_bwd_tri(const SpFrontDev* __re
   constexpr int NW = kTriThreads / 32;
   __shared__ double part[NW][33];
   __shared__ double Dg[32][33];
+  __shared__ double rdg[32];  // reciprocal pivots of the block
   const int m = Fr.m, p = Fr.p, tid = threadIdx.x;
   for (int t = tid; t < p; t += kTriThreads) v[t] = w[Fr.pos0 + t] - tw[Fr.pos0 + t];
   __syncthreads();
@@ -870,7 +872,9 @@ __global__ void __launch_bounds__(kTriThreads) sp_bwd_tri(const SpFrontDev* __re
     part[wp][lane] = s;
     for (int t = tid; t < 32 * 32; t += kTriThreads) {
       const int i = t & 31, j = t >> 5;
-      Dg[i][j] = (i < cb && j < cb) ? double(A[(c0 + i) + int64_t(c0 + j) * m]) : 0.0;
+      const double a = (i < cb && j < cb) ? double(A[(c0 + i) + int64_t(c0 + j) * m]) : 0.0;
+      Dg[i][j] = j > i ? a : 0.0;  // strict upper; the diagonal enters as its reciprocal
+      if (i == j && i < cb) rdg[i] = 1.0 / a;
     }
     __syncthreads();
     if (tid < 32) {
@@ -880,15 +884,13 @@ __global__ void __launch_bounds__(kTriThreads) sp_bwd_tri(const SpFrontDev* __re
 #pragma unroll
         for (int q = 0; q < NW; ++q) b -= part[q][lane];
       }
+      // branch-free: every step updates every lane (zeros at and below the column)
+#pragma unroll 4
       for (int c = cb - 1; c >= 0; --c) {
-        double xc = lane == c ? b / Dg[c][c] : 0.0;
-        xc = __shfl_sync(0xffffffffu, xc, c);
-        if (lane == c)
-          b = xc;
-        else if (lane < c)
-          b -= Dg[lane][c] * xc;
+        const double xc = __shfl_sync(0xffffffffu, b, c) * rdg[c];
+        b = fma(-Dg[lane][c], xc, b);
       }
-      if (lane < cb) v[c0 + lane] = b;
+      if (lane < cb) v[c0 + lane] = b * rdg[lane];
     }
     __syncthreads();
   }
@@ -952,8 +954,8 @@ __device__ __forceinline__ double sb_update(const T* __restrict__ A, int m, int 
   return v;
 }
 
-// stage the strict lower (lower = true) or the upper triangle of the diagonal
-// tile, zeros elsewhere; 8 loads per thread in flight before their stores
+// stage the strict lower (lower = true) or the strict upper triangle of the
+// diagonal tile, zeros elsewhere; 8 loads per thread in flight before their stores
 template <class T>
 __device__ __forceinline__ void sb_stage_diag(const T* __restrict__ A, int m, int r0, int nr, bool lower,
                                               T (*Dg)[kSB + 1]) {
@@ -965,7 +967,7 @@ __device__ __forceinline__ void sb_stage_diag(const T* __restrict__ A, int m, in
     for (int u = 0; u < 8; ++u) {
       const int q = (8 * h + u) * kSBThreads + threadIdx.x;
       const int i = q & (kSB - 1), c = q >> 6;
-      const bool in = i < nr && c < nr && (lower ? c < i : c >= i);
+      const bool in = i < nr && c < nr && (lower ? c < i : c > i);
       v[u] = in ? A[(r0 + i) + int64_t(r0 + c) * m] : T(0);
     }
 #pragma unroll
@@ -987,6 +989,7 @@ __device__ void sb_tri_lower(const T* __restrict__ A, int m, int r0, int nr, T (
   __syncthreads();
   if (tid < 32) {
     T a0 = vs[tid], a1 = vs[tid + 32];
+#pragma unroll 4
     for (int c = 0; c < nr; ++c) {
       const T yc = __shfl_sync(0xffffffffu, c < 32 ? a0 : a1, c & 31);
       a0 = fma(-Dg[tid][c], yc, a0);
@@ -997,24 +1000,27 @@ __device__ void sb_tri_lower(const T* __restrict__ A, int m, int r0, int nr, T (
   }
 }
 
-// x = U⁻¹ v for the staged upper triangle of a diagonal tile (warp 0; lane l
-// holds rows l and l + 32), with the reciprocals rd[] of its diagonal, formed
-// while staging so that no division sits on the substitution's critical path
+// x = U⁻¹ v for the staged strict upper triangle of a diagonal tile (warp 0;
+// lane l holds rows l and l + 32), with the reciprocals rd[] of its diagonal,
+// formed while staging.  Branch-free: every step updates every lane (the
+// staged zeros leave the rows at and below the column as they are), and a
+// row's value times its reciprocal pivot, the solution, is formed at the
+// step of its column for the broadcast and once more at the end in place
+// (lane-dependent branches per step made this solve 2.5 times slower than
+// the forward one).
 template <class T>
 __device__ __forceinline__ void sb_solve_upper(const T (*Dg)[kSB + 1], const T* rd, const T* vs, int nr, int r0,
                                                double* __restrict__ Vf) {
   const int tid = threadIdx.x;
   T a0 = vs[tid], a1 = vs[tid + 32];
+#pragma unroll 4
   for (int c = nr - 1; c >= 0; --c) {
-    T xc = (c < 32 ? a0 : a1) * rd[c];
-    xc = __shfl_sync(0xffffffffu, xc, c & 31);
-    if (tid == c) a0 = xc;
-    else if (tid < c) a0 = fma(-Dg[tid][c], xc, a0);
-    if (tid + 32 == c) a1 = xc;
-    else if (tid + 32 < c) a1 = fma(-Dg[tid + 32][c], xc, a1);
+    const T xc = __shfl_sync(0xffffffffu, c < 32 ? a0 : a1, c & 31) * rd[c];
+    a0 = fma(-Dg[tid][c], xc, a0);
+    a1 = fma(-Dg[tid + 32][c], xc, a1);
   }
-  if (tid < nr) Vf[r0 + tid] = double(a0);
-  if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1);
+  if (tid < nr) Vf[r0 + tid] = double(a0 * rd[tid]);
+  if (tid + 32 < nr) Vf[r0 + tid + 32] = double(a1 * rd[tid + 32]);
 }
 
 // upper triangle of the diagonal tile: x = U⁻¹ v, in place
@@ -1347,6 +1353,7 @@ __global__ void __launch_bounds__(kSBThreads) sp_fwdb_chain(const SpFrontDev* __
     __syncthreads();
     if (tid < 32) {
       T a0 = vs[tid], a1 = vs[tid + 32];
+#pragma unroll 4
       for (int c = 0; c < nr; ++c) {
         const T yc = __shfl_sync(0xffffffffu, c < 32 ? a0 : a1, c & 31);
         a0 = fma(-Dg[tid][c], yc, a0);
