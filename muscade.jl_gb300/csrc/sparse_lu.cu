@@ -630,6 +630,39 @@ __global__ void __launch_bounds__(tc::kTcThreads) sp_trail_tc(const SpFrontDev* 
   if (!ok && threadIdx.x == 0) atomicOr(flags + 3, 4);
 }
 
+// the left-looking column block (mode 0) or row block (mode 1) of pivot block
+// k0 inside a super-panel on the tensor cores: what sp_rect_f32 does in those
+// modes, one 128 × 128 tile per block (the 64-wide side masked)
+__global__ void __launch_bounds__(tc::kTcThreads) sp_rect_tc(const SpFrontDev* __restrict__ fr,
+                                                              const int32_t* __restrict__ flist, int mode, int s0,
+                                                              int k0, int ntc, float* __restrict__ F,
+                                                              int* __restrict__ flags) {
+  const SpFrontDev Fr = fr[flist[blockIdx.y]];
+  const int m = Fr.m, p = Fr.p;
+  if (k0 >= p || k0 <= s0) return;
+  int ra, rb, ca, cb;
+  if (mode == 0) {
+    ra = k0;
+    rb = m;
+    ca = k0;
+    cb = min(k0 + 64, p);
+  } else {
+    ra = k0;
+    rb = min(k0 + 64, p);
+    ca = rb;
+    cb = m;
+  }
+  const int i0 = ra + int(blockIdx.x / ntc) * tc::kTcTile, j0 = ca + int(blockIdx.x % ntc) * tc::kTcTile;
+  if (i0 >= rb || j0 >= cb) return;
+  if (ld_relaxed_i32(flags + 3) & 4) return;
+  float* A = F + Fr.off;
+  extern __shared__ __align__(128) float smem_tc[];
+  __shared__ uint64_t bar[2];
+  __shared__ uint32_t tslot;
+  const bool ok = tc::tile_update_tf32x3(A, m, A, m, A, m, i0, j0, rb, cb, s0, k0, smem_tc, bar, &tslot);
+  if (!ok && threadIdx.x == 0) atomicOr(flags + 3, 4);
+}
+
 // the diagonal block of pivot block k0 factored in place in every listed front
 // (before sp_panel_f, which reads it factored), with the arithmetic of
 // factor_diag: NB threads, thread i owning row i of the staged block; one
@@ -1551,13 +1584,17 @@ cudaError_t factorise(mgpu_ctx* c, SparseDev& sp, T* F, T tau) {
               const unsigned gy = unsigned(std::min(kMaxGridY, cnt - f0));
               if (k0 > s0) {
                 const int ntr = (rest + kTile32 - 1) / kTile32;
-                sp_rect_f32<<<dim3(unsigned(ntr), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 0, s0, k0, 1, F);
-                ++c->launches;
                 const int ntc = (rest + kTile32 - 1) / kTile32;  // columns from min(k0 + 64, p)
-                if (ntc > 0) {
+                if (sp.tensor_cores && sp.tc_left && rest >= kTcMinRest) {
+                  sp_rect_tc<<<dim3(unsigned(ntr), gy), tc::kTcThreads, tc::kTcSmem, st>>>(sp.d_fr, fl, 0, s0, k0, 1,
+                                                                                          F, sp.flags);
+                  sp_rect_tc<<<dim3(unsigned(ntc), gy), tc::kTcThreads, tc::kTcSmem, st>>>(sp.d_fr, fl, 1, s0, k0, ntc,
+                                                                                          F, sp.flags);
+                } else {
+                  sp_rect_f32<<<dim3(unsigned(ntr), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 0, s0, k0, 1, F);
                   sp_rect_f32<<<dim3(unsigned(ntc), gy), kThreads, kUpd32Smem, st>>>(sp.d_fr, fl, 1, s0, k0, ntc, F);
-                  ++c->launches;
                 }
+                c->launches += 2;
               }
               sp_diag_store<T, NB><<<gy, NB, 0, st>>>(sp.d_fr, fl, k0, F, tau, sp.flags);
               sp_panel_f<T, NB><<<dim3(unsigned(nrc + ncc), gy), kThreads, 0, st>>>(sp.d_fr, fl, k0, F);
@@ -2003,6 +2040,8 @@ int sparse_create(mgpu_ctx* c, SparseDev*& spp, const double* dof_xyz, const uin
   ok(cudaFuncSetAttribute(sp_update_tc<kNB32>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
   ok(cudaFuncSetAttribute(sp_rect_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kUpd32Smem)));
   ok(cudaFuncSetAttribute(sp_trail_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
+  ok(cudaFuncSetAttribute(sp_rect_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tc::kTcSmem)));
+  if (const char* ev = getenv("MGPU_SPARSE_TC_LEFT")) sp.tc_left = atoi(ev) != 0;
   if (const char* ev = getenv("MGPU_SPARSE_SUPER")) sp.super_panels = atoi(ev) != 0;
   if (const char* ev = getenv("MGPU_SPARSE_TC")) sp.tensor_cores = atoi(ev) != 0;
   if (e != cudaSuccess) {

@@ -56,6 +56,7 @@ struct SparseDev {
   int max_m_small = 0;                         // largest front of the one-block substitutions
   int big_pivots = 0;                          // fronts with this many pivots or more: blocked substitutions
   bool tensor_cores = true;                    // FP32 trailing updates on the tensor cores (TF32 ×3; MGPU_SPARSE_TC=0: SIMT)
+  bool tc_left = false;                        // the super-panels' left-looking blocks on the tensor cores too (MGPU_SPARSE_TC_LEFT=1)
   bool super_panels = true;                    // FP32 factorisation by super-panels (MGPU_SPARSE_SUPER=0: per 64-column block)
   // per height and child rank: children to add
   std::vector<std::vector<int32_t>> h_ea0, h_nea, h_eumax;
