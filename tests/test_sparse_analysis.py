@@ -258,3 +258,52 @@ def test_chained_substitution_schedule():
             t = npf[k] - 1 - tb
             item = tb * nf + k
             assert all((npf[k] - 1 - b) * nf + k < item for b in range(t + 1, npf[k]))
+
+
+def _partial_lu(A, p):
+    """Right-looking elimination of the first p pivots without row exchanges:
+    L below the diagonal, U on and above, the Schur complement in the rest."""
+    A = A.copy()
+    for k in range(p):
+        A[k + 1:, k] /= A[k, k]
+        A[k + 1:, k + 1:] -= np.outer(A[k + 1:, k], A[k, k + 1:])
+    return A
+
+
+def _super_panel_lu(A, p, nb=64, sup=256):
+    """The FP32 factorisation's block schedule (sparse_lu.cu, factorise): per
+    super-panel of `sup` pivots, each `nb`-column block first takes the
+    super-panel's earlier blocks (column block rows [k0, m) x [k0, min(k0+nb, p)),
+    row block rows [k0, min(k0+nb, p)) x [min(k0+nb, p), m), K [s0, k0)), then its
+    diagonal block is factored and its L and U panels solved against it; the
+    trailing block [e0, m)^2, e0 = min(s0+sup, p), takes K [s0, e0) at once."""
+    A = A.copy()
+    m = A.shape[0]
+    for s0 in range(0, p, sup):
+        e0 = min(s0 + sup, p)
+        for k0 in range(s0, e0, nb):
+            kb = min(nb, p - k0)
+            r1 = k0 + kb
+            if k0 > s0:
+                A[k0:, k0:r1] -= A[k0:, s0:k0] @ A[s0:k0, k0:r1]
+                A[k0:r1, r1:] -= A[k0:r1, s0:k0] @ A[s0:k0, r1:]
+            D = _partial_lu(A[k0:r1, k0:r1], kb)
+            L = np.tril(D, -1) + np.eye(kb)
+            U = np.triu(D)
+            A[r1:, k0:r1] = np.linalg.solve(U.T, A[r1:, k0:r1].T).T
+            A[k0:r1, r1:] = np.linalg.solve(L, A[k0:r1, r1:])
+            A[k0:r1, k0:r1] = D
+        A[e0:, e0:] -= A[e0:, s0:e0] @ A[s0:e0, e0:]
+    return A
+
+
+@pytest.mark.parametrize("m,p", [(300, 300), (700, 520), (600, 257), (900, 64), (513, 300), (130, 70), (1000, 1000)])
+def test_super_panel_schedule(m, p):
+    """The super-panel block schedule gives the partial LU of a front (its
+    factors and Schur complement) to rounding, for pivot counts that are and
+    are not multiples of the 64-column block and of the 256-pivot super-panel."""
+    rng = np.random.default_rng(m + p)
+    A = rng.normal(size=(m, m)) + np.eye(m) * m
+    ref = _partial_lu(A, p)
+    got = _super_panel_lu(A, p)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
