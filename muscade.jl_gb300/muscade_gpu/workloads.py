@@ -42,6 +42,28 @@ def cantilever(nel=20, length=10.0, load=1e3):
     return m, np.round(np.arange(1, 11) * 0.1, 12)
 
 
+def bend45(nel=8, radius=100.0):
+    """The 45° cantilever bend of examples/StaticBeamAnalysis.jl:10-36: a
+    circular arc of radius 100 m in the x-z plane, 8 EulerBeam3D (EA 1e9 N,
+    EI₂ = EI₃ = 833.33e3 N·m², GJ 705e3 N·m²), clamped at the first node, an
+    out-of-plane tip load along y ramped to 300, 450 and 600 N at t = 1, 2, 3.
+    Returns the model, the load times (0, 1, 2, 3) and the tip node."""
+    m = Model("bend45")
+    a = 1.5 * math.pi + np.arange(nel + 1) / nel * (math.pi / 4)
+    xyz = np.stack([radius * np.cos(a), np.zeros(nel + 1), radius + radius * np.sin(a)], axis=1)
+    nodes = m.addnode(xyz)
+    mat = BeamCrossSection(EA=1e9, EI2=833.33e3, EI3=833.33e3, GJ=705e3, mu=1.0, iota1=1.0)
+    m.addelement(EulerBeam3D, np.stack([nodes[:-1], nodes[1:]], axis=1), mat=mat, orient2=(0.0, 1.0, 0.0))
+    for f in ("t1", "t2", "t3", "r1", "r2", "r3"):
+        m.addelement(Hold, [nodes[0]], field=f)
+
+    def load(t):
+        return t * 300.0 if t <= 1.0 else (300.0 + (t - 1.0) * 150.0 if t <= 2.0 else 450.0 + (t - 2.0) * 150.0)
+
+    m.addelement(DofLoad, [nodes[-1]], field="t2", value=load)
+    return m, [0.0, 1.0, 2.0, 3.0], int(nodes[-1])
+
+
 def lattice(nx=60, ny=60, nz=20, seed=2027, sigma=0.1, load_std=100.0):
     rng = np.random.Generator(np.random.PCG64(seed))
     m = Model("lattice")

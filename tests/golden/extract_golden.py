@@ -149,6 +149,21 @@ g["sweepx2_X"] = vec_at(S2, 21)
 g["sweepx2_X1"] = vec_at(S2, 22)
 g["sweepx2_X2"] = vec_at(S2, 23)
 
+# ---- 45° cantilever bend (examples/StaticBeamAnalysis.jl): the tip coordinates
+# of two published solutions that the example quotes in comments, at 300, 450
+# and 600 N (x, y, z each)
+E = "examples/StaticBeamAnalysis.jl"
+
+
+def literature_row(path, lineno):
+    t = line(path, lineno).split("##", 1)[1]
+    nums = [float(x) for x in re.findall(r"-?\d+\.\d+", t)]
+    return {"src": f"{path}:{lineno}", "value": [nums[0:3], nums[3:6], nums[6:9]]}
+
+
+g["bend_tip_longva"] = literature_row(E, 133)
+g["bend_tip_crisfield"] = literature_row(E, 134)
+
 with open(OUT, "w") as f:
     json.dump(g, f, indent=1)
 print(f"wrote {len(g)} golden entries to {OUT}")

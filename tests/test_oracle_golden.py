@@ -282,3 +282,27 @@ def test_dofconstraint_equal(golden):  # test/TestDofConstraints.jl:27-46, gap .
         Ll, nz = REF.assemble(prep, (np.array(x),), (np.zeros(0),), 0.0, "static", REF.newmark_coefficients(0, 1, 0.25, 0.5))
         assert approx(Ll, golden[key]["value"])
         assert approx(prep.matrix(nz).toarray(), [[0, 0, -0.3], [0, 0, -0.4], [-0.3, -0.4, 0]])
+
+
+def _bend_tips(model, dis, states, tip):
+    nod = np.asarray(model.dof_node["X"])
+    fx = list(dis.fieldX)
+    xyz0 = np.asarray(model.coord(tip))
+    idx = [next(i for i in range(len(fx)) if fx[i] == f and nod[i] == tip) for f in ("t1", "t2", "t3")]
+    return [xyz0 + np.asarray(X)[idx] for X in states]
+
+
+def test_bend45_oracle_against_literature(golden):
+    """The 45° cantilever bend of examples/StaticBeamAnalysis.jl:10-36, solved by
+    the oracle's SweepX{0}: the tip coordinates at 300, 450 and 600 N agree with
+    both published solutions the example quotes (:131-134) within 0.1 m (the
+    two solutions differ from each other by up to 0.07 m)."""
+    from muscade_gpu import workloads as W
+    model, times, tip = W.bend45()
+    st = model.initialize()
+    ref = REF.sweepx(model, st.dis, st, times, OX=0, maxdx=1e-9)
+    tips = _bend_tips(model, st.dis, [X[0] for _, X in ref[1:]], tip)
+    for key in ("bend_tip_longva", "bend_tip_crisfield"):
+        lit = np.asarray(golden[key]["value"])
+        err = np.max(np.abs(np.asarray(tips) - lit))
+        assert err <= 0.1, (key, tips, lit)
